@@ -1,0 +1,162 @@
+/*
+ * prtcl_gpu.h -- C ABI of the GB300 (sm_103a) implementation of prtcl's
+ * SPH hot path: the uniform-grid neighbourhood, the generated IISPH
+ * pressure-solve procedures, the WKBB18 implicit-viscosity PCG solver and
+ * the small per-step procedures around them.
+ *
+ * Every entry point returns 0 on success and a negative status on failure;
+ * the message of the last failure on the calling thread is available from
+ * prtcl_gpu_last_error().  Plain pointers and sizes only.  `stream` may be
+ * NULL (the model's own stream) or a cudaStream_t cast to void*.
+ *
+ * Host layouts follow the reference (data/varying_field.hpp:26-58): a field
+ * of type real[3] is 3 contiguous floats per item, real[3][3] is 9 floats per
+ * item in column-major order.  Component types: "f32" (the reference's
+ * `real` for T=f32) and "i32" (the generated schemes' `integer`).
+ */
+#ifndef PRTCL_GPU_H
+#define PRTCL_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct prtcl_gpu_model prtcl_gpu_model;
+typedef struct prtcl_gpu_nhood prtcl_gpu_nhood;
+typedef struct prtcl_gpu_scheme prtcl_gpu_scheme;
+
+/* Status codes. */
+#define PRTCL_GPU_OK 0
+#define PRTCL_GPU_ERROR -1          /* see prtcl_gpu_last_error() */
+#define PRTCL_GPU_NOT_FOUND -2      /* unknown group / field / procedure / scheme */
+#define PRTCL_GPU_INVALID -3        /* invalid argument */
+
+/* Message of the last failure on this thread (never NULL). */
+const char *prtcl_gpu_last_error(void);
+
+/* Library version string. */
+const char *prtcl_gpu_version(void);
+
+/* ---- model: replaces prtcl::Model (data/model.hpp, data/model.cpp:13-34) ---- */
+
+int prtcl_gpu_model_create(prtcl_gpu_model **out);
+int prtcl_gpu_model_destroy(prtcl_gpu_model *model);
+
+/* Model::AddGroup (data/model.cpp:13-34): creates the group (or returns the
+ * existing one of the same type).  Group indices are the alphabetical rank
+ * of the group names and change when a group is added. */
+int prtcl_gpu_group_add(prtcl_gpu_model *model, const char *name, const char *type);
+/* Group::AddTag (data/group.hpp) */
+int prtcl_gpu_group_add_tag(prtcl_gpu_model *model, const char *group, const char *tag);
+/* Group::Resize (data/group.hpp): resizes every varying field, keeping the
+ * first min(old, new) items */
+int prtcl_gpu_group_resize(prtcl_gpu_model *model, const char *group, int64_t count);
+int prtcl_gpu_group_count(prtcl_gpu_model *model, const char *group, int64_t *count_out);
+int prtcl_gpu_group_index(prtcl_gpu_model *model, const char *group, int32_t *index_out);
+int prtcl_gpu_model_group_count(prtcl_gpu_model *model, int32_t *count_out);
+
+/* VaryingManager::AddFieldImpl (data/varying_manager.hpp:33-46): adds a
+ * field (or checks the type of an existing one).  rank 0..2, extents[rank]. */
+int prtcl_gpu_field_add(prtcl_gpu_model *model, const char *group, const char *field, const char *ctype, int32_t rank,
+                        const int32_t *extents);
+/* Copy `count` items (== the group's item count) from host memory in the
+ * reference layout.  Synchronous: returns after the copy completed. */
+int prtcl_gpu_field_upload(prtcl_gpu_model *model, const char *group, const char *field, const void *host,
+                           int64_t count, void *stream);
+/* As above but stream-ordered: `host` must stay valid (pinned memory for
+ * overlap) until the stream reaches the copy. */
+int prtcl_gpu_field_upload_async(prtcl_gpu_model *model, const char *group, const char *field, const void *host,
+                                 int64_t count, void *stream);
+/* Copy the field to host memory in the reference layout (synchronous). */
+int prtcl_gpu_field_download(prtcl_gpu_model *model, const char *group, const char *field, void *host, int64_t count,
+                             void *stream);
+/* Type of a varying field; ctype_out receives "f32" or "i32" (>= 4 bytes). */
+int prtcl_gpu_field_info(prtcl_gpu_model *model, const char *group, const char *field, char *ctype_out,
+                         int32_t *rank_out, int32_t *extents_out /* [2] */);
+
+/* UniformManager (data/uniform_manager.hpp): one value per group.  `value`
+ * holds prod(extents) components of the field's component type. */
+int prtcl_gpu_uniform_add(prtcl_gpu_model *model, const char *group, const char *field, const char *ctype,
+                          int32_t rank, const int32_t *extents);
+int prtcl_gpu_uniform_set(prtcl_gpu_model *model, const char *group, const char *field, const void *value);
+int prtcl_gpu_uniform_get(prtcl_gpu_model *model, const char *group, const char *field, void *value);
+
+/* Global fields of the model (data/model.hpp, Model::AddGlobalFieldImpl). */
+int prtcl_gpu_global_add(prtcl_gpu_model *model, const char *field, const char *ctype, int32_t rank,
+                         const int32_t *extents);
+int prtcl_gpu_global_set(prtcl_gpu_model *model, const char *field, const void *value);
+int prtcl_gpu_global_get(prtcl_gpu_model *model, const char *field, void *value);
+
+/* Types of uniform and global fields (ctype_out >= 4 bytes, extents_out[2]). */
+int prtcl_gpu_uniform_info(prtcl_gpu_model *model, const char *group, const char *field, char *ctype_out,
+                           int32_t *rank_out, int32_t *extents_out);
+int prtcl_gpu_global_info(prtcl_gpu_model *model, const char *field, char *ctype_out, int32_t *rank_out,
+                          int32_t *extents_out);
+
+/* Wait for all work queued on the model's stream (and `stream`, if given). */
+int prtcl_gpu_model_synchronize(prtcl_gpu_model *model, void *stream);
+
+/* ---- neighbourhood: replaces prtcl::Neighborhood (util/neighborhood.hpp:23-42) ---- */
+
+int prtcl_gpu_nhood_create(prtcl_gpu_nhood **out);
+int prtcl_gpu_nhood_destroy(prtcl_gpu_nhood *nhood);
+/* Neighborhood::SetRadius (util/neighborhood.cpp:61-65) */
+int prtcl_gpu_nhood_set_radius(prtcl_gpu_nhood *nhood, double radius);
+/* Neighborhood::Load (util/neighborhood.cpp:67-98): binds the groups'
+ * "position" fields (real[3]) and their cannot_be_neighbor tags */
+int prtcl_gpu_nhood_load(prtcl_gpu_nhood *nhood, prtcl_gpu_model *model);
+/* Neighborhood::Update (util/neighborhood.cpp:100-104 ->
+ * grouped_uniform_grid::update, util/grouped_uniform_grid.hpp:126-337) */
+int prtcl_gpu_nhood_update(prtcl_gpu_nhood *nhood, void *stream);
+/* Neighborhood::Permute (util/neighborhood.cpp:106-154): reorders every
+ * varying field of each neighbour-capable group into cell order, then Update */
+int prtcl_gpu_nhood_permute(prtcl_gpu_nhood *nhood, prtcl_gpu_model *model, void *stream);
+/* Neighborhood::CopyNeighbors (util/neighborhood.cpp:156-166): neighbours of
+ * item `index` of group `group`; counts_out[g] receives the number of
+ * neighbours in group g (group-count entries), indices_out the raw indices
+ * grouped by group in traversal order (at most `capacity` are written);
+ * *total_out the total.  */
+int prtcl_gpu_nhood_copy_neighbors(prtcl_gpu_nhood *nhood, int32_t group, int64_t index, int64_t *counts_out,
+                                   int64_t *indices_out, int64_t capacity, int64_t *total_out);
+/* Bulk form for parity checks: CSR of every item of `query_group` to the
+ * neighbours in `neighbor_group`; offsets_out has count + 1 entries. */
+int prtcl_gpu_nhood_copy_lists(prtcl_gpu_nhood *nhood, int32_t query_group, int32_t neighbor_group,
+                               int64_t *offsets_out, uint32_t *indices_out, int64_t capacity);
+/* Grid introspection for parity checks: the sorted item handles
+ * (group << 28 | raw index, util/grouped_uniform_grid.hpp:104-110), and per
+ * cell its grid index (3 x int32), its [first, last) sorted range and its
+ * 26 adjacent cells (-1 = none).  Any output pointer may be NULL. */
+int prtcl_gpu_nhood_grid_size(prtcl_gpu_nhood *nhood, int64_t *sorted_count_out, int64_t *cell_count_out);
+int prtcl_gpu_nhood_copy_grid(prtcl_gpu_nhood *nhood, uint32_t *sorted_out, int32_t *cell_grid_index_out,
+                              int32_t *cell_range_out, int32_t *cell_adjacency_out);
+
+/* ---- schemes: replaces prtcl::SchemeBase / SchemeRegistry (schemes/scheme_base.hpp:18-105) ---- */
+
+/* SchemeRegistry::NewScheme (schemes/scheme_base.hpp:87-92) by full name,
+ * e.g. "prtcl::schemes::iisph[T=f32, N=3, K=Cubic Spline]";
+ * PRTCL_GPU_NOT_FOUND with "scheme is not registered" otherwise. */
+int prtcl_gpu_scheme_new(const char *full_name, prtcl_gpu_scheme **out);
+int prtcl_gpu_scheme_destroy(prtcl_gpu_scheme *scheme);
+/* SchemeBase::Load (e.g. schemes/iisph.hpp:134-185): creates the global,
+ * uniform and varying fields the scheme uses and binds the groups. */
+int prtcl_gpu_scheme_load(prtcl_gpu_scheme *scheme, prtcl_gpu_model *model);
+/* SchemeBase::RunProcedure (schemes/scheme_base.hpp:33-38): queues the
+ * procedure on `stream`; PRTCL_GPU_NOT_FOUND with "procedure does not
+ * exist" for an unknown name. */
+int prtcl_gpu_scheme_run(prtcl_gpu_scheme *scheme, const char *procedure, prtcl_gpu_nhood *nhood, void *stream);
+/* SchemeBase::GetFullName / GetProcedureNames / GetPrtclSourceCode and
+ * SchemeRegistry::GetSchemeNames: '\n'-separated lists written to `buf`
+ * (NUL-terminated, truncated to `size`); *needed_out gets the full length. */
+int prtcl_gpu_scheme_full_name(prtcl_gpu_scheme *scheme, char *buf, int64_t size, int64_t *needed_out);
+int prtcl_gpu_scheme_procedure_names(prtcl_gpu_scheme *scheme, char *buf, int64_t size, int64_t *needed_out);
+int prtcl_gpu_scheme_source(prtcl_gpu_scheme *scheme, char *buf, int64_t size, int64_t *needed_out);
+int prtcl_gpu_registry_scheme_names(char *buf, int64_t size, int64_t *needed_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PRTCL_GPU_H */

@@ -1,0 +1,128 @@
+"""ctypes binding of the C ABI declared in include/prtcl_gpu.h.
+
+The library is built in-tree (prtcl_gb300/libprtcl_gpu.so) by
+``prtcl_gb300.build.build()``.  There is no CPU fallback: if the library is
+missing, cannot be loaded or no CUDA device is present, the first call
+raises ``PrtclGpuUnavailable``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libprtcl_gpu.so")
+
+OK, ERROR, NOT_FOUND, INVALID = 0, -1, -2, -3
+
+
+class PrtclGpuError(RuntimeError):
+    """A failed call of the C ABI (the message of prtcl_gpu_last_error)."""
+
+
+class PrtclNotFound(PrtclGpuError, LookupError):
+    """Unknown group, field, procedure or scheme ("procedure does not exist",
+    "scheme is not registered" in the reference)."""
+
+
+class PrtclGpuUnavailable(ImportError):
+    """The CUDA library is missing or could not be loaded."""
+
+
+vp, cp, i32, i64, u32p, i64p, i32p, dbl = (C.c_void_p, C.c_char_p, C.c_int32, C.c_int64, C.POINTER(C.c_uint32),
+                                           C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.c_double)
+pp = C.POINTER(C.c_void_p)
+
+# name -> argtypes (all entry points return int unless listed in _RESTYPE)
+SIGNATURES = {
+    "prtcl_gpu_last_error": [],
+    "prtcl_gpu_version": [],
+    "prtcl_gpu_model_create": [pp],
+    "prtcl_gpu_model_destroy": [vp],
+    "prtcl_gpu_group_add": [vp, cp, cp],
+    "prtcl_gpu_group_add_tag": [vp, cp, cp],
+    "prtcl_gpu_group_resize": [vp, cp, i64],
+    "prtcl_gpu_group_count": [vp, cp, i64p],
+    "prtcl_gpu_group_index": [vp, cp, i32p],
+    "prtcl_gpu_model_group_count": [vp, i32p],
+    "prtcl_gpu_field_add": [vp, cp, cp, cp, i32, i32p],
+    "prtcl_gpu_field_upload": [vp, cp, cp, vp, i64, vp],
+    "prtcl_gpu_field_upload_async": [vp, cp, cp, vp, i64, vp],
+    "prtcl_gpu_field_download": [vp, cp, cp, vp, i64, vp],
+    "prtcl_gpu_field_info": [vp, cp, cp, C.c_char_p, i32p, i32p],
+    "prtcl_gpu_uniform_add": [vp, cp, cp, cp, i32, i32p],
+    "prtcl_gpu_uniform_set": [vp, cp, cp, vp],
+    "prtcl_gpu_uniform_get": [vp, cp, cp, vp],
+    "prtcl_gpu_global_add": [vp, cp, cp, i32, i32p],
+    "prtcl_gpu_global_set": [vp, cp, vp],
+    "prtcl_gpu_global_get": [vp, cp, vp],
+    "prtcl_gpu_uniform_info": [vp, cp, cp, C.c_char_p, i32p, i32p],
+    "prtcl_gpu_global_info": [vp, cp, C.c_char_p, i32p, i32p],
+    "prtcl_gpu_model_synchronize": [vp, vp],
+    "prtcl_gpu_nhood_create": [pp],
+    "prtcl_gpu_nhood_destroy": [vp],
+    "prtcl_gpu_nhood_set_radius": [vp, dbl],
+    "prtcl_gpu_nhood_load": [vp, vp],
+    "prtcl_gpu_nhood_update": [vp, vp],
+    "prtcl_gpu_nhood_permute": [vp, vp, vp],
+    "prtcl_gpu_nhood_copy_neighbors": [vp, i32, i64, i64p, i64p, i64, i64p],
+    "prtcl_gpu_nhood_copy_lists": [vp, i32, i32, i64p, u32p, i64],
+    "prtcl_gpu_nhood_grid_size": [vp, i64p, i64p],
+    "prtcl_gpu_nhood_copy_grid": [vp, u32p, i32p, i32p, i32p],
+    "prtcl_gpu_scheme_new": [cp, pp],
+    "prtcl_gpu_scheme_destroy": [vp],
+    "prtcl_gpu_scheme_load": [vp, vp],
+    "prtcl_gpu_scheme_run": [vp, cp, vp, vp],
+    "prtcl_gpu_scheme_full_name": [vp, C.c_char_p, i64, i64p],
+    "prtcl_gpu_scheme_procedure_names": [vp, C.c_char_p, i64, i64p],
+    "prtcl_gpu_scheme_source": [vp, C.c_char_p, i64, i64p],
+    "prtcl_gpu_registry_scheme_names": [C.c_char_p, i64, i64p],
+}
+_RESTYPE = {"prtcl_gpu_last_error": cp, "prtcl_gpu_version": cp}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load (once) and return the ctypes library with all signatures set."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(path):
+            raise PrtclGpuUnavailable(
+                f"{path} is missing: build it with `python -m prtcl_gb300.build` "
+                "(there is no CPU fallback)")
+        try:
+            L = C.CDLL(path)
+        except OSError as e:
+            raise PrtclGpuUnavailable(f"cannot load {path}: {e}") from e
+        for name, args in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = _RESTYPE.get(name, C.c_int)
+        _lib = L
+        return L
+
+
+def check(rc):
+    if rc == OK:
+        return
+    msg = load().prtcl_gpu_last_error().decode()
+    if rc == NOT_FOUND:
+        raise PrtclNotFound(msg)
+    raise PrtclGpuError(msg)
+
+
+def b(s):
+    return s.encode() if isinstance(s, str) else s
+
+
+def read_str(fn, *args):
+    need = C.c_int64(0)
+    check(fn(*args, None, 0, C.byref(need)))
+    buf = C.create_string_buffer(int(need.value))
+    check(fn(*args, buf, need.value, C.byref(need)))
+    return buf.value.decode()

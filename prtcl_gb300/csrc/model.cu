@@ -1,0 +1,338 @@
+// Device data model: groups, varying / uniform / global fields, upload,
+// download and the per-group permutation gather (data/varying_manager.hpp:
+// 86-101 applies new[i] = old[perm[i]] to every varying field of a group).
+#include "model.hpp"
+
+#include <algorithm>
+#include <cstring>
+
+namespace prtcl_gpu {
+
+std::string FieldType::str() const {
+  std::string s = ctype == CType::F32 ? "real" : "integer";
+  for (int r = 0; r < rank; ++r) s += "[" + std::to_string(ext[r]) + "]";
+  return s;
+}
+
+FieldType parse_field_type(char const *ctype, int rank, int const *extents) {
+  FieldType t;
+  std::string c = ctype ? ctype : "";
+  if (c == "f32" || c == "real" || c == "float32") t.ctype = CType::F32;
+  else if (c == "i32" || c == "integer" || c == "int32") t.ctype = CType::I32;
+  else throw Error("unsupported component type '" + c + "' (device fields are f32 or i32)");
+  if (rank < 0 || rank > 2) throw Error("unsupported field rank " + std::to_string(rank));
+  t.rank = rank;
+  for (int r = 0; r < rank; ++r) {
+    if (!extents || extents[r] <= 0) throw Error("invalid field extent");
+    t.ext[r] = extents[r];
+  }
+  return t;
+}
+
+size_t VaryingField::device_item_bytes() const {
+  if (type.is_vec3()) return 16;
+  return type.host_item_bytes();
+}
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+
+__global__ void k_expand_vec3(float const *__restrict__ src, float4 *__restrict__ dst, size_t n) {
+  size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (i < n) dst[i] = make_float4(src[3 * i], src[3 * i + 1], src[3 * i + 2], 0.0f);
+}
+__global__ void k_pack_vec3(float4 const *__restrict__ src, float *__restrict__ dst, size_t n) {
+  size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (i < n) {
+    float4 v = src[i];
+    dst[3 * i] = v.x;
+    dst[3 * i + 1] = v.y;
+    dst[3 * i + 2] = v.z;
+  }
+}
+// host layout: 9 floats per item (column-major); device: plane k at k*cap
+__global__ void k_to_planar9(float const *__restrict__ src, float *__restrict__ dst, size_t n, size_t cap) {
+  size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (i < n)
+    for (int k = 0; k < 9; ++k) dst[k * cap + i] = src[9 * i + k];
+}
+__global__ void k_from_planar9(float const *__restrict__ src, float *__restrict__ dst, size_t n, size_t cap) {
+  size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (i < n)
+    for (int k = 0; k < 9; ++k) dst[9 * i + k] = src[k * cap + i];
+}
+template <class V>
+__global__ void k_gather(V const *__restrict__ src, V *__restrict__ dst, uint32_t const *__restrict__ perm, size_t n) {
+  size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (i < n) dst[i] = src[perm[i]];
+}
+__global__ void k_gather_planar9(float const *__restrict__ src, float *__restrict__ dst, uint32_t const *__restrict__ perm,
+                                 size_t n, size_t scap, size_t dcap) {
+  size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (i < n) {
+    uint32_t j = perm[i];
+    for (int k = 0; k < 9; ++k) dst[k * dcap + i] = src[k * scap + j];
+  }
+}
+// generic item gather in 4-byte words
+__global__ void k_gather_words(uint32_t const *__restrict__ src, uint32_t *__restrict__ dst,
+                               uint32_t const *__restrict__ perm, size_t n, int words) {
+  size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  size_t i = t / words;
+  int w = int(t % words);
+  if (i < n) dst[i * words + w] = src[size_t(perm[i]) * words + w];
+}
+
+// ---------------------------------------------------------------------------
+// storage helpers
+// ---------------------------------------------------------------------------
+
+static void *alloc_field(FieldType const &t, size_t cap, cudaStream_t s) {
+  size_t bytes = t.is_vec3() ? cap * 16 : cap * t.host_item_bytes();
+  if (bytes == 0) return nullptr;
+  void *p = nullptr;
+  PG_CUDA(cudaMallocAsync(&p, bytes, s));
+  PG_CUDA(cudaMemsetAsync(p, 0, bytes, s));
+  return p;
+}
+
+static void copy_items(VaryingField const &src, void *dst, size_t dst_cap, size_t n, cudaStream_t s) {
+  if (n == 0) return;
+  if (src.type.is_mat3()) {
+    for (int k = 0; k < 9; ++k)
+      PG_CUDA(cudaMemcpyAsync(static_cast<float *>(dst) + k * dst_cap, static_cast<float *>(src.d) + k * src.cap,
+                              n * 4, cudaMemcpyDeviceToDevice, s));
+  } else {
+    PG_CUDA(cudaMemcpyAsync(dst, src.d, n * src.device_item_bytes(), cudaMemcpyDeviceToDevice, s));
+  }
+}
+
+void upload_varying(VaryingField &f, size_t count, void const *host, size_t n_items, cudaStream_t s, bool sync) {
+  if (n_items != count)
+    throw Error("upload: item count " + std::to_string(n_items) + " != group count " + std::to_string(count));
+  f.version++;
+  if (count == 0) return;
+  size_t hbytes = count * f.type.host_item_bytes();
+  if (!f.type.is_vec3() && !f.type.is_mat3()) {
+    PG_CUDA(cudaMemcpyAsync(f.d, host, hbytes, cudaMemcpyHostToDevice, s));
+  } else {
+    void *stage = nullptr;
+    PG_CUDA(cudaMallocAsync(&stage, hbytes, s));
+    PG_CUDA(cudaMemcpyAsync(stage, host, hbytes, cudaMemcpyHostToDevice, s));
+    if (f.type.is_vec3())
+      k_expand_vec3<<<div_up(count, 256), 256, 0, s>>>(static_cast<float *>(stage), static_cast<float4 *>(f.d), count);
+    else
+      k_to_planar9<<<div_up(count, 256), 256, 0, s>>>(static_cast<float *>(stage), static_cast<float *>(f.d), count, f.cap);
+    PG_LAUNCH_CHECK();
+    PG_CUDA(cudaFreeAsync(stage, s));
+  }
+  if (sync) PG_CUDA(cudaStreamSynchronize(s));
+}
+
+void download_varying(VaryingField const &f, size_t count, void *host, size_t n_items, cudaStream_t s) {
+  if (n_items != count)
+    throw Error("download: item count " + std::to_string(n_items) + " != group count " + std::to_string(count));
+  if (count == 0) return;
+  size_t hbytes = count * f.type.host_item_bytes();
+  if (!f.type.is_vec3() && !f.type.is_mat3()) {
+    PG_CUDA(cudaMemcpyAsync(host, f.d, hbytes, cudaMemcpyDeviceToHost, s));
+  } else {
+    void *stage = nullptr;
+    PG_CUDA(cudaMallocAsync(&stage, hbytes, s));
+    if (f.type.is_vec3())
+      k_pack_vec3<<<div_up(count, 256), 256, 0, s>>>(static_cast<float4 const *>(f.d), static_cast<float *>(stage), count);
+    else
+      k_from_planar9<<<div_up(count, 256), 256, 0, s>>>(static_cast<float const *>(f.d), static_cast<float *>(stage), count, f.cap);
+    PG_LAUNCH_CHECK();
+    PG_CUDA(cudaMemcpyAsync(host, stage, hbytes, cudaMemcpyDeviceToHost, s));
+    PG_CUDA(cudaFreeAsync(stage, s));
+  }
+  PG_CUDA(cudaStreamSynchronize(s));
+}
+
+// ---------------------------------------------------------------------------
+// Group
+// ---------------------------------------------------------------------------
+
+VaryingField &Group::add_varying(std::string const &n, FieldType const &t) {
+  auto it = varying.find(n);
+  if (it != varying.end()) {
+    if (it->second.type != t) throw Error("field of different type already exists: " + name + "." + n);
+    return it->second;
+  }
+  VaryingField f;
+  f.type = t;
+  f.cap = count;
+  f.d = alloc_field(t, count, model_->stream());
+  model_->layout_version++;
+  return varying.emplace(n, f).first->second;
+}
+
+VaryingField *Group::find_varying(std::string const &n) {
+  auto it = varying.find(n);
+  return it == varying.end() ? nullptr : &it->second;
+}
+
+VaryingField &Group::get_varying(std::string const &n, FieldType const &t) {
+  auto *f = find_varying(n);
+  if (!f) throw Error("field does not exist: " + name + "." + n);
+  if (f->type != t) throw Error("field " + name + "." + n + " is " + f->type.str() + ", expected " + t.str());
+  return *f;
+}
+
+SmallField &Group::add_uniform(std::string const &n, FieldType const &t) {
+  auto it = uniform.find(n);
+  if (it != uniform.end()) {
+    if (it->second.type != t) throw Error("uniform field of different type already exists: " + name + "." + n);
+    return it->second;
+  }
+  SmallField &f = uniform[n];
+  return model_->alloc_small(f, t);
+}
+
+void Group::resize(size_t n, cudaStream_t s) {
+  if (n >= (size_t(1) << 28)) throw Error("group '" + name + "' too large: at most 2^28 - 1 items");
+  if (n == count) return;
+  for (auto &kv : varying) {
+    VaryingField &f = kv.second;
+    void *nd = alloc_field(f.type, n, s);
+    copy_items(f, nd, n, std::min(n, count), s);
+    if (f.d) PG_CUDA(cudaFreeAsync(f.d, s));
+    f.d = nd;
+    f.cap = n;
+    f.version++;
+  }
+  count = n;
+  model_->layout_version++;
+}
+
+void Group::permute(uint32_t const *perm, cudaStream_t s) {
+  size_t n = count;
+  if (n == 0) return;
+  for (auto &kv : varying) {
+    VaryingField &f = kv.second;
+    void *nd = alloc_field(f.type, f.cap, s);
+    unsigned b = 256;
+    if (f.type.is_vec3()) {
+      k_gather<float4><<<div_up(n, b), b, 0, s>>>(static_cast<float4 const *>(f.d), static_cast<float4 *>(nd), perm, n);
+    } else if (f.type.is_mat3()) {
+      k_gather_planar9<<<div_up(n, b), b, 0, s>>>(static_cast<float const *>(f.d), static_cast<float *>(nd), perm, n,
+                                                  f.cap, f.cap);
+    } else if (f.type.host_item_bytes() == 4) {
+      k_gather<uint32_t><<<div_up(n, b), b, 0, s>>>(static_cast<uint32_t const *>(f.d), static_cast<uint32_t *>(nd), perm, n);
+    } else {
+      int words = int(f.type.host_item_bytes() / 4);
+      k_gather_words<<<div_up(n * words, b), b, 0, s>>>(static_cast<uint32_t const *>(f.d), static_cast<uint32_t *>(nd),
+                                                        perm, n, words);
+    }
+    PG_LAUNCH_CHECK();
+    PG_CUDA(cudaFreeAsync(f.d, s));
+    f.d = nd;
+    f.version++;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Model
+// ---------------------------------------------------------------------------
+
+Model::Model() {
+  PG_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  arena_cap_ = 64 * 1024;
+  PG_CUDA(cudaMalloc(&arena_d_, arena_cap_));
+  PG_CUDA(cudaMemset(arena_d_, 0, arena_cap_));
+  PG_CUDA(cudaMalloc(&red_d, 3 * 4096 * sizeof(double)));
+  PG_CUDA(cudaMalloc(&red_count_d, 64 * sizeof(unsigned)));
+  PG_CUDA(cudaMemset(red_count_d, 0, 64 * sizeof(unsigned)));
+  PG_CUDA(cudaMalloc(&scalars_d, 64 * sizeof(double)));
+  PG_CUDA(cudaMemset(scalars_d, 0, 64 * sizeof(double)));
+  PG_CUDA(cudaMalloc(&status_d, 16 * sizeof(int)));
+  PG_CUDA(cudaMemset(status_d, 0, 16 * sizeof(int)));
+}
+
+Model::~Model() {
+  cudaStreamSynchronize(stream_);
+  for (auto &g : groups_)
+    for (auto &kv : g.second->varying)
+      if (kv.second.d) cudaFree(kv.second.d);
+  cudaFree(arena_d_);
+  cudaFree(red_d);
+  cudaFree(red_count_d);
+  cudaFree(scalars_d);
+  cudaFree(status_d);
+  cudaStreamDestroy(stream_);
+}
+
+void Model::reindex() {
+  int i = 0;
+  for (auto &kv : groups_) kv.second->index = i++;
+}
+
+Group &Model::add_group(std::string const &name, std::string const &type) {
+  if (name.empty()) throw Error("invalid group name");
+  auto it = groups_.find(name);
+  if (it != groups_.end()) {
+    if (it->second->type != type) throw Error("group of different type already exists: " + name);
+    return *it->second;
+  }
+  if (groups_.size() >= size_t(kMaxGroups)) throw Error("too many groups (at most 16)");
+  auto &g = groups_[name];
+  g.reset(new Group(this, name, type));
+  reindex();
+  layout_version++;
+  return *g;
+}
+
+Group *Model::find_group(std::string const &name) {
+  auto it = groups_.find(name);
+  return it == groups_.end() ? nullptr : it->second.get();
+}
+
+Group &Model::group(std::string const &name) {
+  auto *g = find_group(name);
+  if (!g) throw Error("group does not exist: " + name);
+  return *g;
+}
+
+std::vector<Group *> Model::groups_by_index() {
+  std::vector<Group *> r;
+  for (auto &kv : groups_) r.push_back(kv.second.get());
+  return r;
+}
+
+SmallField &Model::alloc_small(SmallField &f, FieldType const &t) {
+  size_t bytes = (t.host_item_bytes() + 15) / 16 * 16;
+  if (arena_used_ + bytes > arena_cap_) throw Error("uniform/global field arena exhausted");
+  f.type = t;
+  f.offset = arena_used_;
+  arena_used_ += bytes;
+  return f;
+}
+
+SmallField &Model::add_global(std::string const &name, FieldType const &t) {
+  auto it = global_.find(name);
+  if (it != global_.end()) {
+    if (it->second.type != t) throw Error("global field of different type already exists: " + name);
+    return it->second;
+  }
+  SmallField &f = global_[name];
+  return alloc_small(f, t);
+}
+
+SmallField *Model::find_global(std::string const &name) {
+  auto it = global_.find(name);
+  return it == global_.end() ? nullptr : &it->second;
+}
+
+void Model::small_set(SmallField const &f, void const *host, cudaStream_t s) {
+  PG_CUDA(cudaMemcpyAsync(small_ptr(f), host, f.type.host_item_bytes(), cudaMemcpyHostToDevice, s));
+  PG_CUDA(cudaStreamSynchronize(s));
+}
+
+void Model::small_get(SmallField const &f, void *host, cudaStream_t s) {
+  PG_CUDA(cudaMemcpyAsync(host, small_ptr(f), f.type.host_item_bytes(), cudaMemcpyDeviceToHost, s));
+  PG_CUDA(cudaStreamSynchronize(s));
+}
+
+} // namespace prtcl_gpu

@@ -1,0 +1,134 @@
+// Device-resident mirror of prtcl's data model (data/model.cpp,
+// data/group.hpp, data/varying_manager.hpp, data/uniform_manager.hpp).
+//
+// * Groups are ordered by name; a group's index is the alphabetical rank of
+//   its name (data/model.cpp:26-31), so "b" (boundary) = 0, "f" (fluid) = 1.
+// * Varying fields hold one value per item in HBM, one array per field:
+//     real       -> float[count]
+//     real[3]    -> float4[count]      (12-byte items padded to 16 bytes so a
+//                                       gather is one aligned 16-byte load)
+//     real[3][3] -> float[9][capacity] (planar, plane k = column-major index)
+//     other      -> items back to back in the reference item layout
+//   Upload and download convert from / to the reference's host layout (N
+//   components contiguous per item, matrices column-major).
+// * Uniform and global fields live in one device arena so kernels read them
+//   from device memory: launches need no host round trip and can be captured
+//   in CUDA graphs.
+#pragma once
+
+#include "common.cuh"
+
+#include <map>
+#include <memory>
+#include <set>
+#include <string>
+#include <vector>
+
+namespace prtcl_gpu {
+
+enum class CType : int { F32 = 0, I32 = 1 };
+
+struct FieldType {
+  CType ctype = CType::F32;
+  int rank = 0;
+  int ext[2] = {1, 1};
+  size_t comps() const { return size_t(rank >= 1 ? ext[0] : 1) * size_t(rank >= 2 ? ext[1] : 1); }
+  size_t elem_bytes() const { return 4; }
+  size_t host_item_bytes() const { return comps() * elem_bytes(); }
+  bool operator==(FieldType const &o) const {
+    return ctype == o.ctype && rank == o.rank && (rank < 1 || ext[0] == o.ext[0]) && (rank < 2 || ext[1] == o.ext[1]);
+  }
+  bool operator!=(FieldType const &o) const { return !(*this == o); }
+  bool is_real() const { return ctype == CType::F32; }
+  bool is_vec3() const { return ctype == CType::F32 && rank == 1 && ext[0] == 3; }
+  bool is_mat3() const { return ctype == CType::F32 && rank == 2 && ext[0] == 3 && ext[1] == 3; }
+  std::string str() const;
+};
+
+FieldType parse_field_type(char const *ctype, int rank, int const *extents);
+
+struct VaryingField {
+  FieldType type;
+  void *d = nullptr;   // device storage
+  size_t cap = 0;      // items allocated
+  uint64_t version = 0; // bumped whenever the values may have changed
+  size_t device_item_bytes() const; // bytes per item of the device array (non-planar)
+};
+
+struct SmallField {
+  FieldType type;
+  size_t offset = 0; // byte offset in the model's arena
+};
+
+class Model;
+
+class Group {
+public:
+  Group(Model *m, std::string n, std::string t) : model_(m), name(std::move(n)), type(std::move(t)) {}
+  Model *model_;
+  std::string name, type;
+  std::set<std::string> tags;
+  size_t count = 0;
+  int index = 0;
+  std::map<std::string, VaryingField> varying;
+  std::map<std::string, SmallField> uniform;
+
+  bool has_tag(std::string const &t) const { return tags.count(t) > 0; }
+  VaryingField &add_varying(std::string const &name, FieldType const &t);
+  VaryingField *find_varying(std::string const &name);
+  VaryingField &get_varying(std::string const &name, FieldType const &t);
+  SmallField &add_uniform(std::string const &name, FieldType const &t);
+  void resize(size_t n, cudaStream_t s);
+  // gather every varying field: new[i] = old[perm[i]] (device perm, uint32)
+  void permute(uint32_t const *perm_d, cudaStream_t s);
+};
+
+class Model {
+public:
+  Model();
+  ~Model();
+  Model(Model const &) = delete;
+  Model &operator=(Model const &) = delete;
+
+  Group &add_group(std::string const &name, std::string const &type);
+  Group *find_group(std::string const &name);
+  Group &group(std::string const &name);
+  std::vector<Group *> groups_by_index();
+  size_t group_count() const { return groups_.size(); }
+
+  SmallField &add_global(std::string const &name, FieldType const &t);
+  SmallField *find_global(std::string const &name);
+
+  // arena access
+  SmallField &alloc_small(SmallField &f, FieldType const &t);
+  void *small_ptr(SmallField const &f) const { return arena_d_ + f.offset; }
+  void small_set(SmallField const &f, void const *host, cudaStream_t s);
+  void small_get(SmallField const &f, void *host, cudaStream_t s);
+
+  cudaStream_t stream() const { return stream_; }
+  cudaStream_t pick(void *s) const { return s ? static_cast<cudaStream_t>(s) : stream_; }
+
+  // bumped when groups or fields are added or a group is resized; schemes
+  // loaded before such a change must be loaded again (like `model.dirty`
+  // in the reference's scripts)
+  uint64_t layout_version = 1;
+  // device scratch shared by the procedures of this model (reductions)
+  double *red_d = nullptr;       // 3 x 4096 block partial sums
+  unsigned *red_count_d = nullptr; // last-block tickets
+  double *scalars_d = nullptr;   // 64 FP64 solver scalars
+  int *status_d = nullptr;       // 16 status words (error flags, iteration counts)
+
+private:
+  std::map<std::string, std::unique_ptr<Group>> groups_;
+  std::map<std::string, SmallField> global_;
+  char *arena_d_ = nullptr;
+  size_t arena_cap_ = 0, arena_used_ = 0;
+  cudaStream_t stream_ = nullptr;
+  void reindex();
+};
+
+// field kernels (model.cu)
+void upload_varying(VaryingField &f, size_t count, void const *host, size_t n_items, cudaStream_t s, bool sync);
+void download_varying(VaryingField const &f, size_t count, void *host, size_t n_items, cudaStream_t s);
+
+} // namespace prtcl_gpu

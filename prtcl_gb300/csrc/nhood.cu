@@ -1,0 +1,802 @@
+// Device uniform-grid neighbourhood (see nhood.hpp for the algorithm).
+#include "nhood.hpp"
+
+#include <algorithm>
+#include <cstring>
+
+namespace prtcl_gpu {
+
+namespace {
+
+constexpr uint32_t kFull = 0xffffffffu;
+
+// the 13 half-stencil offsets (util/grouped_uniform_grid.hpp:52-68)
+__constant__ int c_offsets[13][3] = {{1, 0, 0},  {0, 1, 0},   {0, 0, 1},  {1, 1, 0},  {1, 0, 1},
+                                     {0, 1, 1},  {1, 1, 1},   {0, -1, 1}, {1, 0, -1}, {1, 1, -1},
+                                     {1, -1, -1}, {1, -1, 0}, {1, -1, 1}};
+
+// ---------------------------------------------------------------------------
+// key helpers
+// ---------------------------------------------------------------------------
+
+__host__ __device__ __forceinline__ uint32_t unsign(int32_t i) { return uint32_t(i) + 0x7FFFFFFFu; }
+
+// gather the bits of u selected by mask into the low bits (software PEXT)
+__host__ __device__ __forceinline__ uint32_t pext32(uint32_t u, uint32_t mask) {
+  uint32_t r = 0;
+  int k = 0;
+  while (mask) {
+    uint32_t low = mask & (~mask + 1u);
+    if (u & low) r |= (1u << k);
+    ++k;
+    mask &= mask - 1u;
+  }
+  return r;
+}
+
+// spread the low 21 bits of x to every third bit of a 64-bit word
+__host__ __device__ __forceinline__ uint64_t spread3(uint32_t x) {
+  uint64_t v = x & 0x1fffffu;
+  v = (v | v << 32) & 0x1f00000000ffffULL;
+  v = (v | v << 16) & 0x1f0000ff0000ffULL;
+  v = (v | v << 8) & 0x100f00f00f00f00fULL;
+  v = (v | v << 4) & 0x10c30c30c30c30c3ULL;
+  v = (v | v << 2) & 0x1249249249249249ULL;
+  return v;
+}
+
+__host__ __device__ __forceinline__ uint64_t make_key(uint32_t u0, uint32_t u1, uint32_t u2, uint32_t keep) {
+  return (spread3(pext32(u0, keep)) << 2) | (spread3(pext32(u1, keep)) << 1) | spread3(pext32(u2, keep));
+}
+
+// is u consistent with the deleted bit positions (could a cell have it?)
+__host__ __device__ __forceinline__ bool key_valid(uint32_t u, KeyInfo const &k) {
+  uint32_t b = u >> 31;
+  uint32_t t = u ^ (b ? 0xFFFFFFFFu : 0u);
+  if (t & k.rel_eq) return false;
+  if (~t & k.rel_ne) return false;
+  if (!(k.keep & 0x80000000u) && ((u & 0x80000000u) != k.b31_const)) return false;
+  return true;
+}
+
+__device__ __forceinline__ int3 x_to_gi(float4 x, double radius) {
+  return make_int3(int32_t(floor(double(x.x) / radius)), int32_t(floor(double(x.y) / radius)),
+                   int32_t(floor(double(x.z) / radius)));
+}
+
+__device__ __forceinline__ int find_cell(GridView const &gv, int3 gi) {
+  uint32_t u0 = unsign(gi.x), u1 = unsign(gi.y), u2 = unsign(gi.z);
+  if (!key_valid(u0, gv.key) || !key_valid(u1, gv.key) || !key_valid(u2, gv.key)) return -1;
+  uint64_t key = make_key(u0, u1, u2, gv.key.keep);
+  int lo = 0, hi = *gv.ncells;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (gv.cell_key[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  return (lo < *gv.ncells && gv.cell_key[lo] == key) ? lo : -1;
+}
+
+// ---------------------------------------------------------------------------
+// scans
+// ---------------------------------------------------------------------------
+
+template <int NT>
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *sh, uint32_t &total) {
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(kFull, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sh[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    uint32_t z = lane < NT / 32 ? sh[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(kFull, z, o);
+      if (lane >= o) z += y;
+    }
+    if (lane < NT / 32) sh[lane] = z;
+  }
+  __syncthreads();
+  uint32_t pre = (w ? sh[w - 1] : 0u) + x - v;
+  total = sh[NT / 32 - 1];
+  __syncthreads();
+  return pre;
+}
+
+// in-place exclusive scan of a short array by one block of 1024 threads
+__global__ void k_scan_single(uint32_t *data, size_t len) {
+  __shared__ uint32_t sh[32];
+  size_t chunk = (len + 1023) / 1024;
+  size_t b = threadIdx.x * chunk, e = min(b + chunk, len);
+  uint32_t s = 0;
+  for (size_t i = b; i < e; ++i) s += data[i];
+  uint32_t total;
+  uint32_t pre = block_excl_scan<1024>(s, sh, total);
+  for (size_t i = b; i < e; ++i) {
+    uint32_t v = data[i];
+    data[i] = pre;
+    pre += v;
+  }
+}
+
+constexpr int kScanNT = 1024, kScanIPT = 4, kScanTile = kScanNT * kScanIPT;
+
+__global__ void k_scan_reduce(uint32_t const *in, size_t n, uint32_t *sums) {
+  __shared__ uint32_t sh[32];
+  size_t base = size_t(blockIdx.x) * kScanTile + size_t(threadIdx.x) * kScanIPT;
+  uint32_t s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanIPT; ++k)
+    if (base + k < n) s += in[base + k];
+  uint32_t total;
+  block_excl_scan<kScanNT>(s, sh, total);
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+__global__ void k_scan_apply(uint32_t const *in, size_t n, uint32_t const *sums, uint32_t *out) {
+  __shared__ uint32_t sh[32];
+  size_t base = size_t(blockIdx.x) * kScanTile + size_t(threadIdx.x) * kScanIPT;
+  uint32_t v[kScanIPT], s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanIPT; ++k) {
+    v[k] = (base + k < n) ? in[base + k] : 0u;
+    s += v[k];
+  }
+  uint32_t total;
+  uint32_t pre = block_excl_scan<kScanNT>(s, sh, total) + sums[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < kScanIPT; ++k) {
+    if (base + k < n) out[base + k] = pre;
+    pre += v[k];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// stable LSD radix sort of (uint64 key, uint32 value), 8-bit digits
+// ---------------------------------------------------------------------------
+
+constexpr int kRsNT = 256, kRsWarps = kRsNT / 32, kRsWarpItems = 512, kRsTile = kRsWarps * kRsWarpItems;
+
+__global__ void k_rs_hist(uint64_t const *__restrict__ keys, size_t n, int shift, uint32_t *hist, uint32_t tiles) {
+  __shared__ uint32_t h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  size_t base = size_t(blockIdx.x) * kRsTile;
+  for (int k = 0; k < kRsTile / kRsNT; ++k) {
+    size_t i = base + size_t(k) * kRsNT + threadIdx.x;
+    if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  hist[size_t(threadIdx.x) * tiles + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void k_rs_scatter(uint64_t const *__restrict__ kin, uint32_t const *__restrict__ vin,
+                             uint64_t *__restrict__ kout, uint32_t *__restrict__ vout, size_t n, int shift,
+                             uint32_t const *__restrict__ offs, uint32_t tiles) {
+  __shared__ uint32_t cnt[kRsWarps][256];
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int d = threadIdx.x; d < kRsWarps * 256; d += kRsNT) cnt[d / 256][d % 256] = 0;
+  __syncthreads();
+  size_t base = size_t(blockIdx.x) * kRsTile + size_t(w) * kRsWarpItems;
+  for (int step = 0; step < kRsWarpItems / 32; ++step) {
+    size_t i = base + size_t(step) * 32 + lane;
+    uint32_t d = i < n ? uint32_t((kin[i] >> shift) & 255u) : 256u;
+    uint32_t peers = __match_any_sync(kFull, d);
+    if (d != 256u && lane == __ffs(peers) - 1) cnt[w][d] += __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+  {
+    int d = threadIdx.x;
+    uint32_t run = offs[size_t(d) * tiles + blockIdx.x];
+    for (int ww = 0; ww < kRsWarps; ++ww) {
+      uint32_t c = cnt[ww][d];
+      cnt[ww][d] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+  uint32_t lt = (1u << lane) - 1u;
+  for (int step = 0; step < kRsWarpItems / 32; ++step) {
+    size_t i = base + size_t(step) * 32 + lane;
+    uint64_t key = 0;
+    uint32_t val = 0, d = 256u;
+    if (i < n) {
+      key = kin[i];
+      val = vin[i];
+      d = uint32_t((key >> shift) & 255u);
+    }
+    uint32_t peers = __match_any_sync(kFull, d);
+    uint32_t pos = (d != 256u) ? cnt[w][d] : 0u;
+    __syncwarp();
+    if (d != 256u) {
+      uint32_t dst = pos + __popc(peers & lt);
+      kout[dst] = key;
+      vout[dst] = val;
+      if (lane == __ffs(peers) - 1) cnt[w][d] = pos + __popc(peers);
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// grid build kernels
+// ---------------------------------------------------------------------------
+
+struct PosTable {
+  float4 const *pos[kMaxGroups];
+};
+
+__device__ __forceinline__ int group_of(uint32_t const *goff, int G, uint32_t n) {
+  int g = 0;
+  while (g + 1 < G && n >= goff[g + 1]) ++g;
+  return g;
+}
+
+// pass 1: per item in group-major order, the biased grid indices and the
+// handle; OR-reductions of the bit statistics that select the key bits
+__global__ void k_cells_u(PosTable pt, GridView gv, int G, size_t N, uint32_t *ukeys, uint32_t *vals, uint32_t *stats) {
+  size_t n = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  uint32_t ne = 0, eq = 0, a1 = 0, a0 = 0;
+  if (n < N) {
+    int g = group_of(gv.goff, G, uint32_t(n));
+    uint32_t i = uint32_t(n) - gv.goff[g];
+    int3 gi = x_to_gi(pt.pos[g][i], gv.radius);
+    uint32_t u[3] = {unsign(gi.x), unsign(gi.y), unsign(gi.z)};
+    for (int a = 0; a < 3; ++a) {
+      uint32_t t = u[a] ^ ((u[a] >> 31) ? 0xFFFFFFFFu : 0u);
+      ne |= t;
+      eq |= ~t;
+      a1 |= u[a] & 0x80000000u;
+      a0 |= ~u[a] & 0x80000000u;
+    }
+    reinterpret_cast<uint4 *>(ukeys)[n] = make_uint4(u[0], u[1], u[2], 0u);
+    vals[n] = (uint32_t(g) << 28) | i;
+  }
+  ne = __reduce_or_sync(kFull, ne);
+  eq = __reduce_or_sync(kFull, eq);
+  a1 = __reduce_or_sync(kFull, a1);
+  a0 = __reduce_or_sync(kFull, a0);
+  if ((threadIdx.x & 31) == 0) {
+    if (ne) atomicOr(&stats[0], ne);
+    if (eq) atomicOr(&stats[1], eq);
+    if (a1) atomicOr(&stats[2], a1);
+    if (a0) atomicOr(&stats[3], a0);
+  }
+}
+
+__global__ void k_cells_key(uint32_t const *ukeys, size_t N, uint32_t keep, uint64_t *keys) {
+  size_t n = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (n < N) {
+    uint4 u = reinterpret_cast<uint4 const *>(ukeys)[n];
+    keys[n] = make_key(u.x, u.y, u.z, keep);
+  }
+}
+
+__global__ void k_cell_flags(uint64_t const *keys, size_t N, uint32_t *flags) {
+  size_t s = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (s < N) flags[s] = (s == 0 || keys[s] != keys[s - 1]) ? 1u : 0u;
+}
+
+// excl = exclusive scan of flags: cell(s) = excl[s] + flag[s] - 1
+__global__ void k_cells_fill(PosTable pt, GridView gv, uint64_t const *keys, uint32_t const *vals, uint32_t const *flags,
+                             uint32_t const *excl, size_t N, int32_t *s2c, int32_t *r2s, int32_t *cell_start,
+                             uint64_t *cell_key, int4 *cell_gi, int *ncells) {
+  size_t s = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (s >= N) return;
+  uint32_t f = flags[s];
+  int32_t c = int32_t(excl[s] + f) - 1;
+  s2c[s] = c;
+  uint32_t h = vals[s];
+  uint32_t g = h >> 28, i = h & 0x0FFFFFFFu;
+  r2s[gv.goff[g] + i] = int32_t(s);
+  if (f) {
+    cell_start[c] = int32_t(s);
+    cell_key[c] = keys[s];
+    int3 gi = x_to_gi(pt.pos[g][i], gv.radius);
+    cell_gi[c] = make_int4(gi.x, gi.y, gi.z, 0);
+  }
+  if (s == N - 1) {
+    cell_start[c + 1] = int32_t(N);
+    *ncells = c + 1;
+  }
+}
+
+__global__ void k_cells_adj(GridView gv, int4 const *cell_gi, size_t N, int32_t *adj) {
+  size_t c = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (c >= N || int(c) >= *gv.ncells) return;
+  int4 g = cell_gi[c];
+  for (int k = 0; k < 13; ++k) {
+    int3 p = make_int3(g.x + c_offsets[k][0], g.y + c_offsets[k][1], g.z + c_offsets[k][2]);
+    int3 m = make_int3(g.x - c_offsets[k][0], g.y - c_offsets[k][1], g.z - c_offsets[k][2]);
+    adj[c * 26 + k] = find_cell(gv, p);
+    adj[c * 26 + 25 - k] = find_cell(gv, m);
+  }
+}
+
+__global__ void k_xsorted(PosTable pt, uint32_t const *vals, size_t N, float4 *xs) {
+  size_t s = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (s < N) {
+    uint32_t h = vals[s];
+    float4 x = pt.pos[h >> 28][h & 0x0FFFFFFFu];
+    x.w = __uint_as_float(h);
+    xs[s] = x;
+  }
+}
+
+struct ListOut {
+  uint32_t *idx[kMaxGroups];
+  uint32_t cap[kMaxGroups];
+  uint32_t *cnt; // [G][n]
+  uint32_t *maxcnt; // [kMaxGroups]
+  uint32_t n;
+  int G;
+};
+
+__device__ __forceinline__ void visit_cell(GridView const &gv, float4 const *__restrict__ xs, int cell, f3 xi,
+                                           uint32_t i, ListOut const &lo, uint32_t *c) {
+  if (cell < 0) return;
+  int s0 = gv.cell_start[cell], s1 = gv.cell_start[cell + 1];
+  for (int s = s0; s < s1; ++s) {
+    float4 xj = xs[s];
+    float d2 = nsq3(sub3(xi, mk3(xj)));
+    if (double(d2) < gv.r2) {
+      uint32_t h = __float_as_uint(xj.w);
+      uint32_t g = h >> 28, j = h & 0x0FFFFFFFu;
+      uint32_t k = c[g]++;
+      if (k < lo.cap[g]) lo.idx[g][size_t(k) * lo.n + i] = j;
+    }
+  }
+}
+
+// neighbour lists of one query group (grid query of util/grouped_uniform_grid.hpp:407-531)
+__global__ void k_build_lists(GridView gv, float4 const *__restrict__ xs, float4 const *__restrict__ qpos, int q,
+                              ListOut lo) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= lo.n) return;
+  uint32_t c[kMaxGroups];
+#pragma unroll
+  for (int g = 0; g < kMaxGroups; ++g) c[g] = 0;
+  float4 x4 = qpos[i];
+  f3 xi = mk3(x4);
+  int cell = -1;
+  bool fallback = false;
+  int3 gi;
+  if (gv.in_grid[q]) {
+    cell = gv.s2c[gv.r2s[gv.goff[q] + i]];
+  } else {
+    gi = x_to_gi(x4, gv.radius);
+    cell = find_cell(gv, gi);
+    fallback = cell < 0;
+  }
+  if (!fallback) {
+    visit_cell(gv, xs, cell, xi, i, lo, c);
+    for (int k = 0; k < 26; ++k) visit_cell(gv, xs, gv.cell_adj[size_t(cell) * 26 + k], xi, i, lo, c);
+  } else {
+    for (int k = 0; k < 13; ++k) {
+      int3 p = make_int3(gi.x + c_offsets[k][0], gi.y + c_offsets[k][1], gi.z + c_offsets[k][2]);
+      visit_cell(gv, xs, find_cell(gv, p), xi, i, lo, c);
+      int3 m = make_int3(gi.x - c_offsets[k][0], gi.y - c_offsets[k][1], gi.z - c_offsets[k][2]);
+      visit_cell(gv, xs, find_cell(gv, m), xi, i, lo, c);
+    }
+  }
+  for (int g = 0; g < lo.G; ++g) {
+    lo.cnt[size_t(g) * lo.n + i] = c[g];
+    if (c[g] > lo.cap[g]) atomicMax(&lo.maxcnt[g], c[g]);
+  }
+}
+
+__global__ void k_group_flags(uint32_t const *vals, size_t N, uint32_t g, uint32_t *flags) {
+  size_t s = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (s < N) flags[s] = ((vals[s] >> 28) == g) ? 1u : 0u;
+}
+
+__global__ void k_group_perm(uint32_t const *vals, uint32_t const *flags, uint32_t const *excl, size_t N, uint32_t *perm) {
+  size_t s = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (s < N && flags[s]) perm[excl[s]] = vals[s] & 0x0FFFFFFFu;
+}
+
+} // namespace
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+static void exclusive_scan(uint32_t const *in, uint32_t *out, size_t n, uint32_t *&sums, size_t &sums_cap,
+                           cudaStream_t s) {
+  if (n == 0) return;
+  size_t nb = (n + kScanTile - 1) / kScanTile;
+  if (nb > sums_cap) {
+    if (sums) PG_CUDA(cudaFree(sums));
+    sums_cap = std::max<size_t>(nb, 1024);
+    PG_CUDA(cudaMalloc(&sums, sums_cap * sizeof(uint32_t)));
+  }
+  k_scan_reduce<<<unsigned(nb), kScanNT, 0, s>>>(in, n, sums);
+  k_scan_single<<<1, 1024, 0, s>>>(sums, nb);
+  k_scan_apply<<<unsigned(nb), kScanNT, 0, s>>>(in, n, sums, out);
+  PG_LAUNCH_CHECK();
+}
+
+Nhood::Nhood() {
+  PG_CUDA(cudaMalloc(&stats_d_, 16 * sizeof(uint32_t)));
+  PG_CUDA(cudaMalloc(&ncells_d_, sizeof(int)));
+  PG_CUDA(cudaMemset(ncells_d_, 0, sizeof(int)));
+  PG_CUDA(cudaMallocHost(&stats_h_, 16 * sizeof(uint32_t)));
+}
+
+static void free_all(std::initializer_list<void *> ps) {
+  for (void *p : ps)
+    if (p) cudaFree(p);
+}
+
+Nhood::~Nhood() {
+  for (auto &kv : lists_) free_lists(kv.second);
+  free_all({keys_a_, keys_b_, vals_a_, vals_b_, ukeys_, flags_, scan_, r2s_, s2c_, cell_start_, cell_adj_, cell_key_,
+            cell_gi_, xsorted_, hist_, block_sums_, stats_d_, ncells_d_});
+  cudaFreeHost(stats_h_);
+}
+
+void Nhood::free_lists(Lists &L) {
+  for (int g = 0; g < kMaxGroups; ++g)
+    if (L.idx[g]) {
+      cudaFree(L.idx[g]);
+      L.idx[g] = nullptr;
+    }
+  if (L.cnt) cudaFree(L.cnt);
+  L.cnt = nullptr;
+}
+
+// Neighborhood::Load (util/neighborhood.cpp:67-98): remember each group's
+// position field (real[3]) and whether it can be a neighbour
+void Nhood::load(Model &m) {
+  auto gs = m.groups_by_index();
+  std::vector<GG> ng(gs.size(), GG{});
+  int three = 3;
+  FieldType v3 = parse_field_type("f32", 1, &three);
+  for (size_t g = 0; g < gs.size(); ++g) {
+    ng[g].g = gs[g];
+    VaryingField *p = gs[g]->find_varying("position");
+    ng[g].pos = (p && p->type == v3) ? p : nullptr;
+    ng[g].can_be_neighbor = !gs[g]->has_tag("cannot_be_neighbor");
+  }
+  // keep the grid of the last Update when the groups and their bindings are
+  // unchanged (re-loading schemes and the neighbourhood is routine in the
+  // reference's scripts); otherwise it must be updated before use
+  bool same = (&m == model_) && ng.size() == gg_.size();
+  for (size_t g = 0; same && g < ng.size(); ++g)
+    same = ng[g].g == gg_[g].g && ng[g].pos == gg_[g].pos && ng[g].can_be_neighbor == gg_[g].can_be_neighbor;
+  model_ = &m;
+  gg_ = ng;
+  if (!same) {
+    has_grid_ = false;
+    for (auto &kv : lists_) free_lists(kv.second);
+    lists_.clear();
+  }
+}
+
+void Nhood::ensure_grid_capacity(size_t n) {
+  if (n <= cap_) return;
+  size_t c = std::max(n + n / 8, size_t(1024));
+  free_all({keys_a_, keys_b_, vals_a_, vals_b_, ukeys_, flags_, scan_, r2s_, s2c_, cell_start_, cell_adj_, cell_key_,
+            cell_gi_, xsorted_});
+  PG_CUDA(cudaMalloc(&keys_a_, c * 8));
+  PG_CUDA(cudaMalloc(&keys_b_, c * 8));
+  PG_CUDA(cudaMalloc(&vals_a_, c * 4));
+  PG_CUDA(cudaMalloc(&vals_b_, c * 4));
+  PG_CUDA(cudaMalloc(&ukeys_, c * 16));
+  PG_CUDA(cudaMalloc(&flags_, c * 4));
+  PG_CUDA(cudaMalloc(&scan_, c * 4));
+  PG_CUDA(cudaMalloc(&r2s_, c * 4));
+  PG_CUDA(cudaMalloc(&s2c_, c * 4));
+  PG_CUDA(cudaMalloc(&cell_start_, (c + 1) * 4));
+  PG_CUDA(cudaMalloc(&cell_adj_, c * 26 * 4));
+  PG_CUDA(cudaMalloc(&cell_key_, c * 8));
+  PG_CUDA(cudaMalloc(&cell_gi_, c * 16));
+  PG_CUDA(cudaMalloc(&xsorted_, c * 16));
+  cap_ = c;
+}
+
+GridView Nhood::view() const {
+  GridView v{};
+  v.sorted = sorted_vals_;
+  v.r2s = r2s_;
+  v.s2c = s2c_;
+  v.cell_start = cell_start_;
+  v.cell_key = cell_key_;
+  v.cell_adj = cell_adj_;
+  v.ncells = ncells_d_;
+  for (int g = 0; g <= kMaxGroups; ++g) v.goff[g] = goff_[g];
+  for (int g = 0; g < kMaxGroups; ++g) v.in_grid[g] = in_grid_[g];
+  v.key = key_;
+  v.radius = radius_;
+  v.r2 = radius_ * radius_;
+  return v;
+}
+
+// grouped_uniform_grid::update (util/grouped_uniform_grid.hpp:126-337)
+void Nhood::update(cudaStream_t s) {
+  if (!model_) throw Error("Neighborhood::Update before Load");
+  int G = int(gg_.size());
+  PosTable pt{};
+  size_t N = 0;
+  for (int g = 0; g < kMaxGroups; ++g) in_grid_[g] = 0;
+  for (int g = 0; g < G; ++g) {
+    goff_[g] = uint32_t(N);
+    bool in = gg_[g].pos && gg_[g].can_be_neighbor;
+    in_grid_[g] = in ? 1 : 0;
+    if (gg_[g].pos) pt.pos[g] = static_cast<float4 const *>(gg_[g].pos->d);
+    if (in) {
+      if (gg_[g].g->count >= (size_t(1) << 28)) throw Error("group too large for the grid (>= 2^28 items)");
+      N += gg_[g].g->count;
+    }
+  }
+  for (int g = G; g <= kMaxGroups; ++g) goff_[g] = uint32_t(N);
+  if (N >= (size_t(1) << 31)) throw Error("too many items for the grid");
+  N_ = N;
+  ensure_grid_capacity(N);
+  epoch_++;
+  has_grid_ = true;
+  if (N == 0) {
+    PG_CUDA(cudaMemsetAsync(ncells_d_, 0, sizeof(int), s));
+    sorted_keys_ = keys_a_;
+    sorted_vals_ = vals_a_;
+    return;
+  }
+  GridView gv = view();
+  // 1. grid indices, handles, bit statistics
+  PG_CUDA(cudaMemsetAsync(stats_d_, 0, 16 * sizeof(uint32_t), s));
+  unsigned nb = div_up(N, 256);
+  k_cells_u<<<nb, 256, 0, s>>>(pt, gv, G, N, ukeys_, vals_a_, stats_d_);
+  PG_LAUNCH_CHECK();
+  PG_CUDA(cudaMemcpyAsync(stats_h_, stats_d_, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  PG_CUDA(cudaStreamSynchronize(s));
+  uint32_t ne = stats_h_[0], eq = stats_h_[1], a1 = stats_h_[2], a0 = stats_h_[3];
+  KeyInfo k{};
+  k.keep = ne & eq & 0x7FFFFFFFu;
+  k.rel_eq = eq & ~ne & 0x7FFFFFFFu;
+  k.rel_ne = ne & ~eq & 0x7FFFFFFFu;
+  if (a1 && a0) k.keep |= 0x80000000u;
+  else k.b31_const = a1 ? 0x80000000u : 0u;
+  k.bits = __builtin_popcount(k.keep);
+  if (k.bits > 21)
+    throw Error("grid spans too many cells: " + std::to_string(k.bits) +
+                " informative bits per axis (at most 21 are supported)");
+  key_ = k;
+  gv.key = k;
+  // 2. compressed Z-order keys
+  k_cells_key<<<nb, 256, 0, s>>>(ukeys_, N, k.keep, keys_a_);
+  PG_LAUNCH_CHECK();
+  // 3. stable LSD radix sort over the informative bits
+  int total_bits = 3 * k.bits;
+  uint64_t *kin = keys_a_, *kout = keys_b_;
+  uint32_t *vin = vals_a_, *vout = vals_b_;
+  uint32_t tiles = uint32_t((N + kRsTile - 1) / kRsTile);
+  size_t hl = size_t(tiles) * 256;
+  if (hl > hist_cap_) {
+    if (hist_) PG_CUDA(cudaFree(hist_));
+    hist_cap_ = hl + hl / 4;
+    PG_CUDA(cudaMalloc(&hist_, hist_cap_ * 4));
+  }
+  for (int shift = 0; shift < total_bits; shift += 8) {
+    k_rs_hist<<<tiles, kRsNT, 0, s>>>(kin, N, shift, hist_, tiles);
+    k_scan_single<<<1, 1024, 0, s>>>(hist_, hl);
+    k_rs_scatter<<<tiles, kRsNT, 0, s>>>(kin, vin, kout, vout, N, shift, hist_, tiles);
+    PG_LAUNCH_CHECK();
+    std::swap(kin, kout);
+    std::swap(vin, vout);
+  }
+  sorted_keys_ = kin;
+  sorted_vals_ = vin;
+  gv = view();
+  // 4. cells
+  k_cell_flags<<<nb, 256, 0, s>>>(kin, N, flags_);
+  PG_LAUNCH_CHECK();
+  exclusive_scan(flags_, scan_, N, block_sums_, block_sums_cap_, s);
+  k_cells_fill<<<nb, 256, 0, s>>>(pt, gv, kin, vin, flags_, scan_, N, s2c_, r2s_, cell_start_, cell_key_, cell_gi_,
+                                  ncells_d_);
+  PG_LAUNCH_CHECK();
+  // 5. adjacency
+  k_cells_adj<<<nb, 256, 0, s>>>(gv, cell_gi_, N, cell_adj_);
+  PG_LAUNCH_CHECK();
+}
+
+std::vector<uint64_t> Nhood::pos_versions() const {
+  std::vector<uint64_t> v(gg_.size(), 0);
+  for (size_t g = 0; g < gg_.size(); ++g)
+    v[g] = gg_[g].pos ? (gg_[g].pos->version ^ (uint64_t(gg_[g].g->count) << 40)) : 0;
+  return v;
+}
+
+bool Nhood::lists_fresh(Lists const &L) const { return L.epoch == epoch_ && L.pos_versions == pos_versions(); }
+
+void Nhood::build_lists(int q, Lists &L, cudaStream_t s) {
+  int G = int(gg_.size());
+  size_t n = gg_[q].g->count;
+  // sorted positions with handles, from the current positions
+  PosTable pt{};
+  for (int g = 0; g < G; ++g)
+    if (gg_[g].pos) pt.pos[g] = static_cast<float4 const *>(gg_[g].pos->d);
+  if (N_ > 0) {
+    k_xsorted<<<div_up(N_, 256), 256, 0, s>>>(pt, sorted_vals_, N_, xsorted_);
+    PG_LAUNCH_CHECK();
+  }
+  for (int attempt = 0; attempt < 8; ++attempt) {
+    if (L.n != n || !L.cnt) {
+      free_lists(L);
+      L.n = n;
+      if (n > 0) PG_CUDA(cudaMalloc(&L.cnt, size_t(G) * n * 4));
+      for (int g = 0; g < G; ++g) L.cap[g] = 0;
+    }
+    for (int g = 0; g < G; ++g) {
+      uint32_t want = L.cap[g] ? L.cap[g] : 48u;
+      if (!L.idx[g] || want != L.cap[g]) {
+        if (L.idx[g]) PG_CUDA(cudaFree(L.idx[g]));
+        L.idx[g] = nullptr;
+        if (n > 0) PG_CUDA(cudaMalloc(&L.idx[g], size_t(want) * n * 4));
+        L.cap[g] = want;
+      }
+    }
+    if (n == 0) break;
+    ListOut lo{};
+    for (int g = 0; g < G; ++g) {
+      lo.idx[g] = L.idx[g];
+      lo.cap[g] = L.cap[g];
+    }
+    lo.cnt = L.cnt;
+    lo.maxcnt = stats_d_ + 8;
+    lo.n = uint32_t(n);
+    lo.G = G;
+    PG_CUDA(cudaMemsetAsync(stats_d_ + 8, 0, 8 * sizeof(uint32_t), s));
+    GridView gv = view();
+    float4 const *qpos = static_cast<float4 const *>(gg_[q].pos->d);
+    k_build_lists<<<div_up(n, 128), 128, 0, s>>>(gv, xsorted_, qpos, q, lo);
+    PG_LAUNCH_CHECK();
+    PG_CUDA(cudaMemcpyAsync(stats_h_ + 8, stats_d_ + 8, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    PG_CUDA(cudaStreamSynchronize(s));
+    bool grow = false;
+    for (int g = 0; g < std::min(G, 8); ++g)
+      if (stats_h_[8 + g] > L.cap[g]) {
+        uint32_t want = (stats_h_[8 + g] + 15u) / 16u * 16u + 16u;
+        if (L.idx[g]) PG_CUDA(cudaFree(L.idx[g]));
+        L.idx[g] = nullptr;
+        PG_CUDA(cudaMalloc(&L.idx[g], size_t(want) * n * 4));
+        L.cap[g] = want;
+        grow = true;
+      }
+    if (G > 8) throw Error("neighbour lists support at most 8 groups");
+    if (!grow) break;
+    list_rebuilds++;
+  }
+  L.epoch = epoch_;
+  L.pos_versions = pos_versions();
+  L.view = NbrView{};
+  for (int g = 0; g < G; ++g) {
+    L.view.idx[g] = L.idx[g];
+    L.view.cnt[g] = L.cnt ? L.cnt + size_t(g) * n : nullptr;
+    L.view.cap[g] = L.cap[g];
+  }
+  L.view.n = uint32_t(n);
+}
+
+NbrView const &Nhood::lists(int q, cudaStream_t s) {
+  if (!has_grid_) throw Error("Neighborhood has not been updated");
+  if (q < 0 || q >= int(gg_.size())) throw Error("invalid group index");
+  Lists &L = lists_[q];
+  if (!gg_[q].pos) {
+    // CopyNeighbors of a group without position returns nothing
+    if (L.n != gg_[q].g->count || !L.cnt) {
+      free_lists(L);
+      L.n = gg_[q].g->count;
+      if (L.n) {
+        PG_CUDA(cudaMalloc(&L.cnt, gg_.size() * L.n * 4));
+        PG_CUDA(cudaMemsetAsync(L.cnt, 0, gg_.size() * L.n * 4, s));
+      }
+      L.view = NbrView{};
+      for (size_t g = 0; g < gg_.size(); ++g) L.view.cnt[g] = L.cnt ? L.cnt + g * L.n : nullptr;
+      L.view.n = uint32_t(L.n);
+    }
+    return L.view;
+  }
+  if (!lists_fresh(L)) build_lists(q, L, s);
+  return L.view;
+}
+
+// Neighborhood::Permute (util/neighborhood.cpp:106-154): per group the raw
+// indices in sorted order, applied to every varying field, then Update
+void Nhood::permute(Model &m, cudaStream_t s) {
+  if (&m != model_) throw Error("Neighborhood::Permute with a model that was not loaded");
+  if (!has_grid_) update(s);
+  int G = int(gg_.size());
+  for (int g = 0; g < G; ++g) {
+    if (!in_grid_[g] || gg_[g].g->count == 0) continue;
+    size_t n = gg_[g].g->count;
+    k_group_flags<<<div_up(N_, 256), 256, 0, s>>>(sorted_vals_, N_, uint32_t(g), flags_);
+    PG_LAUNCH_CHECK();
+    exclusive_scan(flags_, scan_, N_, block_sums_, block_sums_cap_, s);
+    uint32_t *perm = nullptr;
+    PG_CUDA(cudaMallocAsync(&perm, n * 4, s));
+    k_group_perm<<<div_up(N_, 256), 256, 0, s>>>(sorted_vals_, flags_, scan_, N_, perm);
+    PG_LAUNCH_CHECK();
+    gg_[g].g->permute(perm, s);
+    PG_CUDA(cudaFreeAsync(perm, s));
+  }
+  update(s);
+}
+
+size_t Nhood::cell_count(cudaStream_t s) {
+  int c = 0;
+  PG_CUDA(cudaMemcpyAsync(&c, ncells_d_, sizeof(int), cudaMemcpyDeviceToHost, s));
+  PG_CUDA(cudaStreamSynchronize(s));
+  return size_t(c);
+}
+
+void Nhood::copy_grid(uint32_t *sorted, int32_t *cell_gi, int32_t *cell_range, int32_t *cell_adj, cudaStream_t s) {
+  size_t C = cell_count(s);
+  if (sorted && N_) PG_CUDA(cudaMemcpyAsync(sorted, sorted_vals_, N_ * 4, cudaMemcpyDeviceToHost, s));
+  std::vector<int4> gi(C);
+  std::vector<int32_t> start(C + 1);
+  if (C) {
+    PG_CUDA(cudaMemcpyAsync(gi.data(), cell_gi_, C * 16, cudaMemcpyDeviceToHost, s));
+    PG_CUDA(cudaMemcpyAsync(start.data(), cell_start_, (C + 1) * 4, cudaMemcpyDeviceToHost, s));
+    if (cell_adj) PG_CUDA(cudaMemcpyAsync(cell_adj, cell_adj_, C * 26 * 4, cudaMemcpyDeviceToHost, s));
+  }
+  PG_CUDA(cudaStreamSynchronize(s));
+  for (size_t c = 0; c < C; ++c) {
+    if (cell_gi) {
+      cell_gi[3 * c] = gi[c].x;
+      cell_gi[3 * c + 1] = gi[c].y;
+      cell_gi[3 * c + 2] = gi[c].z;
+    }
+    if (cell_range) {
+      cell_range[2 * c] = start[c];
+      cell_range[2 * c + 1] = start[c + 1];
+    }
+  }
+}
+
+size_t Nhood::copy_neighbors(int g, size_t i, int64_t *counts, int64_t *out, size_t cap, cudaStream_t s) {
+  NbrView const &v = lists(g, s);
+  int G = int(gg_.size());
+  if (i >= v.n) throw Error("CopyNeighbors: index out of range");
+  size_t k = 0;
+  for (int ng = 0; ng < G; ++ng) {
+    uint32_t c = 0;
+    PG_CUDA(cudaMemcpyAsync(&c, v.cnt[ng] + i, 4, cudaMemcpyDeviceToHost, s));
+    PG_CUDA(cudaStreamSynchronize(s));
+    counts[ng] = c;
+    for (uint32_t slot = 0; slot < c; ++slot) {
+      uint32_t j = 0;
+      PG_CUDA(cudaMemcpyAsync(&j, v.idx[ng] + size_t(slot) * v.n + i, 4, cudaMemcpyDeviceToHost, s));
+      PG_CUDA(cudaStreamSynchronize(s));
+      if (k < cap) out[k] = j;
+      ++k;
+    }
+  }
+  return k;
+}
+
+void Nhood::copy_lists(int q, int ng, int64_t *offsets, uint32_t *idx, size_t cap, cudaStream_t s) {
+  NbrView const &v = lists(q, s);
+  size_t n = v.n;
+  std::vector<uint32_t> cnt(n);
+  offsets[0] = 0;
+  if (n == 0) return;
+  PG_CUDA(cudaMemcpyAsync(cnt.data(), v.cnt[ng], n * 4, cudaMemcpyDeviceToHost, s));
+  std::vector<uint32_t> ell;
+  if (v.idx[ng]) {
+    ell.resize(size_t(v.cap[ng]) * n);
+    PG_CUDA(cudaMemcpyAsync(ell.data(), v.idx[ng], ell.size() * 4, cudaMemcpyDeviceToHost, s));
+  }
+  PG_CUDA(cudaStreamSynchronize(s));
+  for (size_t i = 0; i < n; ++i) offsets[i + 1] = offsets[i] + cnt[i];
+  if (size_t(offsets[n]) > cap) throw Error("copy_lists: capacity too small");
+  for (size_t i = 0; i < n; ++i)
+    for (uint32_t k = 0; k < cnt[i]; ++k) idx[offsets[i] + k] = ell[size_t(k) * n + i];
+}
+
+} // namespace prtcl_gpu

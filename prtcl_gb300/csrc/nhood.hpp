@@ -1,0 +1,159 @@
+// Device uniform-grid neighbourhood: the GB300 replacement for prtcl's
+// grouped_uniform_grid (util/grouped_uniform_grid.hpp) behind the
+// Neighborhood interface (util/neighborhood.hpp:23-42).
+//
+// Update():
+//   1. cell of every item of every neighbour-capable group:
+//      gi = (int32) floor((double) x / radius)            (:621-632)
+//   2. a 64-bit Z-order key per item.  The reference compares cells with an
+//      XOR-MSB test on u = (uint32) gi + INT32_MAX (util/morton_order.hpp:
+//      40-82); that order equals the order of the 96-bit interleave of
+//      (u0, u1, u2) with dimension 0 the most significant of each bit triple.
+//      Bit positions that carry no information for the current item set are
+//      deleted before interleaving: bits that are constant, and bits that
+//      are always equal (or always unequal) to bit 31 (with the INT32_MAX bias
+//      every cell near the origin has bits 30..k equal to NOT bit 31).
+//      Deleting such positions keeps both the monotonicity of each axis and
+//      the order of most-significant differing bits across axes, so the
+//      compressed key orders cells exactly like the reference.  At most 21
+//      informative bits per axis are supported (63-bit keys).
+//   3. a stable LSD radix sort of (key, handle) pairs, 8-bit digits, starting
+//      from group-major identity order: cells in the reference's Morton
+//      order; within a cell (group, raw index) order.  The reference's
+//      parallel sort is unstable, so its within-cell order is unspecified;
+//      cell membership and cell order are exact.
+//   4. cell boundaries, cell ids by prefix scan, cell ranges, cell keys and
+//      grid indices, and raw -> sorted.
+//   5. the 26-cell adjacency: slot k < 13 holds the cell at +offset[k],
+//      slot 25-k the cell at -offset[k] (:52-68, :312-337); found by binary
+//      search over the sorted cell keys.
+// Neighbour lists (built lazily per query group, reused by every procedure
+// until positions change or the grid is updated): for each query item the
+// own cell and adjacency slots 0..25 in order, each cell's items in sorted
+// order, kept when (double)(float)|x_i - x_j|^2 < r^2 (:407-422).  One ELL
+// array per neighbour group (idx[slot * n + i]) so that a procedure walks
+// its fluid and boundary neighbours without branching on the group.
+#pragma once
+
+#include "model.hpp"
+
+#include <map>
+#include <vector>
+
+namespace prtcl_gpu {
+
+// device view of a neighbour list set of one query group
+struct NbrView {
+  uint32_t const *idx[kMaxGroups]; // ELL per neighbour group: idx[g][slot * n + i]
+  uint32_t const *cnt[kMaxGroups]; // per neighbour group: count of item i
+  uint32_t cap[kMaxGroups];
+  uint32_t n; // query items
+};
+
+struct KeyInfo {
+  uint32_t keep = 0;   // informative bit positions of u
+  uint32_t rel_eq = 0; // deleted low positions always equal to bit 31
+  uint32_t rel_ne = 0; // deleted low positions always unequal to bit 31
+  uint32_t b31_const = 0; // value of bit 31 if deleted (0 or 0x80000000)
+  int bits = 0;        // informative bits per axis
+};
+
+struct GridView {
+  uint32_t const *sorted;   // sorted -> handle (group << 28 | index)
+  int32_t const *r2s;       // raw -> sorted, at goff[group] + index
+  int32_t const *s2c;       // sorted -> cell
+  int32_t const *cell_start; // cell -> first sorted (C + 1 entries)
+  uint64_t const *cell_key; // cell -> compressed key
+  int32_t const *cell_adj;  // cell -> 26 adjacent cells (-1 none)
+  int const *ncells;        // number of cells (device)
+  uint32_t goff[kMaxGroups + 1];
+  int in_grid[kMaxGroups];
+  KeyInfo key;
+  double radius, r2;
+};
+
+class Nhood {
+public:
+  Nhood();
+  ~Nhood();
+  Nhood(Nhood const &) = delete;
+  Nhood &operator=(Nhood const &) = delete;
+
+  void set_radius(double r) { radius_ = r; }
+  double radius() const { return radius_; }
+  void load(Model &m);
+  void update(cudaStream_t s);
+  void permute(Model &m, cudaStream_t s);
+  bool loaded() const { return model_ != nullptr; }
+  Model *model() const { return model_; }
+
+  // neighbour lists of query group q (rebuilt when stale)
+  NbrView const &lists(int q, cudaStream_t s);
+
+  // introspection (tests): sizes and host copies of the grid
+  size_t sorted_count() const { return N_; }
+  size_t cell_count(cudaStream_t s);
+  void copy_grid(uint32_t *sorted, int32_t *cell_gi, int32_t *cell_range, int32_t *cell_adj, cudaStream_t s);
+  // neighbours of one item, per group, like Neighborhood::CopyNeighbors
+  size_t copy_neighbors(int g, size_t i, int64_t *counts, int64_t *out, size_t cap, cudaStream_t s);
+  // CSR copy of the lists of query group q to neighbour group ng
+  void copy_lists(int q, int ng, int64_t *offsets, uint32_t *idx, size_t cap, cudaStream_t s);
+
+  GridView view() const;
+  uint64_t epoch() const { return epoch_; }
+  // informative-bit overflow and other errors raise; lists growth is handled
+  int list_rebuilds = 0;
+
+private:
+  struct GG {
+    Group *g = nullptr;
+    VaryingField *pos = nullptr;
+    bool can_be_neighbor = false;
+  };
+  struct Lists {
+    size_t n = 0;
+    uint32_t cap[kMaxGroups] = {};
+    uint32_t *idx[kMaxGroups] = {};
+    uint32_t *cnt = nullptr; // [G][n]
+    uint64_t epoch = 0;
+    std::vector<uint64_t> pos_versions;
+    NbrView view{};
+  };
+  void ensure_grid_capacity(size_t n);
+  void build_lists(int q, Lists &L, cudaStream_t s);
+  bool lists_fresh(Lists const &L) const;
+  std::vector<uint64_t> pos_versions() const;
+  void free_lists(Lists &L);
+
+  double radius_ = 1.0;
+  Model *model_ = nullptr;
+  std::vector<GG> gg_;
+  size_t N_ = 0, cap_ = 0;
+  uint32_t goff_[kMaxGroups + 1] = {};
+  int in_grid_[kMaxGroups] = {};
+  KeyInfo key_{};
+  uint64_t epoch_ = 0;
+  bool has_grid_ = false;
+
+  // device arrays (capacity cap_)
+  uint64_t *keys_a_ = nullptr, *keys_b_ = nullptr;
+  uint32_t *vals_a_ = nullptr, *vals_b_ = nullptr;
+  uint32_t *ukeys_ = nullptr; // 4 words per item (u0, u1, u2, pad)
+  uint32_t *flags_ = nullptr, *scan_ = nullptr;
+  int32_t *r2s_ = nullptr, *s2c_ = nullptr, *cell_start_ = nullptr, *cell_adj_ = nullptr;
+  uint64_t *cell_key_ = nullptr;
+  int4 *cell_gi_ = nullptr;
+  float4 *xsorted_ = nullptr;
+  uint32_t *hist_ = nullptr;
+  size_t hist_cap_ = 0;
+  uint32_t *block_sums_ = nullptr;
+  size_t block_sums_cap_ = 0;
+  uint32_t *stats_d_ = nullptr; // bit statistics / counters (16 words)
+  int *ncells_d_ = nullptr;
+  uint32_t *stats_h_ = nullptr; // pinned
+  uint64_t const *sorted_keys_ = nullptr;
+  uint32_t const *sorted_vals_ = nullptr;
+  std::map<int, Lists> lists_;
+};
+
+} // namespace prtcl_gpu

@@ -1,0 +1,1291 @@
+// Device implementations of the generated prtcl procedures on the hot path.
+//
+// Every procedure is one thread per particle: the thread walks its fluid
+// neighbour list(s) and then its boundary neighbour list(s) sequentially, in
+// the grid's traversal order, accumulating in FP32 in exactly the operation
+// order of the generated C++ (the file:line cited at each kernel).  With FMA
+// contraction off this reproduces the reference arithmetic per particle.
+// Reductions that decide convergence (IISPH density error, PCG dot products)
+// are FP64 with a fixed, batch-independent order: per-block tree sums, then
+// the last block of the launch sums the block partials.
+#include "schemes.hpp"
+
+#include <algorithm>
+#include <cstring>
+
+namespace prtcl_gpu {
+
+namespace {
+
+constexpr int kNT = 128;           // threads per block for particle kernels
+constexpr int kMaxRedBlocks = 4096; // block partials per reduced value
+
+// ---------------------------------------------------------------------------
+// argument structs
+// ---------------------------------------------------------------------------
+
+struct NbrList {
+  uint32_t const *idx; // ELL, idx[slot * n + i]
+  uint32_t const *cnt; // count per query item
+};
+
+struct FluidN {
+  NbrList L;
+  float4 const *x;
+  float4 const *v;
+  float4 const *a;
+  float const *m;
+  float const *rho;
+  float const *p;
+};
+
+struct BoundN {
+  NbrList L;
+  float4 const *x;
+  float const *V;
+  float const *mu; // uniform dynamic_viscosity (wkbb18)
+};
+
+template <int NF, int NB> struct Nbrs {
+  FluidN f[NF > 0 ? NF : 1];
+  BoundN b[NB > 0 ? NB : 1];
+};
+
+struct Globals {
+  float const *h;
+  float const *dt;
+  float const *t;
+  float const *fade;
+  float const *omega;
+  float *aprde;
+  int *nprde;
+  float const *gravity; // 3 floats
+  float *max_speed;
+};
+
+struct Red {
+  double *partials; // [3][kMaxRedBlocks]
+  unsigned *ticket;
+  double *scalars;
+  int *status;
+};
+
+__device__ __forceinline__ KernelParams kparams(float h) {
+  KernelParams k;
+  k.h = h;
+  k.h3 = (h * h) * h;
+  k.h4 = ((h * h) * h) * h;
+  k.sigma = 0.0795774715459476678844418816862571810f; // 1/(4 pi), see make_kernel_params
+  k.eps = 3.4526698300124390840e-04f;
+  return k;
+}
+
+__device__ __forceinline__ uint32_t grid_tid() { return blockIdx.x * blockDim.x + threadIdx.x; }
+
+// FP64 block sums of NV values, committed by the last block of the launch.
+// Returns true in the last block; out[] is valid in its thread 0.
+template <int NV>
+__device__ bool reduce_commit(double const (&v)[NV], Red const &R, double (&out)[NV]) {
+  __shared__ double sh[32];
+  __shared__ int last;
+  for (int k = 0; k < NV; ++k) {
+    double s = block_sum(v[k], sh);
+    if (threadIdx.x == 0) R.partials[k * kMaxRedBlocks + blockIdx.x] = s;
+  }
+  __threadfence();
+  if (threadIdx.x == 0) last = (atomicAdd(R.ticket, 1u) == gridDim.x - 1) ? 1 : 0;
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  for (int k = 0; k < NV; ++k) {
+    double acc = 0.0;
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+      acc += __ldcg(&R.partials[k * kMaxRedBlocks + b]);
+    out[k] = block_sum(acc, sh);
+  }
+  if (threadIdx.x == 0) *R.ticket = 0u;
+  return true;
+}
+
+unsigned red_grid(size_t n) { return unsigned(std::min<size_t>(div_up(n, kNT), kMaxRedBlocks)); }
+
+// ---------------------------------------------------------------------------
+// density.compute_density (schemes/density.hpp:160-220)
+//   rho_i = sum_f m_j W(x_ij) + sum_b (V_j rho0) W(x_ij)
+// ---------------------------------------------------------------------------
+
+template <int NF, int NB>
+__global__ void __launch_bounds__(kNT) k_density(uint32_t n, float4 const *__restrict__ x, float *__restrict__ rho,
+                                                 float const *rho0p, Globals G, Nbrs<NF, NB> N) {
+  uint32_t i = grid_tid();
+  if (i >= n) return;
+  KernelParams K = kparams(*G.h);
+  float rho0 = *rho0p;
+  f3 xi = mk3(x[i]);
+  float acc = 0.0f;
+#pragma unroll
+  for (int q = 0; q < NF; ++q) {
+    FluidN const &F = N.f[q];
+    uint32_t c = F.L.cnt[i];
+    for (uint32_t k = 0; k < c; ++k) {
+      uint32_t j = F.L.idx[size_t(k) * n + i];
+      acc += F.m[j] * kW(K, sub3(xi, mk3(F.x[j])));
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    BoundN const &B = N.b[q];
+    uint32_t c = B.L.cnt[i];
+    for (uint32_t k = 0; k < c; ++k) {
+      uint32_t j = B.L.idx[size_t(k) * n + i];
+      acc += (B.V[j] * rho0) * kW(K, sub3(xi, mk3(B.x[j])));
+    }
+  }
+  rho[i] = acc;
+}
+
+// aiast12.compute_volume (schemes/aiast12.hpp:125-175): V_i = 1 / sum_b W
+template <int NB>
+__global__ void __launch_bounds__(kNT) k_volume(uint32_t n, float4 const *__restrict__ x, float *__restrict__ V,
+                                                Globals G, Nbrs<0, NB> N) {
+  uint32_t i = grid_tid();
+  if (i >= n) return;
+  KernelParams K = kparams(*G.h);
+  f3 xi = mk3(x[i]);
+  float acc = 0.0f;
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    BoundN const &B = N.b[q];
+    uint32_t c = B.L.cnt[i];
+    for (uint32_t k = 0; k < c; ++k) {
+      uint32_t j = B.L.idx[size_t(k) * n + i];
+      acc += kW(K, sub3(xi, mk3(B.x[j])));
+    }
+  }
+  V[i] = 1.0f / acc;
+}
+
+// gravity.initialize_acceleration (schemes/gravity.hpp:133-158): a = g
+__global__ void k_gravity(uint32_t n, float4 *__restrict__ a, Globals G) {
+  uint32_t i = grid_tid();
+  if (i < n) a[i] = make_float4(G.gravity[0], G.gravity[1], G.gravity[2], 0.0f);
+}
+
+// symplectic_euler.integrate_velocity_with_hard_fade
+// (schemes/symplectic_euler.hpp:172-201): v += (dt a) * [0 < (t - t_b) - fade]
+__global__ void k_integrate_velocity(uint32_t n, float4 *__restrict__ v, float4 const *__restrict__ a,
+                                     float const *__restrict__ tb, Globals G) {
+  uint32_t i = grid_tid();
+  if (i >= n) return;
+  float dt = *G.dt, t = *G.t, fade = *G.fade;
+  float u = ustep(0.0f, (t - tb[i]) - fade);
+  float4 vi = v[i], ai = a[i];
+  vi.x = vi.x + (dt * ai.x) * u;
+  vi.y = vi.y + (dt * ai.y) * u;
+  vi.z = vi.z + (dt * ai.z) * u;
+  v[i] = vi;
+}
+
+// order-preserving map of floats to unsigned integers (for atomicMax)
+__device__ __forceinline__ unsigned f2ord(float f) {
+  unsigned u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(unsigned u) {
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
+
+// symplectic_euler.integrate_position (schemes/symplectic_euler.hpp:236-270):
+// x += dt v; max_speed = max(max_speed, |v|) over all dynamic particles
+__global__ void k_integrate_position(uint32_t n, float4 *__restrict__ x, float4 const *__restrict__ v, Globals G,
+                                     unsigned *maxord) {
+  uint32_t i = grid_tid();
+  float sp = -INFINITY;
+  if (i < n) {
+    float dt = *G.dt;
+    float4 xi = x[i], vi = v[i];
+    xi.x = xi.x + dt * vi.x;
+    xi.y = xi.y + dt * vi.y;
+    xi.z = xi.z + dt * vi.z;
+    x[i] = xi;
+    sp = sqrtf(nsq3(mk3(vi)));
+  }
+  for (int o = 16; o > 0; o >>= 1) sp = fmaxf(sp, __shfl_down_sync(0xffffffffu, sp, o));
+  if ((threadIdx.x & 31) == 0 && sp > -INFINITY) atomicMax(maxord, f2ord(sp));
+}
+__global__ void k_max_speed_begin(Globals G, unsigned *maxord) { *maxord = f2ord(*G.max_speed); }
+__global__ void k_max_speed_end(Globals G, unsigned const *maxord) { *G.max_speed = ord2f(*maxord); }
+
+// ---------------------------------------------------------------------------
+// iisph.setup pass 1 (schemes/iisph.hpp:197-249)
+//   c_i = -sum_f (m_j / rho_i^2) gradW - sum_b ((0.7*2) rho0 (V_j / rho_i^2)) gradW
+// ---------------------------------------------------------------------------
+
+template <int NF, int NB>
+__global__ void __launch_bounds__(kNT) k_iisph_c(uint32_t n, float4 const *__restrict__ x, float const *__restrict__ rho,
+                                                 float4 *__restrict__ cout, float const *rho0p, Globals G,
+                                                 Nbrs<NF, NB> N) {
+  uint32_t i = grid_tid();
+  if (i >= n) return;
+  KernelParams K = kparams(*G.h);
+  float rho0 = *rho0p;
+  f3 xi = mk3(x[i]);
+  float ri = rho[i];
+  f3 c = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int q = 0; q < NF; ++q) {
+    FluidN const &F = N.f[q];
+    uint32_t cn = F.L.cnt[i];
+    for (uint32_t k = 0; k < cn; ++k) {
+      uint32_t j = F.L.idx[size_t(k) * n + i];
+      c = sub3(c, scl3(F.m[j] / (ri * ri), kgradW(K, sub3(xi, mk3(F.x[j])))));
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    BoundN const &B = N.b[q];
+    uint32_t cn = B.L.cnt[i];
+    for (uint32_t k = 0; k < cn; ++k) {
+      uint32_t j = B.L.idx[size_t(k) * n + i];
+      c = sub3(c, scl3(((0.7f * 2.0f) * rho0) * (B.V[j] / (ri * ri)), kgradW(K, sub3(xi, mk3(B.x[j])))));
+    }
+  }
+  cout[i] = make_float4(c.x, c.y, c.z, 0.0f);
+}
+
+// iisph.setup pass 2 (schemes/iisph.hpp:254-354): p = 0, source term s and
+// diagonal element AA
+template <int NF, int NB>
+__global__ void __launch_bounds__(kNT) k_iisph_s_aa(uint32_t n, float4 const *__restrict__ x, float4 const *__restrict__ v,
+                                                    float4 const *__restrict__ cf, float const *__restrict__ m,
+                                                    float const *__restrict__ rho, float *__restrict__ p,
+                                                    float *__restrict__ s, float *__restrict__ AA, float const *rho0p,
+                                                    Globals G, Nbrs<NF, NB> N) {
+  uint32_t i = grid_tid();
+  if (i >= n) return;
+  KernelParams K = kparams(*G.h);
+  float rho0 = *rho0p, dt = *G.dt;
+  f3 xi = mk3(x[i]), vi = mk3(v[i]), ci = mk3(cf[i]);
+  float mi = m[i], ri = rho[i];
+  float sa = 0.0f, aa = 0.0f;
+#pragma unroll
+  for (int q = 0; q < NF; ++q) {
+    FluidN const &F = N.f[q];
+    uint32_t cn = F.L.cnt[i];
+    for (uint32_t k = 0; k < cn; ++k) {
+      uint32_t j = F.L.idx[size_t(k) * n + i];
+      f3 g = kgradW(K, sub3(xi, mk3(F.x[j])));
+      float mj = F.m[j];
+      sa += mj * dot3(sub3(vi, mk3(F.v[j])), g);
+      aa += mj * dot3(ci, g);
+      aa -= (mj * (mi / (ri * ri))) * nsq3(g);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    BoundN const &B = N.b[q];
+    uint32_t cn = B.L.cnt[i];
+    for (uint32_t k = 0; k < cn; ++k) {
+      uint32_t j = B.L.idx[size_t(k) * n + i];
+      f3 g = kgradW(K, sub3(xi, mk3(B.x[j])));
+      float w = rho0 * B.V[j];
+      sa += w * dot3(sub3(vi, f3{0.0f, 0.0f, 0.0f}), g);
+      aa += w * dot3(ci, g);
+    }
+  }
+  p[i] = 0.0f;
+  s[i] = (rho0 - ri) - ((dt * (rho0 / ri)) * sa);
+  AA[i] = aa * ((dt * dt) * (rho0 / ri));
+}
+
+__global__ void k_set_i32(int *p, int v) { *p = v; }
+__global__ void k_set_f32(float *p, float v) { *p = v; }
+
+// iisph.iteration_pressure_acceleration (schemes/iisph.hpp:358-423)
+template <int NF, int NB>
+__global__ void __launch_bounds__(kNT) k_iisph_accel(uint32_t n, float4 const *__restrict__ x, float const *__restrict__ p,
+                                                     float const *__restrict__ rho, float4 *__restrict__ a,
+                                                     float const *rho0p, Globals G, Nbrs<NF, NB> N) {
+  uint32_t i = grid_tid();
+  if (i >= n) return;
+  KernelParams K = kparams(*G.h);
+  float rho0 = *rho0p;
+  f3 xi = mk3(x[i]);
+  float pi = p[i], ri = rho[i];
+  f3 acc = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int q = 0; q < NF; ++q) {
+    FluidN const &F = N.f[q];
+    uint32_t cn = F.L.cnt[i];
+    for (uint32_t k = 0; k < cn; ++k) {
+      uint32_t j = F.L.idx[size_t(k) * n + i];
+      float rj = F.rho[j];
+      float coef = F.m[j] * ((pi / (ri * ri)) + (F.p[j] / (rj * rj)));
+      acc = sub3(acc, scl3(coef, kgradW(K, sub3(xi, mk3(F.x[j])))));
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    BoundN const &B = N.b[q];
+    uint32_t cn = B.L.cnt[i];
+    for (uint32_t k = 0; k < cn; ++k) {
+      uint32_t j = B.L.idx[size_t(k) * n + i];
+      float coef = ((0.7f * rho0) * B.V[j]) * ((2.0f * pi) / (ri * ri));
+      acc = sub3(acc, scl3(coef, kgradW(K, sub3(xi, mk3(B.x[j])))));
+    }
+  }
+  a[i] = make_float4(acc.x, acc.y, acc.z, 0.0f);
+}
+
+// iisph.iteration_pressure (schemes/iisph.hpp:426-516) with the FP64
+// density-error reduction.  scalars[0] accumulates aprde across the fluid
+// groups of one call; `first` / `last_group` frame the call.
+template <int NF, int NB>
+__global__ void __launch_bounds__(kNT) k_iisph_pressure(uint32_t n, float4 const *__restrict__ x,
+                                                        float4 const *__restrict__ a, float const *__restrict__ rho,
+                                                        float const *__restrict__ s, float const *__restrict__ AA,
+                                                        float *__restrict__ p, float *__restrict__ Ap,
+                                                        float const *rho0p, Globals G, Nbrs<NF, NB> N, Red R, int first,
+                                                        int last_group) {
+  KernelParams K = kparams(*G.h);
+  float rho0 = *rho0p, dt = *G.dt, omega = *G.omega;
+  double part = 0.0;
+  for (uint32_t i = grid_tid(); i < n; i += gridDim.x * blockDim.x) {
+    f3 xi = mk3(x[i]), ai = mk3(a[i]);
+    float ap = 0.0f;
+#pragma unroll
+    for (int q = 0; q < NF; ++q) {
+      FluidN const &F = N.f[q];
+      uint32_t cn = F.L.cnt[i];
+      for (uint32_t k = 0; k < cn; ++k) {
+        uint32_t j = F.L.idx[size_t(k) * n + i];
+        ap += F.m[j] * dot3(sub3(ai, mk3(F.a[j])), kgradW(K, sub3(xi, mk3(F.x[j]))));
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NB; ++q) {
+      BoundN const &B = N.b[q];
+      uint32_t cn = B.L.cnt[i];
+      for (uint32_t k = 0; k < cn; ++k) {
+        uint32_t j = B.L.idx[size_t(k) * n + i];
+        ap += (rho0 * B.V[j]) * dot3(sub3(ai, f3{0.0f, 0.0f, 0.0f}), kgradW(K, sub3(xi, mk3(B.x[j]))));
+      }
+    }
+    float ri = rho[i];
+    ap *= (dt * dt) * (rho0 / ri);
+    Ap[i] = ap;
+    float si = s[i], aai = AA[i];
+    float t = p[i] + ((omega * (si - ap)) * rcp0(aai, 1e-9f));
+    // std::max({0, t}) returns the first largest element: t only if 0 < t
+    float pn = ((0.0f < t) ? t : 0.0f) * ustep(1e-9f, fabsf(aai));
+    p[i] = pn;
+    part += double(((ap - si) / rho0) * ustep(1e-9f, pn));
+  }
+  double v[1] = {part}, out[1];
+  if (reduce_commit<1>(v, R, out) && threadIdx.x == 0) {
+    double acc = (first ? double(*G.aprde) : R.scalars[0]) + out[0];
+    R.scalars[0] = acc;
+    if (last_group) *G.aprde = float(acc);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// WKBB18 (schemes/wkbb18.hpp)
+// ---------------------------------------------------------------------------
+
+struct M3 {
+  float m[9]; // column-major
+};
+
+__device__ __forceinline__ float cof3(M3 const &A, int i, int j) {
+  int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+  return A.m[3 * j1 + i1] * A.m[3 * j2 + i2] - A.m[3 * j2 + i1] * A.m[3 * j1 + i2];
+}
+// inverse by the adjugate (cofactors, determinant along column 0)
+__device__ __forceinline__ M3 minv3(M3 const &A) {
+  float c00 = cof3(A, 0, 0), c10 = cof3(A, 1, 0), c20 = cof3(A, 2, 0);
+  float det = c00 * A.m[0] + (c10 * A.m[1] + c20 * A.m[2]);
+  float inv = 1.0f / det;
+  M3 r;
+  r.m[0] = c00 * inv;          // (0,0)
+  r.m[3] = c10 * inv;          // (0,1)
+  r.m[6] = c20 * inv;          // (0,2)
+  r.m[1] = cof3(A, 0, 1) * inv; // (1,0)
+  r.m[4] = cof3(A, 1, 1) * inv; // (1,1)
+  r.m[7] = cof3(A, 2, 1) * inv; // (1,2)
+  r.m[2] = cof3(A, 0, 2) * inv; // (2,0)
+  r.m[5] = cof3(A, 1, 2) * inv; // (2,1)
+  r.m[8] = cof3(A, 2, 2) * inv; // (2,2)
+  return r;
+}
+
+// wkbb18.compute_diagonal (schemes/wkbb18.hpp:194-270): block-Jacobi
+// preconditioner sp_i = (I - dt S_i)^-1, stored as 9 planes
+template <int NF, int NB>
+__global__ void __launch_bounds__(kNT) k_wkbb18_diag(uint32_t n, uint32_t cap, float4 const *__restrict__ x,
+                                                     float const *__restrict__ m, float const *__restrict__ rho,
+                                                     float *__restrict__ sp, float const *rho0p, float const *mup,
+                                                     Globals G, NbrList self, Nbrs<NF, NB> N) {
+  uint32_t i = grid_tid();
+  if (i >= n) return;
+  KernelParams K = kparams(*G.h);
+  float h = K.h, dt = *G.dt, rho0 = *rho0p, mu = *mup;
+  f3 xi = mk3(x[i]);
+  float ri = rho[i];
+  float S[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) S[k] = 0.0f;
+  float hh = (0.01f * h) * h;
+  uint32_t cn = self.cnt[i];
+  for (uint32_t k = 0; k < cn; ++k) {
+    uint32_t j = self.idx[size_t(k) * n + i];
+    f3 xij = sub3(xi, mk3(x[j]));
+    float coef = ((10.0f * (mu / ri)) * (m[j] / rho[j])) / (nsq3(xij) + hh);
+    f3 g = kgradW(K, xij);
+    float gv[3] = {g.x, g.y, g.z}, xv[3] = {xij.x, xij.y, xij.z};
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int r = 0; r < 3; ++r) S[3 * c + r] += coef * (gv[r] * xv[c]);
+  }
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    BoundN const &B = N.b[q];
+    float bmu = *B.mu;
+    uint32_t cb = B.L.cnt[i];
+    for (uint32_t k = 0; k < cb; ++k) {
+      uint32_t j = B.L.idx[size_t(k) * n + i];
+      f3 xij = sub3(xi, mk3(B.x[j]));
+      float coef = ((10.0f * (bmu / ri)) * ((rho0 * B.V[j]) / ri)) / (nsq3(xij) + hh);
+      f3 g = kgradW(K, xij);
+      float gv[3] = {g.x, g.y, g.z}, xv[3] = {xij.x, xij.y, xij.z};
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int r = 0; r < 3; ++r) S[3 * c + r] += coef * (gv[r] * xv[c]);
+    }
+  }
+  M3 A;
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) A.m[3 * c + r] = (r == c ? 1.0f : 0.0f) - dt * S[3 * c + r];
+  M3 inv = minv3(A);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) sp[size_t(k) * cap + i] = inv.m[k];
+}
+
+// y = sp * r  (row . vector, a0 + (a1 + a2))
+__device__ __forceinline__ f3 precond(float const *__restrict__ sp, uint32_t cap, uint32_t i, f3 r) {
+  float s[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) s[k] = sp[size_t(k) * cap + i];
+  return {s[0] * r.x + (s[3] * r.y + s[6] * r.z), s[1] * r.x + (s[4] * r.y + s[7] * r.z),
+          s[2] * r.x + (s[5] * r.y + s[8] * r.z)};
+}
+
+struct PcgArgs {
+  uint32_t n, cap;
+  float4 const *x;
+  float4 const *v;
+  float const *m;
+  float const *rho;
+  float const *sp;
+  float const *tb;
+  float4 *vd;
+  float4 *a;
+  float4 *X, *Y, *Rr, *P, *Q;
+  float const *rho0, *mu, *tol;
+  int const *max_k;
+  int *iterations; // uniform wkbb18_iterations
+  NbrList self;
+};
+
+// system product of wkbb18.accumulate_acceleration (schemes/wkbb18.hpp:
+// 339-396): (A w)_i = w_i - dt * a_f(w)_i
+template <int NB>
+__device__ __forceinline__ f3 wkbb18_system(PcgArgs const &P, KernelParams const &K, float dt, float rho0, float mu,
+                                            Nbrs<0, NB> const &N, float4 const *__restrict__ w, uint32_t i) {
+  float h = K.h;
+  float hh = (0.01f * h) * h;
+  f3 xi = mk3(P.x[i]), wi = mk3(w[i]);
+  float ri = P.rho[i];
+  f3 af = {0.0f, 0.0f, 0.0f};
+  uint32_t cn = P.self.cnt[i];
+  for (uint32_t k = 0; k < cn; ++k) {
+    uint32_t j = P.self.idx[size_t(k) * P.n + i];
+    f3 xij = sub3(xi, mk3(P.x[j]));
+    float coef = (((10.0f * (mu / ri)) * (P.m[j] / P.rho[j])) * dot3(sub3(wi, mk3(w[j])), xij)) / (nsq3(xij) + hh);
+    af = add3(af, scl3(coef, kgradW(K, xij)));
+  }
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    BoundN const &B = N.b[q];
+    float bmu = *B.mu;
+    uint32_t cb = B.L.cnt[i];
+    for (uint32_t k = 0; k < cb; ++k) {
+      uint32_t j = B.L.idx[size_t(k) * P.n + i];
+      f3 xij = sub3(xi, mk3(B.x[j]));
+      float coef = (((10.0f * (bmu / ri)) * ((rho0 * B.V[j]) / ri)) * dot3(wi, xij)) / (nsq3(xij) + hh);
+      af = add3(af, scl3(coef, kgradW(K, xij)));
+    }
+  }
+  return sub3(wi, scl3(dt, af));
+}
+
+// scalars: 0 b_nsq, 1 thr, 2 r_nsq, 3 next_rdy, 4 prev_rdy, 5 pdq
+// float scalars (as double slots): 6 alpha, 7 beta
+// status: 0 iteration count, 1 active
+__global__ void k_pcg_guess(PcgArgs P) {
+  uint32_t i = grid_tid();
+  if (i < P.n) P.X[i] = P.v[i];
+}
+
+// r = A x - b (b = v: the right-hand side's boundary term has v_b = 0),
+// y = M r, p = -y; dots b.b, r.r, r.y
+template <int NB>
+__global__ void __launch_bounds__(kNT) k_pcg_init(PcgArgs P, Globals G, Nbrs<0, NB> N, Red R) {
+  KernelParams K = kparams(*G.h);
+  float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
+  double bb = 0.0, rr = 0.0, ry = 0.0;
+  for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x) {
+    f3 ax = wkbb18_system<NB>(P, K, dt, rho0, mu, N, P.X, i);
+    f3 b = mk3(P.v[i]);
+    f3 r = sub3(ax, b);
+    f3 y = precond(P.sp, P.cap, i, r);
+    P.Rr[i] = make_float4(r.x, r.y, r.z, 0.0f);
+    P.Y[i] = make_float4(y.x, y.y, y.z, 0.0f);
+    P.P[i] = make_float4(-y.x, -y.y, -y.z, 0.0f);
+    bb += double(dot3(b, b));
+    rr += double(dot3(r, r));
+    ry += double(dot3(r, y));
+  }
+  double v[3] = {bb, rr, ry}, out[3];
+  if (reduce_commit<3>(v, R, out) && threadIdx.x == 0) {
+    double tol = double(*P.tol);
+    R.scalars[0] = out[0];
+    double thr = tol * tol * out[0], fmin_ = double(1.17549435082228750797e-38f);
+    R.scalars[1] = (thr < fmin_) ? fmin_ : thr; // max(tol^2 |b|^2, FLT_MIN)
+    R.scalars[2] = out[1];
+    R.scalars[3] = out[2];
+    R.status[0] = 0;
+    R.status[1] = 1; // iteration 0 always runs (min_k = 1)
+  }
+}
+
+// q = A p; p.q; alpha or break (solver/cg_openmp.hpp:121-151)
+template <int NB>
+__global__ void __launch_bounds__(kNT) k_pcg_q(PcgArgs P, Globals G, Nbrs<0, NB> N, Red R) {
+  if (!*(volatile int *)&R.status[1]) return;
+  KernelParams K = kparams(*G.h);
+  float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
+  double pq = 0.0;
+  for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x) {
+    f3 q = wkbb18_system<NB>(P, K, dt, rho0, mu, N, P.P, i);
+    P.Q[i] = make_float4(q.x, q.y, q.z, 0.0f);
+    pq += double(dot3(mk3(P.P[i]), q));
+  }
+  double v[1] = {pq}, out[1];
+  if (reduce_commit<1>(v, R, out) && threadIdx.x == 0) {
+    double prev = R.scalars[3];
+    R.scalars[4] = prev;
+    R.scalars[5] = out[0];
+    if (fabs(out[0]) < double(*P.tol)) R.status[1] = 0;
+    else R.scalars[6] = double(float(prev / out[0]));
+  }
+}
+
+// x += alpha p; r += alpha q; y = M r; r.r; r.y; break / beta
+// (solver/cg_openmp.hpp:153-191)
+__global__ void __launch_bounds__(kNT) k_pcg_update(PcgArgs P, Red R) {
+  if (!*(volatile int *)&R.status[1]) return;
+  float alpha = float(R.scalars[6]);
+  double rr = 0.0, ry = 0.0;
+  for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x) {
+    f3 x = mk3(P.X[i]), p = mk3(P.P[i]), r = mk3(P.Rr[i]), q = mk3(P.Q[i]);
+    x = add3(x, scl3(alpha, p));
+    r = add3(r, scl3(alpha, q));
+    f3 y = precond(P.sp, P.cap, i, r);
+    P.X[i] = make_float4(x.x, x.y, x.z, 0.0f);
+    P.Rr[i] = make_float4(r.x, r.y, r.z, 0.0f);
+    P.Y[i] = make_float4(y.x, y.y, y.z, 0.0f);
+    rr += double(dot3(r, r));
+    ry += double(dot3(r, y));
+  }
+  double v[2] = {rr, ry}, out[2];
+  if (reduce_commit<2>(v, R, out) && threadIdx.x == 0) {
+    double prev = R.scalars[4];
+    R.scalars[2] = out[0];
+    R.scalars[3] = out[1];
+    if (fabs(prev) < double(*P.tol)) {
+      R.status[1] = 0;
+    } else {
+      R.scalars[7] = double(float(out[1] / prev));
+      int k = R.status[0] + 1;
+      R.status[0] = k;
+      // loop condition ok(k, r_nsq): k < 1 -> run; k > max_k -> stop;
+      // r_nsq < thr -> stop
+      bool ok = (k < 1) || (!(k > *P.max_k) && !(out[0] < R.scalars[1]));
+      R.status[1] = ok ? 1 : 0;
+    }
+  }
+}
+
+// p = -y + beta p (only when the loop continues)
+__global__ void k_pcg_p(PcgArgs P, Red R) {
+  if (!*(volatile int *)&R.status[1]) return;
+  float beta = float(R.scalars[7]);
+  for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x) {
+    f3 y = mk3(P.Y[i]), p = mk3(P.P[i]);
+    f3 r = add3(f3{-y.x, -y.y, -y.z}, scl3(beta, p));
+    P.P[i] = make_float4(r.x, r.y, r.z, 0.0f);
+  }
+}
+
+// apply (schemes/wkbb18.hpp:401-413): vd = (x - v) [0 < (t - t_b) - fade];
+// a = vd / dt
+__global__ void k_pcg_apply(PcgArgs P, Globals G, Red R) {
+  uint32_t i = grid_tid();
+  if (i == 0) *P.iterations = R.status[0];
+  if (i >= P.n) return;
+  float dt = *G.dt, t = *G.t, fade = *G.fade;
+  float u = ustep(0.0f, (t - P.tb[i]) - fade);
+  f3 d = scl3(u, sub3(mk3(P.X[i]), mk3(P.v[i])));
+  P.vd[i] = make_float4(d.x, d.y, d.z, 0.0f);
+  P.a[i] = make_float4(d.x / dt, d.y / dt, d.z / dt, 0.0f);
+}
+
+// ---------------------------------------------------------------------------
+// host helpers
+// ---------------------------------------------------------------------------
+
+FieldType ft_real() { return FieldType{}; }
+FieldType ft_vec3() {
+  FieldType t;
+  t.rank = 1;
+  t.ext[0] = 3;
+  return t;
+}
+FieldType ft_mat3() {
+  FieldType t;
+  t.rank = 2;
+  t.ext[0] = 3;
+  t.ext[1] = 3;
+  return t;
+}
+FieldType ft_int() {
+  FieldType t;
+  t.ctype = CType::I32;
+  return t;
+}
+
+template <class T> T *dptr(VaryingField *f) { return static_cast<T *>(f->d); }
+
+// dispatch on the number of fluid (0..2) and boundary (0..2) neighbour groups
+template <template <int, int> class F, class... A> void dispatch_fb(int nf, int nb, A &&...a) {
+  if (nf == 1 && nb == 1) return F<1, 1>::go(a...);
+  if (nf == 1 && nb == 0) return F<1, 0>::go(a...);
+  if (nf == 1 && nb == 2) return F<1, 2>::go(a...);
+  if (nf == 2 && nb == 1) return F<2, 1>::go(a...);
+  if (nf == 2 && nb == 0) return F<2, 0>::go(a...);
+  if (nf == 2 && nb == 2) return F<2, 2>::go(a...);
+  throw Error("unsupported group configuration: " + std::to_string(nf) + " fluid and " + std::to_string(nb) +
+              " boundary groups (1..2 and 0..2 are supported)");
+}
+
+} // namespace
+
+// ===========================================================================
+// Scheme base
+// ===========================================================================
+
+void Scheme::run(std::string const &procedure, Nhood &nh, cudaStream_t s) {
+  auto it = procs_.find(procedure);
+  if (it == procs_.end()) throw Error("procedure does not exist");
+  if (!model_) throw Error("scheme has not been loaded");
+  it->second(nh, s);
+}
+
+std::vector<std::string> Scheme::procedure_names() const {
+  std::vector<std::string> r;
+  for (auto &kv : procs_) r.push_back(kv.first);
+  return r;
+}
+
+namespace {
+
+// groups of a model selected by type / tag, with their fields
+struct FluidG {
+  Group *g;
+  VaryingField *x, *v, *a, *rho, *p, *m, *c, *s, *AA, *Ap, *tb, *vd, *sp;
+  SmallField *rho0, *mu, *tol, *max_k, *iters;
+};
+struct BoundG {
+  Group *g;
+  VaryingField *x, *V;
+  SmallField *mu;
+};
+
+class SchemeCommon : public Scheme {
+protected:
+  Globals globals(Model &m) {
+    Globals G{};
+    auto gp = [&](char const *n) -> void * {
+      SmallField *f = m.find_global(n);
+      return f ? m.small_ptr(*f) : nullptr;
+    };
+    G.h = static_cast<float const *>(gp("smoothing_scale"));
+    G.dt = static_cast<float const *>(gp("time_step"));
+    G.t = static_cast<float const *>(gp("current_time"));
+    G.fade = static_cast<float const *>(gp("fade_duration"));
+    G.omega = static_cast<float const *>(gp("iisph_relaxation"));
+    G.aprde = static_cast<float *>(gp("iisph_aprde"));
+    G.nprde = static_cast<int *>(gp("iisph_nprde"));
+    G.gravity = static_cast<float const *>(gp("gravity"));
+    G.max_speed = static_cast<float *>(gp("maximum_speed"));
+    return G;
+  }
+  Red red(Model &m, int slot) {
+    Red R;
+    R.partials = m.red_d;
+    R.ticket = m.red_count_d + slot;
+    R.scalars = m.scalars_d;
+    R.status = m.status_d;
+    return R;
+  }
+  std::vector<FluidG> fluid_;
+  std::vector<BoundG> bound_;
+
+  static NbrList nl(NbrView const &v, int g) { return NbrList{v.idx[g], v.cnt[g]}; }
+  FluidN fn(FluidG const &F, NbrView const &v) {
+    FluidN r{};
+    r.L = nl(v, F.g->index);
+    r.x = F.x ? dptr<float4>(F.x) : nullptr;
+    r.v = F.v ? dptr<float4>(F.v) : nullptr;
+    r.a = F.a ? dptr<float4>(F.a) : nullptr;
+    r.m = F.m ? dptr<float>(F.m) : nullptr;
+    r.rho = F.rho ? dptr<float>(F.rho) : nullptr;
+    r.p = F.p ? dptr<float>(F.p) : nullptr;
+    return r;
+  }
+  BoundN bn(BoundG const &B, NbrView const &v) {
+    BoundN r{};
+    r.L = nl(v, B.g->index);
+    r.x = dptr<float4>(B.x);
+    r.V = dptr<float>(B.V);
+    r.mu = B.mu ? static_cast<float const *>(model_->small_ptr(*B.mu)) : nullptr;
+    return r;
+  }
+  template <int NF, int NB> Nbrs<NF, NB> nbrs(NbrView const &v) {
+    Nbrs<NF, NB> N{};
+    for (int q = 0; q < NF; ++q) N.f[q] = fn(fluid_[q], v);
+    for (int q = 0; q < NB; ++q) N.b[q] = bn(bound_[q], v);
+    return N;
+  }
+  float const *u(SmallField *f) { return static_cast<float const *>(model_->small_ptr(*f)); }
+  void need_globals(Globals const &G, std::initializer_list<std::pair<void const *, char const *>> l) {
+    for (auto &p : l)
+      if (!p.first) throw Error(std::string("global field missing: ") + p.second);
+  }
+  void collect(Model &m, bool fluid_fields, bool boundary_fields) {
+    fluid_.clear();
+    bound_.clear();
+    for (Group *g : m.groups_by_index()) {
+      if (g->type == "fluid" && fluid_fields) fluid_.push_back(FluidG{g});
+      if (g->type == "boundary" && boundary_fields) bound_.push_back(BoundG{g});
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// density
+// ---------------------------------------------------------------------------
+
+class Density : public SchemeCommon {
+public:
+  Density() { reg("compute_density", [this](Nhood &nh, cudaStream_t s) { compute_density(nh, s); }); }
+  std::string name() const override { return "density"; }
+  std::string source() const override {
+    return "procedure compute_density: rho_f = sum_fluid m W(x_ff) + sum_boundary V rho0 W(x_fb)";
+  }
+  void load(Model &m) override {
+    m.add_global("smoothing_scale", ft_real());
+    collect(m, true, true);
+    for (auto &F : fluid_) {
+      F.rho0 = &F.g->add_uniform("rest_density", ft_real());
+      F.x = &F.g->add_varying("position", ft_vec3());
+      F.rho = &F.g->add_varying("density", ft_real());
+      F.m = &F.g->add_varying("mass", ft_real());
+    }
+    for (auto &B : bound_) {
+      B.x = &B.g->add_varying("position", ft_vec3());
+      B.V = &B.g->add_varying("volume", ft_real());
+    }
+    bind(m);
+  }
+  template <int NF, int NB> struct L {
+    static void go(Density *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
+      uint32_t n = uint32_t(F.g->count);
+      k_density<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(F.x), dptr<float>(F.rho), S->u(F.rho0), G,
+                                                        S->nbrs<NF, NB>(v));
+    }
+  };
+  void compute_density(Nhood &nh, cudaStream_t s) {
+    Globals G = globals(*model_);
+    for (auto &F : fluid_) {
+      if (F.g->count == 0) continue;
+      NbrView const &v = nh.lists(F.g->index, s);
+      dispatch_fb<L>(int(fluid_.size()), int(bound_.size()), this, F, v, G, s);
+      PG_LAUNCH_CHECK();
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// aiast12
+// ---------------------------------------------------------------------------
+
+class Aiast12 : public SchemeCommon {
+public:
+  Aiast12() { reg("compute_volume", [this](Nhood &nh, cudaStream_t s) { compute_volume(nh, s); }); }
+  std::string name() const override { return "aiast12"; }
+  std::string source() const override { return "procedure compute_volume: V_b = 1 / sum_boundary W(x_bb)"; }
+  void load(Model &m) override {
+    m.add_global("smoothing_scale", ft_real());
+    collect(m, false, true);
+    for (auto &B : bound_) {
+      B.x = &B.g->add_varying("position", ft_vec3());
+      B.V = &B.g->add_varying("volume", ft_real());
+    }
+    bind(m);
+  }
+  void compute_volume(Nhood &nh, cudaStream_t s) {
+    Globals G = globals(*model_);
+    int nb = int(bound_.size());
+    for (auto &B : bound_) {
+      uint32_t n = uint32_t(B.g->count);
+      if (n == 0) continue;
+      NbrView const &v = nh.lists(B.g->index, s);
+      if (nb == 1) {
+        Nbrs<0, 1> N{};
+        N.b[0] = bn(bound_[0], v);
+        k_volume<1><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(B.x), dptr<float>(B.V), G, N);
+      } else if (nb == 2) {
+        Nbrs<0, 2> N{};
+        N.b[0] = bn(bound_[0], v);
+        N.b[1] = bn(bound_[1], v);
+        k_volume<2><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(B.x), dptr<float>(B.V), G, N);
+      } else {
+        throw Error("unsupported group configuration: at most 2 boundary groups");
+      }
+      PG_LAUNCH_CHECK();
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// gravity / symplectic_euler (groups selected by the tag "dynamic")
+// ---------------------------------------------------------------------------
+
+class Gravity : public SchemeCommon {
+public:
+  Gravity() {
+    reg("initialize_acceleration", [this](Nhood &, cudaStream_t s) {
+      Globals G = globals(*model_);
+      for (Group *g : dyn_) {
+        uint32_t n = uint32_t(g->count);
+        if (!n) continue;
+        k_gravity<<<div_up(n, 256), 256, 0, s>>>(n, dptr<float4>(g->find_varying("acceleration")), G);
+        PG_LAUNCH_CHECK();
+      }
+    });
+  }
+  std::string name() const override { return "gravity"; }
+  std::string source() const override { return "procedure initialize_acceleration: a = g"; }
+  void load(Model &m) override {
+    m.add_global("gravity", ft_vec3());
+    m.add_global("gravity_center", ft_vec3());
+    dyn_.clear();
+    for (Group *g : m.groups_by_index())
+      if (g->has_tag("dynamic")) {
+        g->add_varying("position", ft_vec3());
+        g->add_varying("acceleration", ft_vec3());
+        dyn_.push_back(g);
+      }
+    bind(m);
+  }
+
+private:
+  std::vector<Group *> dyn_;
+};
+
+class SymplecticEuler : public SchemeCommon {
+public:
+  SymplecticEuler() {
+    reg("integrate_velocity_with_hard_fade", [this](Nhood &, cudaStream_t s) {
+      Globals G = globals(*model_);
+      for (Group *g : dyn_) {
+        uint32_t n = uint32_t(g->count);
+        if (!n) continue;
+        k_integrate_velocity<<<div_up(n, 256), 256, 0, s>>>(n, dptr<float4>(g->find_varying("velocity")),
+                                                            dptr<float4>(g->find_varying("acceleration")),
+                                                            dptr<float>(g->find_varying("time_of_birth")), G);
+        PG_LAUNCH_CHECK();
+      }
+    });
+    reg("integrate_position", [this](Nhood &, cudaStream_t s) {
+      Globals G = globals(*model_);
+      unsigned *maxord = reinterpret_cast<unsigned *>(model_->status_d + 8);
+      k_max_speed_begin<<<1, 1, 0, s>>>(G, maxord);
+      for (Group *g : dyn_) {
+        uint32_t n = uint32_t(g->count);
+        if (!n) continue;
+        VaryingField *x = g->find_varying("position");
+        k_integrate_position<<<div_up(n, 256), 256, 0, s>>>(n, dptr<float4>(x),
+                                                            dptr<float4>(g->find_varying("velocity")), G, maxord);
+        x->version++;
+      }
+      k_max_speed_end<<<1, 1, 0, s>>>(G, maxord);
+      PG_LAUNCH_CHECK();
+    });
+  }
+  std::string name() const override { return "symplectic_euler"; }
+  std::string source() const override {
+    return "procedures integrate_velocity_with_hard_fade: v += dt a [0 < t - t_birth - dt_fade]; "
+           "integrate_position: x += dt v, max_speed max= |v|";
+  }
+  void load(Model &m) override {
+    m.add_global("time_step", ft_real());
+    m.add_global("current_time", ft_real());
+    m.add_global("fade_duration", ft_real());
+    m.add_global("maximum_speed", ft_real());
+    dyn_.clear();
+    for (Group *g : m.groups_by_index())
+      if (g->has_tag("dynamic")) {
+        g->add_varying("position", ft_vec3());
+        g->add_varying("velocity", ft_vec3());
+        g->add_varying("acceleration", ft_vec3());
+        g->add_varying("time_of_birth", ft_real());
+        dyn_.push_back(g);
+      }
+    bind(m);
+  }
+
+private:
+  std::vector<Group *> dyn_;
+};
+
+// ---------------------------------------------------------------------------
+// iisph
+// ---------------------------------------------------------------------------
+
+class Iisph : public SchemeCommon {
+public:
+  Iisph() {
+    reg("setup", [this](Nhood &nh, cudaStream_t s) { setup(nh, s); });
+    reg("iteration_pressure_acceleration", [this](Nhood &nh, cudaStream_t s) { accel(nh, s); });
+    reg("iteration_pressure", [this](Nhood &nh, cudaStream_t s) { pressure(nh, s); });
+  }
+  std::string name() const override { return "iisph"; }
+  std::string source() const override {
+    return "procedures setup (c, p = 0, s, AA, nprde), iteration_pressure_acceleration (a), "
+           "iteration_pressure (Ap, relaxed Jacobi p, aprde += (Ap - s) / rho0 [p > 1e-9])";
+  }
+  void load(Model &m) override {
+    m.add_global("gravity", ft_vec3());
+    m.add_global("smoothing_scale", ft_real());
+    m.add_global("time_step", ft_real());
+    m.add_global("iisph_relaxation", ft_real());
+    m.add_global("iisph_aprde", ft_real());
+    m.add_global("iisph_nprde", ft_int());
+    collect(m, true, true);
+    for (auto &F : fluid_) {
+      F.rho0 = &F.g->add_uniform("rest_density", ft_real());
+      F.x = &F.g->add_varying("position", ft_vec3());
+      F.v = &F.g->add_varying("velocity", ft_vec3());
+      F.a = &F.g->add_varying("acceleration", ft_vec3());
+      F.rho = &F.g->add_varying("density", ft_real());
+      F.p = &F.g->add_varying("pressure", ft_real());
+      F.m = &F.g->add_varying("mass", ft_real());
+      F.c = &F.g->add_varying("iisph_helper_c", ft_vec3());
+      F.s = &F.g->add_varying("iisph_source_term", ft_real());
+      F.AA = &F.g->add_varying("iisph_diagonal_element", ft_real());
+      F.Ap = &F.g->add_varying("iisph_right_hand_side", ft_real());
+    }
+    for (auto &B : bound_) {
+      B.x = &B.g->add_varying("position", ft_vec3());
+      B.V = &B.g->add_varying("volume", ft_real());
+    }
+    bind(m);
+  }
+  template <int NF, int NB> struct C {
+    static void go(Iisph *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
+      uint32_t n = uint32_t(F.g->count);
+      k_iisph_c<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(F.x), dptr<float>(F.rho), dptr<float4>(F.c),
+                                                        S->u(F.rho0), G, S->nbrs<NF, NB>(v));
+    }
+  };
+  template <int NF, int NB> struct SAA {
+    static void go(Iisph *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
+      uint32_t n = uint32_t(F.g->count);
+      k_iisph_s_aa<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(
+          n, dptr<float4>(F.x), dptr<float4>(F.v), dptr<float4>(F.c), dptr<float>(F.m), dptr<float>(F.rho),
+          dptr<float>(F.p), dptr<float>(F.s), dptr<float>(F.AA), S->u(F.rho0), G, S->nbrs<NF, NB>(v));
+    }
+  };
+  template <int NF, int NB> struct A {
+    static void go(Iisph *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
+      uint32_t n = uint32_t(F.g->count);
+      k_iisph_accel<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(F.x), dptr<float>(F.p), dptr<float>(F.rho),
+                                                            dptr<float4>(F.a), S->u(F.rho0), G, S->nbrs<NF, NB>(v));
+    }
+  };
+  template <int NF, int NB> struct P {
+    static void go(Iisph *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s, int first, int last) {
+      uint32_t n = uint32_t(F.g->count);
+      k_iisph_pressure<NF, NB><<<red_grid(n), kNT, 0, s>>>(
+          n, dptr<float4>(F.x), dptr<float4>(F.a), dptr<float>(F.rho), dptr<float>(F.s), dptr<float>(F.AA),
+          dptr<float>(F.p), dptr<float>(F.Ap), S->u(F.rho0), G, S->nbrs<NF, NB>(v), S->red(*S->model_, 0), first, last);
+    }
+  };
+  Globals checked_globals() {
+    Globals G = globals(*model_);
+    need_globals(G, {{G.h, "smoothing_scale"}, {G.dt, "time_step"}, {G.omega, "iisph_relaxation"},
+                     {G.aprde, "iisph_aprde"}, {G.nprde, "iisph_nprde"}});
+    return G;
+  }
+  void setup(Nhood &nh, cudaStream_t s) {
+    Globals G = checked_globals();
+    int nf = int(fluid_.size()), nb = int(bound_.size());
+    for (auto &F : fluid_) {
+      if (!F.g->count) continue;
+      dispatch_fb<C>(nf, nb, this, F, nh.lists(F.g->index, s), G, s);
+      PG_LAUNCH_CHECK();
+    }
+    long long total = 0;
+    for (auto &F : fluid_) {
+      if (!F.g->count) continue;
+      total += (long long)F.g->count;
+      dispatch_fb<SAA>(nf, nb, this, F, nh.lists(F.g->index, s), G, s);
+      PG_LAUNCH_CHECK();
+    }
+    // nprde = number of fluid particles (the generated reduction adds 1 per particle)
+    k_set_i32<<<1, 1, 0, s>>>(G.nprde, int(total));
+    PG_LAUNCH_CHECK();
+  }
+  void accel(Nhood &nh, cudaStream_t s) {
+    Globals G = checked_globals();
+    int nf = int(fluid_.size()), nb = int(bound_.size());
+    for (auto &F : fluid_) {
+      if (!F.g->count) continue;
+      dispatch_fb<A>(nf, nb, this, F, nh.lists(F.g->index, s), G, s);
+      PG_LAUNCH_CHECK();
+    }
+  }
+  void pressure(Nhood &nh, cudaStream_t s) {
+    Globals G = checked_globals();
+    int nf = int(fluid_.size()), nb = int(bound_.size());
+    std::vector<FluidG *> act;
+    for (auto &F : fluid_)
+      if (F.g->count) act.push_back(&F);
+    for (size_t k = 0; k < act.size(); ++k) {
+      dispatch_fb<P>(nf, nb, this, *act[k], nh.lists(act[k]->g->index, s), G, s, k == 0 ? 1 : 0,
+                     k + 1 == act.size() ? 1 : 0);
+      PG_LAUNCH_CHECK();
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// wkbb18
+// ---------------------------------------------------------------------------
+
+class Wkbb18 : public SchemeCommon {
+public:
+  Wkbb18() {
+    reg("compute_diagonal", [this](Nhood &nh, cudaStream_t s) { diag(nh, s); });
+    reg("accumulate_acceleration", [this](Nhood &nh, cudaStream_t s) { pcg(nh, s); });
+  }
+  ~Wkbb18() override { free_vectors(); }
+  std::string name() const override { return "wkbb18"; }
+  std::string source() const override {
+    return "procedures compute_diagonal (sp = (I - dt S)^-1), accumulate_acceleration (PCG over fluid velocities "
+           "with the implicit viscosity system, Jacobi block preconditioner sp, apply vd and a = vd / dt)";
+  }
+  void load(Model &m) override {
+    m.add_global("smoothing_scale", ft_real());
+    m.add_global("time_step", ft_real());
+    m.add_global("current_time", ft_real());
+    m.add_global("fade_duration", ft_real());
+    collect(m, true, true);
+    for (auto &F : fluid_) {
+      F.rho0 = &F.g->add_uniform("rest_density", ft_real());
+      F.mu = &F.g->add_uniform("dynamic_viscosity", ft_real());
+      F.tol = &F.g->add_uniform("wkbb18_maximum_error", ft_real());
+      F.max_k = &F.g->add_uniform("wkbb18_maximum_iterations", ft_int());
+      F.iters = &F.g->add_uniform("wkbb18_iterations", ft_int());
+      F.x = &F.g->add_varying("position", ft_vec3());
+      F.v = &F.g->add_varying("velocity", ft_vec3());
+      F.a = &F.g->add_varying("acceleration", ft_vec3());
+      F.rho = &F.g->add_varying("density", ft_real());
+      F.m = &F.g->add_varying("mass", ft_real());
+      F.vd = &F.g->add_varying("wkbb18_velocity_delta", ft_vec3());
+      F.sp = &F.g->add_varying("wkbb18_system_diagonal", ft_mat3());
+      F.tb = &F.g->add_varying("time_of_birth", ft_real());
+    }
+    for (auto &B : bound_) {
+      B.mu = &B.g->add_uniform("dynamic_viscosity", ft_real());
+      B.x = &B.g->add_varying("position", ft_vec3());
+      B.V = &B.g->add_varying("volume", ft_real());
+    }
+    bind(m);
+  }
+  // the "foreach _ neighbor" loops use the particle's own group only
+  template <int NB> void diag_launch(FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
+    uint32_t n = uint32_t(F.g->count);
+    Nbrs<0, NB> N{};
+    for (int q = 0; q < NB; ++q) N.b[q] = bn(bound_[q], v);
+    k_wkbb18_diag<0, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, uint32_t(F.sp->cap), dptr<float4>(F.x), dptr<float>(F.m),
+                                                         dptr<float>(F.rho), dptr<float>(F.sp), u(F.rho0), u(F.mu), G,
+                                                         nl(v, F.g->index), N);
+  }
+  void diag(Nhood &nh, cudaStream_t s) {
+    Globals G = globals(*model_);
+    int nb = int(bound_.size());
+    for (auto &F : fluid_) {
+      if (!F.g->count) continue;
+      NbrView const &v = nh.lists(F.g->index, s);
+      if (nb == 0) diag_launch<0>(F, v, G, s);
+      else if (nb == 1) diag_launch<1>(F, v, G, s);
+      else if (nb == 2) diag_launch<2>(F, v, G, s);
+      else throw Error("unsupported group configuration: at most 2 boundary groups");
+      PG_LAUNCH_CHECK();
+    }
+  }
+
+  template <int NB> void pcg_group(FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
+    uint32_t n = uint32_t(F.g->count);
+    ensure_vectors(n);
+    PcgArgs P{};
+    P.n = n;
+    P.cap = uint32_t(F.sp->cap);
+    P.x = dptr<float4>(F.x);
+    P.v = dptr<float4>(F.v);
+    P.m = dptr<float>(F.m);
+    P.rho = dptr<float>(F.rho);
+    P.sp = dptr<float>(F.sp);
+    P.tb = dptr<float>(F.tb);
+    P.vd = dptr<float4>(F.vd);
+    P.a = dptr<float4>(F.a);
+    P.X = vec_[0];
+    P.Y = vec_[1];
+    P.Rr = vec_[2];
+    P.P = vec_[3];
+    P.Q = vec_[4];
+    P.rho0 = u(F.rho0);
+    P.mu = u(F.mu);
+    P.tol = u(F.tol);
+    P.max_k = static_cast<int const *>(model_->small_ptr(*F.max_k));
+    P.iterations = static_cast<int *>(model_->small_ptr(*F.iters));
+    P.self = nl(v, F.g->index);
+    Nbrs<0, NB> N{};
+    for (int q = 0; q < NB; ++q) N.b[q] = bn(bound_[q], v);
+    Red R = red(*model_, 1);
+    unsigned rg = red_grid(n), eg = div_up(n, 256);
+    k_pcg_guess<<<eg, 256, 0, s>>>(P);
+    k_pcg_init<NB><<<rg, kNT, 0, s>>>(P, G, N, R);
+    PG_LAUNCH_CHECK();
+    // The loop runs at most max_k + 1 times; the device decides when to stop
+    // and the host polls the decision every few iterations (the kernels of
+    // iterations past the stop return at once).
+    int max_k = 0;
+    PG_CUDA(cudaMemcpyAsync(&max_k, P.max_k, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PG_CUDA(cudaStreamSynchronize(s));
+    int done = 0, issued = 0, chunk = 2;
+    while (!done && issued < max_k + 1) {
+      for (int k = 0; k < chunk && issued < max_k + 1; ++k, ++issued) {
+        k_pcg_q<NB><<<rg, kNT, 0, s>>>(P, G, N, R);
+        k_pcg_update<<<rg, kNT, 0, s>>>(P, R);
+        k_pcg_p<<<rg, kNT, 0, s>>>(P, R);
+      }
+      PG_LAUNCH_CHECK();
+      int active = 0;
+      PG_CUDA(cudaMemcpyAsync(&active, model_->status_d + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+      PG_CUDA(cudaStreamSynchronize(s));
+      done = !active;
+      chunk = std::min(chunk * 2, 16);
+    }
+    k_pcg_apply<<<eg, 256, 0, s>>>(P, G, R);
+    PG_LAUNCH_CHECK();
+  }
+  void pcg(Nhood &nh, cudaStream_t s) {
+    Globals G = globals(*model_);
+    int nb = int(bound_.size());
+    for (auto &F : fluid_) {
+      if (!F.g->count) {
+        int zero = 0;
+        model_->small_set(*F.iters, &zero, s);
+        continue;
+      }
+      NbrView const &v = nh.lists(F.g->index, s);
+      if (nb == 0) pcg_group<0>(F, v, G, s);
+      else if (nb == 1) pcg_group<1>(F, v, G, s);
+      else if (nb == 2) pcg_group<2>(F, v, G, s);
+      else throw Error("unsupported group configuration: at most 2 boundary groups");
+    }
+  }
+
+private:
+  float4 *vec_[5] = {};
+  size_t vec_cap_ = 0;
+  void free_vectors() {
+    for (auto &p : vec_)
+      if (p) {
+        cudaFree(p);
+        p = nullptr;
+      }
+    vec_cap_ = 0;
+  }
+  void ensure_vectors(size_t n) {
+    if (n <= vec_cap_) return;
+    free_vectors();
+    for (auto &p : vec_) PG_CUDA(cudaMalloc(&p, n * 16));
+    vec_cap_ = n;
+  }
+};
+
+using Factory = std::unique_ptr<Scheme> (*)();
+
+template <class S> std::unique_ptr<Scheme> make() { return std::unique_ptr<Scheme>(new S()); }
+
+std::map<std::string, Factory> const &registry() {
+  static std::map<std::string, Factory> r = [] {
+    std::map<std::string, Factory> m;
+    auto add = [&](Factory f) { m[f()->full_name()] = f; };
+    add(&make<Aiast12>);
+    add(&make<Density>);
+    add(&make<Gravity>);
+    add(&make<Iisph>);
+    add(&make<SymplecticEuler>);
+    add(&make<Wkbb18>);
+    return m;
+  }();
+  return r;
+}
+
+} // namespace
+
+std::unique_ptr<Scheme> new_scheme(std::string const &full_name) {
+  auto const &r = registry();
+  auto it = r.find(full_name);
+  if (it == r.end()) throw Error("scheme is not registered");
+  return it->second();
+}
+
+std::vector<std::string> scheme_names() {
+  std::vector<std::string> v;
+  for (auto &kv : registry()) v.push_back(kv.first);
+  return v;
+}
+
+} // namespace prtcl_gpu

@@ -1,0 +1,127 @@
+"""Device neighbourhood vs the oracle: cell assignment, cell order, cell
+ranges, adjacency and neighbour sets must be bit-exact (grid contract of
+util/grouped_uniform_grid.hpp with the (group, raw index) within-cell
+tie-break)."""
+import numpy as np
+import pytest
+
+from prtcl_gb300 import scenes
+from tests.helpers import assert_bitwise, point_scene
+
+pytestmark = pytest.mark.gpu
+
+
+def make(oracle_mod, groups, radius):
+    from prtcl_gb300.core import DeviceScene
+    d = DeviceScene()
+    o = oracle_mod.Scene(np.float32)
+    point_scene(d, groups, radius)
+    point_scene(o, groups, radius)
+    d.update()
+    o.update()
+    return d, o
+
+
+def compare(d, o, groups):
+    gd, go = d.nhood.grid(), o.grid()
+    for k in ("cell_gi", "cell_range", "cell_adj", "sorted"):
+        assert_bitwise(gd[k], go[k], k)
+    G = len(groups)
+    names = sorted(g[0] for g in groups)
+    counts = {g[0]: len(g[2]) for g in groups}
+    for q in range(G):
+        n = counts[names[q]]
+        for ng in range(G):
+            od, idd = d.nhood.neighbor_lists(q, ng, n)
+            oo, ido = o.neighbor_lists(q, ng, n)
+            assert_bitwise(od, oo, f"offsets {q}->{ng}")
+            assert_bitwise(idd, ido, f"indices {q}->{ng}")
+
+
+@pytest.mark.parametrize("dist", ["uniform", "blobs"])
+def test_random_points(oracle_mod, dist):
+    n = 60000
+    pts = scenes.search_points(n, dist, seed=1 if dist == "uniform" else 2)
+    r = scenes.uniform_radius_for_mean_neighbours(n, 40.0) * (0.4 if dist == "blobs" else 1.0)
+    groups = [("p", "fluid", pts, [])]
+    d, o = make(oracle_mod, groups, r)
+    compare(d, o, groups)
+
+
+def test_negative_coordinates_and_exact_radius(oracle_mod):
+    # a lattice straddling the origin whose spacing is r/2: axis neighbours at
+    # two spacings sit at |d| = r up to rounding, the strict d^2 < r^2 test
+    # must agree bit for bit; cells cross the INT32_MAX bias boundary at 0
+    s = 0.025
+    ax = (np.arange(-10, 10) + 0.5) * s
+    g = np.stack(np.meshgrid(ax, ax, ax, indexing="ij"), -1).reshape(-1, 3)
+    pts = g.astype(np.float32)
+    rng = np.random.default_rng(5)
+    pts2 = (rng.random((3000, 3)) * 0.6 - 0.3).astype(np.float32)
+    groups = [("a", "fluid", pts, []), ("b", "boundary", pts2, [])]
+    d, o = make(oracle_mod, groups, 2 * np.float64(np.float32(s)))
+    compare(d, o, groups)
+
+
+def test_cannot_be_neighbor_group(oracle_mod):
+    rng = np.random.default_rng(7)
+    a = (rng.random((20000, 3)) * 2 - 1).astype(np.float32)
+    c = (rng.random((500, 3)) * 2.4 - 1.2).astype(np.float32)  # some far outside any cell
+    groups = [("a", "fluid", a, []), ("c", "probe", c, ["cannot_be_neighbor"])]
+    d, o = make(oracle_mod, groups, 0.06)
+    compare(d, o, groups)
+
+
+def test_dam_break_initial_grid(oracle_mod):
+    sc = scenes.dam_break()
+    groups = [("f", "fluid", sc["fluid"], ["dynamic"]), ("b", "boundary", sc["boundary"], [])]
+    d, o = make(oracle_mod, groups, 2 * np.float64(np.float32(0.025)))
+    compare(d, o, groups)
+
+
+def test_permute_round_trip(oracle_mod):
+    rng = np.random.default_rng(11)
+    a = (rng.random((30000, 3))).astype(np.float32)
+    groups = [("a", "fluid", a, [])]
+    d, o = make(oracle_mod, groups, 0.03)
+    extra = rng.random((30000, 3)).astype(np.float32)
+    d.set_varying("a", "payload", extra)
+    o.set_varying("a", "payload", extra)
+    d.permute()
+    o.permute()
+    pd, po = d.get_varying("a", "position"), o.get_varying("a", "position", 3)
+    assert_bitwise(pd, po, "permuted positions")
+    assert_bitwise(d.get_varying("a", "payload"), o.get_varying("a", "payload", 3), "permuted payload")
+    # the permutation is a bijection of the original rows
+    assert sorted(map(tuple, pd.tolist())) == sorted(map(tuple, a.tolist()))
+    compare(d, o, groups)
+
+
+def test_full_size_search_properties():
+    """4M uniform points (the search workload): symmetric neighbour relation,
+    every pair within the radius, cells sorted by Morton key and ranges
+    partitioning the sorted sequence."""
+    from prtcl_gb300.core import DeviceScene
+    n = 4_000_000
+    pts = scenes.search_points(n, "uniform", seed=1)
+    r = scenes.uniform_radius_for_mean_neighbours(n, 40.0)
+    d = DeviceScene()
+    point_scene(d, [("p", "fluid", pts, [])], r)
+    d.update()
+    g = d.nhood.grid()
+    rng_ = g["cell_range"]
+    assert rng_[0, 0] == 0 and rng_[-1, 1] == n
+    assert (rng_[1:, 0] == rng_[:-1, 1]).all() and (rng_[:, 1] > rng_[:, 0]).all()
+    assert np.array_equal(np.sort(g["sorted"] & 0x0FFFFFFF), np.arange(n, dtype=np.uint32))
+    offs, idx = d.nhood.neighbor_lists(0, 0, n)
+    cnt = np.diff(offs)
+    assert 35 < cnt.mean() < 45
+    # sample: symmetric relation and distance test
+    rng = np.random.default_rng(3)
+    for i in rng.integers(0, n, 2000):
+        js = idx[offs[i]:offs[i + 1]]
+        assert i in js  # self is a neighbour
+        d2 = ((pts[i] - pts[js]) ** 2).sum(1)
+        assert (d2 < r * r * 1.0001).all()
+        for j in js[:8]:
+            assert i in idx[offs[j]:offs[j + 1]]
