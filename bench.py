@@ -1,0 +1,377 @@
+#!/usr/bin/env python
+"""Benchmark: IISPH particle-steps/s on the 1,000,000-fluid-particle dam break
+with WKBB18 implicit viscosity (IISPH + PCG, dt 5e-4 s), one GB300.
+
+A step is one pass of the reference driver loop
+(share/scripts/prtcl-lua.example.lua:363-461) over the resident scene: grid
+update (permute every 8 steps), density, gravity, velocity integration,
+IISPH set-up + relaxed Jacobi to 0.1 % average density error (<= 100
+iterations), velocity integration, WKBB18 diagonal + PCG (tolerance 1e-4,
+<= 100 iterations), velocity integration, position integration.
+
+Arms:
+  default            the CUDA library through its C ABI.  `value` is timed
+                     with CUDA events on the model's stream around K steps of
+                     the resident scene; `e2e` is the same metric through the
+                     public API with host buffers: the scene is uploaded from
+                     pinned host memory inside the timed region and every
+                     step downloads the fluid positions (a frame) to pinned
+                     host memory.
+  --impl reference   the CPU oracle (OpenMP restatement of the reference's
+                     procedures, f32 reductions, per-procedure neighbour
+                     re-query) on all host threads, same scene and metric.
+
+Prints one JSON line (rank 0).  Inputs are larger than L2 (the 1.36M-particle
+working set is ~270 MB), so no explicit L2 flush is done between steps.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from prtcl_gb300 import driver, scenes  # noqa: E402
+
+METRIC = "IISPH particle-steps/s, plain vs batched, at <=0.1% density error; serve p99"
+UNIT = "particle-steps/s"
+
+# algorithmic bytes per kernel launch: each reference field read or written
+# once per kernel (f32: real 4 B, real[3] 12 B, real[3][3] 36 B); neighbour
+# re-reads and neighbour-list traffic excluded.  (per fluid item, per
+# boundary item)
+ALGO_BYTES = {
+    "density": (20, 16),        # x, m -> rho ; boundary x, V
+    "iisph_c": (32, 16),        # x, m, rho -> c
+    "iisph_s_aa": (56, 16),     # x, v, c, m, rho -> p, s, AA
+    "iisph_accel": (36, 16),    # x, m, p, rho -> a
+    "iisph_pressure": (52, 16),  # x, m, a, rho, s, AA, p -> Ap, p
+    "wkbb18_diag": (56, 16),    # x, m, rho -> sp
+    "pcg_init": (116, 16),      # x, m, rho, x0, v, sp -> r, y, p
+    "pcg_q": (44, 16),          # x, m, rho, p -> q
+    "pcg_update": (120, 0),     # x, p, r, q, sp -> x, r, y
+    "pcg_p": (36, 0),           # y, p -> p
+    "integrate_velocity": (40, 0),  # v, a, t_birth -> v
+    "integrate_position": (36, 0),  # x, v -> x
+    "gravity": (12, 0),
+}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic():
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+class Clocks:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", os.environ.get("LOCAL_RANK", "0")],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                c = [x.strip() for x in line.split(",")]
+                if len(c) < 9:
+                    continue
+                try:
+                    sm.append(float(c[1]))
+                    smax = float(c[2])
+                except ValueError:
+                    continue
+                for n, v in zip(names, c[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(n):
+    rank, world = int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        return rank, world, dist
+    return 0, 1, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def timed_steps(d, loop, K, stats):
+    """K steps bracketed by CUDA events recorded on the model's stream (the
+    stream every kernel of the step is launched on)."""
+    import torch
+
+    from prtcl_gb300 import _lib
+    s = torch.cuda.ExternalStream(d.model.stream_handle())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    d.synchronize()
+    torch.cuda.synchronize()
+    l0 = _lib.load().prtcl_gpu_launch_count()
+    e0.record(s)
+    t0 = time.perf_counter()
+    for _ in range(K):
+        stats.append(loop.step())
+    e1.record(s)
+    e1.synchronize()
+    wall = time.perf_counter() - t0
+    launches = _lib.load().prtcl_gpu_launch_count() - l0
+    return e0.elapsed_time(e1) / 1e3, wall, launches
+
+
+def run_ours(args, rank, world, dist):
+    import ctypes as C
+
+    from prtcl_gb300.core import DeviceScene
+    sc = scenes.dam_break_1m() if args.config == "1m" else scenes.dam_break()
+    p = driver.DAM_BREAK_1M if args.config == "1m" else dict(driver.DAM_BREAK_27K, viscosity=True)
+    nf, nb = len(sc["fluid"]), len(sc["boundary"])
+
+    d = DeviceScene()
+    driver.setup_dam_break(d, sc, p)
+    loop = driver.StepLoop(d, p)
+    for _ in range(args.warmup):
+        loop.step()
+    d.model.profile(True)
+    d.model.profile_reset()
+    clocks = Clocks()
+    barrier(dist)
+    clocks.start()
+    stats = []
+    secs, wall, launches = timed_steps(d, loop, args.steps, stats)
+    clk = clocks.stop()
+    prof = d.model.profile_read()
+    d.model.profile(False)
+    secs = max_over_ranks(dist, secs)
+    value = nf * args.steps * world / secs
+
+    # dominant kernel and its roofline
+    peak, peak_kind = load_peaks()
+    top = max(prof.items(), key=lambda kv: kv[1][1]) if prof else None
+    roof = None
+    if top:
+        name, (cnt, ms) = top
+        bf, bb = ALGO_BYTES.get(name, (0, 0))
+        per_launch = bf * nf + bb * nb
+        avg_s = ms / 1e3 / cnt
+        ach = per_launch / avg_s / 1e9
+        tr = load_traffic().get(name)
+        roof = {"bound": "hbm", "kernel": name, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(ach / peak, 4), "traffic": tr, "peak_kind": peak_kind,
+                "algorithmic_bytes_per_launch": per_launch, "avg_launch_us": round(avg_s * 1e6, 2),
+                "launches": cnt, "share_of_step": round(ms / (secs * 1e3), 4)}
+
+    # end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, sc, p, nf, dist, world)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(sc, p, nf, steps=args.cpu_steps)
+
+    jac = [s["jacobi_iterations"] for s in stats]
+    pcg = [s["pcg_iterations"] for s in stats]
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(secs * 1e3 / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 convergence reductions)",
+        "data": "synthetic (seeded lattice dam break generated in-process)",
+        "config": {"workload": ("dam break 1M fluid + %d boundary, IISPH + WKBB18 PCG, dt 5e-4 s" % nb)
+                   if args.config == "1m" else "dam break 27k fluid, IISPH + WKBB18 PCG, dt 1e-3 s",
+                   "fluid_particles": nf, "boundary_particles": nb, "replicas": world,
+                   "parallelism": "replicas only" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (no flush)",
+                   "jacobi_iterations_mean": float(np.mean(jac)), "jacobi_capped_steps": int(sum(j >= 100 for j in jac)),
+                   "pcg_iterations_mean": float(np.mean(pcg)),
+                   "max_relative_density_error": float(max(s["relative_aprde"] for s in stats)),
+                   "wall_s": round(wall, 3)},
+        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": int(launches),
+        "kernels": {k: {"launches": c, "ms": round(m, 3)} for k, (c, m) in prof.items()},
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def run_e2e(args, sc, p, nf, dist, world):
+    """Same metric through the public API with host buffers: upload of the
+    scene from pinned host memory (set-up included) and a per-step download
+    of the fluid positions, all inside the timed region."""
+    import ctypes as C
+
+    import prtcl_gb300.core as core
+    from prtcl_gb300.core import DeviceScene
+
+    def pinned_copy(a):
+        try:
+            import torch
+            t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+            return t.numpy(), t
+        except Exception:
+            return np.ascontiguousarray(a), None
+
+    keep = []
+    host = {}
+    for k in ("fluid", "boundary"):
+        arr, t = pinned_copy(sc[k])
+        host[k] = arr
+        keep.append(t)
+    frame, t = pinned_copy(np.zeros((nf, 3), np.float32))
+    keep.append(t)
+    scene = dict(sc, fluid=host["fluid"], boundary=host["boundary"])
+    barrier(dist)
+    t0 = time.perf_counter()
+    d = DeviceScene()
+    h2d = 0
+    driver.setup_dam_break(d, scene, p)
+    h2d += sum(a.nbytes for a in host.values()) + nf * (12 + 12 + 4 + 4) + len(sc["boundary"]) * 4
+    loop = driver.StepLoop(d, p)
+    posf = d.model.get_group("f").varying.get_field("position")
+    for _ in range(args.steps):
+        loop.step()
+        posf.download(out=frame)
+    d.synchronize()
+    secs = max_over_ranks(dist, time.perf_counter() - t0)
+    return {"value": round(nf * args.steps * world / secs, 1), "unit": UNIT,
+            "h2d_bytes_per_step": int(h2d / args.steps + 4), "d2h_bytes_per_step": int(nf * 12),
+            "includes": "scene upload + set-up + K steps + per-step position download (pinned host buffers)"}
+
+
+def cpu_baseline(sc, p, nf, steps=2, threads=0):
+    """The CPU oracle in reference mode on the host cores: a bounded sample of
+    `steps` steps of the same scene after set-up."""
+    from oracle import oracle as O
+    O.build()
+    th = O.set_threads(threads)
+    o = O.Scene(np.float32, fp64_reductions=False)
+    driver.setup_dam_break(o, sc, p)
+    o.step(permute=False, max_iters=p["max_iters"], eta=p["eta"], viscosity=p.get("viscosity", False))  # warm
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.step(permute=False, max_iters=p["max_iters"], eta=p["eta"], viscosity=p.get("viscosity", False))
+    secs = time.perf_counter() - t0
+    return {"value": round(nf * steps / secs, 1), "unit": UNIT, "cores": th, "kind": "port",
+            "sample": f"{steps} steps of the same scene after set-up and one warm step ({secs:.1f} s)"}
+
+
+def run_reference(args, rank, world, dist):
+    """Reference arm: the CPU restatement of the reference's OpenMP path on
+    all host threads (the reference itself does not build here: Eigen,
+    Boost, Lua and its submodules are absent)."""
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    th = O.set_threads(0)
+    sc = scenes.dam_break_1m() if args.config == "1m" else scenes.dam_break()
+    p = driver.DAM_BREAK_1M if args.config == "1m" else dict(driver.DAM_BREAK_27K, viscosity=True)
+    nf = len(sc["fluid"])
+    o = O.Scene(np.float32, fp64_reductions=False)
+    driver.setup_dam_break(o, sc, p)
+    visc = p.get("viscosity", False)
+    for _ in range(args.warmup):
+        o.step(permute=False, max_iters=p["max_iters"], eta=p["eta"], viscosity=visc)
+    t0 = time.perf_counter()
+    its = []
+    for k in range(args.steps):
+        st = o.step(permute=((k + 1) % p["permute_every"] == 0), max_iters=p["max_iters"], eta=p["eta"],
+                    viscosity=visc)
+        its.append(st["jacobi_iterations"])
+    secs = time.perf_counter() - t0
+    v = nf * args.steps / secs
+    line = {"impl": "reference", "metric": METRIC, "value": round(v, 1), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs * 1e3 / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded lattice dam break generated in-process)",
+            "config": {"workload": "dam break 1M fluid, IISPH + WKBB18 PCG, dt 5e-4 s" if args.config == "1m"
+                       else "dam break 27k fluid, IISPH + WKBB18 PCG, dt 1e-3 s",
+                       "jacobi_iterations_mean": float(np.mean(its))},
+            "cpu_baseline": {"value": round(v, 1), "unit": UNIT, "cores": th, "kind": "port",
+                             "sample": f"{args.steps} full steps after {args.warmup} warm-up steps"},
+            "e2e": {"value": round(v, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="prtcl_gb300", choices=["prtcl_gb300", "reference"])
+    ap.add_argument("--config", default="1m", choices=["1m", "27k"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl != "reference":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    rank, world, dist = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world, dist)
+    else:
+        from prtcl_gb300 import build
+        build.build()
+        run_ours(args, rank, world, dist)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

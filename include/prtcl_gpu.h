@@ -40,6 +40,10 @@ const char *prtcl_gpu_last_error(void);
 /* Library version string. */
 const char *prtcl_gpu_version(void);
 
+/* Number of CUDA kernels this library has launched in this process (no
+ * counterpart in the reference; used to account for device work). */
+uint64_t prtcl_gpu_launch_count(void);
+
 /* ---- model: replaces prtcl::Model (data/model.hpp, data/model.cpp:13-34) ---- */
 
 int prtcl_gpu_model_create(prtcl_gpu_model **out);
@@ -96,8 +100,21 @@ int prtcl_gpu_uniform_info(prtcl_gpu_model *model, const char *group, const char
 int prtcl_gpu_global_info(prtcl_gpu_model *model, const char *field, char *ctype_out, int32_t *rank_out,
                           int32_t *extents_out);
 
+/* The model's own CUDA stream (a cudaStream_t), used when a call gets
+ * stream == NULL. */
+int prtcl_gpu_model_stream(prtcl_gpu_model *model, void **stream_out);
+
 /* Wait for all work queued on the model's stream (and `stream`, if given). */
 int prtcl_gpu_model_synchronize(prtcl_gpu_model *model, void *stream);
+
+/* Per-kernel timing with CUDA events on the launching stream (no
+ * counterpart in the reference, whose only tracing is a disabled scope
+ * macro, schemes/iisph.hpp:35).  While enabled, every procedure and grid
+ * kernel launch records an event pair; read returns lines
+ * "name count total_ms" for the launches since the last reset. */
+int prtcl_gpu_profile_enable(prtcl_gpu_model *model, int32_t enable);
+int prtcl_gpu_profile_read(prtcl_gpu_model *model, char *buf, int64_t size, int64_t *needed_out);
+int prtcl_gpu_profile_reset(prtcl_gpu_model *model);
 
 /* ---- neighbourhood: replaces prtcl::Neighborhood (util/neighborhood.hpp:23-42) ---- */
 

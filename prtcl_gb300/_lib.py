@@ -38,6 +38,7 @@ pp = C.POINTER(C.c_void_p)
 SIGNATURES = {
     "prtcl_gpu_last_error": [],
     "prtcl_gpu_version": [],
+    "prtcl_gpu_launch_count": [],
     "prtcl_gpu_model_create": [pp],
     "prtcl_gpu_model_destroy": [vp],
     "prtcl_gpu_group_add": [vp, cp, cp],
@@ -59,7 +60,11 @@ SIGNATURES = {
     "prtcl_gpu_global_get": [vp, cp, vp],
     "prtcl_gpu_uniform_info": [vp, cp, cp, C.c_char_p, i32p, i32p],
     "prtcl_gpu_global_info": [vp, cp, C.c_char_p, i32p, i32p],
+    "prtcl_gpu_model_stream": [vp, pp],
     "prtcl_gpu_model_synchronize": [vp, vp],
+    "prtcl_gpu_profile_enable": [vp, i32],
+    "prtcl_gpu_profile_read": [vp, C.c_char_p, i64, i64p],
+    "prtcl_gpu_profile_reset": [vp],
     "prtcl_gpu_nhood_create": [pp],
     "prtcl_gpu_nhood_destroy": [vp],
     "prtcl_gpu_nhood_set_radius": [vp, dbl],
@@ -79,7 +84,7 @@ SIGNATURES = {
     "prtcl_gpu_scheme_source": [vp, C.c_char_p, i64, i64p],
     "prtcl_gpu_registry_scheme_names": [C.c_char_p, i64, i64p],
 }
-_RESTYPE = {"prtcl_gpu_last_error": cp, "prtcl_gpu_version": cp}
+_RESTYPE = {"prtcl_gpu_last_error": cp, "prtcl_gpu_version": cp, "prtcl_gpu_launch_count": C.c_uint64}
 
 _lock = threading.Lock()
 _lib = None

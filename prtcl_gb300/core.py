@@ -246,6 +246,27 @@ class Model:
     def synchronize(self, stream=None):
         check(load().prtcl_gpu_model_synchronize(self._h, _stream(stream)))
 
+    def stream_handle(self):
+        """The model's own cudaStream_t as an integer."""
+        h = C.c_void_p()
+        check(load().prtcl_gpu_model_stream(self._h, C.byref(h)))
+        return int(h.value or 0)
+
+    def profile(self, enable=True):
+        """Enable / disable per-kernel CUDA-event timing."""
+        check(load().prtcl_gpu_profile_enable(self._h, 1 if enable else 0))
+
+    def profile_read(self):
+        """{kernel name: (launches, total ms)} since the last reset."""
+        out = {}
+        for line in read_str(load().prtcl_gpu_profile_read, self._h).splitlines():
+            name, cnt, ms = line.split()
+            out[name] = (int(cnt), float(ms))
+        return out
+
+    def profile_reset(self):
+        check(load().prtcl_gpu_profile_reset(self._h))
+
     AddGroup = add_group
     GetGroup = get_group
     GetGroupCount = lambda self: self.group_count  # noqa: E731

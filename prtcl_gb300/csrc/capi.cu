@@ -2,6 +2,8 @@
 #include "../../include/prtcl_gpu.h"
 #include "schemes.hpp"
 
+#include <atomic>
+#include <cstdio>
 #include <cstring>
 #include <string>
 
@@ -16,6 +18,12 @@ struct prtcl_gpu_nhood {
 struct prtcl_gpu_scheme {
   std::unique_ptr<Scheme> s;
 };
+
+namespace prtcl_gpu {
+static std::atomic<uint64_t> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
+} // namespace prtcl_gpu
 
 namespace {
 
@@ -100,6 +108,7 @@ extern "C" {
 
 const char *prtcl_gpu_last_error(void) { return g_last_error.c_str(); }
 const char *prtcl_gpu_version(void) { return "prtcl_gb300 0.1 (sm_103a)"; }
+uint64_t prtcl_gpu_launch_count(void) { return launch_count(); }
 
 int prtcl_gpu_model_create(prtcl_gpu_model **out) {
   NEED(out);
@@ -266,12 +275,40 @@ int prtcl_gpu_global_info(prtcl_gpu_model *model, const char *field, char *ctype
   NEED(field);
   return guard([&] { write_type(global(model->m, field).type, ctype_out, rank_out, extents_out); });
 }
+int prtcl_gpu_model_stream(prtcl_gpu_model *model, void **stream_out) {
+  NEED(model);
+  NEED(stream_out);
+  *stream_out = static_cast<void *>(model->m.stream());
+  return PRTCL_GPU_OK;
+}
 int prtcl_gpu_model_synchronize(prtcl_gpu_model *model, void *stream) {
   NEED(model);
   return guard([&] {
     if (stream) PG_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
     PG_CUDA(cudaStreamSynchronize(model->m.stream()));
   });
+}
+
+int prtcl_gpu_profile_enable(prtcl_gpu_model *model, int32_t enable) {
+  NEED(model);
+  return guard([&] { model->m.prof.enabled = enable != 0; });
+}
+int prtcl_gpu_profile_read(prtcl_gpu_model *model, char *buf, int64_t size, int64_t *needed_out) {
+  NEED(model);
+  std::string text;
+  int rc = guard([&] {
+    for (auto &kv : model->m.prof.read()) {
+      char line[256];
+      std::snprintf(line, sizeof line, "%s %lld %.6f\n", kv.first.c_str(), kv.second.count, kv.second.ms);
+      text += line;
+    }
+  });
+  if (rc != PRTCL_GPU_OK) return rc;
+  return write_str(text, buf, size, needed_out);
+}
+int prtcl_gpu_profile_reset(prtcl_gpu_model *model) {
+  NEED(model);
+  return guard([&] { model->m.prof.reset(); });
 }
 
 int prtcl_gpu_nhood_create(prtcl_gpu_nhood **out) {

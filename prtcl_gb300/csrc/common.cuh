@@ -36,6 +36,10 @@ constexpr int kMaxNbrGroups = 4;  // fluid / boundary groups a procedure sums ov
 
 inline unsigned div_up(size_t a, size_t b) { return unsigned((a + b - 1) / b); }
 
+// number of kernels this library has launched (process-wide)
+uint64_t launch_count();
+void count_launch();
+
 // ---------------------------------------------------------------------------
 // FP32 vector helpers in the reference's evaluation order
 // ---------------------------------------------------------------------------

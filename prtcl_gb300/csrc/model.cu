@@ -124,6 +124,7 @@ void upload_varying(VaryingField &f, size_t count, void const *host, size_t n_it
       k_expand_vec3<<<div_up(count, 256), 256, 0, s>>>(static_cast<float *>(stage), static_cast<float4 *>(f.d), count);
     else
       k_to_planar9<<<div_up(count, 256), 256, 0, s>>>(static_cast<float *>(stage), static_cast<float *>(f.d), count, f.cap);
+    count_launch();
     PG_LAUNCH_CHECK();
     PG_CUDA(cudaFreeAsync(stage, s));
   }
@@ -144,6 +145,7 @@ void download_varying(VaryingField const &f, size_t count, void *host, size_t n_
       k_pack_vec3<<<div_up(count, 256), 256, 0, s>>>(static_cast<float4 const *>(f.d), static_cast<float *>(stage), count);
     else
       k_from_planar9<<<div_up(count, 256), 256, 0, s>>>(static_cast<float const *>(f.d), static_cast<float *>(stage), count, f.cap);
+    count_launch();
     PG_LAUNCH_CHECK();
     PG_CUDA(cudaMemcpyAsync(host, stage, hbytes, cudaMemcpyDeviceToHost, s));
     PG_CUDA(cudaFreeAsync(stage, s));
@@ -215,16 +217,16 @@ void Group::permute(uint32_t const *perm, cudaStream_t s) {
     void *nd = alloc_field(f.type, f.cap, s);
     unsigned b = 256;
     if (f.type.is_vec3()) {
-      k_gather<float4><<<div_up(n, b), b, 0, s>>>(static_cast<float4 const *>(f.d), static_cast<float4 *>(nd), perm, n);
+      k_gather<float4><<<div_up(n, b), b, 0, s>>>(static_cast<float4 const *>(f.d), static_cast<float4 *>(nd), perm, n); count_launch();
     } else if (f.type.is_mat3()) {
       k_gather_planar9<<<div_up(n, b), b, 0, s>>>(static_cast<float const *>(f.d), static_cast<float *>(nd), perm, n,
-                                                  f.cap, f.cap);
+                                                  f.cap, f.cap); count_launch();
     } else if (f.type.host_item_bytes() == 4) {
-      k_gather<uint32_t><<<div_up(n, b), b, 0, s>>>(static_cast<uint32_t const *>(f.d), static_cast<uint32_t *>(nd), perm, n);
+      k_gather<uint32_t><<<div_up(n, b), b, 0, s>>>(static_cast<uint32_t const *>(f.d), static_cast<uint32_t *>(nd), perm, n); count_launch();
     } else {
       int words = int(f.type.host_item_bytes() / 4);
       k_gather_words<<<div_up(n * words, b), b, 0, s>>>(static_cast<uint32_t const *>(f.d), static_cast<uint32_t *>(nd),
-                                                        perm, n, words);
+                                                        perm, n, words); count_launch();
     }
     PG_LAUNCH_CHECK();
     PG_CUDA(cudaFreeAsync(f.d, s));

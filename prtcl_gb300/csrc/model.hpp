@@ -17,6 +17,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "profile.hpp"
 
 #include <map>
 #include <memory>
@@ -117,6 +118,7 @@ public:
   unsigned *red_count_d = nullptr; // last-block tickets
   double *scalars_d = nullptr;   // 64 FP64 solver scalars
   int *status_d = nullptr;       // 16 status words (error flags, iteration counts)
+  Profiler prof;                 // optional per-kernel CUDA-event timing
 
 private:
   std::map<std::string, std::unique_ptr<Group>> groups_;

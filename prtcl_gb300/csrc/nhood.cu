@@ -416,9 +416,9 @@ static void exclusive_scan(uint32_t const *in, uint32_t *out, size_t n, uint32_t
     sums_cap = std::max<size_t>(nb, 1024);
     PG_CUDA(cudaMalloc(&sums, sums_cap * sizeof(uint32_t)));
   }
-  k_scan_reduce<<<unsigned(nb), kScanNT, 0, s>>>(in, n, sums);
-  k_scan_single<<<1, 1024, 0, s>>>(sums, nb);
-  k_scan_apply<<<unsigned(nb), kScanNT, 0, s>>>(in, n, sums, out);
+  k_scan_reduce<<<unsigned(nb), kScanNT, 0, s>>>(in, n, sums); count_launch();
+  k_scan_single<<<1, 1024, 0, s>>>(sums, nb); count_launch();
+  k_scan_apply<<<unsigned(nb), kScanNT, 0, s>>>(in, n, sums, out); count_launch();
   PG_LAUNCH_CHECK();
 }
 
@@ -551,7 +551,10 @@ void Nhood::update(cudaStream_t s) {
   // 1. grid indices, handles, bit statistics
   PG_CUDA(cudaMemsetAsync(stats_d_, 0, 16 * sizeof(uint32_t), s));
   unsigned nb = div_up(N, 256);
-  k_cells_u<<<nb, 256, 0, s>>>(pt, gv, G, N, ukeys_, vals_a_, stats_d_);
+  {
+    ProfScope ps(model_->prof, "grid_keys", s);
+    k_cells_u<<<nb, 256, 0, s>>>(pt, gv, G, N, ukeys_, vals_a_, stats_d_); count_launch();
+  }
   PG_LAUNCH_CHECK();
   PG_CUDA(cudaMemcpyAsync(stats_h_, stats_d_, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
   PG_CUDA(cudaStreamSynchronize(s));
@@ -569,7 +572,8 @@ void Nhood::update(cudaStream_t s) {
   key_ = k;
   gv.key = k;
   // 2. compressed Z-order keys
-  k_cells_key<<<nb, 256, 0, s>>>(ukeys_, N, k.keep, keys_a_);
+  model_->prof.begin("grid_sort", s);
+  k_cells_key<<<nb, 256, 0, s>>>(ukeys_, N, k.keep, keys_a_); count_launch();
   PG_LAUNCH_CHECK();
   // 3. stable LSD radix sort over the informative bits
   int total_bits = 3 * k.bits;
@@ -583,9 +587,9 @@ void Nhood::update(cudaStream_t s) {
     PG_CUDA(cudaMalloc(&hist_, hist_cap_ * 4));
   }
   for (int shift = 0; shift < total_bits; shift += 8) {
-    k_rs_hist<<<tiles, kRsNT, 0, s>>>(kin, N, shift, hist_, tiles);
-    k_scan_single<<<1, 1024, 0, s>>>(hist_, hl);
-    k_rs_scatter<<<tiles, kRsNT, 0, s>>>(kin, vin, kout, vout, N, shift, hist_, tiles);
+    k_rs_hist<<<tiles, kRsNT, 0, s>>>(kin, N, shift, hist_, tiles); count_launch();
+    k_scan_single<<<1, 1024, 0, s>>>(hist_, hl); count_launch();
+    k_rs_scatter<<<tiles, kRsNT, 0, s>>>(kin, vin, kout, vout, N, shift, hist_, tiles); count_launch();
     PG_LAUNCH_CHECK();
     std::swap(kin, kout);
     std::swap(vin, vout);
@@ -593,15 +597,18 @@ void Nhood::update(cudaStream_t s) {
   sorted_keys_ = kin;
   sorted_vals_ = vin;
   gv = view();
+  model_->prof.end(s); // grid_sort
+  model_->prof.begin("grid_cells", s);
   // 4. cells
-  k_cell_flags<<<nb, 256, 0, s>>>(kin, N, flags_);
+  k_cell_flags<<<nb, 256, 0, s>>>(kin, N, flags_); count_launch();
   PG_LAUNCH_CHECK();
   exclusive_scan(flags_, scan_, N, block_sums_, block_sums_cap_, s);
   k_cells_fill<<<nb, 256, 0, s>>>(pt, gv, kin, vin, flags_, scan_, N, s2c_, r2s_, cell_start_, cell_key_, cell_gi_,
-                                  ncells_d_);
+                                  ncells_d_); count_launch();
   PG_LAUNCH_CHECK();
   // 5. adjacency
-  k_cells_adj<<<nb, 256, 0, s>>>(gv, cell_gi_, N, cell_adj_);
+  k_cells_adj<<<nb, 256, 0, s>>>(gv, cell_gi_, N, cell_adj_); count_launch();
+  model_->prof.end(s); // grid_cells
   PG_LAUNCH_CHECK();
 }
 
@@ -622,7 +629,7 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s) {
   for (int g = 0; g < G; ++g)
     if (gg_[g].pos) pt.pos[g] = static_cast<float4 const *>(gg_[g].pos->d);
   if (N_ > 0) {
-    k_xsorted<<<div_up(N_, 256), 256, 0, s>>>(pt, sorted_vals_, N_, xsorted_);
+    k_xsorted<<<div_up(N_, 256), 256, 0, s>>>(pt, sorted_vals_, N_, xsorted_); count_launch();
     PG_LAUNCH_CHECK();
   }
   for (int attempt = 0; attempt < 8; ++attempt) {
@@ -654,7 +661,10 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s) {
     PG_CUDA(cudaMemsetAsync(stats_d_ + 8, 0, 8 * sizeof(uint32_t), s));
     GridView gv = view();
     float4 const *qpos = static_cast<float4 const *>(gg_[q].pos->d);
-    k_build_lists<<<div_up(n, 128), 128, 0, s>>>(gv, xsorted_, qpos, q, lo);
+    {
+      ProfScope ps(model_->prof, "nhood_lists", s);
+      k_build_lists<<<div_up(n, 128), 128, 0, s>>>(gv, xsorted_, qpos, q, lo); count_launch();
+    }
     PG_LAUNCH_CHECK();
     PG_CUDA(cudaMemcpyAsync(stats_h_ + 8, stats_d_ + 8, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     PG_CUDA(cudaStreamSynchronize(s));
@@ -715,12 +725,12 @@ void Nhood::permute(Model &m, cudaStream_t s) {
   for (int g = 0; g < G; ++g) {
     if (!in_grid_[g] || gg_[g].g->count == 0) continue;
     size_t n = gg_[g].g->count;
-    k_group_flags<<<div_up(N_, 256), 256, 0, s>>>(sorted_vals_, N_, uint32_t(g), flags_);
+    k_group_flags<<<div_up(N_, 256), 256, 0, s>>>(sorted_vals_, N_, uint32_t(g), flags_); count_launch();
     PG_LAUNCH_CHECK();
     exclusive_scan(flags_, scan_, N_, block_sums_, block_sums_cap_, s);
     uint32_t *perm = nullptr;
     PG_CUDA(cudaMallocAsync(&perm, n * 4, s));
-    k_group_perm<<<div_up(N_, 256), 256, 0, s>>>(sorted_vals_, flags_, scan_, N_, perm);
+    k_group_perm<<<div_up(N_, 256), 256, 0, s>>>(sorted_vals_, flags_, scan_, N_, perm); count_launch();
     PG_LAUNCH_CHECK();
     gg_[g].g->permute(perm, s);
     PG_CUDA(cudaFreeAsync(perm, s));

@@ -826,8 +826,9 @@ public:
   template <int NF, int NB> struct L {
     static void go(Density *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
       uint32_t n = uint32_t(F.g->count);
+      ProfScope ps(S->model_->prof, "density", s);
       k_density<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(F.x), dptr<float>(F.rho), S->u(F.rho0), G,
-                                                        S->nbrs<NF, NB>(v));
+                                                        S->nbrs<NF, NB>(v)); count_launch();
     }
   };
   void compute_density(Nhood &nh, cudaStream_t s) {
@@ -869,12 +870,14 @@ public:
       if (nb == 1) {
         Nbrs<0, 1> N{};
         N.b[0] = bn(bound_[0], v);
-        k_volume<1><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(B.x), dptr<float>(B.V), G, N);
+        ProfScope ps(model_->prof, "aiast12_volume", s);
+        k_volume<1><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(B.x), dptr<float>(B.V), G, N); count_launch();
       } else if (nb == 2) {
         Nbrs<0, 2> N{};
         N.b[0] = bn(bound_[0], v);
         N.b[1] = bn(bound_[1], v);
-        k_volume<2><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(B.x), dptr<float>(B.V), G, N);
+        ProfScope ps(model_->prof, "aiast12_volume", s);
+        k_volume<2><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(B.x), dptr<float>(B.V), G, N); count_launch();
       } else {
         throw Error("unsupported group configuration: at most 2 boundary groups");
       }
@@ -895,7 +898,8 @@ public:
       for (Group *g : dyn_) {
         uint32_t n = uint32_t(g->count);
         if (!n) continue;
-        k_gravity<<<div_up(n, 256), 256, 0, s>>>(n, dptr<float4>(g->find_varying("acceleration")), G);
+        ProfScope ps(model_->prof, "gravity", s);
+        k_gravity<<<div_up(n, 256), 256, 0, s>>>(n, dptr<float4>(g->find_varying("acceleration")), G); count_launch();
         PG_LAUNCH_CHECK();
       }
     });
@@ -927,25 +931,27 @@ public:
       for (Group *g : dyn_) {
         uint32_t n = uint32_t(g->count);
         if (!n) continue;
+        ProfScope ps(model_->prof, "integrate_velocity", s);
         k_integrate_velocity<<<div_up(n, 256), 256, 0, s>>>(n, dptr<float4>(g->find_varying("velocity")),
                                                             dptr<float4>(g->find_varying("acceleration")),
-                                                            dptr<float>(g->find_varying("time_of_birth")), G);
+                                                            dptr<float>(g->find_varying("time_of_birth")), G); count_launch();
         PG_LAUNCH_CHECK();
       }
     });
     reg("integrate_position", [this](Nhood &, cudaStream_t s) {
       Globals G = globals(*model_);
       unsigned *maxord = reinterpret_cast<unsigned *>(model_->status_d + 8);
-      k_max_speed_begin<<<1, 1, 0, s>>>(G, maxord);
+      k_max_speed_begin<<<1, 1, 0, s>>>(G, maxord); count_launch();
       for (Group *g : dyn_) {
         uint32_t n = uint32_t(g->count);
         if (!n) continue;
         VaryingField *x = g->find_varying("position");
+        ProfScope ps(model_->prof, "integrate_position", s);
         k_integrate_position<<<div_up(n, 256), 256, 0, s>>>(n, dptr<float4>(x),
-                                                            dptr<float4>(g->find_varying("velocity")), G, maxord);
+                                                            dptr<float4>(g->find_varying("velocity")), G, maxord); count_launch();
         x->version++;
       }
-      k_max_speed_end<<<1, 1, 0, s>>>(G, maxord);
+      k_max_speed_end<<<1, 1, 0, s>>>(G, maxord); count_launch();
       PG_LAUNCH_CHECK();
     });
   }
@@ -1021,31 +1027,35 @@ public:
   template <int NF, int NB> struct C {
     static void go(Iisph *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
       uint32_t n = uint32_t(F.g->count);
+      ProfScope ps(S->model_->prof, "iisph_c", s);
       k_iisph_c<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(F.x), dptr<float>(F.rho), dptr<float4>(F.c),
-                                                        S->u(F.rho0), G, S->nbrs<NF, NB>(v));
+                                                        S->u(F.rho0), G, S->nbrs<NF, NB>(v)); count_launch();
     }
   };
   template <int NF, int NB> struct SAA {
     static void go(Iisph *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
       uint32_t n = uint32_t(F.g->count);
+      ProfScope ps(S->model_->prof, "iisph_s_aa", s);
       k_iisph_s_aa<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(
           n, dptr<float4>(F.x), dptr<float4>(F.v), dptr<float4>(F.c), dptr<float>(F.m), dptr<float>(F.rho),
-          dptr<float>(F.p), dptr<float>(F.s), dptr<float>(F.AA), S->u(F.rho0), G, S->nbrs<NF, NB>(v));
+          dptr<float>(F.p), dptr<float>(F.s), dptr<float>(F.AA), S->u(F.rho0), G, S->nbrs<NF, NB>(v)); count_launch();
     }
   };
   template <int NF, int NB> struct A {
     static void go(Iisph *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
       uint32_t n = uint32_t(F.g->count);
+      ProfScope ps(S->model_->prof, "iisph_accel", s);
       k_iisph_accel<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(F.x), dptr<float>(F.p), dptr<float>(F.rho),
-                                                            dptr<float4>(F.a), S->u(F.rho0), G, S->nbrs<NF, NB>(v));
+                                                            dptr<float4>(F.a), S->u(F.rho0), G, S->nbrs<NF, NB>(v)); count_launch();
     }
   };
   template <int NF, int NB> struct P {
     static void go(Iisph *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s, int first, int last) {
       uint32_t n = uint32_t(F.g->count);
+      ProfScope ps(S->model_->prof, "iisph_pressure", s);
       k_iisph_pressure<NF, NB><<<red_grid(n), kNT, 0, s>>>(
           n, dptr<float4>(F.x), dptr<float4>(F.a), dptr<float>(F.rho), dptr<float>(F.s), dptr<float>(F.AA),
-          dptr<float>(F.p), dptr<float>(F.Ap), S->u(F.rho0), G, S->nbrs<NF, NB>(v), S->red(*S->model_, 0), first, last);
+          dptr<float>(F.p), dptr<float>(F.Ap), S->u(F.rho0), G, S->nbrs<NF, NB>(v), S->red(*S->model_, 0), first, last); count_launch();
     }
   };
   Globals checked_globals() {
@@ -1070,7 +1080,7 @@ public:
       PG_LAUNCH_CHECK();
     }
     // nprde = number of fluid particles (the generated reduction adds 1 per particle)
-    k_set_i32<<<1, 1, 0, s>>>(G.nprde, int(total));
+    k_set_i32<<<1, 1, 0, s>>>(G.nprde, int(total)); count_launch();
     PG_LAUNCH_CHECK();
   }
   void accel(Nhood &nh, cudaStream_t s) {
@@ -1145,9 +1155,10 @@ public:
     uint32_t n = uint32_t(F.g->count);
     Nbrs<0, NB> N{};
     for (int q = 0; q < NB; ++q) N.b[q] = bn(bound_[q], v);
+    ProfScope ps(model_->prof, "wkbb18_diag", s);
     k_wkbb18_diag<0, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, uint32_t(F.sp->cap), dptr<float4>(F.x), dptr<float>(F.m),
                                                          dptr<float>(F.rho), dptr<float>(F.sp), u(F.rho0), u(F.mu), G,
-                                                         nl(v, F.g->index), N);
+                                                         nl(v, F.g->index), N); count_launch();
   }
   void diag(Nhood &nh, cudaStream_t s) {
     Globals G = globals(*model_);
@@ -1192,8 +1203,11 @@ public:
     for (int q = 0; q < NB; ++q) N.b[q] = bn(bound_[q], v);
     Red R = red(*model_, 1);
     unsigned rg = red_grid(n), eg = div_up(n, 256);
-    k_pcg_guess<<<eg, 256, 0, s>>>(P);
-    k_pcg_init<NB><<<rg, kNT, 0, s>>>(P, G, N, R);
+    k_pcg_guess<<<eg, 256, 0, s>>>(P); count_launch();
+    {
+      ProfScope ps(model_->prof, "pcg_init", s);
+      k_pcg_init<NB><<<rg, kNT, 0, s>>>(P, G, N, R); count_launch();
+    }
     PG_LAUNCH_CHECK();
     // The loop runs at most max_k + 1 times; the device decides when to stop
     // and the host polls the decision every few iterations (the kernels of
@@ -1204,9 +1218,18 @@ public:
     int done = 0, issued = 0, chunk = 2;
     while (!done && issued < max_k + 1) {
       for (int k = 0; k < chunk && issued < max_k + 1; ++k, ++issued) {
-        k_pcg_q<NB><<<rg, kNT, 0, s>>>(P, G, N, R);
-        k_pcg_update<<<rg, kNT, 0, s>>>(P, R);
-        k_pcg_p<<<rg, kNT, 0, s>>>(P, R);
+        {
+          ProfScope ps(model_->prof, "pcg_q", s);
+          k_pcg_q<NB><<<rg, kNT, 0, s>>>(P, G, N, R); count_launch();
+        }
+        {
+          ProfScope ps(model_->prof, "pcg_update", s);
+          k_pcg_update<<<rg, kNT, 0, s>>>(P, R); count_launch();
+        }
+        {
+          ProfScope ps(model_->prof, "pcg_p", s);
+          k_pcg_p<<<rg, kNT, 0, s>>>(P, R); count_launch();
+        }
       }
       PG_LAUNCH_CHECK();
       int active = 0;
@@ -1215,7 +1238,7 @@ public:
       done = !active;
       chunk = std::min(chunk * 2, 16);
     }
-    k_pcg_apply<<<eg, 256, 0, s>>>(P, G, R);
+    k_pcg_apply<<<eg, 256, 0, s>>>(P, G, R); count_launch();
     PG_LAUNCH_CHECK();
   }
   void pcg(Nhood &nh, cudaStream_t s) {
