@@ -154,9 +154,10 @@ def max_over_ranks(dist, v):
     return float(t.item())
 
 
-def timed_steps(d, loop, K, stats):
-    """K steps bracketed by CUDA events recorded on the model's stream (the
-    stream every kernel of the step is launched on)."""
+def timed_steps(d, loop, K):
+    """K quiet steps (no host round trip inside a step) bracketed by CUDA
+    events recorded on the model's stream (the stream every kernel of the
+    step is launched on)."""
     import torch
 
     from prtcl_gb300 import _lib
@@ -168,41 +169,52 @@ def timed_steps(d, loop, K, stats):
     e0.record(s)
     t0 = time.perf_counter()
     for _ in range(K):
-        stats.append(loop.step())
+        loop.step(quiet=True)
     e1.record(s)
     e1.synchronize()
     wall = time.perf_counter() - t0
+    d.synchronize()
     launches = _lib.load().prtcl_gpu_launch_count() - l0
     return e0.elapsed_time(e1) / 1e3, wall, launches
 
 
-def run_ours(args, rank, world, dist):
-    import ctypes as C
+def workload(args):
+    if args.config == "1m":
+        return scenes.dam_break_1m(), driver.DAM_BREAK_1M
+    return scenes.dam_break(), dict(driver.DAM_BREAK_27K, viscosity=True)
 
+
+def run_ours(args, rank, world, dist):
     from prtcl_gb300.core import DeviceScene
-    sc = scenes.dam_break_1m() if args.config == "1m" else scenes.dam_break()
-    p = driver.DAM_BREAK_1M if args.config == "1m" else dict(driver.DAM_BREAK_27K, viscosity=True)
+    sc, p = workload(args)
     nf, nb = len(sc["fluid"]), len(sc["boundary"])
 
     d = DeviceScene()
     driver.setup_dam_break(d, sc, p)
-    loop = driver.StepLoop(d, p)
+    loop = driver.StepLoop(d, p, device_loop=True)
     for _ in range(args.warmup):
-        loop.step()
-    d.model.profile(True)
-    d.model.profile_reset()
+        loop.step(quiet=True)
+    d.model.stats(reset=True)
     clocks = Clocks()
     barrier(dist)
     clocks.start()
-    stats = []
-    secs, wall, launches = timed_steps(d, loop, args.steps, stats)
+    secs, wall, launches = timed_steps(d, loop, args.steps)
     clk = clocks.stop()
-    prof = d.model.profile_read()
-    d.model.profile(False)
+    st = d.model.stats(reset=True)
     secs = max_over_ranks(dist, secs)
     value = nf * args.steps * world / secs
 
-    # dominant kernel and its roofline
+    # per-kernel CUDA-event timing, live in this process: a few more steps
+    # with timing events around every launch (device loops driven from the
+    # host so that each launch is timed; same kernels)
+    d.model.profile(True)
+    d.model.profile_reset()
+    for _ in range(args.profile_steps):
+        loop.step(quiet=True)
+    d.synchronize()
+    prof = d.model.profile_read()
+    d.model.profile(False)
+
     peak, peak_kind = load_peaks()
     top = max(prof.items(), key=lambda kv: kv[1][1]) if prof else None
     roof = None
@@ -213,12 +225,13 @@ def run_ours(args, rank, world, dist):
         avg_s = ms / 1e3 / cnt
         ach = per_launch / avg_s / 1e9
         tr = load_traffic().get(name)
+        total_ms = sum(m for _, m in prof.values())
         roof = {"bound": "hbm", "kernel": name, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "traffic": tr, "peak_kind": peak_kind,
                 "algorithmic_bytes_per_launch": per_launch, "avg_launch_us": round(avg_s * 1e6, 2),
-                "launches": cnt, "share_of_step": round(ms / (secs * 1e3), 4)}
+                "launches": cnt, "share_of_kernel_time": round(ms / total_ms, 4),
+                "timing": f"CUDA events around each launch over {args.profile_steps} extra steps"}
 
-    # end to end through the C ABI with host buffers
     e2e = None
     if not args.no_e2e:
         e2e = run_e2e(args, sc, p, nf, dist, world)
@@ -227,8 +240,7 @@ def run_ours(args, rank, world, dist):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(sc, p, nf, steps=args.cpu_steps)
 
-    jac = [s["jacobi_iterations"] for s in stats]
-    pcg = [s["pcg_iterations"] for s in stats]
+    solves = max(st["jacobi_solves"], 1.0)
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(secs * 1e3 / args.steps, 3), "higher_is_better": True,
@@ -239,12 +251,14 @@ def run_ours(args, rank, world, dist):
                    "fluid_particles": nf, "boundary_particles": nb, "replicas": world,
                    "parallelism": "replicas only" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (no flush)",
-                   "jacobi_iterations_mean": float(np.mean(jac)), "jacobi_capped_steps": int(sum(j >= 100 for j in jac)),
-                   "pcg_iterations_mean": float(np.mean(pcg)),
-                   "max_relative_density_error": float(max(s["relative_aprde"] for s in stats)),
+                   "jacobi_iterations_mean": round(st["jacobi_iterations"] / solves, 3),
+                   "jacobi_capped_steps": int(st["jacobi_capped"]),
+                   "max_relative_density_error": st["max_relative_aprde"],
+                   "pcg_iterations_mean": round(st["pcg_iterations"] / max(st["pcg_solves"], 1.0), 3),
                    "wall_s": round(wall, 3)},
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": int(launches),
-        "kernels": {k: {"launches": c, "ms": round(m, 3)} for k, (c, m) in prof.items()},
+        "kernels": {k: {"launches": c, "ms": round(m, 3), "us_per_launch": round(1e3 * m / c, 2)}
+                    for k, (c, m) in prof.items()},
     }
     if rank == 0:
         print(json.dumps(line))
@@ -282,10 +296,10 @@ def run_e2e(args, sc, p, nf, dist, world):
     h2d = 0
     driver.setup_dam_break(d, scene, p)
     h2d += sum(a.nbytes for a in host.values()) + nf * (12 + 12 + 4 + 4) + len(sc["boundary"]) * 4
-    loop = driver.StepLoop(d, p)
+    loop = driver.StepLoop(d, p, device_loop=True)
     posf = d.model.get_group("f").varying.get_field("position")
     for _ in range(args.steps):
-        loop.step()
+        loop.step(quiet=True)
         posf.download(out=frame)
     d.synchronize()
     secs = max_over_ranks(dist, time.perf_counter() - t0)
@@ -320,8 +334,7 @@ def run_reference(args, rank, world, dist):
     from oracle import oracle as O
     O.build()
     th = O.set_threads(0)
-    sc = scenes.dam_break_1m() if args.config == "1m" else scenes.dam_break()
-    p = driver.DAM_BREAK_1M if args.config == "1m" else dict(driver.DAM_BREAK_27K, viscosity=True)
+    sc, p = workload(args)
     nf = len(sc["fluid"])
     o = O.Scene(np.float32, fp64_reductions=False)
     driver.setup_dam_break(o, sc, p)
@@ -359,6 +372,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--profile-steps", type=int, default=3)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

@@ -40,8 +40,10 @@ const char *prtcl_gpu_last_error(void);
 /* Library version string. */
 const char *prtcl_gpu_version(void);
 
-/* Number of CUDA kernels this library has launched in this process (no
- * counterpart in the reference; used to account for device work). */
+/* Number of CUDA kernels this library has launched in this process,
+ * including the kernels its device-side loops (CUDA graphs) executed; call
+ * after the work has completed (no counterpart in the reference; used to
+ * account for device work). */
 uint64_t prtcl_gpu_launch_count(void);
 
 /* ---- model: replaces prtcl::Model (data/model.hpp, data/model.cpp:13-34) ---- */
@@ -93,6 +95,18 @@ int prtcl_gpu_global_add(prtcl_gpu_model *model, const char *field, const char *
                          const int32_t *extents);
 int prtcl_gpu_global_set(prtcl_gpu_model *model, const char *field, const void *value);
 int prtcl_gpu_global_get(prtcl_gpu_model *model, const char *field, void *value);
+/* Stream-ordered set of a global field of at most 64 bytes: returns without
+ * waiting; the value is applied in `stream` order (NULL: the model's
+ * stream).  For per-step values such as current_time. */
+int prtcl_gpu_global_set_async(prtcl_gpu_model *model, const char *field, const void *value, void *stream);
+
+/* Statistics of the device-side loops since the last reset (no counterpart
+ * in the reference, whose script prints the iteration counts per step):
+ * out[0] Jacobi solves, [1] Jacobi iterations, [2] solves stopped at the
+ * iteration cap, [3] largest final aprde / nprde, [4] PCG solves, [5] PCG
+ * iterations, [6] PCG solves stopped by the iteration limit.  Waits for the
+ * model's stream; `reset` != 0 zeroes them afterwards. */
+int prtcl_gpu_model_stats(prtcl_gpu_model *model, double *out, int32_t n, int32_t reset);
 
 /* Types of uniform and global fields (ctype_out >= 4 bytes, extents_out[2]). */
 int prtcl_gpu_uniform_info(prtcl_gpu_model *model, const char *group, const char *field, char *ctype_out,

@@ -686,6 +686,30 @@ template <class T> struct Scene : SceneBase {
     }
   }
 
+  // iisph.solve_pressure: the relaxed-Jacobi loop of the driver script
+  // (share/scripts/prtcl-lua.example.lua:409-420) as one procedure: at least
+  // two iterations, stop when aprde / nprde < iisph_maximum_density_error or
+  // after iisph_maximum_iterations; writes iisph_iterations
+  void iisph_solve_pressure() {
+    int64_t maxit = int64_t(gl("iisph_maximum_iterations", 1)[0]);
+    double eta = double(static_cast<T>(gl("iisph_maximum_density_error", 1)[0]));
+    if (maxit <= 0) maxit = 100;
+    if (!(eta > 0)) eta = double(static_cast<T>(1e-3));
+    double nprde = gl("iisph_nprde", 1)[0];
+    int64_t it = 0;
+    if (nprde >= 1) {
+      for (it = 1; it <= maxit; ++it) {
+        gl("iisph_aprde", 1)[0] = 0.0;
+        iisph_iteration_pressure_acceleration();
+        iisph_iteration_pressure();
+        double rel = gl("iisph_aprde", 1)[0] / nprde;
+        if (it >= 2 && rel < eta) break;
+      }
+      if (it > maxit) it = maxit;
+    }
+    gl("iisph_iterations", 1)[0] = double(it);
+  }
+
   void run(std::string const &scheme, std::string const &proc) override {
     if (scheme == "density" && proc == "compute_density") return density_compute_density();
     if (scheme == "aiast12" && proc == "compute_volume") return aiast12_compute_volume();
@@ -696,6 +720,7 @@ template <class T> struct Scene : SceneBase {
     if (scheme == "iisph" && proc == "setup") return iisph_setup();
     if (scheme == "iisph" && proc == "iteration_pressure_acceleration") return iisph_iteration_pressure_acceleration();
     if (scheme == "iisph" && proc == "iteration_pressure") return iisph_iteration_pressure();
+    if (scheme == "iisph" && proc == "solve_pressure") return iisph_solve_pressure();
     if (scheme == "wkbb18" && proc == "compute_diagonal") return wkbb18_compute_diagonal();
     if (scheme == "wkbb18" && proc == "accumulate_acceleration") return wkbb18_accumulate_acceleration();
     throw std::runtime_error("procedure does not exist: " + scheme + "." + proc);

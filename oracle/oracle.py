@@ -138,7 +138,7 @@ class Scene:
         _check(lib().oracle_get_uniform(self._h, _b(group), _b(name), v.ctypes.data_as(C.POINTER(C.c_double)), n))
         return v if n > 1 else float(v[0])
 
-    def set_global(self, name, value):
+    def set_global(self, name, value, asynchronous=False):
         v = np.atleast_1d(np.asarray(value, dtype=np.float64))
         _check(lib().oracle_set_global(self._h, _b(name), v.ctypes.data_as(C.POINTER(C.c_double)), v.size))
 

@@ -58,6 +58,8 @@ SIGNATURES = {
     "prtcl_gpu_global_add": [vp, cp, cp, i32, i32p],
     "prtcl_gpu_global_set": [vp, cp, vp],
     "prtcl_gpu_global_get": [vp, cp, vp],
+    "prtcl_gpu_global_set_async": [vp, cp, vp, vp],
+    "prtcl_gpu_model_stats": [vp, C.POINTER(C.c_double), i32, i32],
     "prtcl_gpu_uniform_info": [vp, cp, cp, C.c_char_p, i32p, i32p],
     "prtcl_gpu_global_info": [vp, cp, C.c_char_p, i32p, i32p],
     "prtcl_gpu_model_stream": [vp, pp],

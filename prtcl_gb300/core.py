@@ -55,6 +55,7 @@ class _Value:
 
     def __init__(self, model, group, name):
         self._m, self._g, self._n = model, group, name
+        self._type = None
 
     def _info(self):
         ct = C.create_string_buffer(8)
@@ -79,14 +80,17 @@ class _Value:
             return out[0].item()
         return out.reshape(shape, order="F")
 
-    def set(self, value):
-        dt, shape = self._info()
+    def set(self, value, asynchronous=False, stream=None):
+        dt, shape = self._info() if self._type is None else self._type
+        self._type = (dt, shape)
         a = np.asarray(value, dtype=dt)
         if a.size != max(1, int(np.prod(shape))):
             raise PrtclGpuError(f"value of size {a.size} for field {self._n} of shape {shape}")
         a = np.ascontiguousarray(a.reshape(-1, order="F"))
         L = load()
-        if self._g is None:
+        if self._g is None and asynchronous:
+            check(L.prtcl_gpu_global_set_async(self._m._h, b(self._n), a.ctypes.data, _stream(stream)))
+        elif self._g is None:
             check(L.prtcl_gpu_global_set(self._m._h, b(self._n), a.ctypes.data))
         else:
             check(L.prtcl_gpu_uniform_set(self._m._h, b(self._g), b(self._n), a.ctypes.data))
@@ -245,6 +249,15 @@ class Model:
 
     def synchronize(self, stream=None):
         check(load().prtcl_gpu_model_synchronize(self._h, _stream(stream)))
+
+    def stats(self, reset=False):
+        """Device-loop statistics since the last reset (see
+        prtcl_gpu_model_stats)."""
+        out = (C.c_double * 7)()
+        check(load().prtcl_gpu_model_stats(self._h, out, 7, 1 if reset else 0))
+        keys = ["jacobi_solves", "jacobi_iterations", "jacobi_capped", "max_relative_aprde",
+                "pcg_solves", "pcg_iterations", "pcg_capped"]
+        return dict(zip(keys, list(out)))
 
     def stream_handle(self):
         """The model's own cudaStream_t as an integer."""
@@ -440,6 +453,7 @@ class DeviceScene:
         self.stream = stream
         self._loaded_for = None
         self._counts = {}
+        self._globals = {}
 
     # ---- model ----
     def add_group(self, name, type_):
@@ -485,11 +499,14 @@ class DeviceScene:
     def get_uniform(self, group, name, n=1):
         return self.model.get_group(group).uniform.get_field(name).get()
 
-    def set_global(self, name, value):
-        if not self.model.global_.has_field(name):
-            ct, sh = self._small_type(value)
-            self.model.global_.add_field(name, ct, sh)
-        self.model.global_.get_field(name).set(value)
+    def set_global(self, name, value, asynchronous=False):
+        f = self._globals.get(name)
+        if f is None:
+            if not self.model.global_.has_field(name):
+                ct, sh = self._small_type(value)
+                self.model.global_.add_field(name, ct, sh)
+            f = self._globals[name] = self.model.global_.get_field(name)
+        f.set(value, asynchronous=asynchronous, stream=self.stream)
 
     def get_global(self, name, n=1):
         return self.model.global_.get_field(name).get()

@@ -22,6 +22,7 @@ struct prtcl_gpu_scheme {
 namespace prtcl_gpu {
 static std::atomic<uint64_t> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void uncount_launches(uint64_t n) { g_launches.fetch_sub(n, std::memory_order_relaxed); }
 uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 } // namespace prtcl_gpu
 
@@ -108,7 +109,7 @@ extern "C" {
 
 const char *prtcl_gpu_last_error(void) { return g_last_error.c_str(); }
 const char *prtcl_gpu_version(void) { return "prtcl_gb300 0.1 (sm_103a)"; }
-uint64_t prtcl_gpu_launch_count(void) { return launch_count(); }
+uint64_t prtcl_gpu_launch_count(void) { return launch_count() + device_loop_kernels(); }
 
 int prtcl_gpu_model_create(prtcl_gpu_model **out) {
   NEED(out);
@@ -247,6 +248,23 @@ int prtcl_gpu_global_set(prtcl_gpu_model *model, const char *field, const void *
   NEED(field);
   NEED(value);
   return guard([&] { model->m.small_set(global(model->m, field), value, model->m.stream()); });
+}
+int prtcl_gpu_global_set_async(prtcl_gpu_model *model, const char *field, const void *value, void *stream) {
+  NEED(model);
+  NEED(field);
+  NEED(value);
+  return guard([&] { model->m.small_set_async(global(model->m, field), value, model->m.pick(stream)); });
+}
+int prtcl_gpu_model_stats(prtcl_gpu_model *model, double *out, int32_t n, int32_t reset) {
+  NEED(model);
+  if (n > 0) NEED(out);
+  return guard([&] {
+    double st[16];
+    PG_CUDA(cudaMemcpyAsync(st, model->m.stats_d, sizeof st, cudaMemcpyDeviceToHost, model->m.stream()));
+    PG_CUDA(cudaStreamSynchronize(model->m.stream()));
+    for (int i = 0; i < n && i < 16; ++i) out[i] = st[i];
+    if (reset) model->m.stats_reset(model->m.stream());
+  });
 }
 int prtcl_gpu_global_get(prtcl_gpu_model *model, const char *field, void *value) {
   NEED(model);

@@ -36,9 +36,13 @@ constexpr int kMaxNbrGroups = 4;  // fluid / boundary groups a procedure sums ov
 
 inline unsigned div_up(size_t a, size_t b) { return unsigned((a + b - 1) / b); }
 
-// number of kernels this library has launched (process-wide)
+// number of kernels this library has launched from the host (process-wide)
 uint64_t launch_count();
 void count_launch();
+void uncount_launches(uint64_t n);
+// kernels executed inside device-side loops (CUDA graph bodies); reads a
+// device counter
+uint64_t device_loop_kernels();
 
 // ---------------------------------------------------------------------------
 // FP32 vector helpers in the reference's evaluation order
@@ -87,6 +91,18 @@ inline KernelParams make_kernel_params(float h) {
   return k;
 }
 
+// the kernel parameters for smoothing scale h, computed on the device with
+// the same operations as the reference's constpow
+__device__ __forceinline__ KernelParams kparams(float h) {
+  KernelParams k;
+  k.h = h;
+  k.h3 = (h * h) * h;
+  k.h4 = ((h * h) * h) * h;
+  k.sigma = 0.0795774715459476678844418816862571810f; // 1/(4 pi) rounded to f32
+  k.eps = 3.4526698300124390840e-04f;                 // sqrt(FLT_EPSILON)
+  return k;
+}
+
 __device__ __forceinline__ float k_evalq(KernelParams const &k, float q) {
   float result = 0.0f;
   if (q < 1.0f) {
@@ -120,6 +136,21 @@ __device__ __forceinline__ f3 kgradW(KernelParams const &k, f3 v) {
   if (r < k.eps) return {0.0f, 0.0f, 0.0f};
   float dr = -copysignf(k_evaldq(k, fabsf(r) / k.h) / k.h4, r);
   return scl3(dr / r, v);
+}
+
+// The scalar factor of kgradW for a pair with squared distance d2:
+// gradW(v) = factor * v.  +0.0 encodes the exactly-zero gradient below eps;
+// any other factor is <= -0.0, so the encoding is unique.
+__device__ __forceinline__ float kgrad_factor(KernelParams const &k, float d2) {
+  float r = sqrtf(d2);
+  if (r < k.eps) return 0.0f;
+  float dr = -copysignf(k_evaldq(k, fabsf(r) / k.h) / k.h4, r);
+  return dr / r;
+}
+// gradW from a cached factor, bit-identical to kgradW(k, v)
+__device__ __forceinline__ f3 kgrad_from(float factor, f3 v) {
+  if (__float_as_uint(factor) == 0u) return {0.0f, 0.0f, 0.0f};
+  return scl3(factor, v);
 }
 
 // ---------------------------------------------------------------------------

@@ -209,6 +209,8 @@ void Group::resize(size_t n, cudaStream_t s) {
   model_->layout_version++;
 }
 
+// Gathers into scratch and copies back, so that field pointers stay stable
+// (captured CUDA graphs and bound kernels keep working after a permute).
 void Group::permute(uint32_t const *perm, cudaStream_t s) {
   size_t n = count;
   if (n == 0) return;
@@ -229,10 +231,114 @@ void Group::permute(uint32_t const *perm, cudaStream_t s) {
                                                         perm, n, words); count_launch();
     }
     PG_LAUNCH_CHECK();
-    PG_CUDA(cudaFreeAsync(f.d, s));
-    f.d = nd;
+    size_t bytes = f.type.is_vec3() ? f.cap * 16 : f.cap * f.type.host_item_bytes();
+    PG_CUDA(cudaMemcpyAsync(f.d, nd, bytes, cudaMemcpyDeviceToDevice, s));
+    PG_CUDA(cudaFreeAsync(nd, s));
     f.version++;
   }
+}
+
+// ---------------------------------------------------------------------------
+// packed neighbour records
+// ---------------------------------------------------------------------------
+
+__global__ void k_pack_xs(float4 const *__restrict__ x, float const *__restrict__ sc, float4 *__restrict__ out, size_t n) {
+  size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (i < n) {
+    float4 v = x[i];
+    v.w = sc[i];
+    out[i] = v;
+  }
+}
+// x and m / rho (the ratio the viscosity sums use, computed as m_j / rho_j)
+__global__ void k_pack_xmr(float4 const *__restrict__ x, float const *__restrict__ m, float const *__restrict__ rho,
+                           float4 *__restrict__ out, size_t n) {
+  size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (i < n) {
+    float4 v = x[i];
+    v.w = m[i] / rho[i];
+    out[i] = v;
+  }
+}
+// p / (rho rho), the pressure term of the pressure acceleration
+__global__ void k_pack_pr(float const *__restrict__ p, float const *__restrict__ rho, float *__restrict__ out, size_t n) {
+  size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (i < n) {
+    float r = rho[i];
+    out[i] = p[i] / (r * r);
+  }
+}
+
+void *Model::pack_buffer(Group *g, std::string const &kind, size_t item_bytes, std::vector<uint64_t> const &key,
+                         bool &stale, cudaStream_t s) {
+  PackEntry &e = packs_[{g, kind}];
+  size_t n = std::max<size_t>(g->count, 1);
+  if (e.cap < n || e.item_bytes != item_bytes) {
+    if (e.d) PG_CUDA(cudaFreeAsync(e.d, s));
+    PG_CUDA(cudaMallocAsync(&e.d, n * item_bytes, s));
+    e.cap = n;
+    e.item_bytes = item_bytes;
+    e.key.clear();
+  }
+  stale = e.key != key;
+  return e.d;
+}
+
+void Model::pack_commit(Group *g, std::string const &kind, std::vector<uint64_t> const &key) {
+  packs_[{g, kind}].key = key;
+}
+
+static std::vector<uint64_t> vkey(std::initializer_list<VaryingField const *> fs, size_t n) {
+  std::vector<uint64_t> k{uint64_t(n)};
+  for (auto *f : fs) {
+    k.push_back(reinterpret_cast<uint64_t>(f->d));
+    k.push_back(f->version);
+  }
+  return k;
+}
+
+float4 const *Model::packed_xs(Group *g, VaryingField *x, VaryingField *sc, char const *kind, cudaStream_t s) {
+  auto key = vkey({x, sc}, g->count);
+  bool stale = false;
+  auto *out = static_cast<float4 *>(pack_buffer(g, kind, 16, key, stale, s));
+  if (stale && g->count) {
+    k_pack_xs<<<div_up(g->count, 256), 256, 0, s>>>(static_cast<float4 const *>(x->d), static_cast<float const *>(sc->d),
+                                                    out, g->count); count_launch();
+    PG_LAUNCH_CHECK();
+  }
+  pack_commit(g, kind, key);
+  return out;
+}
+
+float4 const *Model::packed_xmr(Group *g, VaryingField *x, VaryingField *m, VaryingField *rho, cudaStream_t s) {
+  auto key = vkey({x, m, rho}, g->count);
+  bool stale = false;
+  auto *out = static_cast<float4 *>(pack_buffer(g, "xmr", 16, key, stale, s));
+  if (stale && g->count) {
+    k_pack_xmr<<<div_up(g->count, 256), 256, 0, s>>>(static_cast<float4 const *>(x->d), static_cast<float const *>(m->d),
+                                                     static_cast<float const *>(rho->d), out, g->count); count_launch();
+    PG_LAUNCH_CHECK();
+  }
+  pack_commit(g, "xmr", key);
+  return out;
+}
+
+float *Model::pr_buffer(Group *g, cudaStream_t s) {
+  bool stale = false;
+  return static_cast<float *>(pack_buffer(g, "pr", 4, {}, stale, s));
+}
+
+float const *Model::packed_pr(Group *g, VaryingField *p, VaryingField *rho, cudaStream_t s) {
+  auto key = vkey({p, rho}, g->count);
+  bool stale = false;
+  auto *out = static_cast<float *>(pack_buffer(g, "pr", 4, key, stale, s));
+  if (stale && g->count) {
+    k_pack_pr<<<div_up(g->count, 256), 256, 0, s>>>(static_cast<float const *>(p->d), static_cast<float const *>(rho->d),
+                                                    out, g->count); count_launch();
+    PG_LAUNCH_CHECK();
+  }
+  pack_commit(g, "pr", key);
+  return out;
 }
 
 // ---------------------------------------------------------------------------
@@ -251,10 +357,15 @@ Model::Model() {
   PG_CUDA(cudaMemset(scalars_d, 0, 64 * sizeof(double)));
   PG_CUDA(cudaMalloc(&status_d, 16 * sizeof(int)));
   PG_CUDA(cudaMemset(status_d, 0, 16 * sizeof(int)));
+  PG_CUDA(cudaMalloc(&stats_d, 16 * sizeof(double)));
+  stats_reset(stream_);
+  PG_CUDA(cudaStreamSynchronize(stream_));
 }
 
 Model::~Model() {
   cudaStreamSynchronize(stream_);
+  for (auto &kv : packs_)
+    if (kv.second.d) cudaFree(kv.second.d);
   for (auto &g : groups_)
     for (auto &kv : g.second->varying)
       if (kv.second.d) cudaFree(kv.second.d);
@@ -263,6 +374,7 @@ Model::~Model() {
   cudaFree(red_count_d);
   cudaFree(scalars_d);
   cudaFree(status_d);
+  cudaFree(stats_d);
   cudaStreamDestroy(stream_);
 }
 
@@ -330,6 +442,35 @@ SmallField *Model::find_global(std::string const &name) {
 void Model::small_set(SmallField const &f, void const *host, cudaStream_t s) {
   PG_CUDA(cudaMemcpyAsync(small_ptr(f), host, f.type.host_item_bytes(), cudaMemcpyHostToDevice, s));
   PG_CUDA(cudaStreamSynchronize(s));
+}
+
+struct Words16 {
+  uint32_t w[16];
+};
+__global__ void k_set_words(uint32_t *dst, Words16 v, int n) {
+  int i = threadIdx.x;
+  if (i < n) dst[i] = v.w[i];
+}
+
+void Model::small_set_async(SmallField const &f, void const *host, cudaStream_t s) {
+  size_t bytes = f.type.host_item_bytes();
+  if (bytes > sizeof(Words16)) {
+    small_set(f, host, s);
+    return;
+  }
+  Words16 v{};
+  std::memcpy(v.w, host, bytes);
+  k_set_words<<<1, 32, 0, s>>>(static_cast<uint32_t *>(small_ptr(f)), v, int(bytes / 4)); count_launch();
+  PG_LAUNCH_CHECK();
+}
+
+__global__ void k_stats_reset(double *st) {
+  int i = threadIdx.x;
+  if (i < 16) st[i] = (i == 3) ? -INFINITY : 0.0;
+}
+void Model::stats_reset(cudaStream_t s) {
+  k_stats_reset<<<1, 32, 0, s>>>(stats_d); count_launch();
+  PG_LAUNCH_CHECK();
 }
 
 void Model::small_get(SmallField const &f, void *host, cudaStream_t s) {

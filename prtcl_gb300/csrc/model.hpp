@@ -104,6 +104,9 @@ public:
   SmallField &alloc_small(SmallField &f, FieldType const &t);
   void *small_ptr(SmallField const &f) const { return arena_d_ + f.offset; }
   void small_set(SmallField const &f, void const *host, cudaStream_t s);
+  // stream-ordered set (the value travels as a kernel parameter; no host
+  // synchronisation, capturable in a CUDA graph)
+  void small_set_async(SmallField const &f, void const *host, cudaStream_t s);
   void small_get(SmallField const &f, void *host, cudaStream_t s);
 
   cudaStream_t stream() const { return stream_; }
@@ -118,9 +121,37 @@ public:
   unsigned *red_count_d = nullptr; // last-block tickets
   double *scalars_d = nullptr;   // 64 FP64 solver scalars
   int *status_d = nullptr;       // 16 status words (error flags, iteration counts)
+  // device-loop statistics (accumulated by the loop control kernels):
+  // 0 Jacobi solves, 1 Jacobi iterations, 2 solves stopped at the cap,
+  // 3 largest final aprde / nprde, 4 PCG solves, 5 PCG iterations,
+  // 6 PCG solves stopped by the iteration limit
+  double *stats_d = nullptr;
+  void stats_reset(cudaStream_t s);
   Profiler prof;                 // optional per-kernel CUDA-event timing
 
+  // Packed per-particle records gathered by the neighbour sweeps, rebuilt
+  // only when one of their source fields changed (keyed on the fields'
+  // pointers and versions):
+  //   packed_xs  (x, y, z, s)       e.g. position + mass, position + volume
+  //   packed_xmr (x, y, z, m / rho)
+  //   packed_pr  p / (rho rho)
+  float4 const *packed_xs(Group *g, VaryingField *x, VaryingField *s, char const *kind, cudaStream_t st);
+  float4 const *packed_xmr(Group *g, VaryingField *x, VaryingField *m, VaryingField *rho, cudaStream_t st);
+  float const *packed_pr(Group *g, VaryingField *p, VaryingField *rho, cudaStream_t st);
+  // the buffer behind packed_pr, for kernels that write p and p / rho^2
+  // together; pack_commit() marks it current for a key
+  float *pr_buffer(Group *g, cudaStream_t st);
+  void pack_commit(Group *g, std::string const &kind, std::vector<uint64_t> const &key);
+
 private:
+  struct PackEntry {
+    void *d = nullptr;
+    size_t cap = 0, item_bytes = 0;
+    std::vector<uint64_t> key;
+  };
+  std::map<std::pair<Group *, std::string>, PackEntry> packs_;
+  void *pack_buffer(Group *g, std::string const &kind, size_t item_bytes, std::vector<uint64_t> const &key, bool &stale,
+                    cudaStream_t s);
   std::map<std::string, std::unique_ptr<Group>> groups_;
   std::map<std::string, SmallField> global_;
   char *arena_d_ = nullptr;

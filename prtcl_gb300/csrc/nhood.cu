@@ -331,6 +331,7 @@ __global__ void k_xsorted(PosTable pt, uint32_t const *vals, size_t N, float4 *x
 
 struct ListOut {
   uint32_t *idx[kMaxGroups];
+  float *gf[kMaxGroups];
   uint32_t cap[kMaxGroups];
   uint32_t *cnt; // [G][n]
   uint32_t *maxcnt; // [kMaxGroups]
@@ -339,7 +340,8 @@ struct ListOut {
 };
 
 __device__ __forceinline__ void visit_cell(GridView const &gv, float4 const *__restrict__ xs, int cell, f3 xi,
-                                           uint32_t i, ListOut const &lo, uint32_t *c) {
+                                           uint32_t i, ListOut const &lo, uint32_t *c, KernelParams const &K,
+                                           bool with_gf) {
   if (cell < 0) return;
   int s0 = gv.cell_start[cell], s1 = gv.cell_start[cell + 1];
   for (int s = s0; s < s1; ++s) {
@@ -349,15 +351,22 @@ __device__ __forceinline__ void visit_cell(GridView const &gv, float4 const *__r
       uint32_t h = __float_as_uint(xj.w);
       uint32_t g = h >> 28, j = h & 0x0FFFFFFFu;
       uint32_t k = c[g]++;
-      if (k < lo.cap[g]) lo.idx[g][size_t(k) * lo.n + i] = j;
+      if (k < lo.cap[g]) {
+        size_t o = size_t(k) * lo.n + i;
+        lo.idx[g][o] = j;
+        if (with_gf) lo.gf[g][o] = kgrad_factor(K, d2);
+      }
     }
   }
 }
 
 // neighbour lists of one query group (grid query of util/grouped_uniform_grid.hpp:407-531)
 __global__ void k_build_lists(GridView gv, float4 const *__restrict__ xs, float4 const *__restrict__ qpos, int q,
-                              ListOut lo) {
+                              ListOut lo, float const *hp, float *hcache) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool with_gf = hp != nullptr;
+  KernelParams K = kparams(with_gf ? *hp : 1.0f);
+  if (i == 0) *hcache = with_gf ? K.h : __int_as_float(0x7fc00000);
   if (i >= lo.n) return;
   uint32_t c[kMaxGroups];
 #pragma unroll
@@ -375,14 +384,14 @@ __global__ void k_build_lists(GridView gv, float4 const *__restrict__ xs, float4
     fallback = cell < 0;
   }
   if (!fallback) {
-    visit_cell(gv, xs, cell, xi, i, lo, c);
-    for (int k = 0; k < 26; ++k) visit_cell(gv, xs, gv.cell_adj[size_t(cell) * 26 + k], xi, i, lo, c);
+    visit_cell(gv, xs, cell, xi, i, lo, c, K, with_gf);
+    for (int k = 0; k < 26; ++k) visit_cell(gv, xs, gv.cell_adj[size_t(cell) * 26 + k], xi, i, lo, c, K, with_gf);
   } else {
     for (int k = 0; k < 13; ++k) {
       int3 p = make_int3(gi.x + c_offsets[k][0], gi.y + c_offsets[k][1], gi.z + c_offsets[k][2]);
-      visit_cell(gv, xs, find_cell(gv, p), xi, i, lo, c);
+      visit_cell(gv, xs, find_cell(gv, p), xi, i, lo, c, K, with_gf);
       int3 m = make_int3(gi.x - c_offsets[k][0], gi.y - c_offsets[k][1], gi.z - c_offsets[k][2]);
-      visit_cell(gv, xs, find_cell(gv, m), xi, i, lo, c);
+      visit_cell(gv, xs, find_cell(gv, m), xi, i, lo, c, K, with_gf);
     }
   }
   for (int g = 0; g < lo.G; ++g) {
@@ -442,13 +451,16 @@ Nhood::~Nhood() {
 }
 
 void Nhood::free_lists(Lists &L) {
-  for (int g = 0; g < kMaxGroups; ++g)
-    if (L.idx[g]) {
-      cudaFree(L.idx[g]);
-      L.idx[g] = nullptr;
-    }
+  for (int g = 0; g < kMaxGroups; ++g) {
+    if (L.idx[g]) cudaFree(L.idx[g]);
+    if (L.gf[g]) cudaFree(L.gf[g]);
+    L.idx[g] = nullptr;
+    L.gf[g] = nullptr;
+  }
   if (L.cnt) cudaFree(L.cnt);
+  if (L.hcache) cudaFree(L.hcache);
   L.cnt = nullptr;
+  L.hcache = nullptr;
 }
 
 // Neighborhood::Load (util/neighborhood.cpp:67-98): remember each group's
@@ -588,7 +600,7 @@ void Nhood::update(cudaStream_t s) {
   }
   for (int shift = 0; shift < total_bits; shift += 8) {
     k_rs_hist<<<tiles, kRsNT, 0, s>>>(kin, N, shift, hist_, tiles); count_launch();
-    k_scan_single<<<1, 1024, 0, s>>>(hist_, hl); count_launch();
+    exclusive_scan(hist_, hist_, hl, block_sums_, block_sums_cap_, s);
     k_rs_scatter<<<tiles, kRsNT, 0, s>>>(kin, vin, kout, vout, N, shift, hist_, tiles); count_launch();
     PG_LAUNCH_CHECK();
     std::swap(kin, kout);
@@ -621,8 +633,9 @@ std::vector<uint64_t> Nhood::pos_versions() const {
 
 bool Nhood::lists_fresh(Lists const &L) const { return L.epoch == epoch_ && L.pos_versions == pos_versions(); }
 
-void Nhood::build_lists(int q, Lists &L, cudaStream_t s) {
+void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
   int G = int(gg_.size());
+  if (G > 8) throw Error("neighbour lists support at most 8 groups");
   size_t n = gg_[q].g->count;
   // sorted positions with handles, from the current positions
   PosTable pt{};
@@ -632,26 +645,39 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s) {
     k_xsorted<<<div_up(N_, 256), 256, 0, s>>>(pt, sorted_vals_, N_, xsorted_); count_launch();
     PG_LAUNCH_CHECK();
   }
+  if (!L.hcache) PG_CUDA(cudaMalloc(&L.hcache, sizeof(float)));
+  auto alloc_slots = [&](int g, uint32_t want) {
+    if (L.idx[g]) PG_CUDA(cudaFree(L.idx[g]));
+    if (L.gf[g]) PG_CUDA(cudaFree(L.gf[g]));
+    L.idx[g] = nullptr;
+    L.gf[g] = nullptr;
+    if (n > 0) {
+      PG_CUDA(cudaMalloc(&L.idx[g], size_t(want) * n * 4));
+      PG_CUDA(cudaMalloc(&L.gf[g], size_t(want) * n * 4));
+    }
+    L.cap[g] = want;
+  };
   for (int attempt = 0; attempt < 8; ++attempt) {
     if (L.n != n || !L.cnt) {
-      free_lists(L);
+      for (int g = 0; g < kMaxGroups; ++g) {
+        if (L.idx[g]) PG_CUDA(cudaFree(L.idx[g]));
+        if (L.gf[g]) PG_CUDA(cudaFree(L.gf[g]));
+        L.idx[g] = nullptr;
+        L.gf[g] = nullptr;
+        L.cap[g] = 0;
+      }
+      if (L.cnt) PG_CUDA(cudaFree(L.cnt));
+      L.cnt = nullptr;
       L.n = n;
       if (n > 0) PG_CUDA(cudaMalloc(&L.cnt, size_t(G) * n * 4));
-      for (int g = 0; g < G; ++g) L.cap[g] = 0;
     }
-    for (int g = 0; g < G; ++g) {
-      uint32_t want = L.cap[g] ? L.cap[g] : 48u;
-      if (!L.idx[g] || want != L.cap[g]) {
-        if (L.idx[g]) PG_CUDA(cudaFree(L.idx[g]));
-        L.idx[g] = nullptr;
-        if (n > 0) PG_CUDA(cudaMalloc(&L.idx[g], size_t(want) * n * 4));
-        L.cap[g] = want;
-      }
-    }
+    for (int g = 0; g < G; ++g)
+      if (!L.idx[g] || L.cap[g] == 0) alloc_slots(g, L.cap[g] ? L.cap[g] : 48u);
     if (n == 0) break;
     ListOut lo{};
     for (int g = 0; g < G; ++g) {
       lo.idx[g] = L.idx[g];
+      lo.gf[g] = L.gf[g];
       lo.cap[g] = L.cap[g];
     }
     lo.cnt = L.cnt;
@@ -663,37 +689,35 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s) {
     float4 const *qpos = static_cast<float4 const *>(gg_[q].pos->d);
     {
       ProfScope ps(model_->prof, "nhood_lists", s);
-      k_build_lists<<<div_up(n, 128), 128, 0, s>>>(gv, xsorted_, qpos, q, lo); count_launch();
+      k_build_lists<<<div_up(n, 128), 128, 0, s>>>(gv, xsorted_, qpos, q, lo, h, L.hcache); count_launch();
     }
     PG_LAUNCH_CHECK();
     PG_CUDA(cudaMemcpyAsync(stats_h_ + 8, stats_d_ + 8, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     PG_CUDA(cudaStreamSynchronize(s));
     bool grow = false;
-    for (int g = 0; g < std::min(G, 8); ++g)
+    for (int g = 0; g < G; ++g)
       if (stats_h_[8 + g] > L.cap[g]) {
-        uint32_t want = (stats_h_[8 + g] + 15u) / 16u * 16u + 16u;
-        if (L.idx[g]) PG_CUDA(cudaFree(L.idx[g]));
-        L.idx[g] = nullptr;
-        PG_CUDA(cudaMalloc(&L.idx[g], size_t(want) * n * 4));
-        L.cap[g] = want;
+        alloc_slots(g, (stats_h_[8 + g] + 15u) / 16u * 16u + 16u);
         grow = true;
       }
-    if (G > 8) throw Error("neighbour lists support at most 8 groups");
     if (!grow) break;
     list_rebuilds++;
   }
   L.epoch = epoch_;
   L.pos_versions = pos_versions();
+  L.has_gf = h != nullptr;
   L.view = NbrView{};
   for (int g = 0; g < G; ++g) {
     L.view.idx[g] = L.idx[g];
+    L.view.gf[g] = L.gf[g];
     L.view.cnt[g] = L.cnt ? L.cnt + size_t(g) * n : nullptr;
     L.view.cap[g] = L.cap[g];
   }
   L.view.n = uint32_t(n);
+  L.view.hcache = L.hcache;
 }
 
-NbrView const &Nhood::lists(int q, cudaStream_t s) {
+NbrView const &Nhood::lists(int q, cudaStream_t s, float const *h) {
   if (!has_grid_) throw Error("Neighborhood has not been updated");
   if (q < 0 || q >= int(gg_.size())) throw Error("invalid group index");
   Lists &L = lists_[q];
@@ -706,13 +730,19 @@ NbrView const &Nhood::lists(int q, cudaStream_t s) {
         PG_CUDA(cudaMalloc(&L.cnt, gg_.size() * L.n * 4));
         PG_CUDA(cudaMemsetAsync(L.cnt, 0, gg_.size() * L.n * 4, s));
       }
+      if (!L.hcache) {
+        PG_CUDA(cudaMalloc(&L.hcache, sizeof(float)));
+        float nan = std::numeric_limits<float>::quiet_NaN();
+        PG_CUDA(cudaMemcpy(L.hcache, &nan, sizeof(float), cudaMemcpyHostToDevice));
+      }
       L.view = NbrView{};
       for (size_t g = 0; g < gg_.size(); ++g) L.view.cnt[g] = L.cnt ? L.cnt + g * L.n : nullptr;
       L.view.n = uint32_t(L.n);
+      L.view.hcache = L.hcache;
     }
     return L.view;
   }
-  if (!lists_fresh(L)) build_lists(q, L, s);
+  if (!lists_fresh(L) || (h && !L.has_gf)) build_lists(q, L, s, h);
   return L.view;
 }
 

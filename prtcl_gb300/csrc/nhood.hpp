@@ -45,9 +45,13 @@ namespace prtcl_gpu {
 // device view of a neighbour list set of one query group
 struct NbrView {
   uint32_t const *idx[kMaxGroups]; // ELL per neighbour group: idx[g][slot * n + i]
+  float const *gf[kMaxGroups];     // ELL: the pair's kernel-gradient factor (kgrad_factor)
   uint32_t const *cnt[kMaxGroups]; // per neighbour group: count of item i
   uint32_t cap[kMaxGroups];
-  uint32_t n; // query items
+  uint32_t n;            // query items
+  float const *hcache;   // smoothing scale the factors were computed with
+                         // (NaN: no factors); kernels compare it with the
+                         // current smoothing scale and recompute on mismatch
 };
 
 struct KeyInfo {
@@ -87,8 +91,10 @@ public:
   bool loaded() const { return model_ != nullptr; }
   Model *model() const { return model_; }
 
-  // neighbour lists of query group q (rebuilt when stale)
-  NbrView const &lists(int q, cudaStream_t s);
+  // neighbour lists of query group q (rebuilt when stale); with `h` (the
+  // device smoothing scale) the lists also cache each pair's kernel
+  // gradient factor
+  NbrView const &lists(int q, cudaStream_t s, float const *h = nullptr);
 
   // introspection (tests): sizes and host copies of the grid
   size_t sorted_count() const { return N_; }
@@ -114,13 +120,16 @@ private:
     size_t n = 0;
     uint32_t cap[kMaxGroups] = {};
     uint32_t *idx[kMaxGroups] = {};
+    float *gf[kMaxGroups] = {};
     uint32_t *cnt = nullptr; // [G][n]
+    float *hcache = nullptr;
+    bool has_gf = false;
     uint64_t epoch = 0;
     std::vector<uint64_t> pos_versions;
     NbrView view{};
   };
   void ensure_grid_capacity(size_t n);
-  void build_lists(int q, Lists &L, cudaStream_t s);
+  void build_lists(int q, Lists &L, cudaStream_t s, float const *h);
   bool lists_fresh(Lists const &L) const;
   std::vector<uint64_t> pos_versions() const;
   void free_lists(Lists &L);

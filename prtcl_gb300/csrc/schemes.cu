@@ -5,9 +5,19 @@
 // the grid's traversal order, accumulating in FP32 in exactly the operation
 // order of the generated C++ (the file:line cited at each kernel).  With FMA
 // contraction off this reproduces the reference arithmetic per particle.
+//
+// Neighbour data is gathered from packed 16-byte records (position + mass,
+// position + volume, position + m/rho) and the kernel gradient of a pair is
+// rebuilt from the factor cached in the neighbour list; both hold values
+// computed with the same operations as the on-the-fly expressions, so the
+// results stay bit-identical (kernels fall back to the full kernel-gradient
+// evaluation if the smoothing scale changed after the lists were built).
+//
 // Reductions that decide convergence (IISPH density error, PCG dot products)
 // are FP64 with a fixed, batch-independent order: per-block tree sums, then
-// the last block of the launch sums the block partials.
+// the last block of the launch sums the block partials.  The relaxed-Jacobi
+// loop (iisph.solve_pressure) and the PCG loop run on the device as CUDA
+// graphs with a conditional while node: no host round trip per iteration.
 #include "schemes.hpp"
 
 #include <algorithm>
@@ -15,10 +25,20 @@
 
 namespace prtcl_gpu {
 
+// kernels executed by device-side loops (graph bodies); read by the host
+// through launch_count()
+__device__ unsigned long long g_loop_kernels = 0;
+
 namespace {
 
-constexpr int kNT = 128;           // threads per block for particle kernels
+constexpr int kNT = 128;            // threads per block for particle kernels
 constexpr int kMaxRedBlocks = 4096; // block partials per reduced value
+
+// model scratch layout
+constexpr int kSPcg = 0;     // scalars[0..7]: PCG
+constexpr int kSJacobi = 16; // scalars[16]: FP64 density error
+constexpr int kStPcgIter = 0, kStPcgActive = 1, kStPcgBody = 2;
+constexpr int kStJacIter = 4, kStJacDone = 5;
 
 // ---------------------------------------------------------------------------
 // argument structs
@@ -26,29 +46,28 @@ constexpr int kMaxRedBlocks = 4096; // block partials per reduced value
 
 struct NbrList {
   uint32_t const *idx; // ELL, idx[slot * n + i]
+  float const *gf;     // ELL, cached kernel-gradient factor of the pair
   uint32_t const *cnt; // count per query item
 };
 
 struct FluidN {
   NbrList L;
-  float4 const *x;
-  float4 const *v;
-  float4 const *a;
-  float const *m;
-  float const *rho;
-  float const *p;
+  float4 const *xm; // (x, y, z, m)
+  float4 const *v;  // velocity
+  float4 const *a;  // acceleration
+  float const *pr;  // p / (rho rho)
 };
 
 struct BoundN {
   NbrList L;
-  float4 const *x;
-  float const *V;
-  float const *mu; // uniform dynamic_viscosity (wkbb18)
+  float4 const *xV; // (x, y, z, V)
+  float const *mu;  // uniform dynamic_viscosity (wkbb18)
 };
 
 template <int NF, int NB> struct Nbrs {
   FluidN f[NF > 0 ? NF : 1];
   BoundN b[NB > 0 ? NB : 1];
+  float const *hcache; // smoothing scale of the cached gradient factors
 };
 
 struct Globals {
@@ -61,6 +80,9 @@ struct Globals {
   int *nprde;
   float const *gravity; // 3 floats
   float *max_speed;
+  int const *jac_max;   // iisph_maximum_iterations
+  float const *jac_eta; // iisph_maximum_density_error
+  int *jac_iters;       // iisph_iterations
 };
 
 struct Red {
@@ -68,19 +90,19 @@ struct Red {
   unsigned *ticket;
   double *scalars;
   int *status;
+  double *stats; // device-loop statistics (Model::stats_d)
 };
 
-__device__ __forceinline__ KernelParams kparams(float h) {
-  KernelParams k;
-  k.h = h;
-  k.h3 = (h * h) * h;
-  k.h4 = ((h * h) * h) * h;
-  k.sigma = 0.0795774715459476678844418816862571810f; // 1/(4 pi), see make_kernel_params
-  k.eps = 3.4526698300124390840e-04f;
-  return k;
-}
-
 __device__ __forceinline__ uint32_t grid_tid() { return blockIdx.x * blockDim.x + threadIdx.x; }
+
+// the pair's kernel gradient: from the cached factor when the lists were
+// built with the current smoothing scale, else evaluated in full
+__device__ __forceinline__ f3 pair_grad(bool cached, NbrList const &L, size_t o, KernelParams const &K, f3 xij) {
+  return cached ? kgrad_from(L.gf[o], xij) : kgradW(K, xij);
+}
+template <class N> __device__ __forceinline__ bool use_cache(N const &nb, KernelParams const &K) {
+  return *nb.hcache == K.h;
+}
 
 // FP64 block sums of NV values, committed by the last block of the launch.
 // Returns true in the last block; out[] is valid in its thread 0.
@@ -127,18 +149,20 @@ __global__ void __launch_bounds__(kNT) k_density(uint32_t n, float4 const *__res
   for (int q = 0; q < NF; ++q) {
     FluidN const &F = N.f[q];
     uint32_t c = F.L.cnt[i];
+#pragma unroll 4
     for (uint32_t k = 0; k < c; ++k) {
-      uint32_t j = F.L.idx[size_t(k) * n + i];
-      acc += F.m[j] * kW(K, sub3(xi, mk3(F.x[j])));
+      float4 xm = F.xm[F.L.idx[size_t(k) * n + i]];
+      acc += xm.w * kW(K, sub3(xi, mk3(xm)));
     }
   }
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
     uint32_t c = B.L.cnt[i];
+#pragma unroll 4
     for (uint32_t k = 0; k < c; ++k) {
-      uint32_t j = B.L.idx[size_t(k) * n + i];
-      acc += (B.V[j] * rho0) * kW(K, sub3(xi, mk3(B.x[j])));
+      float4 xv = B.xV[B.L.idx[size_t(k) * n + i]];
+      acc += (xv.w * rho0) * kW(K, sub3(xi, mk3(xv)));
     }
   }
   rho[i] = acc;
@@ -157,10 +181,7 @@ __global__ void __launch_bounds__(kNT) k_volume(uint32_t n, float4 const *__rest
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
     uint32_t c = B.L.cnt[i];
-    for (uint32_t k = 0; k < c; ++k) {
-      uint32_t j = B.L.idx[size_t(k) * n + i];
-      acc += kW(K, sub3(xi, mk3(B.x[j])));
-    }
+    for (uint32_t k = 0; k < c; ++k) acc += kW(K, sub3(xi, mk3(B.xV[B.L.idx[size_t(k) * n + i]])));
   }
   V[i] = 1.0f / acc;
 }
@@ -228,6 +249,7 @@ __global__ void __launch_bounds__(kNT) k_iisph_c(uint32_t n, float4 const *__res
   uint32_t i = grid_tid();
   if (i >= n) return;
   KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
   float rho0 = *rho0p;
   f3 xi = mk3(x[i]);
   float ri = rho[i];
@@ -236,34 +258,40 @@ __global__ void __launch_bounds__(kNT) k_iisph_c(uint32_t n, float4 const *__res
   for (int q = 0; q < NF; ++q) {
     FluidN const &F = N.f[q];
     uint32_t cn = F.L.cnt[i];
+#pragma unroll 4
     for (uint32_t k = 0; k < cn; ++k) {
-      uint32_t j = F.L.idx[size_t(k) * n + i];
-      c = sub3(c, scl3(F.m[j] / (ri * ri), kgradW(K, sub3(xi, mk3(F.x[j])))));
+      size_t o = size_t(k) * n + i;
+      float4 xm = F.xm[F.L.idx[o]];
+      c = sub3(c, scl3(xm.w / (ri * ri), pair_grad(uc, F.L, o, K, sub3(xi, mk3(xm)))));
     }
   }
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
     uint32_t cn = B.L.cnt[i];
+#pragma unroll 4
     for (uint32_t k = 0; k < cn; ++k) {
-      uint32_t j = B.L.idx[size_t(k) * n + i];
-      c = sub3(c, scl3(((0.7f * 2.0f) * rho0) * (B.V[j] / (ri * ri)), kgradW(K, sub3(xi, mk3(B.x[j])))));
+      size_t o = size_t(k) * n + i;
+      float4 xv = B.xV[B.L.idx[o]];
+      c = sub3(c, scl3(((0.7f * 2.0f) * rho0) * (xv.w / (ri * ri)), pair_grad(uc, B.L, o, K, sub3(xi, mk3(xv)))));
     }
   }
   cout[i] = make_float4(c.x, c.y, c.z, 0.0f);
 }
 
 // iisph.setup pass 2 (schemes/iisph.hpp:254-354): p = 0, source term s and
-// diagonal element AA
+// diagonal element AA; also p / rho^2 (= 0) for the pressure acceleration
 template <int NF, int NB>
 __global__ void __launch_bounds__(kNT) k_iisph_s_aa(uint32_t n, float4 const *__restrict__ x, float4 const *__restrict__ v,
                                                     float4 const *__restrict__ cf, float const *__restrict__ m,
                                                     float const *__restrict__ rho, float *__restrict__ p,
-                                                    float *__restrict__ s, float *__restrict__ AA, float const *rho0p,
-                                                    Globals G, Nbrs<NF, NB> N) {
+                                                    float *__restrict__ pr, float *__restrict__ s,
+                                                    float *__restrict__ AA, float const *rho0p, Globals G,
+                                                    Nbrs<NF, NB> N) {
   uint32_t i = grid_tid();
   if (i >= n) return;
   KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
   float rho0 = *rho0p, dt = *G.dt;
   f3 xi = mk3(x[i]), vi = mk3(v[i]), ci = mk3(cf[i]);
   float mi = m[i], ri = rho[i];
@@ -272,10 +300,13 @@ __global__ void __launch_bounds__(kNT) k_iisph_s_aa(uint32_t n, float4 const *__
   for (int q = 0; q < NF; ++q) {
     FluidN const &F = N.f[q];
     uint32_t cn = F.L.cnt[i];
+#pragma unroll 2
     for (uint32_t k = 0; k < cn; ++k) {
-      uint32_t j = F.L.idx[size_t(k) * n + i];
-      f3 g = kgradW(K, sub3(xi, mk3(F.x[j])));
-      float mj = F.m[j];
+      size_t o = size_t(k) * n + i;
+      uint32_t j = F.L.idx[o];
+      float4 xm = F.xm[j];
+      f3 g = pair_grad(uc, F.L, o, K, sub3(xi, mk3(xm)));
+      float mj = xm.w;
       sa += mj * dot3(sub3(vi, mk3(F.v[j])), g);
       aa += mj * dot3(ci, g);
       aa -= (mj * (mi / (ri * ri))) * nsq3(g);
@@ -285,69 +316,86 @@ __global__ void __launch_bounds__(kNT) k_iisph_s_aa(uint32_t n, float4 const *__
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
     uint32_t cn = B.L.cnt[i];
+#pragma unroll 2
     for (uint32_t k = 0; k < cn; ++k) {
-      uint32_t j = B.L.idx[size_t(k) * n + i];
-      f3 g = kgradW(K, sub3(xi, mk3(B.x[j])));
-      float w = rho0 * B.V[j];
+      size_t o = size_t(k) * n + i;
+      float4 xv = B.xV[B.L.idx[o]];
+      f3 g = pair_grad(uc, B.L, o, K, sub3(xi, mk3(xv)));
+      float w = rho0 * xv.w;
       sa += w * dot3(sub3(vi, f3{0.0f, 0.0f, 0.0f}), g);
       aa += w * dot3(ci, g);
     }
   }
   p[i] = 0.0f;
+  pr[i] = 0.0f / (ri * ri);
   s[i] = (rho0 - ri) - ((dt * (rho0 / ri)) * sa);
   AA[i] = aa * ((dt * dt) * (rho0 / ri));
 }
 
 __global__ void k_set_i32(int *p, int v) { *p = v; }
-__global__ void k_set_f32(float *p, float v) { *p = v; }
 
-// iisph.iteration_pressure_acceleration (schemes/iisph.hpp:358-423)
+// iisph.iteration_pressure_acceleration (schemes/iisph.hpp:358-423).
+// `done` (device-loop mode) skips the work once the loop has converged.
 template <int NF, int NB>
 __global__ void __launch_bounds__(kNT) k_iisph_accel(uint32_t n, float4 const *__restrict__ x, float const *__restrict__ p,
                                                      float const *__restrict__ rho, float4 *__restrict__ a,
-                                                     float const *rho0p, Globals G, Nbrs<NF, NB> N) {
+                                                     float const *rho0p, Globals G, Nbrs<NF, NB> N,
+                                                     int const *done) {
+  if (done && *(volatile int const *)done) return;
   uint32_t i = grid_tid();
   if (i >= n) return;
   KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
   float rho0 = *rho0p;
   f3 xi = mk3(x[i]);
   float pi = p[i], ri = rho[i];
+  float pri = pi / (ri * ri);
   f3 acc = {0.0f, 0.0f, 0.0f};
 #pragma unroll
   for (int q = 0; q < NF; ++q) {
     FluidN const &F = N.f[q];
     uint32_t cn = F.L.cnt[i];
+#pragma unroll 4
     for (uint32_t k = 0; k < cn; ++k) {
-      uint32_t j = F.L.idx[size_t(k) * n + i];
-      float rj = F.rho[j];
-      float coef = F.m[j] * ((pi / (ri * ri)) + (F.p[j] / (rj * rj)));
-      acc = sub3(acc, scl3(coef, kgradW(K, sub3(xi, mk3(F.x[j])))));
+      size_t o = size_t(k) * n + i;
+      uint32_t j = F.L.idx[o];
+      float4 xm = F.xm[j];
+      float coef = xm.w * (pri + F.pr[j]);
+      acc = sub3(acc, scl3(coef, pair_grad(uc, F.L, o, K, sub3(xi, mk3(xm)))));
     }
   }
+  float bterm = (2.0f * pi) / (ri * ri);
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
     uint32_t cn = B.L.cnt[i];
+#pragma unroll 4
     for (uint32_t k = 0; k < cn; ++k) {
-      uint32_t j = B.L.idx[size_t(k) * n + i];
-      float coef = ((0.7f * rho0) * B.V[j]) * ((2.0f * pi) / (ri * ri));
-      acc = sub3(acc, scl3(coef, kgradW(K, sub3(xi, mk3(B.x[j])))));
+      size_t o = size_t(k) * n + i;
+      float4 xv = B.xV[B.L.idx[o]];
+      float coef = ((0.7f * rho0) * xv.w) * bterm;
+      acc = sub3(acc, scl3(coef, pair_grad(uc, B.L, o, K, sub3(xi, mk3(xv)))));
     }
   }
   a[i] = make_float4(acc.x, acc.y, acc.z, 0.0f);
 }
 
 // iisph.iteration_pressure (schemes/iisph.hpp:426-516) with the FP64
-// density-error reduction.  scalars[0] accumulates aprde across the fluid
-// groups of one call; `first` / `last_group` frame the call.
+// density-error reduction.  scalars[kSJacobi] accumulates aprde across the
+// fluid groups of one call: `first` starts it from the global aprde (or
+// from 0 in device-loop mode, where aprde := 0 precedes every iteration),
+// `last_group` stores it.  Also writes p / rho^2 for the next acceleration.
 template <int NF, int NB>
 __global__ void __launch_bounds__(kNT) k_iisph_pressure(uint32_t n, float4 const *__restrict__ x,
                                                         float4 const *__restrict__ a, float const *__restrict__ rho,
                                                         float const *__restrict__ s, float const *__restrict__ AA,
-                                                        float *__restrict__ p, float *__restrict__ Ap,
-                                                        float const *rho0p, Globals G, Nbrs<NF, NB> N, Red R, int first,
-                                                        int last_group) {
+                                                        float *__restrict__ p, float *__restrict__ pr,
+                                                        float *__restrict__ Ap, float const *rho0p, Globals G,
+                                                        Nbrs<NF, NB> N, Red R, int first, int last_group,
+                                                        int const *done) {
+  if (done && *(volatile int const *)done) return;
   KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
   float rho0 = *rho0p, dt = *G.dt, omega = *G.omega;
   double part = 0.0;
   for (uint32_t i = grid_tid(); i < n; i += gridDim.x * blockDim.x) {
@@ -357,18 +405,23 @@ __global__ void __launch_bounds__(kNT) k_iisph_pressure(uint32_t n, float4 const
     for (int q = 0; q < NF; ++q) {
       FluidN const &F = N.f[q];
       uint32_t cn = F.L.cnt[i];
+#pragma unroll 4
       for (uint32_t k = 0; k < cn; ++k) {
-        uint32_t j = F.L.idx[size_t(k) * n + i];
-        ap += F.m[j] * dot3(sub3(ai, mk3(F.a[j])), kgradW(K, sub3(xi, mk3(F.x[j]))));
+        size_t o = size_t(k) * n + i;
+        uint32_t j = F.L.idx[o];
+        float4 xm = F.xm[j];
+        ap += xm.w * dot3(sub3(ai, mk3(F.a[j])), pair_grad(uc, F.L, o, K, sub3(xi, mk3(xm))));
       }
     }
 #pragma unroll
     for (int q = 0; q < NB; ++q) {
       BoundN const &B = N.b[q];
       uint32_t cn = B.L.cnt[i];
+#pragma unroll 4
       for (uint32_t k = 0; k < cn; ++k) {
-        uint32_t j = B.L.idx[size_t(k) * n + i];
-        ap += (rho0 * B.V[j]) * dot3(sub3(ai, f3{0.0f, 0.0f, 0.0f}), kgradW(K, sub3(xi, mk3(B.x[j]))));
+        size_t o = size_t(k) * n + i;
+        float4 xv = B.xV[B.L.idx[o]];
+        ap += (rho0 * xv.w) * dot3(sub3(ai, f3{0.0f, 0.0f, 0.0f}), pair_grad(uc, B.L, o, K, sub3(xi, mk3(xv))));
       }
     }
     float ri = rho[i];
@@ -379,14 +432,46 @@ __global__ void __launch_bounds__(kNT) k_iisph_pressure(uint32_t n, float4 const
     // std::max({0, t}) returns the first largest element: t only if 0 < t
     float pn = ((0.0f < t) ? t : 0.0f) * ustep(1e-9f, fabsf(aai));
     p[i] = pn;
+    pr[i] = pn / (ri * ri);
     part += double(((ap - si) / rho0) * ustep(1e-9f, pn));
   }
   double v[1] = {part}, out[1];
   if (reduce_commit<1>(v, R, out) && threadIdx.x == 0) {
-    double acc = (first ? double(*G.aprde) : R.scalars[0]) + out[0];
-    R.scalars[0] = acc;
+    double start = first ? (done ? 0.0 : double(*G.aprde)) : R.scalars[kSJacobi];
+    double acc = start + out[0];
+    R.scalars[kSJacobi] = acc;
     if (last_group) *G.aprde = float(acc);
   }
+}
+
+// relaxed-Jacobi loop control (share/scripts/prtcl-lua.example.lua:409-420):
+// at least two iterations; stop when aprde / nprde < eta or at the cap
+__global__ void k_jacobi_begin(Globals G, Red R) {
+  R.status[kStJacIter] = 0;
+  R.status[kStJacDone] = (*G.nprde >= 1) ? 0 : 1;
+  *G.jac_iters = 0;
+}
+__global__ void k_jacobi_control(Globals G, Red R, cudaGraphConditionalHandle h, int use_handle, int kernels) {
+  int done = R.status[kStJacDone];
+  if (!done) {
+    int it = R.status[kStJacIter] + 1;
+    R.status[kStJacIter] = it;
+    int maxit = *G.jac_max > 0 ? *G.jac_max : 100;
+    float eta = *G.jac_eta > 0.0f ? *G.jac_eta : 1e-3f;
+    double rel = R.scalars[kSJacobi] / double(*G.nprde);
+    bool converged = it >= 2 && rel < double(eta);
+    if (converged || it >= maxit || it >= 100000) done = 1;
+    R.status[kStJacDone] = done;
+    *G.jac_iters = it;
+    if (kernels) atomicAdd(&g_loop_kernels, (unsigned long long)kernels);
+    if (done) {
+      R.stats[0] += 1.0;
+      R.stats[1] += double(it);
+      if (!converged) R.stats[2] += 1.0;
+      if (rel > R.stats[3]) R.stats[3] = rel;
+    }
+  }
+  if (use_handle) cudaGraphSetConditional(h, done ? 0u : 1u);
 }
 
 // ---------------------------------------------------------------------------
@@ -407,9 +492,9 @@ __device__ __forceinline__ M3 minv3(M3 const &A) {
   float det = c00 * A.m[0] + (c10 * A.m[1] + c20 * A.m[2]);
   float inv = 1.0f / det;
   M3 r;
-  r.m[0] = c00 * inv;          // (0,0)
-  r.m[3] = c10 * inv;          // (0,1)
-  r.m[6] = c20 * inv;          // (0,2)
+  r.m[0] = c00 * inv;           // (0,0)
+  r.m[3] = c10 * inv;           // (0,1)
+  r.m[6] = c20 * inv;           // (0,2)
   r.m[1] = cof3(A, 0, 1) * inv; // (1,0)
   r.m[4] = cof3(A, 1, 1) * inv; // (1,1)
   r.m[7] = cof3(A, 2, 1) * inv; // (1,2)
@@ -420,28 +505,33 @@ __device__ __forceinline__ M3 minv3(M3 const &A) {
 }
 
 // wkbb18.compute_diagonal (schemes/wkbb18.hpp:194-270): block-Jacobi
-// preconditioner sp_i = (I - dt S_i)^-1, stored as 9 planes
-template <int NF, int NB>
-__global__ void __launch_bounds__(kNT) k_wkbb18_diag(uint32_t n, uint32_t cap, float4 const *__restrict__ x,
-                                                     float const *__restrict__ m, float const *__restrict__ rho,
-                                                     float *__restrict__ sp, float const *rho0p, float const *mup,
-                                                     Globals G, NbrList self, Nbrs<NF, NB> N) {
+// preconditioner sp_i = (I - dt S_i)^-1, stored as 9 planes.  The fluid sum
+// runs over the particle's own group (`foreach _ neighbor`); xmr holds
+// (x, m / rho).
+template <int NB>
+__global__ void __launch_bounds__(kNT) k_wkbb18_diag(uint32_t n, uint32_t cap, float4 const *__restrict__ xmr,
+                                                     float const *__restrict__ rho, float *__restrict__ sp,
+                                                     float const *rho0p, float const *mup, Globals G, NbrList self,
+                                                     Nbrs<0, NB> N) {
   uint32_t i = grid_tid();
   if (i >= n) return;
   KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
   float h = K.h, dt = *G.dt, rho0 = *rho0p, mu = *mup;
-  f3 xi = mk3(x[i]);
+  f3 xi = mk3(xmr[i]);
   float ri = rho[i];
   float S[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) S[k] = 0.0f;
   float hh = (0.01f * h) * h;
+  float cmu = 10.0f * (mu / ri);
   uint32_t cn = self.cnt[i];
   for (uint32_t k = 0; k < cn; ++k) {
-    uint32_t j = self.idx[size_t(k) * n + i];
-    f3 xij = sub3(xi, mk3(x[j]));
-    float coef = ((10.0f * (mu / ri)) * (m[j] / rho[j])) / (nsq3(xij) + hh);
-    f3 g = kgradW(K, xij);
+    size_t o = size_t(k) * n + i;
+    float4 xj = xmr[self.idx[o]];
+    f3 xij = sub3(xi, mk3(xj));
+    float coef = (cmu * xj.w) / (nsq3(xij) + hh);
+    f3 g = pair_grad(uc, self, o, K, xij);
     float gv[3] = {g.x, g.y, g.z}, xv[3] = {xij.x, xij.y, xij.z};
 #pragma unroll
     for (int c = 0; c < 3; ++c)
@@ -454,15 +544,16 @@ __global__ void __launch_bounds__(kNT) k_wkbb18_diag(uint32_t n, uint32_t cap, f
     float bmu = *B.mu;
     uint32_t cb = B.L.cnt[i];
     for (uint32_t k = 0; k < cb; ++k) {
-      uint32_t j = B.L.idx[size_t(k) * n + i];
-      f3 xij = sub3(xi, mk3(B.x[j]));
-      float coef = ((10.0f * (bmu / ri)) * ((rho0 * B.V[j]) / ri)) / (nsq3(xij) + hh);
-      f3 g = kgradW(K, xij);
-      float gv[3] = {g.x, g.y, g.z}, xv[3] = {xij.x, xij.y, xij.z};
+      size_t o = size_t(k) * n + i;
+      float4 xv = B.xV[B.L.idx[o]];
+      f3 xij = sub3(xi, mk3(xv));
+      float coef = ((10.0f * (bmu / ri)) * ((rho0 * xv.w) / ri)) / (nsq3(xij) + hh);
+      f3 g = pair_grad(uc, B.L, o, K, xij);
+      float gv[3] = {g.x, g.y, g.z}, xw[3] = {xij.x, xij.y, xij.z};
 #pragma unroll
       for (int c = 0; c < 3; ++c)
 #pragma unroll
-        for (int r = 0; r < 3; ++r) S[3 * c + r] += coef * (gv[r] * xv[c]);
+        for (int r = 0; r < 3; ++r) S[3 * c + r] += coef * (gv[r] * xw[c]);
     }
   }
   M3 A;
@@ -486,9 +577,8 @@ __device__ __forceinline__ f3 precond(float const *__restrict__ sp, uint32_t cap
 
 struct PcgArgs {
   uint32_t n, cap;
-  float4 const *x;
+  float4 const *xmr; // (x, m / rho)
   float4 const *v;
-  float const *m;
   float const *rho;
   float const *sp;
   float const *tb;
@@ -504,52 +594,59 @@ struct PcgArgs {
 // system product of wkbb18.accumulate_acceleration (schemes/wkbb18.hpp:
 // 339-396): (A w)_i = w_i - dt * a_f(w)_i
 template <int NB>
-__device__ __forceinline__ f3 wkbb18_system(PcgArgs const &P, KernelParams const &K, float dt, float rho0, float mu,
-                                            Nbrs<0, NB> const &N, float4 const *__restrict__ w, uint32_t i) {
+__device__ __forceinline__ f3 wkbb18_system(PcgArgs const &P, KernelParams const &K, bool uc, float dt, float rho0,
+                                            float mu, Nbrs<0, NB> const &N, float4 const *__restrict__ w, uint32_t i) {
   float h = K.h;
   float hh = (0.01f * h) * h;
-  f3 xi = mk3(P.x[i]), wi = mk3(w[i]);
+  f3 xi = mk3(P.xmr[i]), wi = mk3(w[i]);
   float ri = P.rho[i];
+  float cmu = 10.0f * (mu / ri);
   f3 af = {0.0f, 0.0f, 0.0f};
   uint32_t cn = P.self.cnt[i];
+#pragma unroll 4
   for (uint32_t k = 0; k < cn; ++k) {
-    uint32_t j = P.self.idx[size_t(k) * P.n + i];
-    f3 xij = sub3(xi, mk3(P.x[j]));
-    float coef = (((10.0f * (mu / ri)) * (P.m[j] / P.rho[j])) * dot3(sub3(wi, mk3(w[j])), xij)) / (nsq3(xij) + hh);
-    af = add3(af, scl3(coef, kgradW(K, xij)));
+    size_t o = size_t(k) * P.n + i;
+    uint32_t j = P.self.idx[o];
+    float4 xj = P.xmr[j];
+    f3 xij = sub3(xi, mk3(xj));
+    float coef = ((cmu * xj.w) * dot3(sub3(wi, mk3(w[j])), xij)) / (nsq3(xij) + hh);
+    af = add3(af, scl3(coef, pair_grad(uc, P.self, o, K, xij)));
   }
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
     float bmu = *B.mu;
+    float cb_mu = 10.0f * (bmu / ri);
     uint32_t cb = B.L.cnt[i];
+#pragma unroll 4
     for (uint32_t k = 0; k < cb; ++k) {
-      uint32_t j = B.L.idx[size_t(k) * P.n + i];
-      f3 xij = sub3(xi, mk3(B.x[j]));
-      float coef = (((10.0f * (bmu / ri)) * ((rho0 * B.V[j]) / ri)) * dot3(wi, xij)) / (nsq3(xij) + hh);
-      af = add3(af, scl3(coef, kgradW(K, xij)));
+      size_t o = size_t(k) * P.n + i;
+      float4 xv = B.xV[B.L.idx[o]];
+      f3 xij = sub3(xi, mk3(xv));
+      float coef = ((cb_mu * ((rho0 * xv.w) / ri)) * dot3(wi, xij)) / (nsq3(xij) + hh);
+      af = add3(af, scl3(coef, pair_grad(uc, B.L, o, K, xij)));
     }
   }
   return sub3(wi, scl3(dt, af));
 }
 
-// scalars: 0 b_nsq, 1 thr, 2 r_nsq, 3 next_rdy, 4 prev_rdy, 5 pdq
-// float scalars (as double slots): 6 alpha, 7 beta
-// status: 0 iteration count, 1 active
+// scalars: 0 b_nsq, 1 thr, 2 r_nsq, 3 next_rdy, 4 prev_rdy, 5 pdq,
+// 6 alpha, 7 beta (f32 values held in double slots)
 __global__ void k_pcg_guess(PcgArgs P) {
   uint32_t i = grid_tid();
   if (i < P.n) P.X[i] = P.v[i];
 }
 
 // r = A x - b (b = v: the right-hand side's boundary term has v_b = 0),
-// y = M r, p = -y; dots b.b, r.r, r.y
+// y = M r, p = -y; dots b.b, r.r, r.y (solver/cg_openmp.hpp:48-96)
 template <int NB>
 __global__ void __launch_bounds__(kNT) k_pcg_init(PcgArgs P, Globals G, Nbrs<0, NB> N, Red R) {
   KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
   float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
   double bb = 0.0, rr = 0.0, ry = 0.0;
   for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x) {
-    f3 ax = wkbb18_system<NB>(P, K, dt, rho0, mu, N, P.X, i);
+    f3 ax = wkbb18_system<NB>(P, K, uc, dt, rho0, mu, N, P.X, i);
     f3 b = mk3(P.v[i]);
     f3 r = sub3(ax, b);
     f3 y = precond(P.sp, P.cap, i, r);
@@ -563,43 +660,45 @@ __global__ void __launch_bounds__(kNT) k_pcg_init(PcgArgs P, Globals G, Nbrs<0, 
   double v[3] = {bb, rr, ry}, out[3];
   if (reduce_commit<3>(v, R, out) && threadIdx.x == 0) {
     double tol = double(*P.tol);
-    R.scalars[0] = out[0];
+    R.scalars[kSPcg + 0] = out[0];
     double thr = tol * tol * out[0], fmin_ = double(1.17549435082228750797e-38f);
-    R.scalars[1] = (thr < fmin_) ? fmin_ : thr; // max(tol^2 |b|^2, FLT_MIN)
-    R.scalars[2] = out[1];
-    R.scalars[3] = out[2];
-    R.status[0] = 0;
-    R.status[1] = 1; // iteration 0 always runs (min_k = 1)
+    R.scalars[kSPcg + 1] = (thr < fmin_) ? fmin_ : thr; // max(tol^2 |b|^2, FLT_MIN)
+    R.scalars[kSPcg + 2] = out[1];
+    R.scalars[kSPcg + 3] = out[2];
+    R.status[kStPcgIter] = 0;
+    R.status[kStPcgActive] = 1; // iteration 0 always runs (min_k = 1)
+    R.status[kStPcgBody] = 0;
   }
 }
 
 // q = A p; p.q; alpha or break (solver/cg_openmp.hpp:121-151)
 template <int NB>
 __global__ void __launch_bounds__(kNT) k_pcg_q(PcgArgs P, Globals G, Nbrs<0, NB> N, Red R) {
-  if (!*(volatile int *)&R.status[1]) return;
+  if (!*(volatile int *)&R.status[kStPcgActive]) return;
   KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
   float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
   double pq = 0.0;
   for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x) {
-    f3 q = wkbb18_system<NB>(P, K, dt, rho0, mu, N, P.P, i);
+    f3 q = wkbb18_system<NB>(P, K, uc, dt, rho0, mu, N, P.P, i);
     P.Q[i] = make_float4(q.x, q.y, q.z, 0.0f);
     pq += double(dot3(mk3(P.P[i]), q));
   }
   double v[1] = {pq}, out[1];
   if (reduce_commit<1>(v, R, out) && threadIdx.x == 0) {
-    double prev = R.scalars[3];
-    R.scalars[4] = prev;
-    R.scalars[5] = out[0];
-    if (fabs(out[0]) < double(*P.tol)) R.status[1] = 0;
-    else R.scalars[6] = double(float(prev / out[0]));
+    double prev = R.scalars[kSPcg + 3];
+    R.scalars[kSPcg + 4] = prev;
+    R.scalars[kSPcg + 5] = out[0];
+    if (fabs(out[0]) < double(*P.tol)) R.status[kStPcgActive] = 0;
+    else R.scalars[kSPcg + 6] = double(float(prev / out[0]));
   }
 }
 
 // x += alpha p; r += alpha q; y = M r; r.r; r.y; break / beta
 // (solver/cg_openmp.hpp:153-191)
 __global__ void __launch_bounds__(kNT) k_pcg_update(PcgArgs P, Red R) {
-  if (!*(volatile int *)&R.status[1]) return;
-  float alpha = float(R.scalars[6]);
+  if (!*(volatile int *)&R.status[kStPcgActive]) return;
+  float alpha = float(R.scalars[kSPcg + 6]);
   double rr = 0.0, ry = 0.0;
   for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x) {
     f3 x = mk3(P.X[i]), p = mk3(P.P[i]), r = mk3(P.Rr[i]), q = mk3(P.Q[i]);
@@ -614,27 +713,27 @@ __global__ void __launch_bounds__(kNT) k_pcg_update(PcgArgs P, Red R) {
   }
   double v[2] = {rr, ry}, out[2];
   if (reduce_commit<2>(v, R, out) && threadIdx.x == 0) {
-    double prev = R.scalars[4];
-    R.scalars[2] = out[0];
-    R.scalars[3] = out[1];
+    double prev = R.scalars[kSPcg + 4];
+    R.scalars[kSPcg + 2] = out[0];
+    R.scalars[kSPcg + 3] = out[1];
     if (fabs(prev) < double(*P.tol)) {
-      R.status[1] = 0;
+      R.status[kStPcgActive] = 0;
     } else {
-      R.scalars[7] = double(float(out[1] / prev));
-      int k = R.status[0] + 1;
-      R.status[0] = k;
+      R.scalars[kSPcg + 7] = double(float(out[1] / prev));
+      int k = R.status[kStPcgIter] + 1;
+      R.status[kStPcgIter] = k;
       // loop condition ok(k, r_nsq): k < 1 -> run; k > max_k -> stop;
       // r_nsq < thr -> stop
-      bool ok = (k < 1) || (!(k > *P.max_k) && !(out[0] < R.scalars[1]));
-      R.status[1] = ok ? 1 : 0;
+      bool ok = (k < 1) || (!(k > *P.max_k) && !(out[0] < R.scalars[kSPcg + 1]));
+      R.status[kStPcgActive] = ok ? 1 : 0;
     }
   }
 }
 
 // p = -y + beta p (only when the loop continues)
 __global__ void k_pcg_p(PcgArgs P, Red R) {
-  if (!*(volatile int *)&R.status[1]) return;
-  float beta = float(R.scalars[7]);
+  if (!*(volatile int *)&R.status[kStPcgActive]) return;
+  float beta = float(R.scalars[kSPcg + 7]);
   for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x) {
     f3 y = mk3(P.Y[i]), p = mk3(P.P[i]);
     f3 r = add3(f3{-y.x, -y.y, -y.z}, scl3(beta, p));
@@ -642,11 +741,28 @@ __global__ void k_pcg_p(PcgArgs P, Red R) {
   }
 }
 
+// loop control of the device PCG loop: continue while active, and never run
+// more than max_k + 1 bodies
+__global__ void k_pcg_control(PcgArgs P, Red R, cudaGraphConditionalHandle h, int use_handle, int kernels) {
+  int body = R.status[kStPcgBody] + 1;
+  R.status[kStPcgBody] = body;
+  if (kernels) atomicAdd(&g_loop_kernels, (unsigned long long)kernels);
+  int maxk = *P.max_k;
+  bool cont = R.status[kStPcgActive] && body < (maxk < 0 ? 0 : maxk) + 1 && body < 1000000;
+  if (!cont) {
+    R.stats[4] += 1.0;
+    R.stats[5] += double(R.status[kStPcgIter]);
+    if (R.status[kStPcgActive]) R.stats[6] += 1.0;
+    R.status[kStPcgActive] = 0;
+  }
+  if (use_handle) cudaGraphSetConditional(h, cont ? 1u : 0u);
+}
+
 // apply (schemes/wkbb18.hpp:401-413): vd = (x - v) [0 < (t - t_b) - fade];
 // a = vd / dt
 __global__ void k_pcg_apply(PcgArgs P, Globals G, Red R) {
   uint32_t i = grid_tid();
-  if (i == 0) *P.iterations = R.status[0];
+  if (i == 0) *P.iterations = R.status[kStPcgIter];
   if (i >= P.n) return;
   float dt = *G.dt, t = *G.t, fade = *G.fade;
   float u = ustep(0.0f, (t - P.tb[i]) - fade);
@@ -681,7 +797,7 @@ FieldType ft_int() {
 
 template <class T> T *dptr(VaryingField *f) { return static_cast<T *>(f->d); }
 
-// dispatch on the number of fluid (0..2) and boundary (0..2) neighbour groups
+// dispatch on the number of fluid (1..2) and boundary (0..2) neighbour groups
 template <template <int, int> class F, class... A> void dispatch_fb(int nf, int nb, A &&...a) {
   if (nf == 1 && nb == 1) return F<1, 1>::go(a...);
   if (nf == 1 && nb == 0) return F<1, 0>::go(a...);
@@ -692,6 +808,67 @@ template <template <int, int> class F, class... A> void dispatch_fb(int nf, int 
   throw Error("unsupported group configuration: " + std::to_string(nf) + " fluid and " + std::to_string(nb) +
               " boundary groups (1..2 and 0..2 are supported)");
 }
+
+// A CUDA graph holding one conditional while node; the body is captured from
+// the launches `body(stream, handle)` queues.  Rebuilt when the signature
+// (the bytes of every kernel argument of the body) changes.
+class WhileLoop {
+public:
+  ~WhileLoop() { reset(); }
+  void reset() {
+    if (exec_) cudaGraphExecDestroy(exec_);
+    if (graph_) cudaGraphDestroy(graph_);
+    exec_ = nullptr;
+    graph_ = nullptr;
+    sig_.clear();
+  }
+  template <class Body> void run(cudaStream_t s, std::string const &sig, Body &&body) {
+    if (!exec_ || sig != sig_) {
+      reset();
+      PG_CUDA(cudaGraphCreate(&graph_, 0));
+      cudaGraphConditionalHandle h;
+      PG_CUDA(cudaGraphConditionalHandleCreate(&h, graph_, 1, cudaGraphCondAssignDefault));
+      cudaGraphNodeParams p{};
+      p.type = cudaGraphNodeTypeConditional;
+      p.conditional.handle = h;
+      p.conditional.type = cudaGraphCondTypeWhile;
+      p.conditional.size = 1;
+      cudaGraphNode_t node;
+      PG_CUDA(cudaGraphAddNode(&node, graph_, nullptr, nullptr, 0, &p));
+      cudaGraph_t bodyg = p.conditional.phGraph_out[0];
+      cudaStream_t cs;
+      PG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+      PG_CUDA(cudaStreamBeginCaptureToGraph(cs, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+      uint64_t counted = launch_count();
+      try {
+        body(cs, h);
+      } catch (...) {
+        cudaGraph_t dummy;
+        cudaStreamEndCapture(cs, &dummy);
+        cudaStreamDestroy(cs);
+        reset();
+        throw;
+      }
+      uncount_launches(launch_count() - counted); // captured, not launched
+      cudaGraph_t out;
+      cudaError_t err = cudaStreamEndCapture(cs, &out);
+      cudaStreamDestroy(cs);
+      PG_CUDA(err);
+      PG_CUDA(cudaGraphInstantiate(&exec_, graph_, 0));
+      sig_ = sig;
+      builds++;
+    }
+    PG_CUDA(cudaGraphLaunch(exec_, s));
+  }
+  int builds = 0;
+
+private:
+  cudaGraph_t graph_ = nullptr;
+  cudaGraphExec_t exec_ = nullptr;
+  std::string sig_;
+};
+
+template <class T> void sig_add(std::string &s, T const &v) { s.append(reinterpret_cast<char const *>(&v), sizeof(T)); }
 
 } // namespace
 
@@ -710,6 +887,15 @@ std::vector<std::string> Scheme::procedure_names() const {
   std::vector<std::string> r;
   for (auto &kv : procs_) r.push_back(kv.first);
   return r;
+}
+
+uint64_t device_loop_kernels() {
+  unsigned long long v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_loop_kernels, sizeof(v)) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return uint64_t(v);
 }
 
 namespace {
@@ -743,6 +929,9 @@ protected:
     G.nprde = static_cast<int *>(gp("iisph_nprde"));
     G.gravity = static_cast<float const *>(gp("gravity"));
     G.max_speed = static_cast<float *>(gp("maximum_speed"));
+    G.jac_max = static_cast<int const *>(gp("iisph_maximum_iterations"));
+    G.jac_eta = static_cast<float const *>(gp("iisph_maximum_density_error"));
+    G.jac_iters = static_cast<int *>(gp("iisph_iterations"));
     return G;
   }
   Red red(Model &m, int slot) {
@@ -751,39 +940,49 @@ protected:
     R.ticket = m.red_count_d + slot;
     R.scalars = m.scalars_d;
     R.status = m.status_d;
+    R.stats = m.stats_d;
     return R;
   }
   std::vector<FluidG> fluid_;
   std::vector<BoundG> bound_;
 
-  static NbrList nl(NbrView const &v, int g) { return NbrList{v.idx[g], v.cnt[g]}; }
-  FluidN fn(FluidG const &F, NbrView const &v) {
+  static NbrList nl(NbrView const &v, int g) { return NbrList{v.idx[g], v.gf[g], v.cnt[g]}; }
+  // packed neighbour records of the fluid / boundary groups (made current
+  // here: may launch a pack kernel on `s`)
+  FluidN fn(FluidG const &F, NbrView const &v, cudaStream_t s) {
     FluidN r{};
     r.L = nl(v, F.g->index);
-    r.x = F.x ? dptr<float4>(F.x) : nullptr;
+    r.xm = model_->packed_xs(F.g, F.x, F.m, "xm", s);
     r.v = F.v ? dptr<float4>(F.v) : nullptr;
     r.a = F.a ? dptr<float4>(F.a) : nullptr;
-    r.m = F.m ? dptr<float>(F.m) : nullptr;
-    r.rho = F.rho ? dptr<float>(F.rho) : nullptr;
-    r.p = F.p ? dptr<float>(F.p) : nullptr;
+    r.pr = nullptr;
     return r;
   }
-  BoundN bn(BoundG const &B, NbrView const &v) {
+  BoundN bn(BoundG const &B, NbrView const &v, cudaStream_t s) {
     BoundN r{};
     r.L = nl(v, B.g->index);
-    r.x = dptr<float4>(B.x);
-    r.V = dptr<float>(B.V);
+    r.xV = model_->packed_xs(B.g, B.x, B.V, "xV", s);
     r.mu = B.mu ? static_cast<float const *>(model_->small_ptr(*B.mu)) : nullptr;
     return r;
   }
-  template <int NF, int NB> Nbrs<NF, NB> nbrs(NbrView const &v) {
+  template <int NF, int NB> Nbrs<NF, NB> nbrs(NbrView const &v, cudaStream_t s) {
     Nbrs<NF, NB> N{};
-    for (int q = 0; q < NF; ++q) N.f[q] = fn(fluid_[q], v);
-    for (int q = 0; q < NB; ++q) N.b[q] = bn(bound_[q], v);
+    for (int q = 0; q < NF; ++q) N.f[q] = fn(fluid_[q], v, s);
+    for (int q = 0; q < NB; ++q) N.b[q] = bn(bound_[q], v, s);
+    N.hcache = v.hcache;
     return N;
   }
+  template <int NB> Nbrs<0, NB> bnbrs(NbrView const &v, cudaStream_t s) {
+    Nbrs<0, NB> N{};
+    for (int q = 0; q < NB; ++q) N.b[q] = bn(bound_[q], v, s);
+    N.hcache = v.hcache;
+    return N;
+  }
+  NbrView const &lists(Nhood &nh, Group *g, Globals const &G, cudaStream_t s) {
+    return nh.lists(g->index, s, G.h);
+  }
   float const *u(SmallField *f) { return static_cast<float const *>(model_->small_ptr(*f)); }
-  void need_globals(Globals const &G, std::initializer_list<std::pair<void const *, char const *>> l) {
+  void need(std::initializer_list<std::pair<void const *, char const *>> l) {
     for (auto &p : l)
       if (!p.first) throw Error(std::string("global field missing: ") + p.second);
   }
@@ -826,18 +1025,20 @@ public:
   template <int NF, int NB> struct L {
     static void go(Density *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
       uint32_t n = uint32_t(F.g->count);
+      auto N = S->nbrs<NF, NB>(v, s);
       ProfScope ps(S->model_->prof, "density", s);
-      k_density<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(F.x), dptr<float>(F.rho), S->u(F.rho0), G,
-                                                        S->nbrs<NF, NB>(v)); count_launch();
+      k_density<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(F.x), dptr<float>(F.rho), S->u(F.rho0), G, N);
+      count_launch();
     }
   };
   void compute_density(Nhood &nh, cudaStream_t s) {
     Globals G = globals(*model_);
     for (auto &F : fluid_) {
       if (F.g->count == 0) continue;
-      NbrView const &v = nh.lists(F.g->index, s);
+      NbrView const &v = lists(nh, F.g, G, s);
       dispatch_fb<L>(int(fluid_.size()), int(bound_.size()), this, F, v, G, s);
       PG_LAUNCH_CHECK();
+      F.rho->version++;
     }
   }
 };
@@ -863,26 +1064,26 @@ public:
   void compute_volume(Nhood &nh, cudaStream_t s) {
     Globals G = globals(*model_);
     int nb = int(bound_.size());
-    for (auto &B : bound_) {
+    if (nb > 2) throw Error("unsupported group configuration: at most 2 boundary groups");
+    // every group's sums read the positions before any volume is written
+    std::vector<std::pair<BoundG *, NbrView const *>> todo;
+    for (auto &B : bound_)
+      if (B.g->count) todo.push_back({&B, &lists(nh, B.g, G, s)});
+    for (auto &t : todo) {
+      BoundG &B = *t.first;
       uint32_t n = uint32_t(B.g->count);
-      if (n == 0) continue;
-      NbrView const &v = nh.lists(B.g->index, s);
+      NbrView const &v = *t.second;
+      ProfScope ps(model_->prof, "aiast12_volume", s);
       if (nb == 1) {
-        Nbrs<0, 1> N{};
-        N.b[0] = bn(bound_[0], v);
-        ProfScope ps(model_->prof, "aiast12_volume", s);
-        k_volume<1><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(B.x), dptr<float>(B.V), G, N); count_launch();
-      } else if (nb == 2) {
-        Nbrs<0, 2> N{};
-        N.b[0] = bn(bound_[0], v);
-        N.b[1] = bn(bound_[1], v);
-        ProfScope ps(model_->prof, "aiast12_volume", s);
-        k_volume<2><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(B.x), dptr<float>(B.V), G, N); count_launch();
+        k_volume<1><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(B.x), dptr<float>(B.V), G, bnbrs<1>(v, s));
+        count_launch();
       } else {
-        throw Error("unsupported group configuration: at most 2 boundary groups");
+        k_volume<2><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(B.x), dptr<float>(B.V), G, bnbrs<2>(v, s));
+        count_launch();
       }
       PG_LAUNCH_CHECK();
     }
+    for (auto &t : todo) t.first->V->version++;
   }
 };
 
@@ -898,9 +1099,11 @@ public:
       for (Group *g : dyn_) {
         uint32_t n = uint32_t(g->count);
         if (!n) continue;
+        VaryingField *a = g->find_varying("acceleration");
         ProfScope ps(model_->prof, "gravity", s);
-        k_gravity<<<div_up(n, 256), 256, 0, s>>>(n, dptr<float4>(g->find_varying("acceleration")), G); count_launch();
+        k_gravity<<<div_up(n, 256), 256, 0, s>>>(n, dptr<float4>(a), G); count_launch();
         PG_LAUNCH_CHECK();
+        a->version++;
       }
     });
   }
@@ -931,11 +1134,14 @@ public:
       for (Group *g : dyn_) {
         uint32_t n = uint32_t(g->count);
         if (!n) continue;
+        VaryingField *v = g->find_varying("velocity");
         ProfScope ps(model_->prof, "integrate_velocity", s);
-        k_integrate_velocity<<<div_up(n, 256), 256, 0, s>>>(n, dptr<float4>(g->find_varying("velocity")),
+        k_integrate_velocity<<<div_up(n, 256), 256, 0, s>>>(n, dptr<float4>(v),
                                                             dptr<float4>(g->find_varying("acceleration")),
-                                                            dptr<float>(g->find_varying("time_of_birth")), G); count_launch();
+                                                            dptr<float>(g->find_varying("time_of_birth")), G);
+        count_launch();
         PG_LAUNCH_CHECK();
+        v->version++;
       }
     });
     reg("integrate_position", [this](Nhood &, cudaStream_t s) {
@@ -948,7 +1154,8 @@ public:
         VaryingField *x = g->find_varying("position");
         ProfScope ps(model_->prof, "integrate_position", s);
         k_integrate_position<<<div_up(n, 256), 256, 0, s>>>(n, dptr<float4>(x),
-                                                            dptr<float4>(g->find_varying("velocity")), G, maxord); count_launch();
+                                                            dptr<float4>(g->find_varying("velocity")), G, maxord);
+        count_launch();
         x->version++;
       }
       k_max_speed_end<<<1, 1, 0, s>>>(G, maxord); count_launch();
@@ -991,11 +1198,15 @@ public:
     reg("setup", [this](Nhood &nh, cudaStream_t s) { setup(nh, s); });
     reg("iteration_pressure_acceleration", [this](Nhood &nh, cudaStream_t s) { accel(nh, s); });
     reg("iteration_pressure", [this](Nhood &nh, cudaStream_t s) { pressure(nh, s); });
+    // the whole relaxed-Jacobi loop of the driver script on the device
+    reg("solve_pressure", [this](Nhood &nh, cudaStream_t s) { solve(nh, s); });
   }
   std::string name() const override { return "iisph"; }
   std::string source() const override {
     return "procedures setup (c, p = 0, s, AA, nprde), iteration_pressure_acceleration (a), "
-           "iteration_pressure (Ap, relaxed Jacobi p, aprde += (Ap - s) / rho0 [p > 1e-9])";
+           "iteration_pressure (Ap, relaxed Jacobi p, aprde += (Ap - s) / rho0 [p > 1e-9]), "
+           "solve_pressure (repeat aprde := 0, acceleration, pressure while the iteration count is < 2 or "
+           "aprde / nprde >= iisph_maximum_density_error, at most iisph_maximum_iterations times)";
   }
   void load(Model &m) override {
     m.add_global("gravity", ft_vec3());
@@ -1004,6 +1215,9 @@ public:
     m.add_global("iisph_relaxation", ft_real());
     m.add_global("iisph_aprde", ft_real());
     m.add_global("iisph_nprde", ft_int());
+    m.add_global("iisph_maximum_iterations", ft_int());
+    m.add_global("iisph_maximum_density_error", ft_real());
+    m.add_global("iisph_iterations", ft_int());
     collect(m, true, true);
     for (auto &F : fluid_) {
       F.rho0 = &F.g->add_uniform("rest_density", ft_real());
@@ -1023,61 +1237,120 @@ public:
       B.V = &B.g->add_varying("volume", ft_real());
     }
     bind(m);
+    loop_.reset();
   }
   template <int NF, int NB> struct C {
     static void go(Iisph *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
       uint32_t n = uint32_t(F.g->count);
+      auto N = S->nbrs<NF, NB>(v, s);
       ProfScope ps(S->model_->prof, "iisph_c", s);
       k_iisph_c<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(F.x), dptr<float>(F.rho), dptr<float4>(F.c),
-                                                        S->u(F.rho0), G, S->nbrs<NF, NB>(v)); count_launch();
+                                                        S->u(F.rho0), G, N);
+      count_launch();
     }
   };
   template <int NF, int NB> struct SAA {
     static void go(Iisph *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
       uint32_t n = uint32_t(F.g->count);
+      auto N = S->nbrs<NF, NB>(v, s);
+      float *pr = S->model_->pr_buffer(F.g, s);
       ProfScope ps(S->model_->prof, "iisph_s_aa", s);
-      k_iisph_s_aa<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(
-          n, dptr<float4>(F.x), dptr<float4>(F.v), dptr<float4>(F.c), dptr<float>(F.m), dptr<float>(F.rho),
-          dptr<float>(F.p), dptr<float>(F.s), dptr<float>(F.AA), S->u(F.rho0), G, S->nbrs<NF, NB>(v)); count_launch();
+      k_iisph_s_aa<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(F.x), dptr<float4>(F.v), dptr<float4>(F.c),
+                                                           dptr<float>(F.m), dptr<float>(F.rho), dptr<float>(F.p), pr,
+                                                           dptr<float>(F.s), dptr<float>(F.AA), S->u(F.rho0), G, N);
+      count_launch();
     }
   };
+  // Pressure-acceleration / pressure launches of one group.  With `sig`
+  // non-null nothing is launched: the kernel arguments are appended to the
+  // signature of the device loop instead.  `done` is the loop flag
+  // (nullptr outside the device loop); `prof` brackets the launch with
+  // timing events (never on a capture stream).
   template <int NF, int NB> struct A {
-    static void go(Iisph *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
+    static void go(Iisph *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s, int const *done, bool prof,
+                   std::string *sig) {
       uint32_t n = uint32_t(F.g->count);
-      ProfScope ps(S->model_->prof, "iisph_accel", s);
-      k_iisph_accel<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(F.x), dptr<float>(F.p), dptr<float>(F.rho),
-                                                            dptr<float4>(F.a), S->u(F.rho0), G, S->nbrs<NF, NB>(v)); count_launch();
+      auto N = S->nbrs<NF, NB>(v, s);
+      for (int q = 0; q < NF; ++q) N.f[q].pr = S->model_->packed_pr(S->fluid_[q].g, S->fluid_[q].p, S->fluid_[q].rho, s);
+      float4 const *x = dptr<float4>(F.x);
+      float const *p = dptr<float>(F.p), *rho = dptr<float>(F.rho);
+      float4 *a = dptr<float4>(F.a);
+      float const *rho0 = S->u(F.rho0);
+      if (sig) {
+        sig_add(*sig, n);
+        sig_add(*sig, N);
+        sig_add(*sig, x);
+        sig_add(*sig, p);
+        sig_add(*sig, rho);
+        sig_add(*sig, a);
+        sig_add(*sig, rho0);
+        return;
+      }
+      if (prof) S->model_->prof.begin("iisph_accel", s);
+      k_iisph_accel<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, x, p, rho, a, rho0, G, N, done); count_launch();
+      if (prof) S->model_->prof.end(s);
     }
   };
   template <int NF, int NB> struct P {
-    static void go(Iisph *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s, int first, int last) {
+    static void go(Iisph *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s, int first, int last,
+                   int const *done, bool prof, std::string *sig) {
       uint32_t n = uint32_t(F.g->count);
-      ProfScope ps(S->model_->prof, "iisph_pressure", s);
+      auto N = S->nbrs<NF, NB>(v, s);
+      float *pr = S->model_->pr_buffer(F.g, s);
+      Red R = S->red(*S->model_, 0);
+      if (sig) {
+        sig_add(*sig, n);
+        sig_add(*sig, N);
+        sig_add(*sig, pr);
+        sig_add(*sig, R);
+        void const *ptrs[] = {F.x->d, F.a->d, F.rho->d, F.s->d, F.AA->d, F.p->d, F.Ap->d, S->u(F.rho0)};
+        sig_add(*sig, ptrs);
+        sig_add(*sig, first);
+        sig_add(*sig, last);
+        return;
+      }
+      if (prof) S->model_->prof.begin("iisph_pressure", s);
       k_iisph_pressure<NF, NB><<<red_grid(n), kNT, 0, s>>>(
           n, dptr<float4>(F.x), dptr<float4>(F.a), dptr<float>(F.rho), dptr<float>(F.s), dptr<float>(F.AA),
-          dptr<float>(F.p), dptr<float>(F.Ap), S->u(F.rho0), G, S->nbrs<NF, NB>(v), S->red(*S->model_, 0), first, last); count_launch();
+          dptr<float>(F.p), pr, dptr<float>(F.Ap), S->u(F.rho0), G, N, R, first, last, done);
+      count_launch();
+      if (prof) S->model_->prof.end(s);
     }
   };
   Globals checked_globals() {
     Globals G = globals(*model_);
-    need_globals(G, {{G.h, "smoothing_scale"}, {G.dt, "time_step"}, {G.omega, "iisph_relaxation"},
-                     {G.aprde, "iisph_aprde"}, {G.nprde, "iisph_nprde"}});
+    need({{G.h, "smoothing_scale"}, {G.dt, "time_step"}, {G.omega, "iisph_relaxation"}, {G.aprde, "iisph_aprde"},
+          {G.nprde, "iisph_nprde"}, {G.jac_max, "iisph_maximum_iterations"}});
     return G;
+  }
+  std::vector<FluidG *> active() {
+    std::vector<FluidG *> act;
+    for (auto &F : fluid_)
+      if (F.g->count) act.push_back(&F);
+    return act;
+  }
+  // p and p / rho^2 were written together by a kernel
+  void wrote_pressure(FluidG &F) {
+    F.p->version++;
+    model_->pack_commit(F.g, "pr", {uint64_t(F.g->count), reinterpret_cast<uint64_t>(F.p->d), F.p->version,
+                                    reinterpret_cast<uint64_t>(F.rho->d), F.rho->version});
   }
   void setup(Nhood &nh, cudaStream_t s) {
     Globals G = checked_globals();
     int nf = int(fluid_.size()), nb = int(bound_.size());
-    for (auto &F : fluid_) {
-      if (!F.g->count) continue;
-      dispatch_fb<C>(nf, nb, this, F, nh.lists(F.g->index, s), G, s);
+    for (auto *F : active()) {
+      dispatch_fb<C>(nf, nb, this, *F, lists(nh, F->g, G, s), G, s);
       PG_LAUNCH_CHECK();
+      F->c->version++;
     }
     long long total = 0;
-    for (auto &F : fluid_) {
-      if (!F.g->count) continue;
-      total += (long long)F.g->count;
-      dispatch_fb<SAA>(nf, nb, this, F, nh.lists(F.g->index, s), G, s);
+    for (auto *F : active()) {
+      total += (long long)F->g->count;
+      dispatch_fb<SAA>(nf, nb, this, *F, lists(nh, F->g, G, s), G, s);
       PG_LAUNCH_CHECK();
+      F->s->version++;
+      F->AA->version++;
+      wrote_pressure(*F);
     }
     // nprde = number of fluid particles (the generated reduction adds 1 per particle)
     k_set_i32<<<1, 1, 0, s>>>(G.nprde, int(total)); count_launch();
@@ -1086,24 +1359,87 @@ public:
   void accel(Nhood &nh, cudaStream_t s) {
     Globals G = checked_globals();
     int nf = int(fluid_.size()), nb = int(bound_.size());
-    for (auto &F : fluid_) {
-      if (!F.g->count) continue;
-      dispatch_fb<A>(nf, nb, this, F, nh.lists(F.g->index, s), G, s);
+    for (auto *F : active()) {
+      dispatch_fb<A>(nf, nb, this, *F, lists(nh, F->g, G, s), G, s, static_cast<int const *>(nullptr), true,
+                     static_cast<std::string *>(nullptr));
       PG_LAUNCH_CHECK();
+      F->a->version++;
     }
   }
   void pressure(Nhood &nh, cudaStream_t s) {
     Globals G = checked_globals();
     int nf = int(fluid_.size()), nb = int(bound_.size());
-    std::vector<FluidG *> act;
-    for (auto &F : fluid_)
-      if (F.g->count) act.push_back(&F);
+    auto act = active();
     for (size_t k = 0; k < act.size(); ++k) {
-      dispatch_fb<P>(nf, nb, this, *act[k], nh.lists(act[k]->g->index, s), G, s, k == 0 ? 1 : 0,
-                     k + 1 == act.size() ? 1 : 0);
+      dispatch_fb<P>(nf, nb, this, *act[k], lists(nh, act[k]->g, G, s), G, s, k == 0 ? 1 : 0,
+                     k + 1 == act.size() ? 1 : 0, static_cast<int const *>(nullptr), true,
+                     static_cast<std::string *>(nullptr));
       PG_LAUNCH_CHECK();
+      act[k]->Ap->version++;
+      wrote_pressure(*act[k]);
     }
   }
+  // The relaxed-Jacobi loop on the device: a CUDA graph whose conditional
+  // while node repeats [acceleration, pressure, control] until the control
+  // kernel clears the condition.  With profiling enabled the same kernels
+  // are driven from the host, one iteration at a time, so that each launch
+  // can be timed.
+  void solve(Nhood &nh, cudaStream_t s) {
+    Globals G = checked_globals();
+    need({{G.jac_eta, "iisph_maximum_density_error"}, {G.jac_iters, "iisph_iterations"}});
+    int nf = int(fluid_.size()), nb = int(bound_.size());
+    auto act = active();
+    Red R = red(*model_, 0);
+    int const *done = R.status + kStJacDone;
+    // lists and packed records are made current before the loop, so that
+    // building the loop launches nothing else
+    std::vector<NbrView const *> views;
+    for (auto *F : act) {
+      views.push_back(&lists(nh, F->g, G, s));
+      model_->packed_xs(F->g, F->x, F->m, "xm", s);
+      model_->packed_pr(F->g, F->p, F->rho, s);
+    }
+    for (auto &B : bound_)
+      if (B.g->count) model_->packed_xs(B.g, B.x, B.V, "xV", s);
+    k_jacobi_begin<<<1, 1, 0, s>>>(G, R); count_launch();
+    PG_LAUNCH_CHECK();
+    int kernels = 2 * int(act.size()) + 1;
+    auto body = [&](cudaStream_t cs, cudaGraphConditionalHandle h, bool use_handle, bool prof, std::string *sig) {
+      for (size_t k = 0; k < act.size(); ++k)
+        dispatch_fb<A>(nf, nb, this, *act[k], *views[k], G, cs, done, prof, sig);
+      for (size_t k = 0; k < act.size(); ++k)
+        dispatch_fb<P>(nf, nb, this, *act[k], *views[k], G, cs, k == 0 ? 1 : 0, k + 1 == act.size() ? 1 : 0, done,
+                       prof, sig);
+      if (sig) return;
+      k_jacobi_control<<<1, 1, 0, cs>>>(G, R, h, use_handle ? 1 : 0, use_handle ? kernels : 0); count_launch();
+    };
+    if (model_->prof.enabled) {
+      // host-driven: one iteration per round trip
+      for (int it = 0; it < 100000; ++it) {
+        body(s, cudaGraphConditionalHandle{}, false, true, nullptr);
+        PG_LAUNCH_CHECK();
+        int d = 0;
+        PG_CUDA(cudaMemcpyAsync(&d, done, sizeof(int), cudaMemcpyDeviceToHost, s));
+        PG_CUDA(cudaStreamSynchronize(s));
+        if (d) break;
+      }
+    } else {
+      std::string sig;
+      body(s, cudaGraphConditionalHandle{}, true, false, &sig);
+      sig_add(sig, G);
+      sig_add(sig, R);
+      loop_.run(s, sig, [&](cudaStream_t cs, cudaGraphConditionalHandle h) { body(cs, h, true, false, nullptr); });
+      PG_LAUNCH_CHECK();
+    }
+    for (auto *F : act) {
+      F->a->version++;
+      F->Ap->version++;
+      wrote_pressure(*F);
+    }
+  }
+
+private:
+  WhileLoop loop_;
 };
 
 // ---------------------------------------------------------------------------
@@ -1149,40 +1485,42 @@ public:
       B.V = &B.g->add_varying("volume", ft_real());
     }
     bind(m);
+    loops_.clear();
   }
-  // the "foreach _ neighbor" loops use the particle's own group only
   template <int NB> void diag_launch(FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
     uint32_t n = uint32_t(F.g->count);
-    Nbrs<0, NB> N{};
-    for (int q = 0; q < NB; ++q) N.b[q] = bn(bound_[q], v);
+    auto N = bnbrs<NB>(v, s);
+    float4 const *xmr = model_->packed_xmr(F.g, F.x, F.m, F.rho, s);
     ProfScope ps(model_->prof, "wkbb18_diag", s);
-    k_wkbb18_diag<0, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, uint32_t(F.sp->cap), dptr<float4>(F.x), dptr<float>(F.m),
-                                                         dptr<float>(F.rho), dptr<float>(F.sp), u(F.rho0), u(F.mu), G,
-                                                         nl(v, F.g->index), N); count_launch();
+    k_wkbb18_diag<NB><<<div_up(n, kNT), kNT, 0, s>>>(n, uint32_t(F.sp->cap), xmr, dptr<float>(F.rho),
+                                                      dptr<float>(F.sp), u(F.rho0), u(F.mu), G, nl(v, F.g->index), N);
+    count_launch();
   }
   void diag(Nhood &nh, cudaStream_t s) {
     Globals G = globals(*model_);
     int nb = int(bound_.size());
     for (auto &F : fluid_) {
       if (!F.g->count) continue;
-      NbrView const &v = nh.lists(F.g->index, s);
+      NbrView const &v = lists(nh, F.g, G, s);
       if (nb == 0) diag_launch<0>(F, v, G, s);
       else if (nb == 1) diag_launch<1>(F, v, G, s);
       else if (nb == 2) diag_launch<2>(F, v, G, s);
       else throw Error("unsupported group configuration: at most 2 boundary groups");
       PG_LAUNCH_CHECK();
+      F.sp->version++;
     }
   }
 
+  // solver/cg_openmp.hpp:35-215 on the device: guess and initial residual,
+  // then a device loop of [q = A p, update, p update, control], then apply
   template <int NB> void pcg_group(FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
     uint32_t n = uint32_t(F.g->count);
     ensure_vectors(n);
     PcgArgs P{};
     P.n = n;
     P.cap = uint32_t(F.sp->cap);
-    P.x = dptr<float4>(F.x);
+    P.xmr = model_->packed_xmr(F.g, F.x, F.m, F.rho, s);
     P.v = dptr<float4>(F.v);
-    P.m = dptr<float>(F.m);
     P.rho = dptr<float>(F.rho);
     P.sp = dptr<float>(F.sp);
     P.tb = dptr<float>(F.tb);
@@ -1199,8 +1537,7 @@ public:
     P.max_k = static_cast<int const *>(model_->small_ptr(*F.max_k));
     P.iterations = static_cast<int *>(model_->small_ptr(*F.iters));
     P.self = nl(v, F.g->index);
-    Nbrs<0, NB> N{};
-    for (int q = 0; q < NB; ++q) N.b[q] = bn(bound_[q], v);
+    auto N = bnbrs<NB>(v, s);
     Red R = red(*model_, 1);
     unsigned rg = red_grid(n), eg = div_up(n, 256);
     k_pcg_guess<<<eg, 256, 0, s>>>(P); count_launch();
@@ -1209,37 +1546,42 @@ public:
       k_pcg_init<NB><<<rg, kNT, 0, s>>>(P, G, N, R); count_launch();
     }
     PG_LAUNCH_CHECK();
-    // The loop runs at most max_k + 1 times; the device decides when to stop
-    // and the host polls the decision every few iterations (the kernels of
-    // iterations past the stop return at once).
-    int max_k = 0;
-    PG_CUDA(cudaMemcpyAsync(&max_k, P.max_k, sizeof(int), cudaMemcpyDeviceToHost, s));
-    PG_CUDA(cudaStreamSynchronize(s));
-    int done = 0, issued = 0, chunk = 2;
-    while (!done && issued < max_k + 1) {
-      for (int k = 0; k < chunk && issued < max_k + 1; ++k, ++issued) {
-        {
-          ProfScope ps(model_->prof, "pcg_q", s);
-          k_pcg_q<NB><<<rg, kNT, 0, s>>>(P, G, N, R); count_launch();
-        }
-        {
-          ProfScope ps(model_->prof, "pcg_update", s);
-          k_pcg_update<<<rg, kNT, 0, s>>>(P, R); count_launch();
-        }
-        {
-          ProfScope ps(model_->prof, "pcg_p", s);
-          k_pcg_p<<<rg, kNT, 0, s>>>(P, R); count_launch();
-        }
+    auto body = [&](cudaStream_t cs, cudaGraphConditionalHandle h, bool use_handle, bool prof) {
+      if (prof) model_->prof.begin("pcg_q", cs);
+      k_pcg_q<NB><<<rg, kNT, 0, cs>>>(P, G, N, R); count_launch();
+      if (prof) model_->prof.end(cs);
+      if (prof) model_->prof.begin("pcg_update", cs);
+      k_pcg_update<<<rg, kNT, 0, cs>>>(P, R); count_launch();
+      if (prof) model_->prof.end(cs);
+      if (prof) model_->prof.begin("pcg_p", cs);
+      k_pcg_p<<<rg, kNT, 0, cs>>>(P, R); count_launch();
+      if (prof) model_->prof.end(cs);
+      k_pcg_control<<<1, 1, 0, cs>>>(P, R, h, use_handle ? 1 : 0, use_handle ? 4 : 0); count_launch();
+    };
+    if (model_->prof.enabled) {
+      // host-driven (timed launches): one iteration per round trip
+      for (int it = 0; it < 1000000; ++it) {
+        body(s, cudaGraphConditionalHandle{}, false, true);
+        PG_LAUNCH_CHECK();
+        int active = 0;
+        PG_CUDA(cudaMemcpyAsync(&active, R.status + kStPcgActive, sizeof(int), cudaMemcpyDeviceToHost, s));
+        PG_CUDA(cudaStreamSynchronize(s));
+        if (!active) break;
       }
+    } else {
+      std::string sig;
+      sig_add(sig, P);
+      sig_add(sig, N);
+      sig_add(sig, R);
+      sig_add(sig, G);
+      sig_add(sig, rg);
+      loops_[F.g].run(s, sig, [&](cudaStream_t cs, cudaGraphConditionalHandle h) { body(cs, h, true, false); });
       PG_LAUNCH_CHECK();
-      int active = 0;
-      PG_CUDA(cudaMemcpyAsync(&active, model_->status_d + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
-      PG_CUDA(cudaStreamSynchronize(s));
-      done = !active;
-      chunk = std::min(chunk * 2, 16);
     }
     k_pcg_apply<<<eg, 256, 0, s>>>(P, G, R); count_launch();
     PG_LAUNCH_CHECK();
+    F.vd->version++;
+    F.a->version++;
   }
   void pcg(Nhood &nh, cudaStream_t s) {
     Globals G = globals(*model_);
@@ -1250,7 +1592,7 @@ public:
         model_->small_set(*F.iters, &zero, s);
         continue;
       }
-      NbrView const &v = nh.lists(F.g->index, s);
+      NbrView const &v = lists(nh, F.g, G, s);
       if (nb == 0) pcg_group<0>(F, v, G, s);
       else if (nb == 1) pcg_group<1>(F, v, G, s);
       else if (nb == 2) pcg_group<2>(F, v, G, s);
@@ -1261,6 +1603,7 @@ public:
 private:
   float4 *vec_[5] = {};
   size_t vec_cap_ = 0;
+  std::map<Group *, WhileLoop> loops_;
   void free_vectors() {
     for (auto &p : vec_)
       if (p) {
@@ -1271,6 +1614,7 @@ private:
   }
   void ensure_vectors(size_t n) {
     if (n <= vec_cap_) return;
+    loops_.clear(); // the captured loops hold the old vectors
     free_vectors();
     for (auto &p : vec_) PG_CUDA(cudaMalloc(&p, n * 16));
     vec_cap_ = n;

@@ -67,6 +67,10 @@ def setup_dam_break(m, scene, p):
     m.set_global("fade_duration", float(np.float32(p["fade_duration"])))
     m.set_global("current_time", 0.0)
     m.set_global("maximum_speed", 0.0)
+    # parameters of the device-side relaxed-Jacobi loop (iisph.solve_pressure)
+    m.set_global("iisph_maximum_iterations", int(p["max_iters"]))
+    m.set_global("iisph_maximum_density_error", float(np.float32(p["eta"])))
+    m.set_global("iisph_iterations", 0)
     m.set_uniform("f", "rest_density", float(rho0))
     m.set_uniform("f", "dynamic_viscosity", float(np.float32(p["dynamic_viscosity"])))
     m.set_uniform("f", "wkbb18_maximum_error", float(np.float32(p["wkbb18_maximum_error"])))
@@ -89,16 +93,27 @@ def setup_dam_break(m, scene, p):
 
 class StepLoop:
     """The reference driver loop; ``t`` is kept in double like the script's
-    virtual clock and written to ``current_time`` each step."""
+    virtual clock and written to ``current_time`` each step.
 
-    def __init__(self, m, p):
+    ``device_loop=False`` runs the relaxed-Jacobi loop on the host exactly as
+    the script does (iteration_pressure_acceleration + iteration_pressure,
+    reading aprde after every iteration); ``device_loop=True`` runs the same
+    loop as one procedure, ``iisph.solve_pressure``, on the device."""
+
+    def __init__(self, m, p, device_loop=False):
         self.m, self.p = m, p
+        self.device_loop = device_loop
         self.t = 0.0
         self.steps_since_permute = 0
         self.dt = float(np.float32(p["time_step"]))
 
-    def step(self):
+    def step(self, quiet=False):
+        """One step.  ``quiet`` (device loop only) reads nothing back: the
+        step is queued without a host round trip and the returned counts are
+        None (the device-loop statistics of the model hold them)."""
         m, p = self.m, self.p
+        if quiet and self.device_loop:
+            return self._quiet_step()
         self.steps_since_permute += 1
         m.set_global("current_time", float(np.float32(self.t)))
         m.update()
@@ -111,7 +126,11 @@ class StepLoop:
         m.run("iisph", "setup")
         nprde = m.get_global("iisph_nprde")
         it, rel = 0, 0.0
-        if nprde >= 1:
+        if self.device_loop:
+            m.run("iisph", "solve_pressure")
+            it = int(m.get_global("iisph_iterations"))
+            rel = m.get_global("iisph_aprde") / nprde if nprde >= 1 else 0.0
+        elif nprde >= 1:
             for it in range(1, p["max_iters"] + 1):
                 m.set_global("iisph_aprde", 0.0)
                 m.run("iisph", "iteration_pressure_acceleration")
@@ -129,3 +148,25 @@ class StepLoop:
         m.run("symplectic_euler", "integrate_position")
         self.t += self.dt
         return {"jacobi_iterations": it, "relative_aprde": rel, "pcg_iterations": pcg}
+
+    def _quiet_step(self):
+        m, p = self.m, self.p
+        self.steps_since_permute += 1
+        m.set_global("current_time", float(np.float32(self.t)), asynchronous=True)
+        m.update()
+        if self.steps_since_permute >= p["permute_every"]:
+            m.permute()
+            self.steps_since_permute = 0
+        m.run("density", "compute_density")
+        m.run("gravity", "initialize_acceleration")
+        m.run("symplectic_euler", "integrate_velocity_with_hard_fade")
+        m.run("iisph", "setup")
+        m.run("iisph", "solve_pressure")
+        m.run("symplectic_euler", "integrate_velocity_with_hard_fade")
+        if p.get("viscosity"):
+            m.run("wkbb18", "compute_diagonal")
+            m.run("wkbb18", "accumulate_acceleration")
+            m.run("symplectic_euler", "integrate_velocity_with_hard_fade")
+        m.run("symplectic_euler", "integrate_position")
+        self.t += self.dt
+        return {"jacobi_iterations": None, "relative_aprde": None, "pcg_iterations": None}

@@ -84,3 +84,32 @@ def test_unknown_procedure_and_scheme(pair):
         d.run("iisph", "no_such_procedure")
     with pytest.raises(PrtclNotFound, match="scheme is not registered"):
         make_scheme("prtcl::schemes::iisph[T=f64, N=3, K=Cubic Spline]")
+
+
+def test_solve_pressure_matches_host_loop(oracle_mod):
+    """iisph.solve_pressure (device loop in a CUDA graph) == the script's
+    host loop of iteration_pressure_acceleration + iteration_pressure."""
+    sc = scenes.dam_break(fluid_cells=(14, 18, 10), spacing=0.025, box=(0.7, 0.6, 0.5))
+    p = dict(driver.DAM_BREAK_27K)
+    d1, o = both_scenes(sc, p, oracle_mod)
+    from tests.helpers import both_scenes as _b
+    d2, _ = _b(sc, p, oracle_mod)
+    for m in (d1, d2, o):
+        m.update()
+        m.run("density", "compute_density")
+        m.run("gravity", "initialize_acceleration")
+        m.run("symplectic_euler", "integrate_velocity_with_hard_fade")
+        m.run("iisph", "setup")
+    s1 = driver.StepLoop(d1, p, device_loop=True)
+    d1.run("iisph", "solve_pressure")
+    o.run("iisph", "solve_pressure")
+    it = int(d1.get_global("iisph_iterations"))
+    assert it == int(o.get_global("iisph_iterations")) and it >= 2
+    # host loop with the same number of iterations
+    for k in range(it):
+        d2.set_global("iisph_aprde", 0.0)
+        d2.run("iisph", "iteration_pressure_acceleration")
+        d2.run("iisph", "iteration_pressure")
+    for name, nc in [("pressure", 1), ("acceleration", 3), ("iisph_right_hand_side", 1)]:
+        assert_bitwise(fld(d1, "f", name, nc), fld(d2, "f", name, nc), name + " (device vs host loop)")
+        assert_bitwise(fld(d1, "f", name, nc), fld(o, "f", name, nc), name + " (device vs oracle)")

@@ -10,12 +10,16 @@ from tests.helpers import both_scenes
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("viscosity", [False, True])
-def test_dam_break_steps(oracle_mod, viscosity):
+@pytest.mark.parametrize("viscosity,device_loop,profiled", [(False, False, False), (True, False, False),
+                                                          (True, True, False), (True, True, True)])
+def test_dam_break_steps(oracle_mod, viscosity, device_loop, profiled):
     sc = scenes.dam_break()
     p = dict(driver.DAM_BREAK_27K, viscosity=viscosity)
     d, o = both_scenes(sc, p, oracle_mod)
-    ld, lo = driver.StepLoop(d, p), driver.StepLoop(o, p)
+    if profiled:
+        # per-launch timing drives the device loops from the host: same kernels
+        d.model.profile(True)
+    ld, lo = driver.StepLoop(d, p, device_loop=device_loop), driver.StepLoop(o, p, device_loop=device_loop)
     exact = 0
     steps = 12
     for k in range(steps):
@@ -30,3 +34,6 @@ def test_dam_break_steps(oracle_mod, viscosity):
     # with identical iteration counts every field is computed in the same
     # order; report how many steps stayed bit-identical
     print(f"bit-identical steps: {exact}/{steps}")
+    if profiled:
+        prof = d.model.profile_read()
+        assert prof["iisph_accel"][0] > 0 and prof["pcg_q"][0] > 0
