@@ -330,18 +330,19 @@ __global__ void k_xsorted(PosTable pt, uint32_t const *vals, size_t N, float4 *x
 }
 
 struct ListOut {
-  uint32_t *idx[kMaxGroups];
-  float *gf[kMaxGroups];
+  uint32_t *idx32[kMaxGroups];
+  uint16_t *idx16[kMaxGroups];
   uint32_t cap[kMaxGroups];
-  uint32_t *cnt; // [G][n]
+  uint32_t *cnt;  // [G][n]
+  uint32_t *base; // [G][n]
   uint32_t *maxcnt; // [kMaxGroups]
   uint32_t n;
   int G;
 };
 
 __device__ __forceinline__ void visit_cell(GridView const &gv, float4 const *__restrict__ xs, int cell, f3 xi,
-                                           uint32_t i, ListOut const &lo, uint32_t *c, KernelParams const &K,
-                                           bool with_gf) {
+                                           uint32_t i, ListOut const &lo, uint32_t *c, uint32_t *lo_j,
+                                           uint32_t *hi_j) {
   if (cell < 0) return;
   int s0 = gv.cell_start[cell], s1 = gv.cell_start[cell + 1];
   for (int s = s0; s < s1; ++s) {
@@ -351,26 +352,25 @@ __device__ __forceinline__ void visit_cell(GridView const &gv, float4 const *__r
       uint32_t h = __float_as_uint(xj.w);
       uint32_t g = h >> 28, j = h & 0x0FFFFFFFu;
       uint32_t k = c[g]++;
-      if (k < lo.cap[g]) {
-        size_t o = size_t(k) * lo.n + i;
-        lo.idx[g][o] = j;
-        if (with_gf) lo.gf[g][o] = kgrad_factor(K, d2);
-      }
+      lo_j[g] = min(lo_j[g], j);
+      hi_j[g] = max(hi_j[g], j);
+      if (k < lo.cap[g]) lo.idx32[g][size_t(k) * lo.n + i] = j;
     }
   }
 }
 
 // neighbour lists of one query group (grid query of util/grouped_uniform_grid.hpp:407-531)
 __global__ void k_build_lists(GridView gv, float4 const *__restrict__ xs, float4 const *__restrict__ qpos, int q,
-                              ListOut lo, float const *hp, float *hcache) {
+                              ListOut lo) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  bool with_gf = hp != nullptr;
-  KernelParams K = kparams(with_gf ? *hp : 1.0f);
-  if (i == 0) *hcache = with_gf ? K.h : __int_as_float(0x7fc00000);
   if (i >= lo.n) return;
-  uint32_t c[kMaxGroups];
+  uint32_t c[kMaxGroups], lo_j[kMaxGroups], hi_j[kMaxGroups];
 #pragma unroll
-  for (int g = 0; g < kMaxGroups; ++g) c[g] = 0;
+  for (int g = 0; g < kMaxGroups; ++g) {
+    c[g] = 0;
+    lo_j[g] = 0xFFFFFFFFu;
+    hi_j[g] = 0;
+  }
   float4 x4 = qpos[i];
   f3 xi = mk3(x4);
   int cell = -1;
@@ -384,19 +384,28 @@ __global__ void k_build_lists(GridView gv, float4 const *__restrict__ xs, float4
     fallback = cell < 0;
   }
   if (!fallback) {
-    visit_cell(gv, xs, cell, xi, i, lo, c, K, with_gf);
-    for (int k = 0; k < 26; ++k) visit_cell(gv, xs, gv.cell_adj[size_t(cell) * 26 + k], xi, i, lo, c, K, with_gf);
+    visit_cell(gv, xs, cell, xi, i, lo, c, lo_j, hi_j);
+    for (int k = 0; k < 26; ++k) visit_cell(gv, xs, gv.cell_adj[size_t(cell) * 26 + k], xi, i, lo, c, lo_j, hi_j);
   } else {
     for (int k = 0; k < 13; ++k) {
       int3 p = make_int3(gi.x + c_offsets[k][0], gi.y + c_offsets[k][1], gi.z + c_offsets[k][2]);
-      visit_cell(gv, xs, find_cell(gv, p), xi, i, lo, c, K, with_gf);
+      visit_cell(gv, xs, find_cell(gv, p), xi, i, lo, c, lo_j, hi_j);
       int3 m = make_int3(gi.x - c_offsets[k][0], gi.y - c_offsets[k][1], gi.z - c_offsets[k][2]);
-      visit_cell(gv, xs, find_cell(gv, m), xi, i, lo, c, K, with_gf);
+      visit_cell(gv, xs, find_cell(gv, m), xi, i, lo, c, lo_j, hi_j);
     }
   }
   for (int g = 0; g < lo.G; ++g) {
-    lo.cnt[size_t(g) * lo.n + i] = c[g];
-    if (c[g] > lo.cap[g]) atomicMax(&lo.maxcnt[g], c[g]);
+    uint32_t n = c[g];
+    bool wide = n > 0 && hi_j[g] - lo_j[g] > 0xFFFFu;
+    uint32_t b = n > 0 ? lo_j[g] : 0u;
+    lo.cnt[size_t(g) * lo.n + i] = n | (wide ? kWide : 0u);
+    lo.base[size_t(g) * lo.n + i] = b;
+    if (n > lo.cap[g]) atomicMax(&lo.maxcnt[g], n);
+    else if (!wide)
+      for (uint32_t k = 0; k < n; ++k) {
+        size_t o = size_t(k) * lo.n + i;
+        lo.idx16[g][o] = uint16_t(lo.idx32[g][o] - b);
+      }
   }
 }
 
@@ -452,15 +461,15 @@ Nhood::~Nhood() {
 
 void Nhood::free_lists(Lists &L) {
   for (int g = 0; g < kMaxGroups; ++g) {
-    if (L.idx[g]) cudaFree(L.idx[g]);
-    if (L.gf[g]) cudaFree(L.gf[g]);
-    L.idx[g] = nullptr;
-    L.gf[g] = nullptr;
+    if (L.idx32[g]) cudaFree(L.idx32[g]);
+    if (L.idx16[g]) cudaFree(L.idx16[g]);
+    L.idx32[g] = nullptr;
+    L.idx16[g] = nullptr;
   }
   if (L.cnt) cudaFree(L.cnt);
-  if (L.hcache) cudaFree(L.hcache);
+  if (L.base) cudaFree(L.base);
   L.cnt = nullptr;
-  L.hcache = nullptr;
+  L.base = nullptr;
 }
 
 // Neighborhood::Load (util/neighborhood.cpp:67-98): remember each group's
@@ -633,7 +642,7 @@ std::vector<uint64_t> Nhood::pos_versions() const {
 
 bool Nhood::lists_fresh(Lists const &L) const { return L.epoch == epoch_ && L.pos_versions == pos_versions(); }
 
-void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
+void Nhood::build_lists(int q, Lists &L, cudaStream_t s) {
   int G = int(gg_.size());
   if (G > 8) throw Error("neighbour lists support at most 8 groups");
   size_t n = gg_[q].g->count;
@@ -645,42 +654,38 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
     k_xsorted<<<div_up(N_, 256), 256, 0, s>>>(pt, sorted_vals_, N_, xsorted_); count_launch();
     PG_LAUNCH_CHECK();
   }
-  if (!L.hcache) PG_CUDA(cudaMalloc(&L.hcache, sizeof(float)));
   auto alloc_slots = [&](int g, uint32_t want) {
-    if (L.idx[g]) PG_CUDA(cudaFree(L.idx[g]));
-    if (L.gf[g]) PG_CUDA(cudaFree(L.gf[g]));
-    L.idx[g] = nullptr;
-    L.gf[g] = nullptr;
+    if (L.idx32[g]) PG_CUDA(cudaFree(L.idx32[g]));
+    if (L.idx16[g]) PG_CUDA(cudaFree(L.idx16[g]));
+    L.idx32[g] = nullptr;
+    L.idx16[g] = nullptr;
     if (n > 0) {
-      PG_CUDA(cudaMalloc(&L.idx[g], size_t(want) * n * 4));
-      PG_CUDA(cudaMalloc(&L.gf[g], size_t(want) * n * 4));
+      PG_CUDA(cudaMalloc(&L.idx32[g], size_t(want) * n * 4));
+      PG_CUDA(cudaMalloc(&L.idx16[g], size_t(want) * n * 2));
     }
     L.cap[g] = want;
   };
   for (int attempt = 0; attempt < 8; ++attempt) {
     if (L.n != n || !L.cnt) {
-      for (int g = 0; g < kMaxGroups; ++g) {
-        if (L.idx[g]) PG_CUDA(cudaFree(L.idx[g]));
-        if (L.gf[g]) PG_CUDA(cudaFree(L.gf[g]));
-        L.idx[g] = nullptr;
-        L.gf[g] = nullptr;
-        L.cap[g] = 0;
-      }
-      if (L.cnt) PG_CUDA(cudaFree(L.cnt));
-      L.cnt = nullptr;
+      free_lists(L);
+      for (int g = 0; g < kMaxGroups; ++g) L.cap[g] = 0;
       L.n = n;
-      if (n > 0) PG_CUDA(cudaMalloc(&L.cnt, size_t(G) * n * 4));
+      if (n > 0) {
+        PG_CUDA(cudaMalloc(&L.cnt, size_t(G) * n * 4));
+        PG_CUDA(cudaMalloc(&L.base, size_t(G) * n * 4));
+      }
     }
     for (int g = 0; g < G; ++g)
-      if (!L.idx[g] || L.cap[g] == 0) alloc_slots(g, L.cap[g] ? L.cap[g] : 48u);
+      if (!L.idx32[g] || L.cap[g] == 0) alloc_slots(g, L.cap[g] ? L.cap[g] : 48u);
     if (n == 0) break;
     ListOut lo{};
     for (int g = 0; g < G; ++g) {
-      lo.idx[g] = L.idx[g];
-      lo.gf[g] = L.gf[g];
+      lo.idx32[g] = L.idx32[g];
+      lo.idx16[g] = L.idx16[g];
       lo.cap[g] = L.cap[g];
     }
     lo.cnt = L.cnt;
+    lo.base = L.base;
     lo.maxcnt = stats_d_ + 8;
     lo.n = uint32_t(n);
     lo.G = G;
@@ -689,7 +694,7 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
     float4 const *qpos = static_cast<float4 const *>(gg_[q].pos->d);
     {
       ProfScope ps(model_->prof, "nhood_lists", s);
-      k_build_lists<<<div_up(n, 128), 128, 0, s>>>(gv, xsorted_, qpos, q, lo, h, L.hcache); count_launch();
+      k_build_lists<<<div_up(n, 128), 128, 0, s>>>(gv, xsorted_, qpos, q, lo); count_launch();
     }
     PG_LAUNCH_CHECK();
     PG_CUDA(cudaMemcpyAsync(stats_h_ + 8, stats_d_ + 8, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -705,19 +710,18 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
   }
   L.epoch = epoch_;
   L.pos_versions = pos_versions();
-  L.has_gf = h != nullptr;
   L.view = NbrView{};
   for (int g = 0; g < G; ++g) {
-    L.view.idx[g] = L.idx[g];
-    L.view.gf[g] = L.gf[g];
+    L.view.idx32[g] = L.idx32[g];
+    L.view.idx16[g] = L.idx16[g];
     L.view.cnt[g] = L.cnt ? L.cnt + size_t(g) * n : nullptr;
+    L.view.base[g] = L.base ? L.base + size_t(g) * n : nullptr;
     L.view.cap[g] = L.cap[g];
   }
   L.view.n = uint32_t(n);
-  L.view.hcache = L.hcache;
 }
 
-NbrView const &Nhood::lists(int q, cudaStream_t s, float const *h) {
+NbrView const &Nhood::lists(int q, cudaStream_t s) {
   if (!has_grid_) throw Error("Neighborhood has not been updated");
   if (q < 0 || q >= int(gg_.size())) throw Error("invalid group index");
   Lists &L = lists_[q];
@@ -729,20 +733,19 @@ NbrView const &Nhood::lists(int q, cudaStream_t s, float const *h) {
       if (L.n) {
         PG_CUDA(cudaMalloc(&L.cnt, gg_.size() * L.n * 4));
         PG_CUDA(cudaMemsetAsync(L.cnt, 0, gg_.size() * L.n * 4, s));
-      }
-      if (!L.hcache) {
-        PG_CUDA(cudaMalloc(&L.hcache, sizeof(float)));
-        float nan = std::numeric_limits<float>::quiet_NaN();
-        PG_CUDA(cudaMemcpy(L.hcache, &nan, sizeof(float), cudaMemcpyHostToDevice));
+        PG_CUDA(cudaMalloc(&L.base, gg_.size() * L.n * 4));
+        PG_CUDA(cudaMemsetAsync(L.base, 0, gg_.size() * L.n * 4, s));
       }
       L.view = NbrView{};
-      for (size_t g = 0; g < gg_.size(); ++g) L.view.cnt[g] = L.cnt ? L.cnt + g * L.n : nullptr;
+      for (size_t g = 0; g < gg_.size(); ++g) {
+        L.view.cnt[g] = L.cnt ? L.cnt + g * L.n : nullptr;
+        L.view.base[g] = L.base ? L.base + g * L.n : nullptr;
+      }
       L.view.n = uint32_t(L.n);
-      L.view.hcache = L.hcache;
     }
     return L.view;
   }
-  if (!lists_fresh(L) || (h && !L.has_gf)) build_lists(q, L, s, h);
+  if (!lists_fresh(L)) build_lists(q, L, s);
   return L.view;
 }
 
@@ -805,15 +808,20 @@ size_t Nhood::copy_neighbors(int g, size_t i, int64_t *counts, int64_t *out, siz
   if (i >= v.n) throw Error("CopyNeighbors: index out of range");
   size_t k = 0;
   for (int ng = 0; ng < G; ++ng) {
-    uint32_t c = 0;
+    uint32_t c = 0, b = 0;
     PG_CUDA(cudaMemcpyAsync(&c, v.cnt[ng] + i, 4, cudaMemcpyDeviceToHost, s));
+    PG_CUDA(cudaMemcpyAsync(&b, v.base[ng] + i, 4, cudaMemcpyDeviceToHost, s));
     PG_CUDA(cudaStreamSynchronize(s));
-    counts[ng] = c;
-    for (uint32_t slot = 0; slot < c; ++slot) {
-      uint32_t j = 0;
-      PG_CUDA(cudaMemcpyAsync(&j, v.idx[ng] + size_t(slot) * v.n + i, 4, cudaMemcpyDeviceToHost, s));
+    uint32_t cn = c & ~kWide;
+    counts[ng] = cn;
+    for (uint32_t slot = 0; slot < cn; ++slot) {
+      uint32_t j32 = 0;
+      uint16_t j16 = 0;
+      size_t o = size_t(slot) * v.n + i;
+      PG_CUDA(cudaMemcpyAsync(&j32, v.idx32[ng] + o, 4, cudaMemcpyDeviceToHost, s));
+      PG_CUDA(cudaMemcpyAsync(&j16, v.idx16[ng] + o, 2, cudaMemcpyDeviceToHost, s));
       PG_CUDA(cudaStreamSynchronize(s));
-      if (k < cap) out[k] = j;
+      if (k < cap) out[k] = nbr_host_decode(c, b, j16, j32);
       ++k;
     }
   }
@@ -823,20 +831,27 @@ size_t Nhood::copy_neighbors(int g, size_t i, int64_t *counts, int64_t *out, siz
 void Nhood::copy_lists(int q, int ng, int64_t *offsets, uint32_t *idx, size_t cap, cudaStream_t s) {
   NbrView const &v = lists(q, s);
   size_t n = v.n;
-  std::vector<uint32_t> cnt(n);
+  std::vector<uint32_t> cnt(n), base(n);
   offsets[0] = 0;
   if (n == 0) return;
   PG_CUDA(cudaMemcpyAsync(cnt.data(), v.cnt[ng], n * 4, cudaMemcpyDeviceToHost, s));
-  std::vector<uint32_t> ell;
-  if (v.idx[ng]) {
-    ell.resize(size_t(v.cap[ng]) * n);
-    PG_CUDA(cudaMemcpyAsync(ell.data(), v.idx[ng], ell.size() * 4, cudaMemcpyDeviceToHost, s));
+  PG_CUDA(cudaMemcpyAsync(base.data(), v.base[ng], n * 4, cudaMemcpyDeviceToHost, s));
+  std::vector<uint32_t> e32;
+  std::vector<uint16_t> e16;
+  if (v.idx32[ng]) {
+    e32.resize(size_t(v.cap[ng]) * n);
+    e16.resize(size_t(v.cap[ng]) * n);
+    PG_CUDA(cudaMemcpyAsync(e32.data(), v.idx32[ng], e32.size() * 4, cudaMemcpyDeviceToHost, s));
+    PG_CUDA(cudaMemcpyAsync(e16.data(), v.idx16[ng], e16.size() * 2, cudaMemcpyDeviceToHost, s));
   }
   PG_CUDA(cudaStreamSynchronize(s));
-  for (size_t i = 0; i < n; ++i) offsets[i + 1] = offsets[i] + cnt[i];
+  for (size_t i = 0; i < n; ++i) offsets[i + 1] = offsets[i] + (cnt[i] & ~kWide);
   if (size_t(offsets[n]) > cap) throw Error("copy_lists: capacity too small");
   for (size_t i = 0; i < n; ++i)
-    for (uint32_t k = 0; k < cnt[i]; ++k) idx[offsets[i] + k] = ell[size_t(k) * n + i];
+    for (uint32_t k = 0; k < (cnt[i] & ~kWide); ++k) {
+      size_t o = size_t(k) * n + i;
+      idx[offsets[i] + k] = nbr_host_decode(cnt[i], base[i], e16[o], e32[o]);
+    }
 }
 
 } // namespace prtcl_gpu

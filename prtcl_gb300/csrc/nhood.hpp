@@ -42,17 +42,29 @@
 
 namespace prtcl_gpu {
 
-// device view of a neighbour list set of one query group
+// Device view of the neighbour lists of one query group, one ELL set per
+// neighbour group g (entry k of item i at [k * n + i], so a warp reading
+// entry k of 32 consecutive items touches one contiguous segment):
+//   cnt[g][i]   neighbour count; bit 31 set = "wide" item
+//   base[g][i]  smallest neighbour index of item i
+//   idx16[g]    j - base as 16-bit offsets (items whose neighbours span
+//               fewer than 65536 indices: nearly all after a permute)
+//   idx32[g]    j as 32-bit indices (read for wide items only)
 struct NbrView {
-  uint32_t const *idx[kMaxGroups]; // ELL per neighbour group: idx[g][slot * n + i]
-  float const *gf[kMaxGroups];     // ELL: the pair's kernel-gradient factor (kgrad_factor)
-  uint32_t const *cnt[kMaxGroups]; // per neighbour group: count of item i
+  uint16_t const *idx16[kMaxGroups];
+  uint32_t const *idx32[kMaxGroups];
+  uint32_t const *base[kMaxGroups];
+  uint32_t const *cnt[kMaxGroups];
   uint32_t cap[kMaxGroups];
-  uint32_t n;            // query items
-  float const *hcache;   // smoothing scale the factors were computed with
-                         // (NaN: no factors); kernels compare it with the
-                         // current smoothing scale and recompute on mismatch
+  uint32_t n; // query items
 };
+
+constexpr uint32_t kWide = 0x80000000u;
+
+// host decode of one list entry (tests / CopyNeighbors)
+inline uint32_t nbr_host_decode(uint32_t c, uint32_t base, uint16_t d16, uint32_t d32) {
+  return (c & kWide) ? d32 : base + d16;
+}
 
 struct KeyInfo {
   uint32_t keep = 0;   // informative bit positions of u
@@ -91,10 +103,8 @@ public:
   bool loaded() const { return model_ != nullptr; }
   Model *model() const { return model_; }
 
-  // neighbour lists of query group q (rebuilt when stale); with `h` (the
-  // device smoothing scale) the lists also cache each pair's kernel
-  // gradient factor
-  NbrView const &lists(int q, cudaStream_t s, float const *h = nullptr);
+  // neighbour lists of query group q (rebuilt when stale)
+  NbrView const &lists(int q, cudaStream_t s);
 
   // introspection (tests): sizes and host copies of the grid
   size_t sorted_count() const { return N_; }
@@ -119,17 +129,16 @@ private:
   struct Lists {
     size_t n = 0;
     uint32_t cap[kMaxGroups] = {};
-    uint32_t *idx[kMaxGroups] = {};
-    float *gf[kMaxGroups] = {};
-    uint32_t *cnt = nullptr; // [G][n]
-    float *hcache = nullptr;
-    bool has_gf = false;
+    uint32_t *idx32[kMaxGroups] = {};
+    uint16_t *idx16[kMaxGroups] = {};
+    uint32_t *cnt = nullptr;  // [G][n]
+    uint32_t *base = nullptr; // [G][n]
     uint64_t epoch = 0;
     std::vector<uint64_t> pos_versions;
     NbrView view{};
   };
   void ensure_grid_capacity(size_t n);
-  void build_lists(int q, Lists &L, cudaStream_t s, float const *h);
+  void build_lists(int q, Lists &L, cudaStream_t s);
   bool lists_fresh(Lists const &L) const;
   std::vector<uint64_t> pos_versions() const;
   void free_lists(Lists &L);

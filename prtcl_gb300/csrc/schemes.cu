@@ -45,10 +45,36 @@ constexpr int kStJacIter = 4, kStJacDone = 5;
 // ---------------------------------------------------------------------------
 
 struct NbrList {
-  uint32_t const *idx; // ELL, idx[slot * n + i]
-  float const *gf;     // ELL, cached kernel-gradient factor of the pair
-  uint32_t const *cnt; // count per query item
+  uint16_t const *idx16; // ELL, entry k of item i at [k * n + i]: j - base
+  uint32_t const *idx32; // ELL: j (read for wide items only)
+  uint32_t const *base;  // per item: smallest neighbour index
+  uint32_t const *cnt;   // per item: count, bit 31 = wide
 };
+
+// the neighbour list of one item: count and decoder
+struct NbrIter {
+  uint16_t const *i16;
+  uint32_t const *i32;
+  uint32_t n, b, c;
+  bool wide;
+};
+__device__ __forceinline__ NbrIter nbr_begin(NbrList const &L, uint32_t i, uint32_t n) {
+  NbrIter it;
+  uint32_t c = __ldg(L.cnt + i);
+  it.wide = (c & kWide) != 0;
+  it.c = c & ~kWide;
+  it.b = __ldg(L.base + i);
+  it.i16 = L.idx16 + i;
+  it.i32 = L.idx32 + i;
+  it.n = n;
+  return it;
+}
+// entry k (list entries are streamed once per sweep: evict-first loads keep
+// the gathered particle records in L2)
+__device__ __forceinline__ uint32_t nbr_at(NbrIter const &it, uint32_t k) {
+  size_t o = size_t(k) * it.n;
+  return it.wide ? __ldcs(it.i32 + o) : it.b + uint32_t(__ldcs(it.i16 + o));
+}
 
 struct FluidN {
   NbrList L;
@@ -67,7 +93,6 @@ struct BoundN {
 template <int NF, int NB> struct Nbrs {
   FluidN f[NF > 0 ? NF : 1];
   BoundN b[NB > 0 ? NB : 1];
-  float const *hcache; // smoothing scale of the cached gradient factors
 };
 
 struct Globals {
@@ -95,14 +120,6 @@ struct Red {
 
 __device__ __forceinline__ uint32_t grid_tid() { return blockIdx.x * blockDim.x + threadIdx.x; }
 
-// the pair's kernel gradient: from the cached factor when the lists were
-// built with the current smoothing scale, else evaluated in full
-__device__ __forceinline__ f3 pair_grad(bool cached, NbrList const &L, size_t o, KernelParams const &K, f3 xij) {
-  return cached ? kgrad_from(L.gf[o], xij) : kgradW(K, xij);
-}
-template <class N> __device__ __forceinline__ bool use_cache(N const &nb, KernelParams const &K) {
-  return *nb.hcache == K.h;
-}
 
 // FP64 block sums of NV values, committed by the last block of the launch.
 // Returns true in the last block; out[] is valid in its thread 0.
@@ -148,20 +165,20 @@ __global__ void __launch_bounds__(kNT) k_density(uint32_t n, float4 const *__res
 #pragma unroll
   for (int q = 0; q < NF; ++q) {
     FluidN const &F = N.f[q];
-    uint32_t c = F.L.cnt[i];
+    NbrIter it = nbr_begin(F.L, i, n);
 #pragma unroll 4
-    for (uint32_t k = 0; k < c; ++k) {
-      float4 xm = F.xm[F.L.idx[size_t(k) * n + i]];
+    for (uint32_t k = 0; k < it.c; ++k) {
+      float4 xm = __ldg(F.xm + nbr_at(it, k));
       acc += xm.w * kW(K, sub3(xi, mk3(xm)));
     }
   }
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
-    uint32_t c = B.L.cnt[i];
+    NbrIter it = nbr_begin(B.L, i, n);
 #pragma unroll 4
-    for (uint32_t k = 0; k < c; ++k) {
-      float4 xv = B.xV[B.L.idx[size_t(k) * n + i]];
+    for (uint32_t k = 0; k < it.c; ++k) {
+      float4 xv = __ldg(B.xV + nbr_at(it, k));
       acc += (xv.w * rho0) * kW(K, sub3(xi, mk3(xv)));
     }
   }
@@ -180,8 +197,8 @@ __global__ void __launch_bounds__(kNT) k_volume(uint32_t n, float4 const *__rest
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
-    uint32_t c = B.L.cnt[i];
-    for (uint32_t k = 0; k < c; ++k) acc += kW(K, sub3(xi, mk3(B.xV[B.L.idx[size_t(k) * n + i]])));
+    NbrIter it = nbr_begin(B.L, i, n);
+    for (uint32_t k = 0; k < it.c; ++k) acc += kW(K, sub3(xi, mk3(__ldg(B.xV + nbr_at(it, k)))));
   }
   V[i] = 1.0f / acc;
 }
@@ -249,7 +266,6 @@ __global__ void __launch_bounds__(kNT) k_iisph_c(uint32_t n, float4 const *__res
   uint32_t i = grid_tid();
   if (i >= n) return;
   KernelParams K = kparams(*G.h);
-  bool uc = use_cache(N, K);
   float rho0 = *rho0p;
   f3 xi = mk3(x[i]);
   float ri = rho[i];
@@ -257,23 +273,21 @@ __global__ void __launch_bounds__(kNT) k_iisph_c(uint32_t n, float4 const *__res
 #pragma unroll
   for (int q = 0; q < NF; ++q) {
     FluidN const &F = N.f[q];
-    uint32_t cn = F.L.cnt[i];
+    NbrIter it = nbr_begin(F.L, i, n);
 #pragma unroll 4
-    for (uint32_t k = 0; k < cn; ++k) {
-      size_t o = size_t(k) * n + i;
-      float4 xm = F.xm[F.L.idx[o]];
-      c = sub3(c, scl3(xm.w / (ri * ri), pair_grad(uc, F.L, o, K, sub3(xi, mk3(xm)))));
+    for (uint32_t k = 0; k < it.c; ++k) {
+      float4 xm = __ldg(F.xm + nbr_at(it, k));
+      c = sub3(c, scl3(xm.w / (ri * ri), kgradW(K, sub3(xi, mk3(xm)))));
     }
   }
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
-    uint32_t cn = B.L.cnt[i];
+    NbrIter it = nbr_begin(B.L, i, n);
 #pragma unroll 4
-    for (uint32_t k = 0; k < cn; ++k) {
-      size_t o = size_t(k) * n + i;
-      float4 xv = B.xV[B.L.idx[o]];
-      c = sub3(c, scl3(((0.7f * 2.0f) * rho0) * (xv.w / (ri * ri)), pair_grad(uc, B.L, o, K, sub3(xi, mk3(xv)))));
+    for (uint32_t k = 0; k < it.c; ++k) {
+      float4 xv = __ldg(B.xV + nbr_at(it, k));
+      c = sub3(c, scl3(((0.7f * 2.0f) * rho0) * (xv.w / (ri * ri)), kgradW(K, sub3(xi, mk3(xv)))));
     }
   }
   cout[i] = make_float4(c.x, c.y, c.z, 0.0f);
@@ -291,7 +305,6 @@ __global__ void __launch_bounds__(kNT) k_iisph_s_aa(uint32_t n, float4 const *__
   uint32_t i = grid_tid();
   if (i >= n) return;
   KernelParams K = kparams(*G.h);
-  bool uc = use_cache(N, K);
   float rho0 = *rho0p, dt = *G.dt;
   f3 xi = mk3(x[i]), vi = mk3(v[i]), ci = mk3(cf[i]);
   float mi = m[i], ri = rho[i];
@@ -299,15 +312,14 @@ __global__ void __launch_bounds__(kNT) k_iisph_s_aa(uint32_t n, float4 const *__
 #pragma unroll
   for (int q = 0; q < NF; ++q) {
     FluidN const &F = N.f[q];
-    uint32_t cn = F.L.cnt[i];
+    NbrIter it = nbr_begin(F.L, i, n);
 #pragma unroll 2
-    for (uint32_t k = 0; k < cn; ++k) {
-      size_t o = size_t(k) * n + i;
-      uint32_t j = F.L.idx[o];
-      float4 xm = F.xm[j];
-      f3 g = pair_grad(uc, F.L, o, K, sub3(xi, mk3(xm)));
+    for (uint32_t k = 0; k < it.c; ++k) {
+      uint32_t j = nbr_at(it, k);
+      float4 xm = __ldg(F.xm + j);
+      f3 g = kgradW(K, sub3(xi, mk3(xm)));
       float mj = xm.w;
-      sa += mj * dot3(sub3(vi, mk3(F.v[j])), g);
+      sa += mj * dot3(sub3(vi, mk3(__ldg(F.v + j))), g);
       aa += mj * dot3(ci, g);
       aa -= (mj * (mi / (ri * ri))) * nsq3(g);
     }
@@ -315,12 +327,11 @@ __global__ void __launch_bounds__(kNT) k_iisph_s_aa(uint32_t n, float4 const *__
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
-    uint32_t cn = B.L.cnt[i];
+    NbrIter it = nbr_begin(B.L, i, n);
 #pragma unroll 2
-    for (uint32_t k = 0; k < cn; ++k) {
-      size_t o = size_t(k) * n + i;
-      float4 xv = B.xV[B.L.idx[o]];
-      f3 g = pair_grad(uc, B.L, o, K, sub3(xi, mk3(xv)));
+    for (uint32_t k = 0; k < it.c; ++k) {
+      float4 xv = __ldg(B.xV + nbr_at(it, k));
+      f3 g = kgradW(K, sub3(xi, mk3(xv)));
       float w = rho0 * xv.w;
       sa += w * dot3(sub3(vi, f3{0.0f, 0.0f, 0.0f}), g);
       aa += w * dot3(ci, g);
@@ -345,7 +356,6 @@ __global__ void __launch_bounds__(kNT) k_iisph_accel(uint32_t n, float4 const *_
   uint32_t i = grid_tid();
   if (i >= n) return;
   KernelParams K = kparams(*G.h);
-  bool uc = use_cache(N, K);
   float rho0 = *rho0p;
   f3 xi = mk3(x[i]);
   float pi = p[i], ri = rho[i];
@@ -354,27 +364,25 @@ __global__ void __launch_bounds__(kNT) k_iisph_accel(uint32_t n, float4 const *_
 #pragma unroll
   for (int q = 0; q < NF; ++q) {
     FluidN const &F = N.f[q];
-    uint32_t cn = F.L.cnt[i];
+    NbrIter it = nbr_begin(F.L, i, n);
 #pragma unroll 4
-    for (uint32_t k = 0; k < cn; ++k) {
-      size_t o = size_t(k) * n + i;
-      uint32_t j = F.L.idx[o];
-      float4 xm = F.xm[j];
-      float coef = xm.w * (pri + F.pr[j]);
-      acc = sub3(acc, scl3(coef, pair_grad(uc, F.L, o, K, sub3(xi, mk3(xm)))));
+    for (uint32_t k = 0; k < it.c; ++k) {
+      uint32_t j = nbr_at(it, k);
+      float4 xm = __ldg(F.xm + j);
+      float coef = xm.w * (pri + __ldg(F.pr + j));
+      acc = sub3(acc, scl3(coef, kgradW(K, sub3(xi, mk3(xm)))));
     }
   }
   float bterm = (2.0f * pi) / (ri * ri);
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
-    uint32_t cn = B.L.cnt[i];
+    NbrIter it = nbr_begin(B.L, i, n);
 #pragma unroll 4
-    for (uint32_t k = 0; k < cn; ++k) {
-      size_t o = size_t(k) * n + i;
-      float4 xv = B.xV[B.L.idx[o]];
+    for (uint32_t k = 0; k < it.c; ++k) {
+      float4 xv = __ldg(B.xV + nbr_at(it, k));
       float coef = ((0.7f * rho0) * xv.w) * bterm;
-      acc = sub3(acc, scl3(coef, pair_grad(uc, B.L, o, K, sub3(xi, mk3(xv)))));
+      acc = sub3(acc, scl3(coef, kgradW(K, sub3(xi, mk3(xv)))));
     }
   }
   a[i] = make_float4(acc.x, acc.y, acc.z, 0.0f);
@@ -395,7 +403,6 @@ __global__ void __launch_bounds__(kNT) k_iisph_pressure(uint32_t n, float4 const
                                                         int const *done) {
   if (done && *(volatile int const *)done) return;
   KernelParams K = kparams(*G.h);
-  bool uc = use_cache(N, K);
   float rho0 = *rho0p, dt = *G.dt, omega = *G.omega;
   double part = 0.0;
   for (uint32_t i = grid_tid(); i < n; i += gridDim.x * blockDim.x) {
@@ -404,24 +411,22 @@ __global__ void __launch_bounds__(kNT) k_iisph_pressure(uint32_t n, float4 const
 #pragma unroll
     for (int q = 0; q < NF; ++q) {
       FluidN const &F = N.f[q];
-      uint32_t cn = F.L.cnt[i];
+      NbrIter it = nbr_begin(F.L, i, n);
 #pragma unroll 4
-      for (uint32_t k = 0; k < cn; ++k) {
-        size_t o = size_t(k) * n + i;
-        uint32_t j = F.L.idx[o];
-        float4 xm = F.xm[j];
-        ap += xm.w * dot3(sub3(ai, mk3(F.a[j])), pair_grad(uc, F.L, o, K, sub3(xi, mk3(xm))));
+      for (uint32_t k = 0; k < it.c; ++k) {
+        uint32_t j = nbr_at(it, k);
+        float4 xm = __ldg(F.xm + j);
+        ap += xm.w * dot3(sub3(ai, mk3(__ldg(F.a + j))), kgradW(K, sub3(xi, mk3(xm))));
       }
     }
 #pragma unroll
     for (int q = 0; q < NB; ++q) {
       BoundN const &B = N.b[q];
-      uint32_t cn = B.L.cnt[i];
+      NbrIter it = nbr_begin(B.L, i, n);
 #pragma unroll 4
-      for (uint32_t k = 0; k < cn; ++k) {
-        size_t o = size_t(k) * n + i;
-        float4 xv = B.xV[B.L.idx[o]];
-        ap += (rho0 * xv.w) * dot3(sub3(ai, f3{0.0f, 0.0f, 0.0f}), pair_grad(uc, B.L, o, K, sub3(xi, mk3(xv))));
+      for (uint32_t k = 0; k < it.c; ++k) {
+        float4 xv = __ldg(B.xV + nbr_at(it, k));
+        ap += (rho0 * xv.w) * dot3(sub3(ai, f3{0.0f, 0.0f, 0.0f}), kgradW(K, sub3(xi, mk3(xv))));
       }
     }
     float ri = rho[i];
@@ -516,7 +521,6 @@ __global__ void __launch_bounds__(kNT) k_wkbb18_diag(uint32_t n, uint32_t cap, f
   uint32_t i = grid_tid();
   if (i >= n) return;
   KernelParams K = kparams(*G.h);
-  bool uc = use_cache(N, K);
   float h = K.h, dt = *G.dt, rho0 = *rho0p, mu = *mup;
   f3 xi = mk3(xmr[i]);
   float ri = rho[i];
@@ -525,13 +529,12 @@ __global__ void __launch_bounds__(kNT) k_wkbb18_diag(uint32_t n, uint32_t cap, f
   for (int k = 0; k < 9; ++k) S[k] = 0.0f;
   float hh = (0.01f * h) * h;
   float cmu = 10.0f * (mu / ri);
-  uint32_t cn = self.cnt[i];
-  for (uint32_t k = 0; k < cn; ++k) {
-    size_t o = size_t(k) * n + i;
-    float4 xj = xmr[self.idx[o]];
+  NbrIter it = nbr_begin(self, i, n);
+  for (uint32_t k = 0; k < it.c; ++k) {
+    float4 xj = __ldg(xmr + nbr_at(it, k));
     f3 xij = sub3(xi, mk3(xj));
     float coef = (cmu * xj.w) / (nsq3(xij) + hh);
-    f3 g = pair_grad(uc, self, o, K, xij);
+    f3 g = kgradW(K, xij);
     float gv[3] = {g.x, g.y, g.z}, xv[3] = {xij.x, xij.y, xij.z};
 #pragma unroll
     for (int c = 0; c < 3; ++c)
@@ -542,13 +545,12 @@ __global__ void __launch_bounds__(kNT) k_wkbb18_diag(uint32_t n, uint32_t cap, f
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
     float bmu = *B.mu;
-    uint32_t cb = B.L.cnt[i];
-    for (uint32_t k = 0; k < cb; ++k) {
-      size_t o = size_t(k) * n + i;
-      float4 xv = B.xV[B.L.idx[o]];
+    NbrIter it = nbr_begin(B.L, i, n);
+    for (uint32_t k = 0; k < it.c; ++k) {
+      float4 xv = __ldg(B.xV + nbr_at(it, k));
       f3 xij = sub3(xi, mk3(xv));
       float coef = ((10.0f * (bmu / ri)) * ((rho0 * xv.w) / ri)) / (nsq3(xij) + hh);
-      f3 g = pair_grad(uc, B.L, o, K, xij);
+      f3 g = kgradW(K, xij);
       float gv[3] = {g.x, g.y, g.z}, xw[3] = {xij.x, xij.y, xij.z};
 #pragma unroll
       for (int c = 0; c < 3; ++c)
@@ -594,7 +596,7 @@ struct PcgArgs {
 // system product of wkbb18.accumulate_acceleration (schemes/wkbb18.hpp:
 // 339-396): (A w)_i = w_i - dt * a_f(w)_i
 template <int NB>
-__device__ __forceinline__ f3 wkbb18_system(PcgArgs const &P, KernelParams const &K, bool uc, float dt, float rho0,
+__device__ __forceinline__ f3 wkbb18_system(PcgArgs const &P, KernelParams const &K, float dt, float rho0,
                                             float mu, Nbrs<0, NB> const &N, float4 const *__restrict__ w, uint32_t i) {
   float h = K.h;
   float hh = (0.01f * h) * h;
@@ -602,29 +604,27 @@ __device__ __forceinline__ f3 wkbb18_system(PcgArgs const &P, KernelParams const
   float ri = P.rho[i];
   float cmu = 10.0f * (mu / ri);
   f3 af = {0.0f, 0.0f, 0.0f};
-  uint32_t cn = P.self.cnt[i];
+  NbrIter it = nbr_begin(P.self, i, P.n);
 #pragma unroll 4
-  for (uint32_t k = 0; k < cn; ++k) {
-    size_t o = size_t(k) * P.n + i;
-    uint32_t j = P.self.idx[o];
-    float4 xj = P.xmr[j];
+  for (uint32_t k = 0; k < it.c; ++k) {
+    uint32_t j = nbr_at(it, k);
+    float4 xj = __ldg(P.xmr + j);
     f3 xij = sub3(xi, mk3(xj));
-    float coef = ((cmu * xj.w) * dot3(sub3(wi, mk3(w[j])), xij)) / (nsq3(xij) + hh);
-    af = add3(af, scl3(coef, pair_grad(uc, P.self, o, K, xij)));
+    float coef = ((cmu * xj.w) * dot3(sub3(wi, mk3(__ldg(w + j))), xij)) / (nsq3(xij) + hh);
+    af = add3(af, scl3(coef, kgradW(K, xij)));
   }
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
     float bmu = *B.mu;
     float cb_mu = 10.0f * (bmu / ri);
-    uint32_t cb = B.L.cnt[i];
+    NbrIter it = nbr_begin(B.L, i, P.n);
 #pragma unroll 4
-    for (uint32_t k = 0; k < cb; ++k) {
-      size_t o = size_t(k) * P.n + i;
-      float4 xv = B.xV[B.L.idx[o]];
+    for (uint32_t k = 0; k < it.c; ++k) {
+      float4 xv = __ldg(B.xV + nbr_at(it, k));
       f3 xij = sub3(xi, mk3(xv));
       float coef = ((cb_mu * ((rho0 * xv.w) / ri)) * dot3(wi, xij)) / (nsq3(xij) + hh);
-      af = add3(af, scl3(coef, pair_grad(uc, B.L, o, K, xij)));
+      af = add3(af, scl3(coef, kgradW(K, xij)));
     }
   }
   return sub3(wi, scl3(dt, af));
@@ -642,11 +642,10 @@ __global__ void k_pcg_guess(PcgArgs P) {
 template <int NB>
 __global__ void __launch_bounds__(kNT) k_pcg_init(PcgArgs P, Globals G, Nbrs<0, NB> N, Red R) {
   KernelParams K = kparams(*G.h);
-  bool uc = use_cache(N, K);
   float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
   double bb = 0.0, rr = 0.0, ry = 0.0;
   for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x) {
-    f3 ax = wkbb18_system<NB>(P, K, uc, dt, rho0, mu, N, P.X, i);
+    f3 ax = wkbb18_system<NB>(P, K, dt, rho0, mu, N, P.X, i);
     f3 b = mk3(P.v[i]);
     f3 r = sub3(ax, b);
     f3 y = precond(P.sp, P.cap, i, r);
@@ -676,11 +675,10 @@ template <int NB>
 __global__ void __launch_bounds__(kNT) k_pcg_q(PcgArgs P, Globals G, Nbrs<0, NB> N, Red R) {
   if (!*(volatile int *)&R.status[kStPcgActive]) return;
   KernelParams K = kparams(*G.h);
-  bool uc = use_cache(N, K);
   float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
   double pq = 0.0;
   for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x) {
-    f3 q = wkbb18_system<NB>(P, K, uc, dt, rho0, mu, N, P.P, i);
+    f3 q = wkbb18_system<NB>(P, K, dt, rho0, mu, N, P.P, i);
     P.Q[i] = make_float4(q.x, q.y, q.z, 0.0f);
     pq += double(dot3(mk3(P.P[i]), q));
   }
@@ -946,7 +944,7 @@ protected:
   std::vector<FluidG> fluid_;
   std::vector<BoundG> bound_;
 
-  static NbrList nl(NbrView const &v, int g) { return NbrList{v.idx[g], v.gf[g], v.cnt[g]}; }
+  static NbrList nl(NbrView const &v, int g) { return NbrList{v.idx16[g], v.idx32[g], v.base[g], v.cnt[g]}; }
   // packed neighbour records of the fluid / boundary groups (made current
   // here: may launch a pack kernel on `s`)
   FluidN fn(FluidG const &F, NbrView const &v, cudaStream_t s) {
@@ -969,18 +967,14 @@ protected:
     Nbrs<NF, NB> N{};
     for (int q = 0; q < NF; ++q) N.f[q] = fn(fluid_[q], v, s);
     for (int q = 0; q < NB; ++q) N.b[q] = bn(bound_[q], v, s);
-    N.hcache = v.hcache;
     return N;
   }
   template <int NB> Nbrs<0, NB> bnbrs(NbrView const &v, cudaStream_t s) {
     Nbrs<0, NB> N{};
     for (int q = 0; q < NB; ++q) N.b[q] = bn(bound_[q], v, s);
-    N.hcache = v.hcache;
     return N;
   }
-  NbrView const &lists(Nhood &nh, Group *g, Globals const &G, cudaStream_t s) {
-    return nh.lists(g->index, s, G.h);
-  }
+  NbrView const &lists(Nhood &nh, Group *g, Globals const &, cudaStream_t s) { return nh.lists(g->index, s); }
   float const *u(SmallField *f) { return static_cast<float const *>(model_->small_ptr(*f)); }
   void need(std::initializer_list<std::pair<void const *, char const *>> l) {
     for (auto &p : l)
