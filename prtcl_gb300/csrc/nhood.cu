@@ -2,7 +2,9 @@
 #include "nhood.hpp"
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
+#include <limits>
 
 namespace prtcl_gpu {
 
@@ -59,9 +61,22 @@ __host__ __device__ __forceinline__ bool key_valid(uint32_t u, KeyInfo const &k)
   return true;
 }
 
-__device__ __forceinline__ int3 x_to_gi(float4 x, double radius) {
-  return make_int3(int32_t(floor(double(x.x) / radius)), int32_t(floor(double(x.y) / radius)),
-                   int32_t(floor(double(x.z) / radius)));
+// (int32) floor((double) x / radius) (util/grouped_uniform_grid.hpp:621-632).
+// FP32 fast path: t = x * (1/radius) is within 2^-22.4 |t| of x / radius, so
+// floor(t) is exact unless t lies within that distance of an integer; then
+// (near cell faces) the FP64 division decides.  GB300's FP64 rate is a small
+// fraction of its FP32 rate.
+__device__ __forceinline__ int32_t axis_gi(float x, float rinv, double radius) {
+  float t = x * rinv;
+  float f = floorf(t);
+  float d = t - f;
+  float near = fminf(d, 1.0f - d);
+  if (near > fabsf(t) * 4.76837158203125e-07f + 1e-30f) return int32_t(f);
+  return int32_t(floor(double(x) / radius));
+}
+__device__ __forceinline__ int3 x_to_gi(float4 x, GridView const &gv) {
+  return make_int3(axis_gi(x.x, gv.rinv, gv.radius), axis_gi(x.y, gv.rinv, gv.radius),
+                   axis_gi(x.z, gv.rinv, gv.radius));
 }
 
 __device__ __forceinline__ int find_cell(GridView const &gv, int3 gi) {
@@ -246,7 +261,7 @@ __global__ void k_cells_u(PosTable pt, GridView gv, int G, size_t N, uint32_t *u
   if (n < N) {
     int g = group_of(gv.goff, G, uint32_t(n));
     uint32_t i = uint32_t(n) - gv.goff[g];
-    int3 gi = x_to_gi(pt.pos[g][i], gv.radius);
+    int3 gi = x_to_gi(pt.pos[g][i], gv);
     uint32_t u[3] = {unsign(gi.x), unsign(gi.y), unsign(gi.z)};
     for (int a = 0; a < 3; ++a) {
       uint32_t t = u[a] ^ ((u[a] >> 31) ? 0xFFFFFFFFu : 0u);
@@ -298,7 +313,7 @@ __global__ void k_cells_fill(PosTable pt, GridView gv, uint64_t const *keys, uin
   if (f) {
     cell_start[c] = int32_t(s);
     cell_key[c] = keys[s];
-    int3 gi = x_to_gi(pt.pos[g][i], gv.radius);
+    int3 gi = x_to_gi(pt.pos[g][i], gv);
     cell_gi[c] = make_int4(gi.x, gi.y, gi.z, 0);
   }
   if (s == N - 1) {
@@ -330,46 +345,66 @@ __global__ void k_xsorted(PosTable pt, uint32_t const *vals, size_t N, float4 *x
 }
 
 struct ListOut {
-  uint32_t *idx32[kMaxGroups];
-  uint16_t *idx16[kMaxGroups];
-  uint32_t cap[kMaxGroups];
+  uint32_t *idx32[kMaxListGroups];
+  uint16_t *idx16[kMaxListGroups];
+  float *gf[kMaxListGroups];
+  uint32_t cap[kMaxListGroups];
   uint32_t *cnt;  // [G][n]
   uint32_t *base; // [G][n]
-  uint32_t *maxcnt; // [kMaxGroups]
+  uint32_t *maxcnt; // [kMaxListGroups]
   uint32_t n;
   int G;
 };
 
+// per-group counters of one query item, kept in registers (the group index
+// of a neighbour selects the slot through unrolled compares)
+struct ListAcc {
+  uint32_t c[kMaxListGroups], lo[kMaxListGroups], hi[kMaxListGroups];
+};
+
 __device__ __forceinline__ void visit_cell(GridView const &gv, float4 const *__restrict__ xs, int cell, f3 xi,
-                                           uint32_t i, ListOut const &lo, uint32_t *c, uint32_t *lo_j,
-                                           uint32_t *hi_j) {
+                                           uint32_t i, ListOut const &lo, ListAcc &A, KernelParams const &K,
+                                           bool with_gf) {
   if (cell < 0) return;
   int s0 = gv.cell_start[cell], s1 = gv.cell_start[cell + 1];
   for (int s = s0; s < s1; ++s) {
     float4 xj = xs[s];
     float d2 = nsq3(sub3(xi, mk3(xj)));
-    if (double(d2) < gv.r2) {
+    if (d2 < gv.r2lt) { // == (double) d2 < r^2
       uint32_t h = __float_as_uint(xj.w);
       uint32_t g = h >> 28, j = h & 0x0FFFFFFFu;
-      uint32_t k = c[g]++;
-      lo_j[g] = min(lo_j[g], j);
-      hi_j[g] = max(hi_j[g], j);
-      if (k < lo.cap[g]) lo.idx32[g][size_t(k) * lo.n + i] = j;
+      float f = with_gf ? kgrad_factor(K, d2) : 0.0f;
+#pragma unroll
+      for (int q = 0; q < kMaxListGroups; ++q)
+        if (q == int(g)) {
+          uint32_t k = A.c[q]++;
+          A.lo[q] = min(A.lo[q], j);
+          A.hi[q] = max(A.hi[q], j);
+          if (k < lo.cap[q]) {
+            size_t o = size_t(k) * lo.n + i;
+            lo.idx32[q][o] = j;
+            if (with_gf) lo.gf[q][o] = f;
+          }
+        }
     }
   }
 }
 
 // neighbour lists of one query group (grid query of util/grouped_uniform_grid.hpp:407-531)
-__global__ void k_build_lists(GridView gv, float4 const *__restrict__ xs, float4 const *__restrict__ qpos, int q,
-                              ListOut lo) {
+__global__ void __launch_bounds__(128) k_build_lists(GridView gv, float4 const *__restrict__ xs,
+                                                     float4 const *__restrict__ qpos, int q, ListOut lo,
+                                                     float const *hp, float *hcache) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool with_gf = hp != nullptr;
+  KernelParams K = kparams(with_gf ? *hp : 1.0f);
+  if (i == 0) *hcache = with_gf ? K.h : __int_as_float(0x7fc00000);
   if (i >= lo.n) return;
-  uint32_t c[kMaxGroups], lo_j[kMaxGroups], hi_j[kMaxGroups];
+  ListAcc A;
 #pragma unroll
-  for (int g = 0; g < kMaxGroups; ++g) {
-    c[g] = 0;
-    lo_j[g] = 0xFFFFFFFFu;
-    hi_j[g] = 0;
+  for (int g = 0; g < kMaxListGroups; ++g) {
+    A.c[g] = 0;
+    A.lo[g] = 0xFFFFFFFFu;
+    A.hi[g] = 0;
   }
   float4 x4 = qpos[i];
   f3 xi = mk3(x4);
@@ -379,25 +414,27 @@ __global__ void k_build_lists(GridView gv, float4 const *__restrict__ xs, float4
   if (gv.in_grid[q]) {
     cell = gv.s2c[gv.r2s[gv.goff[q] + i]];
   } else {
-    gi = x_to_gi(x4, gv.radius);
+    gi = x_to_gi(x4, gv);
     cell = find_cell(gv, gi);
     fallback = cell < 0;
   }
   if (!fallback) {
-    visit_cell(gv, xs, cell, xi, i, lo, c, lo_j, hi_j);
-    for (int k = 0; k < 26; ++k) visit_cell(gv, xs, gv.cell_adj[size_t(cell) * 26 + k], xi, i, lo, c, lo_j, hi_j);
+    visit_cell(gv, xs, cell, xi, i, lo, A, K, with_gf);
+    for (int k = 0; k < 26; ++k) visit_cell(gv, xs, gv.cell_adj[size_t(cell) * 26 + k], xi, i, lo, A, K, with_gf);
   } else {
     for (int k = 0; k < 13; ++k) {
       int3 p = make_int3(gi.x + c_offsets[k][0], gi.y + c_offsets[k][1], gi.z + c_offsets[k][2]);
-      visit_cell(gv, xs, find_cell(gv, p), xi, i, lo, c, lo_j, hi_j);
+      visit_cell(gv, xs, find_cell(gv, p), xi, i, lo, A, K, with_gf);
       int3 m = make_int3(gi.x - c_offsets[k][0], gi.y - c_offsets[k][1], gi.z - c_offsets[k][2]);
-      visit_cell(gv, xs, find_cell(gv, m), xi, i, lo, c, lo_j, hi_j);
+      visit_cell(gv, xs, find_cell(gv, m), xi, i, lo, A, K, with_gf);
     }
   }
-  for (int g = 0; g < lo.G; ++g) {
-    uint32_t n = c[g];
-    bool wide = n > 0 && hi_j[g] - lo_j[g] > 0xFFFFu;
-    uint32_t b = n > 0 ? lo_j[g] : 0u;
+#pragma unroll
+  for (int g = 0; g < kMaxListGroups; ++g) {
+    if (g >= lo.G) break;
+    uint32_t n = A.c[g];
+    bool wide = n > 0 && A.hi[g] - A.lo[g] > 0xFFFFu;
+    uint32_t b = n > 0 ? A.lo[g] : 0u;
     lo.cnt[size_t(g) * lo.n + i] = n | (wide ? kWide : 0u);
     lo.base[size_t(g) * lo.n + i] = b;
     if (n > lo.cap[g]) atomicMax(&lo.maxcnt[g], n);
@@ -463,13 +500,17 @@ void Nhood::free_lists(Lists &L) {
   for (int g = 0; g < kMaxGroups; ++g) {
     if (L.idx32[g]) cudaFree(L.idx32[g]);
     if (L.idx16[g]) cudaFree(L.idx16[g]);
+    if (L.gf[g]) cudaFree(L.gf[g]);
     L.idx32[g] = nullptr;
     L.idx16[g] = nullptr;
+    L.gf[g] = nullptr;
   }
   if (L.cnt) cudaFree(L.cnt);
   if (L.base) cudaFree(L.base);
+  if (L.hcache) cudaFree(L.hcache);
   L.cnt = nullptr;
   L.base = nullptr;
+  L.hcache = nullptr;
 }
 
 // Neighborhood::Load (util/neighborhood.cpp:67-98): remember each group's
@@ -536,6 +577,11 @@ GridView Nhood::view() const {
   v.key = key_;
   v.radius = radius_;
   v.r2 = radius_ * radius_;
+  v.rinv = float(1.0 / radius_);
+  // the float threshold T with  d2 < T  <=>  (double) d2 < r2
+  float a = float(v.r2);
+  if (double(a) > v.r2) a = std::nextafter(a, -std::numeric_limits<float>::infinity());
+  v.r2lt = (double(a) == v.r2) ? a : std::nextafter(a, std::numeric_limits<float>::infinity());
   return v;
 }
 
@@ -642,9 +688,9 @@ std::vector<uint64_t> Nhood::pos_versions() const {
 
 bool Nhood::lists_fresh(Lists const &L) const { return L.epoch == epoch_ && L.pos_versions == pos_versions(); }
 
-void Nhood::build_lists(int q, Lists &L, cudaStream_t s) {
+void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
   int G = int(gg_.size());
-  if (G > 8) throw Error("neighbour lists support at most 8 groups");
+  if (G > kMaxListGroups) throw Error("neighbour lists support at most 8 groups");
   size_t n = gg_[q].g->count;
   // sorted positions with handles, from the current positions
   PosTable pt{};
@@ -657,14 +703,18 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s) {
   auto alloc_slots = [&](int g, uint32_t want) {
     if (L.idx32[g]) PG_CUDA(cudaFree(L.idx32[g]));
     if (L.idx16[g]) PG_CUDA(cudaFree(L.idx16[g]));
+    if (L.gf[g]) PG_CUDA(cudaFree(L.gf[g]));
     L.idx32[g] = nullptr;
     L.idx16[g] = nullptr;
+    L.gf[g] = nullptr;
     if (n > 0) {
       PG_CUDA(cudaMalloc(&L.idx32[g], size_t(want) * n * 4));
       PG_CUDA(cudaMalloc(&L.idx16[g], size_t(want) * n * 2));
+      PG_CUDA(cudaMalloc(&L.gf[g], size_t(want) * n * 4));
     }
     L.cap[g] = want;
   };
+  if (!L.hcache) PG_CUDA(cudaMalloc(&L.hcache, sizeof(float)));
   for (int attempt = 0; attempt < 8; ++attempt) {
     if (L.n != n || !L.cnt) {
       free_lists(L);
@@ -682,6 +732,7 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s) {
     for (int g = 0; g < G; ++g) {
       lo.idx32[g] = L.idx32[g];
       lo.idx16[g] = L.idx16[g];
+      lo.gf[g] = L.gf[g];
       lo.cap[g] = L.cap[g];
     }
     lo.cnt = L.cnt;
@@ -694,7 +745,7 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s) {
     float4 const *qpos = static_cast<float4 const *>(gg_[q].pos->d);
     {
       ProfScope ps(model_->prof, "nhood_lists", s);
-      k_build_lists<<<div_up(n, 128), 128, 0, s>>>(gv, xsorted_, qpos, q, lo); count_launch();
+      k_build_lists<<<div_up(n, 128), 128, 0, s>>>(gv, xsorted_, qpos, q, lo, h, L.hcache); count_launch();
     }
     PG_LAUNCH_CHECK();
     PG_CUDA(cudaMemcpyAsync(stats_h_ + 8, stats_d_ + 8, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -710,10 +761,13 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s) {
   }
   L.epoch = epoch_;
   L.pos_versions = pos_versions();
+  L.has_gf = h != nullptr;
   L.view = NbrView{};
+  L.view.hcache = L.hcache;
   for (int g = 0; g < G; ++g) {
     L.view.idx32[g] = L.idx32[g];
     L.view.idx16[g] = L.idx16[g];
+    L.view.gf[g] = L.gf[g];
     L.view.cnt[g] = L.cnt ? L.cnt + size_t(g) * n : nullptr;
     L.view.base[g] = L.base ? L.base + size_t(g) * n : nullptr;
     L.view.cap[g] = L.cap[g];
@@ -721,7 +775,7 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s) {
   L.view.n = uint32_t(n);
 }
 
-NbrView const &Nhood::lists(int q, cudaStream_t s) {
+NbrView const &Nhood::lists(int q, cudaStream_t s, float const *h) {
   if (!has_grid_) throw Error("Neighborhood has not been updated");
   if (q < 0 || q >= int(gg_.size())) throw Error("invalid group index");
   Lists &L = lists_[q];
@@ -736,16 +790,22 @@ NbrView const &Nhood::lists(int q, cudaStream_t s) {
         PG_CUDA(cudaMalloc(&L.base, gg_.size() * L.n * 4));
         PG_CUDA(cudaMemsetAsync(L.base, 0, gg_.size() * L.n * 4, s));
       }
+      if (!L.hcache) {
+        PG_CUDA(cudaMalloc(&L.hcache, sizeof(float)));
+        float nan = std::numeric_limits<float>::quiet_NaN();
+        PG_CUDA(cudaMemcpy(L.hcache, &nan, sizeof(float), cudaMemcpyHostToDevice));
+      }
       L.view = NbrView{};
       for (size_t g = 0; g < gg_.size(); ++g) {
         L.view.cnt[g] = L.cnt ? L.cnt + g * L.n : nullptr;
         L.view.base[g] = L.base ? L.base + g * L.n : nullptr;
       }
       L.view.n = uint32_t(L.n);
+      L.view.hcache = L.hcache;
     }
     return L.view;
   }
-  if (!lists_fresh(L)) build_lists(q, L, s);
+  if (!lists_fresh(L) || (h && !L.has_gf)) build_lists(q, L, s, h);
   return L.view;
 }
 

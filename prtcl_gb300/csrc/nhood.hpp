@@ -50,14 +50,22 @@ namespace prtcl_gpu {
 //   idx16[g]    j - base as 16-bit offsets (items whose neighbours span
 //               fewer than 65536 indices: nearly all after a permute)
 //   idx32[g]    j as 32-bit indices (read for wide items only)
+//   gf[g]       the pair's kernel-gradient factor (kgrad_factor), when the
+//               lists were built with a smoothing scale (hcache, device);
+//               kernels use it only while hcache equals the current
+//               smoothing scale and evaluate the gradient in full otherwise
 struct NbrView {
   uint16_t const *idx16[kMaxGroups];
   uint32_t const *idx32[kMaxGroups];
+  float const *gf[kMaxGroups];
   uint32_t const *base[kMaxGroups];
   uint32_t const *cnt[kMaxGroups];
   uint32_t cap[kMaxGroups];
-  uint32_t n; // query items
+  uint32_t n;          // query items
+  float const *hcache; // NaN when no factors were computed
 };
+
+constexpr int kMaxListGroups = 8; // groups a neighbour-list build supports
 
 constexpr uint32_t kWide = 0x80000000u;
 
@@ -86,6 +94,8 @@ struct GridView {
   int in_grid[kMaxGroups];
   KeyInfo key;
   double radius, r2;
+  float rinv;  // 1 / radius rounded to f32 (fast path of the cell index)
+  float r2lt;  // d2 < r2lt  <=>  (double) d2 < r2, for every float d2
 };
 
 class Nhood {
@@ -103,8 +113,10 @@ public:
   bool loaded() const { return model_ != nullptr; }
   Model *model() const { return model_; }
 
-  // neighbour lists of query group q (rebuilt when stale)
-  NbrView const &lists(int q, cudaStream_t s);
+  // neighbour lists of query group q (rebuilt when stale); with `h` (the
+  // smoothing scale on the device) they also hold each pair's kernel
+  // gradient factor
+  NbrView const &lists(int q, cudaStream_t s, float const *h = nullptr);
 
   // introspection (tests): sizes and host copies of the grid
   size_t sorted_count() const { return N_; }
@@ -131,14 +143,17 @@ private:
     uint32_t cap[kMaxGroups] = {};
     uint32_t *idx32[kMaxGroups] = {};
     uint16_t *idx16[kMaxGroups] = {};
+    float *gf[kMaxGroups] = {};
     uint32_t *cnt = nullptr;  // [G][n]
     uint32_t *base = nullptr; // [G][n]
+    float *hcache = nullptr;
+    bool has_gf = false;
     uint64_t epoch = 0;
     std::vector<uint64_t> pos_versions;
     NbrView view{};
   };
   void ensure_grid_capacity(size_t n);
-  void build_lists(int q, Lists &L, cudaStream_t s);
+  void build_lists(int q, Lists &L, cudaStream_t s, float const *h);
   bool lists_fresh(Lists const &L) const;
   std::vector<uint64_t> pos_versions() const;
   void free_lists(Lists &L);

@@ -47,6 +47,7 @@ constexpr int kStJacIter = 4, kStJacDone = 5;
 struct NbrList {
   uint16_t const *idx16; // ELL, entry k of item i at [k * n + i]: j - base
   uint32_t const *idx32; // ELL: j (read for wide items only)
+  float const *gf;       // ELL: the pair's kernel-gradient factor
   uint32_t const *base;  // per item: smallest neighbour index
   uint32_t const *cnt;   // per item: count, bit 31 = wide
 };
@@ -55,6 +56,7 @@ struct NbrList {
 struct NbrIter {
   uint16_t const *i16;
   uint32_t const *i32;
+  float const *gf;
   uint32_t n, b, c;
   bool wide;
 };
@@ -66,6 +68,7 @@ __device__ __forceinline__ NbrIter nbr_begin(NbrList const &L, uint32_t i, uint3
   it.b = __ldg(L.base + i);
   it.i16 = L.idx16 + i;
   it.i32 = L.idx32 + i;
+  it.gf = L.gf + i;
   it.n = n;
   return it;
 }
@@ -74,6 +77,11 @@ __device__ __forceinline__ NbrIter nbr_begin(NbrList const &L, uint32_t i, uint3
 __device__ __forceinline__ uint32_t nbr_at(NbrIter const &it, uint32_t k) {
   size_t o = size_t(k) * it.n;
   return it.wide ? __ldcs(it.i32 + o) : it.b + uint32_t(__ldcs(it.i16 + o));
+}
+// kernel gradient of entry k: from the cached factor (bit-identical to
+// kgradW) when the lists were built with the current smoothing scale
+__device__ __forceinline__ f3 nbr_grad(NbrIter const &it, uint32_t k, bool cached, KernelParams const &K, f3 xij) {
+  return cached ? kgrad_from(__ldcs(it.gf + size_t(k) * it.n), xij) : kgradW(K, xij);
 }
 
 struct FluidN {
@@ -93,7 +101,11 @@ struct BoundN {
 template <int NF, int NB> struct Nbrs {
   FluidN f[NF > 0 ? NF : 1];
   BoundN b[NB > 0 ? NB : 1];
+  float const *hcache; // smoothing scale of the cached gradient factors
 };
+template <class N> __device__ __forceinline__ bool use_cache(N const &nb, KernelParams const &K) {
+  return *nb.hcache == K.h;
+}
 
 struct Globals {
   float const *h;
@@ -266,6 +278,7 @@ __global__ void __launch_bounds__(kNT) k_iisph_c(uint32_t n, float4 const *__res
   uint32_t i = grid_tid();
   if (i >= n) return;
   KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
   float rho0 = *rho0p;
   f3 xi = mk3(x[i]);
   float ri = rho[i];
@@ -277,7 +290,7 @@ __global__ void __launch_bounds__(kNT) k_iisph_c(uint32_t n, float4 const *__res
 #pragma unroll 4
     for (uint32_t k = 0; k < it.c; ++k) {
       float4 xm = __ldg(F.xm + nbr_at(it, k));
-      c = sub3(c, scl3(xm.w / (ri * ri), kgradW(K, sub3(xi, mk3(xm)))));
+      c = sub3(c, scl3(xm.w / (ri * ri), nbr_grad(it, k, uc, K, sub3(xi, mk3(xm)))));
     }
   }
 #pragma unroll
@@ -287,7 +300,7 @@ __global__ void __launch_bounds__(kNT) k_iisph_c(uint32_t n, float4 const *__res
 #pragma unroll 4
     for (uint32_t k = 0; k < it.c; ++k) {
       float4 xv = __ldg(B.xV + nbr_at(it, k));
-      c = sub3(c, scl3(((0.7f * 2.0f) * rho0) * (xv.w / (ri * ri)), kgradW(K, sub3(xi, mk3(xv)))));
+      c = sub3(c, scl3(((0.7f * 2.0f) * rho0) * (xv.w / (ri * ri)), nbr_grad(it, k, uc, K, sub3(xi, mk3(xv)))));
     }
   }
   cout[i] = make_float4(c.x, c.y, c.z, 0.0f);
@@ -305,6 +318,7 @@ __global__ void __launch_bounds__(kNT) k_iisph_s_aa(uint32_t n, float4 const *__
   uint32_t i = grid_tid();
   if (i >= n) return;
   KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
   float rho0 = *rho0p, dt = *G.dt;
   f3 xi = mk3(x[i]), vi = mk3(v[i]), ci = mk3(cf[i]);
   float mi = m[i], ri = rho[i];
@@ -317,7 +331,7 @@ __global__ void __launch_bounds__(kNT) k_iisph_s_aa(uint32_t n, float4 const *__
     for (uint32_t k = 0; k < it.c; ++k) {
       uint32_t j = nbr_at(it, k);
       float4 xm = __ldg(F.xm + j);
-      f3 g = kgradW(K, sub3(xi, mk3(xm)));
+      f3 g = nbr_grad(it, k, uc, K, sub3(xi, mk3(xm)));
       float mj = xm.w;
       sa += mj * dot3(sub3(vi, mk3(__ldg(F.v + j))), g);
       aa += mj * dot3(ci, g);
@@ -331,7 +345,7 @@ __global__ void __launch_bounds__(kNT) k_iisph_s_aa(uint32_t n, float4 const *__
 #pragma unroll 2
     for (uint32_t k = 0; k < it.c; ++k) {
       float4 xv = __ldg(B.xV + nbr_at(it, k));
-      f3 g = kgradW(K, sub3(xi, mk3(xv)));
+      f3 g = nbr_grad(it, k, uc, K, sub3(xi, mk3(xv)));
       float w = rho0 * xv.w;
       sa += w * dot3(sub3(vi, f3{0.0f, 0.0f, 0.0f}), g);
       aa += w * dot3(ci, g);
@@ -356,6 +370,7 @@ __global__ void __launch_bounds__(kNT) k_iisph_accel(uint32_t n, float4 const *_
   uint32_t i = grid_tid();
   if (i >= n) return;
   KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
   float rho0 = *rho0p;
   f3 xi = mk3(x[i]);
   float pi = p[i], ri = rho[i];
@@ -370,7 +385,7 @@ __global__ void __launch_bounds__(kNT) k_iisph_accel(uint32_t n, float4 const *_
       uint32_t j = nbr_at(it, k);
       float4 xm = __ldg(F.xm + j);
       float coef = xm.w * (pri + __ldg(F.pr + j));
-      acc = sub3(acc, scl3(coef, kgradW(K, sub3(xi, mk3(xm)))));
+      acc = sub3(acc, scl3(coef, nbr_grad(it, k, uc, K, sub3(xi, mk3(xm)))));
     }
   }
   float bterm = (2.0f * pi) / (ri * ri);
@@ -382,7 +397,7 @@ __global__ void __launch_bounds__(kNT) k_iisph_accel(uint32_t n, float4 const *_
     for (uint32_t k = 0; k < it.c; ++k) {
       float4 xv = __ldg(B.xV + nbr_at(it, k));
       float coef = ((0.7f * rho0) * xv.w) * bterm;
-      acc = sub3(acc, scl3(coef, kgradW(K, sub3(xi, mk3(xv)))));
+      acc = sub3(acc, scl3(coef, nbr_grad(it, k, uc, K, sub3(xi, mk3(xv)))));
     }
   }
   a[i] = make_float4(acc.x, acc.y, acc.z, 0.0f);
@@ -403,6 +418,7 @@ __global__ void __launch_bounds__(kNT) k_iisph_pressure(uint32_t n, float4 const
                                                         int const *done) {
   if (done && *(volatile int const *)done) return;
   KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
   float rho0 = *rho0p, dt = *G.dt, omega = *G.omega;
   double part = 0.0;
   for (uint32_t i = grid_tid(); i < n; i += gridDim.x * blockDim.x) {
@@ -416,7 +432,7 @@ __global__ void __launch_bounds__(kNT) k_iisph_pressure(uint32_t n, float4 const
       for (uint32_t k = 0; k < it.c; ++k) {
         uint32_t j = nbr_at(it, k);
         float4 xm = __ldg(F.xm + j);
-        ap += xm.w * dot3(sub3(ai, mk3(__ldg(F.a + j))), kgradW(K, sub3(xi, mk3(xm))));
+        ap += xm.w * dot3(sub3(ai, mk3(__ldg(F.a + j))), nbr_grad(it, k, uc, K, sub3(xi, mk3(xm))));
       }
     }
 #pragma unroll
@@ -426,7 +442,7 @@ __global__ void __launch_bounds__(kNT) k_iisph_pressure(uint32_t n, float4 const
 #pragma unroll 4
       for (uint32_t k = 0; k < it.c; ++k) {
         float4 xv = __ldg(B.xV + nbr_at(it, k));
-        ap += (rho0 * xv.w) * dot3(sub3(ai, f3{0.0f, 0.0f, 0.0f}), kgradW(K, sub3(xi, mk3(xv))));
+        ap += (rho0 * xv.w) * dot3(sub3(ai, f3{0.0f, 0.0f, 0.0f}), nbr_grad(it, k, uc, K, sub3(xi, mk3(xv))));
       }
     }
     float ri = rho[i];
@@ -521,6 +537,7 @@ __global__ void __launch_bounds__(kNT) k_wkbb18_diag(uint32_t n, uint32_t cap, f
   uint32_t i = grid_tid();
   if (i >= n) return;
   KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
   float h = K.h, dt = *G.dt, rho0 = *rho0p, mu = *mup;
   f3 xi = mk3(xmr[i]);
   float ri = rho[i];
@@ -534,7 +551,7 @@ __global__ void __launch_bounds__(kNT) k_wkbb18_diag(uint32_t n, uint32_t cap, f
     float4 xj = __ldg(xmr + nbr_at(it, k));
     f3 xij = sub3(xi, mk3(xj));
     float coef = (cmu * xj.w) / (nsq3(xij) + hh);
-    f3 g = kgradW(K, xij);
+    f3 g = nbr_grad(it, k, uc, K, xij);
     float gv[3] = {g.x, g.y, g.z}, xv[3] = {xij.x, xij.y, xij.z};
 #pragma unroll
     for (int c = 0; c < 3; ++c)
@@ -550,7 +567,7 @@ __global__ void __launch_bounds__(kNT) k_wkbb18_diag(uint32_t n, uint32_t cap, f
       float4 xv = __ldg(B.xV + nbr_at(it, k));
       f3 xij = sub3(xi, mk3(xv));
       float coef = ((10.0f * (bmu / ri)) * ((rho0 * xv.w) / ri)) / (nsq3(xij) + hh);
-      f3 g = kgradW(K, xij);
+      f3 g = nbr_grad(it, k, uc, K, xij);
       float gv[3] = {g.x, g.y, g.z}, xw[3] = {xij.x, xij.y, xij.z};
 #pragma unroll
       for (int c = 0; c < 3; ++c)
@@ -596,7 +613,7 @@ struct PcgArgs {
 // system product of wkbb18.accumulate_acceleration (schemes/wkbb18.hpp:
 // 339-396): (A w)_i = w_i - dt * a_f(w)_i
 template <int NB>
-__device__ __forceinline__ f3 wkbb18_system(PcgArgs const &P, KernelParams const &K, float dt, float rho0,
+__device__ __forceinline__ f3 wkbb18_system(PcgArgs const &P, KernelParams const &K, bool uc, float dt, float rho0,
                                             float mu, Nbrs<0, NB> const &N, float4 const *__restrict__ w, uint32_t i) {
   float h = K.h;
   float hh = (0.01f * h) * h;
@@ -611,7 +628,7 @@ __device__ __forceinline__ f3 wkbb18_system(PcgArgs const &P, KernelParams const
     float4 xj = __ldg(P.xmr + j);
     f3 xij = sub3(xi, mk3(xj));
     float coef = ((cmu * xj.w) * dot3(sub3(wi, mk3(__ldg(w + j))), xij)) / (nsq3(xij) + hh);
-    af = add3(af, scl3(coef, kgradW(K, xij)));
+    af = add3(af, scl3(coef, nbr_grad(it, k, uc, K, xij)));
   }
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
@@ -624,7 +641,7 @@ __device__ __forceinline__ f3 wkbb18_system(PcgArgs const &P, KernelParams const
       float4 xv = __ldg(B.xV + nbr_at(it, k));
       f3 xij = sub3(xi, mk3(xv));
       float coef = ((cb_mu * ((rho0 * xv.w) / ri)) * dot3(wi, xij)) / (nsq3(xij) + hh);
-      af = add3(af, scl3(coef, kgradW(K, xij)));
+      af = add3(af, scl3(coef, nbr_grad(it, k, uc, K, xij)));
     }
   }
   return sub3(wi, scl3(dt, af));
@@ -642,10 +659,11 @@ __global__ void k_pcg_guess(PcgArgs P) {
 template <int NB>
 __global__ void __launch_bounds__(kNT) k_pcg_init(PcgArgs P, Globals G, Nbrs<0, NB> N, Red R) {
   KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
   float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
   double bb = 0.0, rr = 0.0, ry = 0.0;
   for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x) {
-    f3 ax = wkbb18_system<NB>(P, K, dt, rho0, mu, N, P.X, i);
+    f3 ax = wkbb18_system<NB>(P, K, uc, dt, rho0, mu, N, P.X, i);
     f3 b = mk3(P.v[i]);
     f3 r = sub3(ax, b);
     f3 y = precond(P.sp, P.cap, i, r);
@@ -675,10 +693,11 @@ template <int NB>
 __global__ void __launch_bounds__(kNT) k_pcg_q(PcgArgs P, Globals G, Nbrs<0, NB> N, Red R) {
   if (!*(volatile int *)&R.status[kStPcgActive]) return;
   KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
   float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
   double pq = 0.0;
   for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x) {
-    f3 q = wkbb18_system<NB>(P, K, dt, rho0, mu, N, P.P, i);
+    f3 q = wkbb18_system<NB>(P, K, uc, dt, rho0, mu, N, P.P, i);
     P.Q[i] = make_float4(q.x, q.y, q.z, 0.0f);
     pq += double(dot3(mk3(P.P[i]), q));
   }
@@ -944,7 +963,7 @@ protected:
   std::vector<FluidG> fluid_;
   std::vector<BoundG> bound_;
 
-  static NbrList nl(NbrView const &v, int g) { return NbrList{v.idx16[g], v.idx32[g], v.base[g], v.cnt[g]}; }
+  static NbrList nl(NbrView const &v, int g) { return NbrList{v.idx16[g], v.idx32[g], v.gf[g], v.base[g], v.cnt[g]}; }
   // packed neighbour records of the fluid / boundary groups (made current
   // here: may launch a pack kernel on `s`)
   FluidN fn(FluidG const &F, NbrView const &v, cudaStream_t s) {
@@ -967,14 +986,16 @@ protected:
     Nbrs<NF, NB> N{};
     for (int q = 0; q < NF; ++q) N.f[q] = fn(fluid_[q], v, s);
     for (int q = 0; q < NB; ++q) N.b[q] = bn(bound_[q], v, s);
+    N.hcache = v.hcache;
     return N;
   }
   template <int NB> Nbrs<0, NB> bnbrs(NbrView const &v, cudaStream_t s) {
     Nbrs<0, NB> N{};
     for (int q = 0; q < NB; ++q) N.b[q] = bn(bound_[q], v, s);
+    N.hcache = v.hcache;
     return N;
   }
-  NbrView const &lists(Nhood &nh, Group *g, Globals const &, cudaStream_t s) { return nh.lists(g->index, s); }
+  NbrView const &lists(Nhood &nh, Group *g, Globals const &G, cudaStream_t s) { return nh.lists(g->index, s, G.h); }
   float const *u(SmallField *f) { return static_cast<float const *>(model_->small_ptr(*f)); }
   void need(std::initializer_list<std::pair<void const *, char const *>> l) {
     for (auto &p : l)
