@@ -714,7 +714,6 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
     }
     L.cap[g] = want;
   };
-  if (!L.hcache) PG_CUDA(cudaMalloc(&L.hcache, sizeof(float)));
   for (int attempt = 0; attempt < 8; ++attempt) {
     if (L.n != n || !L.cnt) {
       free_lists(L);
@@ -727,6 +726,8 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
     }
     for (int g = 0; g < G; ++g)
       if (!L.idx32[g] || L.cap[g] == 0) alloc_slots(g, L.cap[g] ? L.cap[g] : 48u);
+    // after any free_lists() above: the kernel always writes *hcache
+    if (!L.hcache) PG_CUDA(cudaMalloc(&L.hcache, sizeof(float)));
     if (n == 0) break;
     ListOut lo{};
     for (int g = 0; g < G; ++g) {
