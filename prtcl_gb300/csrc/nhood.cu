@@ -349,8 +349,7 @@ struct ListOut {
   uint16_t *idx16[kMaxListGroups];
   float *gf[kMaxListGroups];
   uint32_t cap[kMaxListGroups];
-  uint32_t *cnt;  // [G][n]
-  uint32_t *base; // [G][n]
+  uint2 *cb;        // [G][n]
   uint32_t *maxcnt; // [kMaxListGroups]
   uint32_t n;
   int G;
@@ -381,7 +380,7 @@ __device__ __forceinline__ void visit_cell(GridView const &gv, float4 const *__r
           A.lo[q] = min(A.lo[q], j);
           A.hi[q] = max(A.hi[q], j);
           if (k < lo.cap[q]) {
-            size_t o = size_t(k) * lo.n + i;
+            size_t o = size_t(i) * lo.cap[q] + k;
             lo.idx32[q][o] = j;
             if (with_gf) lo.gf[q][o] = f;
           }
@@ -435,14 +434,12 @@ __global__ void __launch_bounds__(128) k_build_lists(GridView gv, float4 const *
     uint32_t n = A.c[g];
     bool wide = n > 0 && A.hi[g] - A.lo[g] > 0xFFFFu;
     uint32_t b = n > 0 ? A.lo[g] : 0u;
-    lo.cnt[size_t(g) * lo.n + i] = n | (wide ? kWide : 0u);
-    lo.base[size_t(g) * lo.n + i] = b;
+    lo.cb[size_t(g) * lo.n + i] = make_uint2(n | (wide ? kWide : 0u), b);
     if (n > lo.cap[g]) atomicMax(&lo.maxcnt[g], n);
-    else if (!wide)
-      for (uint32_t k = 0; k < n; ++k) {
-        size_t o = size_t(k) * lo.n + i;
-        lo.idx16[g][o] = uint16_t(lo.idx32[g][o] - b);
-      }
+    else if (!wide) {
+      size_t row = size_t(i) * lo.cap[g];
+      for (uint32_t k = 0; k < n; ++k) lo.idx16[g][row + k] = uint16_t(lo.idx32[g][row + k] - b);
+    }
   }
 }
 
@@ -505,11 +502,9 @@ void Nhood::free_lists(Lists &L) {
     L.idx16[g] = nullptr;
     L.gf[g] = nullptr;
   }
-  if (L.cnt) cudaFree(L.cnt);
-  if (L.base) cudaFree(L.base);
+  if (L.cb) cudaFree(L.cb);
   if (L.hcache) cudaFree(L.hcache);
-  L.cnt = nullptr;
-  L.base = nullptr;
+  L.cb = nullptr;
   L.hcache = nullptr;
 }
 
@@ -715,14 +710,11 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
     L.cap[g] = want;
   };
   for (int attempt = 0; attempt < 8; ++attempt) {
-    if (L.n != n || !L.cnt) {
+    if (L.n != n || !L.cb) {
       free_lists(L);
       for (int g = 0; g < kMaxGroups; ++g) L.cap[g] = 0;
       L.n = n;
-      if (n > 0) {
-        PG_CUDA(cudaMalloc(&L.cnt, size_t(G) * n * 4));
-        PG_CUDA(cudaMalloc(&L.base, size_t(G) * n * 4));
-      }
+      if (n > 0) PG_CUDA(cudaMalloc(&L.cb, size_t(G) * n * sizeof(uint2)));
     }
     for (int g = 0; g < G; ++g)
       if (!L.idx32[g] || L.cap[g] == 0) alloc_slots(g, L.cap[g] ? L.cap[g] : 48u);
@@ -736,8 +728,7 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
       lo.gf[g] = L.gf[g];
       lo.cap[g] = L.cap[g];
     }
-    lo.cnt = L.cnt;
-    lo.base = L.base;
+    lo.cb = L.cb;
     lo.maxcnt = stats_d_ + 8;
     lo.n = uint32_t(n);
     lo.G = G;
@@ -754,11 +745,12 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
     bool grow = false;
     for (int g = 0; g < G; ++g)
       if (stats_h_[8 + g] > L.cap[g]) {
-        alloc_slots(g, (stats_h_[8 + g] + 15u) / 16u * 16u + 16u);
+        alloc_slots(g, (stats_h_[8 + g] + 7u) / 8u * 8u + 16u);
         grow = true;
       }
     if (!grow) break;
     list_rebuilds++;
+    if (attempt == 7) throw Error("neighbour lists kept overflowing their capacity");
   }
   L.epoch = epoch_;
   L.pos_versions = pos_versions();
@@ -769,8 +761,7 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
     L.view.idx32[g] = L.idx32[g];
     L.view.idx16[g] = L.idx16[g];
     L.view.gf[g] = L.gf[g];
-    L.view.cnt[g] = L.cnt ? L.cnt + size_t(g) * n : nullptr;
-    L.view.base[g] = L.base ? L.base + size_t(g) * n : nullptr;
+    L.view.cb[g] = L.cb ? L.cb + size_t(g) * n : nullptr;
     L.view.cap[g] = L.cap[g];
   }
   L.view.n = uint32_t(n);
@@ -782,14 +773,12 @@ NbrView const &Nhood::lists(int q, cudaStream_t s, float const *h) {
   Lists &L = lists_[q];
   if (!gg_[q].pos) {
     // CopyNeighbors of a group without position returns nothing
-    if (L.n != gg_[q].g->count || !L.cnt) {
+    if (L.n != gg_[q].g->count || !L.cb) {
       free_lists(L);
       L.n = gg_[q].g->count;
       if (L.n) {
-        PG_CUDA(cudaMalloc(&L.cnt, gg_.size() * L.n * 4));
-        PG_CUDA(cudaMemsetAsync(L.cnt, 0, gg_.size() * L.n * 4, s));
-        PG_CUDA(cudaMalloc(&L.base, gg_.size() * L.n * 4));
-        PG_CUDA(cudaMemsetAsync(L.base, 0, gg_.size() * L.n * 4, s));
+        PG_CUDA(cudaMalloc(&L.cb, gg_.size() * L.n * sizeof(uint2)));
+        PG_CUDA(cudaMemsetAsync(L.cb, 0, gg_.size() * L.n * sizeof(uint2), s));
       }
       if (!L.hcache) {
         PG_CUDA(cudaMalloc(&L.hcache, sizeof(float)));
@@ -797,10 +786,7 @@ NbrView const &Nhood::lists(int q, cudaStream_t s, float const *h) {
         PG_CUDA(cudaMemcpy(L.hcache, &nan, sizeof(float), cudaMemcpyHostToDevice));
       }
       L.view = NbrView{};
-      for (size_t g = 0; g < gg_.size(); ++g) {
-        L.view.cnt[g] = L.cnt ? L.cnt + g * L.n : nullptr;
-        L.view.base[g] = L.base ? L.base + g * L.n : nullptr;
-      }
+      for (size_t g = 0; g < gg_.size(); ++g) L.view.cb[g] = L.cb ? L.cb + g * L.n : nullptr;
       L.view.n = uint32_t(L.n);
       L.view.hcache = L.hcache;
     }
@@ -869,20 +855,21 @@ size_t Nhood::copy_neighbors(int g, size_t i, int64_t *counts, int64_t *out, siz
   if (i >= v.n) throw Error("CopyNeighbors: index out of range");
   size_t k = 0;
   for (int ng = 0; ng < G; ++ng) {
-    uint32_t c = 0, b = 0;
-    PG_CUDA(cudaMemcpyAsync(&c, v.cnt[ng] + i, 4, cudaMemcpyDeviceToHost, s));
-    PG_CUDA(cudaMemcpyAsync(&b, v.base[ng] + i, 4, cudaMemcpyDeviceToHost, s));
+    uint2 cb{0, 0};
+    PG_CUDA(cudaMemcpyAsync(&cb, v.cb[ng] + i, sizeof(uint2), cudaMemcpyDeviceToHost, s));
     PG_CUDA(cudaStreamSynchronize(s));
-    uint32_t cn = c & ~kWide;
+    uint32_t cn = cb.x & ~kWide;
     counts[ng] = cn;
-    for (uint32_t slot = 0; slot < cn; ++slot) {
-      uint32_t j32 = 0;
-      uint16_t j16 = 0;
-      size_t o = size_t(slot) * v.n + i;
-      PG_CUDA(cudaMemcpyAsync(&j32, v.idx32[ng] + o, 4, cudaMemcpyDeviceToHost, s));
-      PG_CUDA(cudaMemcpyAsync(&j16, v.idx16[ng] + o, 2, cudaMemcpyDeviceToHost, s));
+    std::vector<uint32_t> e32(cn);
+    std::vector<uint16_t> e16(cn);
+    if (cn) {
+      size_t row = i * v.cap[ng];
+      PG_CUDA(cudaMemcpyAsync(e32.data(), v.idx32[ng] + row, cn * 4, cudaMemcpyDeviceToHost, s));
+      PG_CUDA(cudaMemcpyAsync(e16.data(), v.idx16[ng] + row, cn * 2, cudaMemcpyDeviceToHost, s));
       PG_CUDA(cudaStreamSynchronize(s));
-      if (k < cap) out[k] = nbr_host_decode(c, b, j16, j32);
+    }
+    for (uint32_t slot = 0; slot < cn; ++slot) {
+      if (k < cap) out[k] = nbr_host_decode(cb.x, cb.y, e16[slot], e32[slot]);
       ++k;
     }
   }
@@ -892,11 +879,10 @@ size_t Nhood::copy_neighbors(int g, size_t i, int64_t *counts, int64_t *out, siz
 void Nhood::copy_lists(int q, int ng, int64_t *offsets, uint32_t *idx, size_t cap, cudaStream_t s) {
   NbrView const &v = lists(q, s);
   size_t n = v.n;
-  std::vector<uint32_t> cnt(n), base(n);
+  std::vector<uint2> cb(n);
   offsets[0] = 0;
   if (n == 0) return;
-  PG_CUDA(cudaMemcpyAsync(cnt.data(), v.cnt[ng], n * 4, cudaMemcpyDeviceToHost, s));
-  PG_CUDA(cudaMemcpyAsync(base.data(), v.base[ng], n * 4, cudaMemcpyDeviceToHost, s));
+  PG_CUDA(cudaMemcpyAsync(cb.data(), v.cb[ng], n * sizeof(uint2), cudaMemcpyDeviceToHost, s));
   std::vector<uint32_t> e32;
   std::vector<uint16_t> e16;
   if (v.idx32[ng]) {
@@ -906,12 +892,12 @@ void Nhood::copy_lists(int q, int ng, int64_t *offsets, uint32_t *idx, size_t ca
     PG_CUDA(cudaMemcpyAsync(e16.data(), v.idx16[ng], e16.size() * 2, cudaMemcpyDeviceToHost, s));
   }
   PG_CUDA(cudaStreamSynchronize(s));
-  for (size_t i = 0; i < n; ++i) offsets[i + 1] = offsets[i] + (cnt[i] & ~kWide);
+  for (size_t i = 0; i < n; ++i) offsets[i + 1] = offsets[i] + (cb[i].x & ~kWide);
   if (size_t(offsets[n]) > cap) throw Error("copy_lists: capacity too small");
   for (size_t i = 0; i < n; ++i)
-    for (uint32_t k = 0; k < (cnt[i] & ~kWide); ++k) {
-      size_t o = size_t(k) * n + i;
-      idx[offsets[i] + k] = nbr_host_decode(cnt[i], base[i], e16[o], e32[o]);
+    for (uint32_t k = 0; k < (cb[i].x & ~kWide); ++k) {
+      size_t o = i * v.cap[ng] + k;
+      idx[offsets[i] + k] = nbr_host_decode(cb[i].x, cb[i].y, e16[o], e32[o]);
     }
 }
 

@@ -42,11 +42,11 @@
 
 namespace prtcl_gpu {
 
-// Device view of the neighbour lists of one query group, one ELL set per
-// neighbour group g (entry k of item i at [k * n + i], so a warp reading
-// entry k of 32 consecutive items touches one contiguous segment):
-//   cnt[g][i]   neighbour count; bit 31 set = "wide" item
-//   base[g][i]  smallest neighbour index of item i
+// Device view of the neighbour lists of one query group, one set per
+// neighbour group g.  Row-major: the entries of item i are contiguous at
+// [i * cap + k] (cap a multiple of 8, so 8 entries are one 16-byte vector
+// load of 16-bit offsets):
+//   cb[g][i]    (count | kWide if "wide", smallest neighbour index = base)
 //   idx16[g]    j - base as 16-bit offsets (items whose neighbours span
 //               fewer than 65536 indices: nearly all after a permute)
 //   idx32[g]    j as 32-bit indices (read for wide items only)
@@ -58,14 +58,11 @@ struct NbrView {
   uint16_t const *idx16[kMaxGroups];
   uint32_t const *idx32[kMaxGroups];
   float const *gf[kMaxGroups];
-  uint32_t const *base[kMaxGroups];
-  uint32_t const *cnt[kMaxGroups];
+  uint2 const *cb[kMaxGroups];
   uint32_t cap[kMaxGroups];
   uint32_t n;          // query items
   float const *hcache; // NaN when no factors were computed
 };
-
-constexpr int kMaxListGroups = 8; // groups a neighbour-list build supports
 
 constexpr uint32_t kWide = 0x80000000u;
 
@@ -73,6 +70,8 @@ constexpr uint32_t kWide = 0x80000000u;
 inline uint32_t nbr_host_decode(uint32_t c, uint32_t base, uint16_t d16, uint32_t d32) {
   return (c & kWide) ? d32 : base + d16;
 }
+
+constexpr int kMaxListGroups = 8; // groups a neighbour-list build supports
 
 struct KeyInfo {
   uint32_t keep = 0;   // informative bit positions of u
@@ -144,8 +143,7 @@ private:
     uint32_t *idx32[kMaxGroups] = {};
     uint16_t *idx16[kMaxGroups] = {};
     float *gf[kMaxGroups] = {};
-    uint32_t *cnt = nullptr;  // [G][n]
-    uint32_t *base = nullptr; // [G][n]
+    uint2 *cb = nullptr; // [G][n]
     float *hcache = nullptr;
     bool has_gf = false;
     uint64_t epoch = 0;

@@ -45,43 +45,59 @@ constexpr int kStJacIter = 4, kStJacDone = 5;
 // ---------------------------------------------------------------------------
 
 struct NbrList {
-  uint16_t const *idx16; // ELL, entry k of item i at [k * n + i]: j - base
-  uint32_t const *idx32; // ELL: j (read for wide items only)
-  float const *gf;       // ELL: the pair's kernel-gradient factor
-  uint32_t const *base;  // per item: smallest neighbour index
-  uint32_t const *cnt;   // per item: count, bit 31 = wide
+  uint16_t const *idx16; // row-major, entry k of item i at [i * cap + k]: j - base
+  uint32_t const *idx32; // row-major: j (read for wide items only)
+  float const *gf;       // row-major: the pair's kernel-gradient factor
+  uint2 const *cb;       // per item: (count | kWide, base)
+  uint32_t cap;          // row length, a multiple of 8
 };
 
-// the neighbour list of one item: count and decoder
-struct NbrIter {
-  uint16_t const *i16;
-  uint32_t const *i32;
-  float const *gf;
-  uint32_t n, b, c;
-  bool wide;
-};
-__device__ __forceinline__ NbrIter nbr_begin(NbrList const &L, uint32_t i, uint32_t n) {
-  NbrIter it;
-  uint32_t c = __ldg(L.cnt + i);
-  it.wide = (c & kWide) != 0;
-  it.c = c & ~kWide;
-  it.b = __ldg(L.base + i);
-  it.i16 = L.idx16 + i;
-  it.i32 = L.idx32 + i;
-  it.gf = L.gf + i;
-  it.n = n;
-  return it;
+// Calls f(j, factor) for the neighbours of item i, in list order.  Entries
+// are fetched 8 at a time with 16-byte streaming loads (evict-first: the
+// lists are read once per sweep, the gathered particle records should stay
+// in L2), so that the 8 gathers of a chunk can be in flight together.
+template <class F>
+__device__ __forceinline__ void for_each_nbr(NbrList const &L, uint32_t i, bool with_gf, F &&f) {
+  uint2 cb = __ldg(L.cb + i);
+  uint32_t c = min(cb.x & ~kWide, L.cap);
+  bool wide = (cb.x & kWide) != 0;
+  size_t row = size_t(i) * L.cap;
+  for (uint32_t kb = 0; kb < c; kb += 8) {
+    uint32_t j[8];
+    if (wide) {
+      uint4 a = __ldcs(reinterpret_cast<uint4 const *>(L.idx32 + row + kb));
+      uint4 b = __ldcs(reinterpret_cast<uint4 const *>(L.idx32 + row + kb + 4));
+      j[0] = a.x; j[1] = a.y; j[2] = a.z; j[3] = a.w;
+      j[4] = b.x; j[5] = b.y; j[6] = b.z; j[7] = b.w;
+    } else {
+      uint4 a = __ldcs(reinterpret_cast<uint4 const *>(L.idx16 + row + kb));
+      uint32_t w[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        j[2 * t] = cb.y + (w[t] & 0xFFFFu);
+        j[2 * t + 1] = cb.y + (w[t] >> 16);
+      }
+    }
+    float g[8];
+    if (with_gf) {
+      float4 a = __ldcs(reinterpret_cast<float4 const *>(L.gf + row + kb));
+      float4 b = __ldcs(reinterpret_cast<float4 const *>(L.gf + row + kb + 4));
+      g[0] = a.x; g[1] = a.y; g[2] = a.z; g[3] = a.w;
+      g[4] = b.x; g[5] = b.y; g[6] = b.z; g[7] = b.w;
+    } else {
+#pragma unroll
+      for (int t = 0; t < 8; ++t) g[t] = 0.0f;
+    }
+#pragma unroll
+    for (int t = 0; t < 8; ++t)
+      if (kb + t < c) f(j[t], g[t]);
+  }
 }
-// entry k (list entries are streamed once per sweep: evict-first loads keep
-// the gathered particle records in L2)
-__device__ __forceinline__ uint32_t nbr_at(NbrIter const &it, uint32_t k) {
-  size_t o = size_t(k) * it.n;
-  return it.wide ? __ldcs(it.i32 + o) : it.b + uint32_t(__ldcs(it.i16 + o));
-}
-// kernel gradient of entry k: from the cached factor (bit-identical to
+
+// the pair's kernel gradient: from the cached factor (bit-identical to
 // kgradW) when the lists were built with the current smoothing scale
-__device__ __forceinline__ f3 nbr_grad(NbrIter const &it, uint32_t k, bool cached, KernelParams const &K, f3 xij) {
-  return cached ? kgrad_from(__ldcs(it.gf + size_t(k) * it.n), xij) : kgradW(K, xij);
+__device__ __forceinline__ f3 pgrad(bool cached, float factor, KernelParams const &K, f3 xij) {
+  return cached ? kgrad_from(factor, xij) : kgradW(K, xij);
 }
 
 struct FluidN {
@@ -177,22 +193,18 @@ __global__ void __launch_bounds__(kNT) k_density(uint32_t n, float4 const *__res
 #pragma unroll
   for (int q = 0; q < NF; ++q) {
     FluidN const &F = N.f[q];
-    NbrIter it = nbr_begin(F.L, i, n);
-#pragma unroll 4
-    for (uint32_t k = 0; k < it.c; ++k) {
-      float4 xm = __ldg(F.xm + nbr_at(it, k));
+    for_each_nbr(F.L, i, false, [&](uint32_t j_, float) {
+      float4 xm = __ldg(F.xm + j_);
       acc += xm.w * kW(K, sub3(xi, mk3(xm)));
-    }
+    });
   }
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
-    NbrIter it = nbr_begin(B.L, i, n);
-#pragma unroll 4
-    for (uint32_t k = 0; k < it.c; ++k) {
-      float4 xv = __ldg(B.xV + nbr_at(it, k));
+    for_each_nbr(B.L, i, false, [&](uint32_t j_, float) {
+      float4 xv = __ldg(B.xV + j_);
       acc += (xv.w * rho0) * kW(K, sub3(xi, mk3(xv)));
-    }
+    });
   }
   rho[i] = acc;
 }
@@ -209,8 +221,8 @@ __global__ void __launch_bounds__(kNT) k_volume(uint32_t n, float4 const *__rest
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
-    NbrIter it = nbr_begin(B.L, i, n);
-    for (uint32_t k = 0; k < it.c; ++k) acc += kW(K, sub3(xi, mk3(__ldg(B.xV + nbr_at(it, k)))));
+    for_each_nbr(B.L, i, false, [&](uint32_t j_, float) { acc += kW(K, sub3(xi, mk3(__ldg(B.xV + j_))));
+    });
   }
   V[i] = 1.0f / acc;
 }
@@ -286,22 +298,18 @@ __global__ void __launch_bounds__(kNT) k_iisph_c(uint32_t n, float4 const *__res
 #pragma unroll
   for (int q = 0; q < NF; ++q) {
     FluidN const &F = N.f[q];
-    NbrIter it = nbr_begin(F.L, i, n);
-#pragma unroll 4
-    for (uint32_t k = 0; k < it.c; ++k) {
-      float4 xm = __ldg(F.xm + nbr_at(it, k));
-      c = sub3(c, scl3(xm.w / (ri * ri), nbr_grad(it, k, uc, K, sub3(xi, mk3(xm)))));
-    }
+    for_each_nbr(F.L, i, uc, [&](uint32_t j_, float gf_) {
+      float4 xm = __ldg(F.xm + j_);
+      c = sub3(c, scl3(xm.w / (ri * ri), pgrad(uc, gf_, K, sub3(xi, mk3(xm)))));
+    });
   }
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
-    NbrIter it = nbr_begin(B.L, i, n);
-#pragma unroll 4
-    for (uint32_t k = 0; k < it.c; ++k) {
-      float4 xv = __ldg(B.xV + nbr_at(it, k));
-      c = sub3(c, scl3(((0.7f * 2.0f) * rho0) * (xv.w / (ri * ri)), nbr_grad(it, k, uc, K, sub3(xi, mk3(xv)))));
-    }
+    for_each_nbr(B.L, i, uc, [&](uint32_t j_, float gf_) {
+      float4 xv = __ldg(B.xV + j_);
+      c = sub3(c, scl3(((0.7f * 2.0f) * rho0) * (xv.w / (ri * ri)), pgrad(uc, gf_, K, sub3(xi, mk3(xv)))));
+    });
   }
   cout[i] = make_float4(c.x, c.y, c.z, 0.0f);
 }
@@ -326,30 +334,26 @@ __global__ void __launch_bounds__(kNT) k_iisph_s_aa(uint32_t n, float4 const *__
 #pragma unroll
   for (int q = 0; q < NF; ++q) {
     FluidN const &F = N.f[q];
-    NbrIter it = nbr_begin(F.L, i, n);
-#pragma unroll 2
-    for (uint32_t k = 0; k < it.c; ++k) {
-      uint32_t j = nbr_at(it, k);
+    for_each_nbr(F.L, i, uc, [&](uint32_t j_, float gf_) {
+      uint32_t j = j_;
       float4 xm = __ldg(F.xm + j);
-      f3 g = nbr_grad(it, k, uc, K, sub3(xi, mk3(xm)));
+      f3 g = pgrad(uc, gf_, K, sub3(xi, mk3(xm)));
       float mj = xm.w;
       sa += mj * dot3(sub3(vi, mk3(__ldg(F.v + j))), g);
       aa += mj * dot3(ci, g);
       aa -= (mj * (mi / (ri * ri))) * nsq3(g);
-    }
+    });
   }
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
-    NbrIter it = nbr_begin(B.L, i, n);
-#pragma unroll 2
-    for (uint32_t k = 0; k < it.c; ++k) {
-      float4 xv = __ldg(B.xV + nbr_at(it, k));
-      f3 g = nbr_grad(it, k, uc, K, sub3(xi, mk3(xv)));
+    for_each_nbr(B.L, i, uc, [&](uint32_t j_, float gf_) {
+      float4 xv = __ldg(B.xV + j_);
+      f3 g = pgrad(uc, gf_, K, sub3(xi, mk3(xv)));
       float w = rho0 * xv.w;
       sa += w * dot3(sub3(vi, f3{0.0f, 0.0f, 0.0f}), g);
       aa += w * dot3(ci, g);
-    }
+    });
   }
   p[i] = 0.0f;
   pr[i] = 0.0f / (ri * ri);
@@ -379,26 +383,22 @@ __global__ void __launch_bounds__(kNT) k_iisph_accel(uint32_t n, float4 const *_
 #pragma unroll
   for (int q = 0; q < NF; ++q) {
     FluidN const &F = N.f[q];
-    NbrIter it = nbr_begin(F.L, i, n);
-#pragma unroll 4
-    for (uint32_t k = 0; k < it.c; ++k) {
-      uint32_t j = nbr_at(it, k);
+    for_each_nbr(F.L, i, uc, [&](uint32_t j_, float gf_) {
+      uint32_t j = j_;
       float4 xm = __ldg(F.xm + j);
       float coef = xm.w * (pri + __ldg(F.pr + j));
-      acc = sub3(acc, scl3(coef, nbr_grad(it, k, uc, K, sub3(xi, mk3(xm)))));
-    }
+      acc = sub3(acc, scl3(coef, pgrad(uc, gf_, K, sub3(xi, mk3(xm)))));
+    });
   }
   float bterm = (2.0f * pi) / (ri * ri);
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
-    NbrIter it = nbr_begin(B.L, i, n);
-#pragma unroll 4
-    for (uint32_t k = 0; k < it.c; ++k) {
-      float4 xv = __ldg(B.xV + nbr_at(it, k));
+    for_each_nbr(B.L, i, uc, [&](uint32_t j_, float gf_) {
+      float4 xv = __ldg(B.xV + j_);
       float coef = ((0.7f * rho0) * xv.w) * bterm;
-      acc = sub3(acc, scl3(coef, nbr_grad(it, k, uc, K, sub3(xi, mk3(xv)))));
-    }
+      acc = sub3(acc, scl3(coef, pgrad(uc, gf_, K, sub3(xi, mk3(xv)))));
+    });
   }
   a[i] = make_float4(acc.x, acc.y, acc.z, 0.0f);
 }
@@ -427,23 +427,19 @@ __global__ void __launch_bounds__(kNT) k_iisph_pressure(uint32_t n, float4 const
 #pragma unroll
     for (int q = 0; q < NF; ++q) {
       FluidN const &F = N.f[q];
-      NbrIter it = nbr_begin(F.L, i, n);
-#pragma unroll 4
-      for (uint32_t k = 0; k < it.c; ++k) {
-        uint32_t j = nbr_at(it, k);
+      for_each_nbr(F.L, i, uc, [&](uint32_t j_, float gf_) {
+        uint32_t j = j_;
         float4 xm = __ldg(F.xm + j);
-        ap += xm.w * dot3(sub3(ai, mk3(__ldg(F.a + j))), nbr_grad(it, k, uc, K, sub3(xi, mk3(xm))));
-      }
+        ap += xm.w * dot3(sub3(ai, mk3(__ldg(F.a + j))), pgrad(uc, gf_, K, sub3(xi, mk3(xm))));
+      });
     }
 #pragma unroll
     for (int q = 0; q < NB; ++q) {
       BoundN const &B = N.b[q];
-      NbrIter it = nbr_begin(B.L, i, n);
-#pragma unroll 4
-      for (uint32_t k = 0; k < it.c; ++k) {
-        float4 xv = __ldg(B.xV + nbr_at(it, k));
-        ap += (rho0 * xv.w) * dot3(sub3(ai, f3{0.0f, 0.0f, 0.0f}), nbr_grad(it, k, uc, K, sub3(xi, mk3(xv))));
-      }
+      for_each_nbr(B.L, i, uc, [&](uint32_t j_, float gf_) {
+        float4 xv = __ldg(B.xV + j_);
+        ap += (rho0 * xv.w) * dot3(sub3(ai, f3{0.0f, 0.0f, 0.0f}), pgrad(uc, gf_, K, sub3(xi, mk3(xv))));
+      });
     }
     float ri = rho[i];
     ap *= (dt * dt) * (rho0 / ri);
@@ -546,34 +542,33 @@ __global__ void __launch_bounds__(kNT) k_wkbb18_diag(uint32_t n, uint32_t cap, f
   for (int k = 0; k < 9; ++k) S[k] = 0.0f;
   float hh = (0.01f * h) * h;
   float cmu = 10.0f * (mu / ri);
-  NbrIter it = nbr_begin(self, i, n);
-  for (uint32_t k = 0; k < it.c; ++k) {
-    float4 xj = __ldg(xmr + nbr_at(it, k));
+  for_each_nbr(self, i, uc, [&](uint32_t j_, float gf_) {
+    float4 xj = __ldg(xmr + j_);
     f3 xij = sub3(xi, mk3(xj));
     float coef = (cmu * xj.w) / (nsq3(xij) + hh);
-    f3 g = nbr_grad(it, k, uc, K, xij);
+    f3 g = pgrad(uc, gf_, K, xij);
     float gv[3] = {g.x, g.y, g.z}, xv[3] = {xij.x, xij.y, xij.z};
 #pragma unroll
     for (int c = 0; c < 3; ++c)
 #pragma unroll
       for (int r = 0; r < 3; ++r) S[3 * c + r] += coef * (gv[r] * xv[c]);
-  }
+    });
+
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
     float bmu = *B.mu;
-    NbrIter it = nbr_begin(B.L, i, n);
-    for (uint32_t k = 0; k < it.c; ++k) {
-      float4 xv = __ldg(B.xV + nbr_at(it, k));
+    for_each_nbr(B.L, i, uc, [&](uint32_t j_, float gf_) {
+      float4 xv = __ldg(B.xV + j_);
       f3 xij = sub3(xi, mk3(xv));
       float coef = ((10.0f * (bmu / ri)) * ((rho0 * xv.w) / ri)) / (nsq3(xij) + hh);
-      f3 g = nbr_grad(it, k, uc, K, xij);
+      f3 g = pgrad(uc, gf_, K, xij);
       float gv[3] = {g.x, g.y, g.z}, xw[3] = {xij.x, xij.y, xij.z};
 #pragma unroll
       for (int c = 0; c < 3; ++c)
 #pragma unroll
         for (int r = 0; r < 3; ++r) S[3 * c + r] += coef * (gv[r] * xw[c]);
-    }
+    });
   }
   M3 A;
 #pragma unroll
@@ -621,28 +616,25 @@ __device__ __forceinline__ f3 wkbb18_system(PcgArgs const &P, KernelParams const
   float ri = P.rho[i];
   float cmu = 10.0f * (mu / ri);
   f3 af = {0.0f, 0.0f, 0.0f};
-  NbrIter it = nbr_begin(P.self, i, P.n);
-#pragma unroll 4
-  for (uint32_t k = 0; k < it.c; ++k) {
-    uint32_t j = nbr_at(it, k);
+  for_each_nbr(P.self, i, uc, [&](uint32_t j_, float gf_) {
+    uint32_t j = j_;
     float4 xj = __ldg(P.xmr + j);
     f3 xij = sub3(xi, mk3(xj));
     float coef = ((cmu * xj.w) * dot3(sub3(wi, mk3(__ldg(w + j))), xij)) / (nsq3(xij) + hh);
-    af = add3(af, scl3(coef, nbr_grad(it, k, uc, K, xij)));
-  }
+    af = add3(af, scl3(coef, pgrad(uc, gf_, K, xij)));
+    });
+
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
     float bmu = *B.mu;
     float cb_mu = 10.0f * (bmu / ri);
-    NbrIter it = nbr_begin(B.L, i, P.n);
-#pragma unroll 4
-    for (uint32_t k = 0; k < it.c; ++k) {
-      float4 xv = __ldg(B.xV + nbr_at(it, k));
+    for_each_nbr(B.L, i, uc, [&](uint32_t j_, float gf_) {
+      float4 xv = __ldg(B.xV + j_);
       f3 xij = sub3(xi, mk3(xv));
       float coef = ((cb_mu * ((rho0 * xv.w) / ri)) * dot3(wi, xij)) / (nsq3(xij) + hh);
-      af = add3(af, scl3(coef, nbr_grad(it, k, uc, K, xij)));
-    }
+      af = add3(af, scl3(coef, pgrad(uc, gf_, K, xij)));
+    });
   }
   return sub3(wi, scl3(dt, af));
 }
@@ -963,7 +955,7 @@ protected:
   std::vector<FluidG> fluid_;
   std::vector<BoundG> bound_;
 
-  static NbrList nl(NbrView const &v, int g) { return NbrList{v.idx16[g], v.idx32[g], v.gf[g], v.base[g], v.cnt[g]}; }
+  static NbrList nl(NbrView const &v, int g) { return NbrList{v.idx16[g], v.idx32[g], v.gf[g], v.cb[g], v.cap[g]}; }
   // packed neighbour records of the fluid / boundary groups (made current
   // here: may launch a pack kernel on `s`)
   FluidN fn(FluidG const &F, NbrView const &v, cudaStream_t s) {
