@@ -344,13 +344,16 @@ __global__ void k_xsorted(PosTable pt, uint32_t const *vals, size_t N, float4 *x
   }
 }
 
+constexpr int kBuildNT = 64; // query items (threads) per list-build block
+
 struct ListOut {
+  unsigned char *chunks[kMaxListGroups];
   uint32_t *idx32[kMaxListGroups];
-  uint16_t *idx16[kMaxListGroups];
-  float *gf[kMaxListGroups];
   uint32_t cap[kMaxListGroups];
-  uint2 *cb;        // [G][n]
-  uint32_t *maxcnt; // [kMaxListGroups]
+  uint32_t soff[kMaxListGroups]; // staging row offset of group g (sum of the caps before it)
+  uint32_t scap;                 // sum of the caps
+  uint2 *cb;                     // [G][n]
+  uint32_t *maxcnt;              // [kMaxListGroups]
   uint32_t n;
   int G;
 };
@@ -361,9 +364,11 @@ struct ListAcc {
   uint32_t c[kMaxListGroups], lo[kMaxListGroups], hi[kMaxListGroups];
 };
 
+// staged entries: index j at sj[(soff[g] + k) * NT + t], factor bits at
+// sf[...] (consecutive threads on consecutive words)
 __device__ __forceinline__ void visit_cell(GridView const &gv, float4 const *__restrict__ xs, int cell, f3 xi,
-                                           uint32_t i, ListOut const &lo, ListAcc &A, KernelParams const &K,
-                                           bool with_gf) {
+                                           ListOut const &lo, ListAcc &A, KernelParams const &K, bool with_gf,
+                                           uint32_t *sj, uint32_t *sf) {
   if (cell < 0) return;
   int s0 = gv.cell_start[cell], s1 = gv.cell_start[cell + 1];
   for (int s = s0; s < s1; ++s) {
@@ -380,24 +385,31 @@ __device__ __forceinline__ void visit_cell(GridView const &gv, float4 const *__r
           A.lo[q] = min(A.lo[q], j);
           A.hi[q] = max(A.hi[q], j);
           if (k < lo.cap[q]) {
-            size_t o = size_t(i) * lo.cap[q] + k;
-            lo.idx32[q][o] = j;
-            if (with_gf) lo.gf[q][o] = f;
+            size_t o = size_t(lo.soff[q] + k) * kBuildNT + threadIdx.x;
+            sj[o] = j;
+            sf[o] = __float_as_uint(f);
           }
         }
     }
   }
 }
 
-// neighbour lists of one query group (grid query of util/grouped_uniform_grid.hpp:407-531)
-__global__ void __launch_bounds__(128) k_build_lists(GridView gv, float4 const *__restrict__ xs,
-                                                     float4 const *__restrict__ qpos, int q, ListOut lo,
-                                                     float const *hp, float *hcache) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+// Neighbour lists of one query group (grid query of
+// util/grouped_uniform_grid.hpp:407-531).  Each thread gathers its item's
+// neighbours into shared memory in traversal order; the block then writes
+// its rows of chunks with coalesced 16-byte stores.
+__global__ void __launch_bounds__(kBuildNT) k_build_lists(GridView gv, float4 const *__restrict__ xs,
+                                                          float4 const *__restrict__ qpos, int q, ListOut lo,
+                                                          float const *hp, float *hcache) {
+  extern __shared__ uint32_t smem[];
+  uint32_t *sj = smem;
+  uint32_t *sf = smem + size_t(lo.scap) * kBuildNT;
+  __shared__ uint2 s_cb[kMaxListGroups][kBuildNT];
+  uint32_t i0 = blockIdx.x * kBuildNT;
+  uint32_t i = i0 + threadIdx.x;
   bool with_gf = hp != nullptr;
   KernelParams K = kparams(with_gf ? *hp : 1.0f);
   if (i == 0) *hcache = with_gf ? K.h : __int_as_float(0x7fc00000);
-  if (i >= lo.n) return;
   ListAcc A;
 #pragma unroll
   for (int g = 0; g < kMaxListGroups; ++g) {
@@ -405,27 +417,30 @@ __global__ void __launch_bounds__(128) k_build_lists(GridView gv, float4 const *
     A.lo[g] = 0xFFFFFFFFu;
     A.hi[g] = 0;
   }
-  float4 x4 = qpos[i];
-  f3 xi = mk3(x4);
-  int cell = -1;
-  bool fallback = false;
-  int3 gi;
-  if (gv.in_grid[q]) {
-    cell = gv.s2c[gv.r2s[gv.goff[q] + i]];
-  } else {
-    gi = x_to_gi(x4, gv);
-    cell = find_cell(gv, gi);
-    fallback = cell < 0;
-  }
-  if (!fallback) {
-    visit_cell(gv, xs, cell, xi, i, lo, A, K, with_gf);
-    for (int k = 0; k < 26; ++k) visit_cell(gv, xs, gv.cell_adj[size_t(cell) * 26 + k], xi, i, lo, A, K, with_gf);
-  } else {
-    for (int k = 0; k < 13; ++k) {
-      int3 p = make_int3(gi.x + c_offsets[k][0], gi.y + c_offsets[k][1], gi.z + c_offsets[k][2]);
-      visit_cell(gv, xs, find_cell(gv, p), xi, i, lo, A, K, with_gf);
-      int3 m = make_int3(gi.x - c_offsets[k][0], gi.y - c_offsets[k][1], gi.z - c_offsets[k][2]);
-      visit_cell(gv, xs, find_cell(gv, m), xi, i, lo, A, K, with_gf);
+  if (i < lo.n) {
+    float4 x4 = qpos[i];
+    f3 xi = mk3(x4);
+    int cell = -1;
+    bool fallback = false;
+    int3 gi;
+    if (gv.in_grid[q]) {
+      cell = gv.s2c[gv.r2s[gv.goff[q] + i]];
+    } else {
+      gi = x_to_gi(x4, gv);
+      cell = find_cell(gv, gi);
+      fallback = cell < 0;
+    }
+    if (!fallback) {
+      visit_cell(gv, xs, cell, xi, lo, A, K, with_gf, sj, sf);
+      for (int k = 0; k < 26; ++k)
+        visit_cell(gv, xs, gv.cell_adj[size_t(cell) * 26 + k], xi, lo, A, K, with_gf, sj, sf);
+    } else {
+      for (int k = 0; k < 13; ++k) {
+        int3 p = make_int3(gi.x + c_offsets[k][0], gi.y + c_offsets[k][1], gi.z + c_offsets[k][2]);
+        visit_cell(gv, xs, find_cell(gv, p), xi, lo, A, K, with_gf, sj, sf);
+        int3 m = make_int3(gi.x - c_offsets[k][0], gi.y - c_offsets[k][1], gi.z - c_offsets[k][2]);
+        visit_cell(gv, xs, find_cell(gv, m), xi, lo, A, K, with_gf, sj, sf);
+      }
     }
   }
 #pragma unroll
@@ -433,12 +448,46 @@ __global__ void __launch_bounds__(128) k_build_lists(GridView gv, float4 const *
     if (g >= lo.G) break;
     uint32_t n = A.c[g];
     bool wide = n > 0 && A.hi[g] - A.lo[g] > 0xFFFFu;
-    uint32_t b = n > 0 ? A.lo[g] : 0u;
-    lo.cb[size_t(g) * lo.n + i] = make_uint2(n | (wide ? kWide : 0u), b);
-    if (n > lo.cap[g]) atomicMax(&lo.maxcnt[g], n);
-    else if (!wide) {
-      size_t row = size_t(i) * lo.cap[g];
-      for (uint32_t k = 0; k < n; ++k) lo.idx16[g][row + k] = uint16_t(lo.idx32[g][row + k] - b);
+    uint2 cb = make_uint2(n | (wide ? kWide : 0u), n > 0 ? A.lo[g] : 0u);
+    s_cb[g][threadIdx.x] = cb;
+    if (i < lo.n) {
+      lo.cb[size_t(g) * lo.n + i] = cb;
+      if (n > lo.cap[g]) atomicMax(&lo.maxcnt[g], n);
+      else if (wide)
+        for (uint32_t k = 0; k < n; ++k) lo.idx32[g][size_t(i) * lo.cap[g] + k] = sj[size_t(lo.soff[g] + k) * kBuildNT + threadIdx.x];
+    }
+  }
+  __syncthreads();
+  // coalesced copy-out: the block's rows are one contiguous range per group
+  uint32_t rows = min(uint32_t(kBuildNT), lo.n - i0);
+  for (int g = 0; g < lo.G; ++g) {
+    uint32_t nch = lo.cap[g] / kChunk;
+    uint32_t pieces = rows * nch * 6u;
+    uint4 *dst = reinterpret_cast<uint4 *>(lo.chunks[g] + size_t(i0) * nch * kChunkBytes);
+    for (uint32_t p = threadIdx.x; p < pieces; p += kBuildNT) {
+      uint32_t r = p / (nch * 6u), rem = p % (nch * 6u), c = rem / 6u, part = rem % 6u;
+      uint2 cb = s_cb[g][r];
+      uint32_t cnt = cb.x & ~kWide;
+      bool ok = !(cb.x & kWide) && cnt <= lo.cap[g];
+      uint32_t w[4];
+      if (part < 2) {
+        uint32_t k0 = c * kChunk + part * 8u;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          uint32_t ka = k0 + 2 * e, kb = ka + 1;
+          uint32_t da = (ok && ka < cnt) ? sj[size_t(lo.soff[g] + ka) * kBuildNT + r] - cb.y : 0u;
+          uint32_t db = (ok && kb < cnt) ? sj[size_t(lo.soff[g] + kb) * kBuildNT + r] - cb.y : 0u;
+          w[e] = (da & 0xFFFFu) | (db << 16);
+        }
+      } else {
+        uint32_t k0 = c * kChunk + (part - 2u) * 4u;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          uint32_t k = k0 + e;
+          w[e] = (k < cnt && cnt <= lo.cap[g]) ? sf[size_t(lo.soff[g] + k) * kBuildNT + r] : 0u;
+        }
+      }
+      dst[p] = make_uint4(w[0], w[1], w[2], w[3]);
     }
   }
 }
@@ -496,11 +545,9 @@ Nhood::~Nhood() {
 void Nhood::free_lists(Lists &L) {
   for (int g = 0; g < kMaxGroups; ++g) {
     if (L.idx32[g]) cudaFree(L.idx32[g]);
-    if (L.idx16[g]) cudaFree(L.idx16[g]);
-    if (L.gf[g]) cudaFree(L.gf[g]);
+    if (L.chunks[g]) cudaFree(L.chunks[g]);
     L.idx32[g] = nullptr;
-    L.idx16[g] = nullptr;
-    L.gf[g] = nullptr;
+    L.chunks[g] = nullptr;
   }
   if (L.cb) cudaFree(L.cb);
   if (L.hcache) cudaFree(L.hcache);
@@ -697,15 +744,12 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
   }
   auto alloc_slots = [&](int g, uint32_t want) {
     if (L.idx32[g]) PG_CUDA(cudaFree(L.idx32[g]));
-    if (L.idx16[g]) PG_CUDA(cudaFree(L.idx16[g]));
-    if (L.gf[g]) PG_CUDA(cudaFree(L.gf[g]));
+    if (L.chunks[g]) PG_CUDA(cudaFree(L.chunks[g]));
     L.idx32[g] = nullptr;
-    L.idx16[g] = nullptr;
-    L.gf[g] = nullptr;
+    L.chunks[g] = nullptr;
     if (n > 0) {
       PG_CUDA(cudaMalloc(&L.idx32[g], size_t(want) * n * 4));
-      PG_CUDA(cudaMalloc(&L.idx16[g], size_t(want) * n * 2));
-      PG_CUDA(cudaMalloc(&L.gf[g], size_t(want) * n * 4));
+      PG_CUDA(cudaMalloc(&L.chunks[g], size_t(want / kChunk) * kChunkBytes * n));
     }
     L.cap[g] = want;
   };
@@ -722,12 +766,18 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
     if (!L.hcache) PG_CUDA(cudaMalloc(&L.hcache, sizeof(float)));
     if (n == 0) break;
     ListOut lo{};
+    uint32_t scap = 0;
     for (int g = 0; g < G; ++g) {
       lo.idx32[g] = L.idx32[g];
-      lo.idx16[g] = L.idx16[g];
-      lo.gf[g] = L.gf[g];
+      lo.chunks[g] = L.chunks[g];
       lo.cap[g] = L.cap[g];
+      lo.soff[g] = scap;
+      scap += L.cap[g];
     }
+    lo.scap = scap;
+    size_t smem = size_t(scap) * kBuildNT * 8;
+    if (smem > 200 * 1024) throw Error("neighbour lists: too many neighbours per item for the list build");
+    PG_CUDA(cudaFuncSetAttribute(k_build_lists, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     lo.cb = L.cb;
     lo.maxcnt = stats_d_ + 8;
     lo.n = uint32_t(n);
@@ -737,7 +787,7 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
     float4 const *qpos = static_cast<float4 const *>(gg_[q].pos->d);
     {
       ProfScope ps(model_->prof, "nhood_lists", s);
-      k_build_lists<<<div_up(n, 128), 128, 0, s>>>(gv, xsorted_, qpos, q, lo, h, L.hcache); count_launch();
+      k_build_lists<<<div_up(n, kBuildNT), kBuildNT, smem, s>>>(gv, xsorted_, qpos, q, lo, h, L.hcache); count_launch();
     }
     PG_LAUNCH_CHECK();
     PG_CUDA(cudaMemcpyAsync(stats_h_ + 8, stats_d_ + 8, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -745,7 +795,7 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
     bool grow = false;
     for (int g = 0; g < G; ++g)
       if (stats_h_[8 + g] > L.cap[g]) {
-        alloc_slots(g, (stats_h_[8 + g] + 7u) / 8u * 8u + 16u);
+        alloc_slots(g, (stats_h_[8 + g] + kChunk - 1) / kChunk * kChunk + kChunk);
         grow = true;
       }
     if (!grow) break;
@@ -759,8 +809,7 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
   L.view.hcache = L.hcache;
   for (int g = 0; g < G; ++g) {
     L.view.idx32[g] = L.idx32[g];
-    L.view.idx16[g] = L.idx16[g];
-    L.view.gf[g] = L.gf[g];
+    L.view.chunks[g] = L.chunks[g];
     L.view.cb[g] = L.cb ? L.cb + size_t(g) * n : nullptr;
     L.view.cap[g] = L.cap[g];
   }
@@ -860,16 +909,15 @@ size_t Nhood::copy_neighbors(int g, size_t i, int64_t *counts, int64_t *out, siz
     PG_CUDA(cudaStreamSynchronize(s));
     uint32_t cn = cb.x & ~kWide;
     counts[ng] = cn;
-    std::vector<uint32_t> e32(cn);
-    std::vector<uint16_t> e16(cn);
-    if (cn) {
-      size_t row = i * v.cap[ng];
-      PG_CUDA(cudaMemcpyAsync(e32.data(), v.idx32[ng] + row, cn * 4, cudaMemcpyDeviceToHost, s));
-      PG_CUDA(cudaMemcpyAsync(e16.data(), v.idx16[ng] + row, cn * 2, cudaMemcpyDeviceToHost, s));
-      PG_CUDA(cudaStreamSynchronize(s));
-    }
+    if (!cn) continue;
+    size_t rowbytes = size_t(v.cap[ng] / kChunk) * kChunkBytes;
+    std::vector<unsigned char> row(rowbytes);
+    std::vector<uint32_t> e32(v.cap[ng]);
+    PG_CUDA(cudaMemcpyAsync(row.data(), v.chunks[ng] + i * rowbytes, rowbytes, cudaMemcpyDeviceToHost, s));
+    PG_CUDA(cudaMemcpyAsync(e32.data(), v.idx32[ng] + i * v.cap[ng], v.cap[ng] * 4, cudaMemcpyDeviceToHost, s));
+    PG_CUDA(cudaStreamSynchronize(s));
     for (uint32_t slot = 0; slot < cn; ++slot) {
-      if (k < cap) out[k] = nbr_host_decode(cb.x, cb.y, e16[slot], e32[slot]);
+      if (k < cap) out[k] = nbr_host_decode(cb, row.data(), e32.data(), slot);
       ++k;
     }
   }
@@ -883,22 +931,21 @@ void Nhood::copy_lists(int q, int ng, int64_t *offsets, uint32_t *idx, size_t ca
   offsets[0] = 0;
   if (n == 0) return;
   PG_CUDA(cudaMemcpyAsync(cb.data(), v.cb[ng], n * sizeof(uint2), cudaMemcpyDeviceToHost, s));
+  size_t rowbytes = size_t(v.cap[ng] / kChunk) * kChunkBytes;
+  std::vector<unsigned char> ch;
   std::vector<uint32_t> e32;
-  std::vector<uint16_t> e16;
-  if (v.idx32[ng]) {
+  if (v.chunks[ng]) {
+    ch.resize(rowbytes * n);
     e32.resize(size_t(v.cap[ng]) * n);
-    e16.resize(size_t(v.cap[ng]) * n);
+    PG_CUDA(cudaMemcpyAsync(ch.data(), v.chunks[ng], ch.size(), cudaMemcpyDeviceToHost, s));
     PG_CUDA(cudaMemcpyAsync(e32.data(), v.idx32[ng], e32.size() * 4, cudaMemcpyDeviceToHost, s));
-    PG_CUDA(cudaMemcpyAsync(e16.data(), v.idx16[ng], e16.size() * 2, cudaMemcpyDeviceToHost, s));
   }
   PG_CUDA(cudaStreamSynchronize(s));
   for (size_t i = 0; i < n; ++i) offsets[i + 1] = offsets[i] + (cb[i].x & ~kWide);
   if (size_t(offsets[n]) > cap) throw Error("copy_lists: capacity too small");
   for (size_t i = 0; i < n; ++i)
-    for (uint32_t k = 0; k < (cb[i].x & ~kWide); ++k) {
-      size_t o = i * v.cap[ng] + k;
-      idx[offsets[i] + k] = nbr_host_decode(cb[i].x, cb[i].y, e16[o], e32[o]);
-    }
+    for (uint32_t k = 0; k < (cb[i].x & ~kWide); ++k)
+      idx[offsets[i] + k] = nbr_host_decode(cb[i], ch.data() + i * rowbytes, e32.data() + i * v.cap[ng], k);
 }
 
 } // namespace prtcl_gpu

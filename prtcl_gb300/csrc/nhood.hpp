@@ -43,32 +43,38 @@
 namespace prtcl_gpu {
 
 // Device view of the neighbour lists of one query group, one set per
-// neighbour group g.  Row-major: the entries of item i are contiguous at
-// [i * cap + k] (cap a multiple of 8, so 8 entries are one 16-byte vector
-// load of 16-bit offsets):
+// neighbour group g.  Row-major in 16-entry chunks: item i owns cap / 16
+// consecutive 96-byte chunks; chunk c holds entries 16c..16c+15 as
+//   16 x uint16  j - base   (32 bytes)
+//   16 x float   the pair's kernel-gradient factor (64 bytes)
+// so a chunk is exactly three 32-byte sectors and every fetched sector is
+// used once.  Also per item:
 //   cb[g][i]    (count | kWide if "wide", smallest neighbour index = base)
-//   idx16[g]    j - base as 16-bit offsets (items whose neighbours span
-//               fewer than 65536 indices: nearly all after a permute)
-//   idx32[g]    j as 32-bit indices (read for wide items only)
-//   gf[g]       the pair's kernel-gradient factor (kgrad_factor), when the
-//               lists were built with a smoothing scale (hcache, device);
-//               kernels use it only while hcache equals the current
-//               smoothing scale and evaluate the gradient in full otherwise
+//   idx32[g]    j as 32-bit indices at [i * cap + k], written and read for
+//               "wide" items only (neighbours spanning >= 65536 indices)
+// The factors are present when the lists were built with a smoothing scale
+// (hcache, device); kernels use them only while hcache equals the current
+// smoothing scale and evaluate the gradient in full otherwise.
+constexpr uint32_t kChunk = 16;
+constexpr uint32_t kChunkBytes = kChunk * 2 + kChunk * 4;
 struct NbrView {
-  uint16_t const *idx16[kMaxGroups];
+  unsigned char const *chunks[kMaxGroups];
   uint32_t const *idx32[kMaxGroups];
-  float const *gf[kMaxGroups];
   uint2 const *cb[kMaxGroups];
-  uint32_t cap[kMaxGroups];
-  uint32_t n;          // query items
-  float const *hcache; // NaN when no factors were computed
+  uint32_t cap[kMaxGroups]; // a multiple of kChunk
+  uint32_t n;               // query items
+  float const *hcache;      // NaN when no factors were computed
 };
 
 constexpr uint32_t kWide = 0x80000000u;
 
-// host decode of one list entry (tests / CopyNeighbors)
-inline uint32_t nbr_host_decode(uint32_t c, uint32_t base, uint16_t d16, uint32_t d32) {
-  return (c & kWide) ? d32 : base + d16;
+// host decode of entry k of an item whose row of chunks is `row`
+inline uint32_t nbr_host_decode(uint2 cb, unsigned char const *row, uint32_t const *idx32row, uint32_t k) {
+  if (cb.x & kWide) return idx32row[k];
+  uint16_t d;
+  unsigned char const *p = row + size_t(k / kChunk) * kChunkBytes + (k % kChunk) * 2;
+  d = uint16_t(p[0] | (p[1] << 8));
+  return cb.y + d;
 }
 
 constexpr int kMaxListGroups = 8; // groups a neighbour-list build supports
@@ -141,8 +147,7 @@ private:
     size_t n = 0;
     uint32_t cap[kMaxGroups] = {};
     uint32_t *idx32[kMaxGroups] = {};
-    uint16_t *idx16[kMaxGroups] = {};
-    float *gf[kMaxGroups] = {};
+    unsigned char *chunks[kMaxGroups] = {};
     uint2 *cb = nullptr; // [G][n]
     float *hcache = nullptr;
     bool has_gf = false;

@@ -45,51 +45,63 @@ constexpr int kStJacIter = 4, kStJacDone = 5;
 // ---------------------------------------------------------------------------
 
 struct NbrList {
-  uint16_t const *idx16; // row-major, entry k of item i at [i * cap + k]: j - base
-  uint32_t const *idx32; // row-major: j (read for wide items only)
-  float const *gf;       // row-major: the pair's kernel-gradient factor
-  uint2 const *cb;       // per item: (count | kWide, base)
-  uint32_t cap;          // row length, a multiple of 8
+  unsigned char const *chunks; // rows of 96-byte chunks (16 offsets + 16 factors)
+  uint32_t const *idx32;       // [i * cap + k]: j (read for wide items only)
+  uint2 const *cb;             // per item: (count | kWide, base)
+  uint32_t cap;                // row length in entries, a multiple of 16
 };
 
-// Calls f(j, factor) for the neighbours of item i, in list order.  Entries
-// are fetched 8 at a time with 16-byte streaming loads (evict-first: the
-// lists are read once per sweep, the gathered particle records should stay
-// in L2), so that the 8 gathers of a chunk can be in flight together.
+// Calls f(j, factor) for the neighbours of item i, in list order.  A chunk
+// of 16 entries is fetched with six 16-byte streaming loads (evict-first:
+// the lists are read once per sweep, the gathered particle records should
+// stay in L2), so that its 16 gathers can be in flight together.
 template <class F>
 __device__ __forceinline__ void for_each_nbr(NbrList const &L, uint32_t i, bool with_gf, F &&f) {
   uint2 cb = __ldg(L.cb + i);
   uint32_t c = min(cb.x & ~kWide, L.cap);
   bool wide = (cb.x & kWide) != 0;
-  size_t row = size_t(i) * L.cap;
-  for (uint32_t kb = 0; kb < c; kb += 8) {
-    uint32_t j[8];
+  unsigned char const *row = L.chunks + size_t(i) * (L.cap / kChunk) * kChunkBytes;
+  for (uint32_t kb = 0; kb < c; kb += kChunk) {
+    uint4 const *ch = reinterpret_cast<uint4 const *>(row + size_t(kb / kChunk) * kChunkBytes);
+    uint32_t j[kChunk];
     if (wide) {
-      uint4 a = __ldcs(reinterpret_cast<uint4 const *>(L.idx32 + row + kb));
-      uint4 b = __ldcs(reinterpret_cast<uint4 const *>(L.idx32 + row + kb + 4));
-      j[0] = a.x; j[1] = a.y; j[2] = a.z; j[3] = a.w;
-      j[4] = b.x; j[5] = b.y; j[6] = b.z; j[7] = b.w;
-    } else {
-      uint4 a = __ldcs(reinterpret_cast<uint4 const *>(L.idx16 + row + kb));
-      uint32_t w[4] = {a.x, a.y, a.z, a.w};
+      uint4 const *w32 = reinterpret_cast<uint4 const *>(L.idx32 + size_t(i) * L.cap + kb);
 #pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        j[2 * t] = cb.y + (w[t] & 0xFFFFu);
-        j[2 * t + 1] = cb.y + (w[t] >> 16);
+      for (int v = 0; v < 4; ++v) {
+        uint4 a = __ldcs(w32 + v);
+        j[4 * v] = a.x;
+        j[4 * v + 1] = a.y;
+        j[4 * v + 2] = a.z;
+        j[4 * v + 3] = a.w;
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < 2; ++v) {
+        uint4 a = __ldcs(ch + v);
+        uint32_t w[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          j[8 * v + 2 * t] = cb.y + (w[t] & 0xFFFFu);
+          j[8 * v + 2 * t + 1] = cb.y + (w[t] >> 16);
+        }
       }
     }
-    float g[8];
+    float g[kChunk];
     if (with_gf) {
-      float4 a = __ldcs(reinterpret_cast<float4 const *>(L.gf + row + kb));
-      float4 b = __ldcs(reinterpret_cast<float4 const *>(L.gf + row + kb + 4));
-      g[0] = a.x; g[1] = a.y; g[2] = a.z; g[3] = a.w;
-      g[4] = b.x; g[5] = b.y; g[6] = b.z; g[7] = b.w;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        uint4 a = __ldcs(ch + 2 + v);
+        g[4 * v] = __uint_as_float(a.x);
+        g[4 * v + 1] = __uint_as_float(a.y);
+        g[4 * v + 2] = __uint_as_float(a.z);
+        g[4 * v + 3] = __uint_as_float(a.w);
+      }
     } else {
 #pragma unroll
-      for (int t = 0; t < 8; ++t) g[t] = 0.0f;
+      for (int t = 0; t < int(kChunk); ++t) g[t] = 0.0f;
     }
 #pragma unroll
-    for (int t = 0; t < 8; ++t)
+    for (int t = 0; t < int(kChunk); ++t)
       if (kb + t < c) f(j[t], g[t]);
   }
 }
@@ -955,7 +967,7 @@ protected:
   std::vector<FluidG> fluid_;
   std::vector<BoundG> bound_;
 
-  static NbrList nl(NbrView const &v, int g) { return NbrList{v.idx16[g], v.idx32[g], v.gf[g], v.cb[g], v.cap[g]}; }
+  static NbrList nl(NbrView const &v, int g) { return NbrList{v.chunks[g], v.idx32[g], v.cb[g], v.cap[g]}; }
   // packed neighbour records of the fluid / boundary groups (made current
   // here: may launch a pack kernel on `s`)
   FluidN fn(FluidG const &F, NbrView const &v, cudaStream_t s) {
