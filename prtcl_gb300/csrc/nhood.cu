@@ -344,31 +344,73 @@ __global__ void k_xsorted(PosTable pt, uint32_t const *vals, size_t N, float4 *x
   }
 }
 
-constexpr int kBuildNT = 64; // query items (threads) per list-build block
+constexpr int kBuildNT = 128; // query items (threads) per list-build block
 
 struct ListOut {
   unsigned char *chunks[kMaxListGroups];
   uint32_t *idx32[kMaxListGroups];
   uint32_t cap[kMaxListGroups];
-  uint32_t soff[kMaxListGroups]; // staging row offset of group g (sum of the caps before it)
-  uint32_t scap;                 // sum of the caps
-  uint2 *cb;                     // [G][n]
-  uint32_t *maxcnt;              // [kMaxListGroups]
+  uint2 *cb;        // [G][n]
+  uint32_t *maxcnt; // [kMaxListGroups]
   uint32_t n;
   int G;
 };
 
-// per-group counters of one query item, kept in registers (the group index
-// of a neighbour selects the slot through unrolled compares)
-struct ListAcc {
-  uint32_t c[kMaxListGroups], lo[kMaxListGroups], hi[kMaxListGroups];
+// State of one item's list towards one neighbour group.  The current chunk
+// is buffered in shared memory (24 words per thread and group: 8 words of
+// packed 16-bit deltas, 16 factor words; word w of thread t at
+// buf[(g * 24 + w) * NT + t]) and written as six 16-byte stores when full.
+// Deltas are signed, relative to the row's first neighbour j0 (the row's
+// base); a row whose neighbours do not all fit becomes "wide": its indices
+// then go to idx32 (the entries already written are converted on the spot).
+struct RowState {
+  uint32_t c, j0;
+  bool wide;
 };
 
-// staged entries: index j at sj[(soff[g] + k) * NT + t], factor bits at
-// sf[...] (consecutive threads on consecutive words)
+__device__ __forceinline__ uint32_t &bufw(uint32_t *buf, int g, int w) {
+  return buf[(size_t(g) * 24 + w) * kBuildNT + threadIdx.x];
+}
+
+__device__ __forceinline__ void flush_chunk(ListOut const &lo, int g, uint32_t i, uint32_t chunk, uint32_t *buf) {
+  size_t nch = lo.cap[g] / kChunk;
+  uint4 *dst = reinterpret_cast<uint4 *>(lo.chunks[g] + (size_t(i) * nch + chunk) * kChunkBytes);
+#pragma unroll
+  for (int v = 0; v < 6; ++v)
+    dst[v] = make_uint4(bufw(buf, g, 4 * v), bufw(buf, g, 4 * v + 1), bufw(buf, g, 4 * v + 2), bufw(buf, g, 4 * v + 3));
+}
+
+__device__ __forceinline__ void row_add(ListOut const &lo, int g, uint32_t i, RowState &R, uint32_t j, float f,
+                                        uint32_t *buf) {
+  uint32_t k = R.c++;
+  if (k >= lo.cap[g]) return; // overflow: the host grows the lists and builds again
+  if (k == 0) R.j0 = j;
+  int32_t d = int32_t(j - R.j0);
+  uint32_t slot = k % kChunk;
+  if (!R.wide && (d < -32768 || d > 32767)) {
+    // becomes wide: entries 0..k-1 to idx32 (full chunks from global memory,
+    // the current one from the buffer)
+    R.wide = true;
+    size_t nch = lo.cap[g] / kChunk;
+    for (uint32_t e = 0; e < k; ++e) {
+      uint32_t w;
+      if (e / kChunk == k / kChunk) w = bufw(buf, g, int((e % kChunk) / 2));
+      else w = reinterpret_cast<uint32_t const *>(lo.chunks[g] + (size_t(i) * nch + e / kChunk) * kChunkBytes)[(e % kChunk) / 2];
+      int32_t de = int32_t(int16_t((e & 1) ? (w >> 16) : (w & 0xFFFFu)));
+      lo.idx32[g][size_t(i) * lo.cap[g] + e] = R.j0 + uint32_t(de);
+    }
+  }
+  if (R.wide) lo.idx32[g][size_t(i) * lo.cap[g] + k] = j;
+  uint32_t &w = bufw(buf, g, int(slot / 2));
+  uint32_t h = R.wide ? 0u : (uint32_t(d) & 0xFFFFu);
+  w = (slot & 1) ? ((w & 0xFFFFu) | (h << 16)) : h;
+  bufw(buf, g, 8 + int(slot)) = __float_as_uint(f);
+  if (slot == kChunk - 1) flush_chunk(lo, g, i, k / kChunk, buf);
+}
+
 __device__ __forceinline__ void visit_cell(GridView const &gv, float4 const *__restrict__ xs, int cell, f3 xi,
-                                           ListOut const &lo, ListAcc &A, KernelParams const &K, bool with_gf,
-                                           uint32_t *sj, uint32_t *sf) {
+                                           uint32_t i, ListOut const &lo, RowState *R, KernelParams const &K,
+                                           bool with_gf, uint32_t *buf) {
   if (cell < 0) return;
   int s0 = gv.cell_start[cell], s1 = gv.cell_start[cell + 1];
   for (int s = s0; s < s1; ++s) {
@@ -380,114 +422,62 @@ __device__ __forceinline__ void visit_cell(GridView const &gv, float4 const *__r
       float f = with_gf ? kgrad_factor(K, d2) : 0.0f;
 #pragma unroll
       for (int q = 0; q < kMaxListGroups; ++q)
-        if (q == int(g)) {
-          uint32_t k = A.c[q]++;
-          A.lo[q] = min(A.lo[q], j);
-          A.hi[q] = max(A.hi[q], j);
-          if (k < lo.cap[q]) {
-            size_t o = size_t(lo.soff[q] + k) * kBuildNT + threadIdx.x;
-            sj[o] = j;
-            sf[o] = __float_as_uint(f);
-          }
-        }
+        if (q == int(g)) row_add(lo, q, i, R[q], j, f, buf);
     }
   }
 }
 
-// Neighbour lists of one query group (grid query of
-// util/grouped_uniform_grid.hpp:407-531).  Each thread gathers its item's
-// neighbours into shared memory in traversal order; the block then writes
-// its rows of chunks with coalesced 16-byte stores.
+// neighbour lists of one query group (grid query of util/grouped_uniform_grid.hpp:407-531)
 __global__ void __launch_bounds__(kBuildNT) k_build_lists(GridView gv, float4 const *__restrict__ xs,
                                                           float4 const *__restrict__ qpos, int q, ListOut lo,
                                                           float const *hp, float *hcache) {
-  extern __shared__ uint32_t smem[];
-  uint32_t *sj = smem;
-  uint32_t *sf = smem + size_t(lo.scap) * kBuildNT;
-  __shared__ uint2 s_cb[kMaxListGroups][kBuildNT];
-  uint32_t i0 = blockIdx.x * kBuildNT;
-  uint32_t i = i0 + threadIdx.x;
+  extern __shared__ uint32_t buf[];
+  uint32_t i = blockIdx.x * kBuildNT + threadIdx.x;
   bool with_gf = hp != nullptr;
   KernelParams K = kparams(with_gf ? *hp : 1.0f);
   if (i == 0) *hcache = with_gf ? K.h : __int_as_float(0x7fc00000);
-  ListAcc A;
+  if (i >= lo.n) return;
+  RowState R[kMaxListGroups];
 #pragma unroll
-  for (int g = 0; g < kMaxListGroups; ++g) {
-    A.c[g] = 0;
-    A.lo[g] = 0xFFFFFFFFu;
-    A.hi[g] = 0;
+  for (int g = 0; g < kMaxListGroups; ++g) R[g] = RowState{0u, 0u, false};
+  float4 x4 = qpos[i];
+  f3 xi = mk3(x4);
+  int cell = -1;
+  bool fallback = false;
+  int3 gi;
+  if (gv.in_grid[q]) {
+    cell = gv.s2c[gv.r2s[gv.goff[q] + i]];
+  } else {
+    gi = x_to_gi(x4, gv);
+    cell = find_cell(gv, gi);
+    fallback = cell < 0;
   }
-  if (i < lo.n) {
-    float4 x4 = qpos[i];
-    f3 xi = mk3(x4);
-    int cell = -1;
-    bool fallback = false;
-    int3 gi;
-    if (gv.in_grid[q]) {
-      cell = gv.s2c[gv.r2s[gv.goff[q] + i]];
-    } else {
-      gi = x_to_gi(x4, gv);
-      cell = find_cell(gv, gi);
-      fallback = cell < 0;
-    }
-    if (!fallback) {
-      visit_cell(gv, xs, cell, xi, lo, A, K, with_gf, sj, sf);
-      for (int k = 0; k < 26; ++k)
-        visit_cell(gv, xs, gv.cell_adj[size_t(cell) * 26 + k], xi, lo, A, K, with_gf, sj, sf);
-    } else {
-      for (int k = 0; k < 13; ++k) {
-        int3 p = make_int3(gi.x + c_offsets[k][0], gi.y + c_offsets[k][1], gi.z + c_offsets[k][2]);
-        visit_cell(gv, xs, find_cell(gv, p), xi, lo, A, K, with_gf, sj, sf);
-        int3 m = make_int3(gi.x - c_offsets[k][0], gi.y - c_offsets[k][1], gi.z - c_offsets[k][2]);
-        visit_cell(gv, xs, find_cell(gv, m), xi, lo, A, K, with_gf, sj, sf);
-      }
+  if (!fallback) {
+    visit_cell(gv, xs, cell, xi, i, lo, R, K, with_gf, buf);
+    for (int k = 0; k < 26; ++k) visit_cell(gv, xs, gv.cell_adj[size_t(cell) * 26 + k], xi, i, lo, R, K, with_gf, buf);
+  } else {
+    for (int k = 0; k < 13; ++k) {
+      int3 p = make_int3(gi.x + c_offsets[k][0], gi.y + c_offsets[k][1], gi.z + c_offsets[k][2]);
+      visit_cell(gv, xs, find_cell(gv, p), xi, i, lo, R, K, with_gf, buf);
+      int3 m = make_int3(gi.x - c_offsets[k][0], gi.y - c_offsets[k][1], gi.z - c_offsets[k][2]);
+      visit_cell(gv, xs, find_cell(gv, m), xi, i, lo, R, K, with_gf, buf);
     }
   }
 #pragma unroll
   for (int g = 0; g < kMaxListGroups; ++g) {
     if (g >= lo.G) break;
-    uint32_t n = A.c[g];
-    bool wide = n > 0 && A.hi[g] - A.lo[g] > 0xFFFFu;
-    uint2 cb = make_uint2(n | (wide ? kWide : 0u), n > 0 ? A.lo[g] : 0u);
-    s_cb[g][threadIdx.x] = cb;
-    if (i < lo.n) {
-      lo.cb[size_t(g) * lo.n + i] = cb;
-      if (n > lo.cap[g]) atomicMax(&lo.maxcnt[g], n);
-      else if (wide)
-        for (uint32_t k = 0; k < n; ++k) lo.idx32[g][size_t(i) * lo.cap[g] + k] = sj[size_t(lo.soff[g] + k) * kBuildNT + threadIdx.x];
-    }
-  }
-  __syncthreads();
-  // coalesced copy-out: the block's rows are one contiguous range per group
-  uint32_t rows = min(uint32_t(kBuildNT), lo.n - i0);
-  for (int g = 0; g < lo.G; ++g) {
-    uint32_t nch = lo.cap[g] / kChunk;
-    uint32_t pieces = rows * nch * 6u;
-    uint4 *dst = reinterpret_cast<uint4 *>(lo.chunks[g] + size_t(i0) * nch * kChunkBytes);
-    for (uint32_t p = threadIdx.x; p < pieces; p += kBuildNT) {
-      uint32_t r = p / (nch * 6u), rem = p % (nch * 6u), c = rem / 6u, part = rem % 6u;
-      uint2 cb = s_cb[g][r];
-      uint32_t cnt = cb.x & ~kWide;
-      bool ok = !(cb.x & kWide) && cnt <= lo.cap[g];
-      uint32_t w[4];
-      if (part < 2) {
-        uint32_t k0 = c * kChunk + part * 8u;
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          uint32_t ka = k0 + 2 * e, kb = ka + 1;
-          uint32_t da = (ok && ka < cnt) ? sj[size_t(lo.soff[g] + ka) * kBuildNT + r] - cb.y : 0u;
-          uint32_t db = (ok && kb < cnt) ? sj[size_t(lo.soff[g] + kb) * kBuildNT + r] - cb.y : 0u;
-          w[e] = (da & 0xFFFFu) | (db << 16);
-        }
-      } else {
-        uint32_t k0 = c * kChunk + (part - 2u) * 4u;
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          uint32_t k = k0 + e;
-          w[e] = (k < cnt && cnt <= lo.cap[g]) ? sf[size_t(lo.soff[g] + k) * kBuildNT + r] : 0u;
-        }
+    uint32_t n = R[g].c;
+    lo.cb[size_t(g) * lo.n + i] = make_uint2(n | (R[g].wide ? kWide : 0u), R[g].j0);
+    if (n > lo.cap[g]) {
+      atomicMax(&lo.maxcnt[g], n);
+    } else if (n % kChunk) {
+      // the partial last chunk, zero-filled
+      for (uint32_t slot = n % kChunk; slot < kChunk; ++slot) {
+        uint32_t &w = bufw(buf, g, int(slot / 2));
+        w = (slot & 1) ? (w & 0xFFFFu) : 0u;
+        bufw(buf, g, 8 + int(slot)) = 0u;
       }
-      dst[p] = make_uint4(w[0], w[1], w[2], w[3]);
+      flush_chunk(lo, g, i, n / kChunk, buf);
     }
   }
 }
@@ -766,17 +756,12 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
     if (!L.hcache) PG_CUDA(cudaMalloc(&L.hcache, sizeof(float)));
     if (n == 0) break;
     ListOut lo{};
-    uint32_t scap = 0;
     for (int g = 0; g < G; ++g) {
       lo.idx32[g] = L.idx32[g];
       lo.chunks[g] = L.chunks[g];
       lo.cap[g] = L.cap[g];
-      lo.soff[g] = scap;
-      scap += L.cap[g];
     }
-    lo.scap = scap;
-    size_t smem = size_t(scap) * kBuildNT * 8;
-    if (smem > 200 * 1024) throw Error("neighbour lists: too many neighbours per item for the list build");
+    size_t smem = size_t(G) * 24 * kBuildNT * 4;
     PG_CUDA(cudaFuncSetAttribute(k_build_lists, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     lo.cb = L.cb;
     lo.maxcnt = stats_d_ + 8;

@@ -48,8 +48,8 @@ namespace prtcl_gpu {
 //   16 x uint16  j - base   (32 bytes)
 //   16 x float   the pair's kernel-gradient factor (64 bytes)
 // so a chunk is exactly three 32-byte sectors and every fetched sector is
-// used once.  Also per item:
-//   cb[g][i]    (count | kWide if "wide", smallest neighbour index = base)
+// used once (offsets are signed 16-bit: j = base + offset).  Also per item:
+//   cb[g][i]    (count | kWide if "wide", base = the first neighbour's index)
 //   idx32[g]    j as 32-bit indices at [i * cap + k], written and read for
 //               "wide" items only (neighbours spanning >= 65536 indices)
 // The factors are present when the lists were built with a smoothing scale
@@ -68,13 +68,14 @@ struct NbrView {
 
 constexpr uint32_t kWide = 0x80000000u;
 
-// host decode of entry k of an item whose row of chunks is `row`
+// host decode of entry k of an item whose row of chunks is `row`: the
+// 16-bit entries are signed offsets from the row's base (its first
+// neighbour)
 inline uint32_t nbr_host_decode(uint2 cb, unsigned char const *row, uint32_t const *idx32row, uint32_t k) {
   if (cb.x & kWide) return idx32row[k];
-  uint16_t d;
   unsigned char const *p = row + size_t(k / kChunk) * kChunkBytes + (k % kChunk) * 2;
-  d = uint16_t(p[0] | (p[1] << 8));
-  return cb.y + d;
+  int16_t d = int16_t(uint16_t(p[0] | (p[1] << 8)));
+  return cb.y + uint32_t(int32_t(d));
 }
 
 constexpr int kMaxListGroups = 8; // groups a neighbour-list build supports

@@ -81,8 +81,9 @@ __device__ __forceinline__ void for_each_nbr(NbrList const &L, uint32_t i, bool 
         uint32_t w[4] = {a.x, a.y, a.z, a.w};
 #pragma unroll
         for (int t = 0; t < 4; ++t) {
-          j[8 * v + 2 * t] = cb.y + (w[t] & 0xFFFFu);
-          j[8 * v + 2 * t + 1] = cb.y + (w[t] >> 16);
+          // signed 16-bit offsets from the row's base
+          j[8 * v + 2 * t] = cb.y + uint32_t(int32_t(int16_t(w[t] & 0xFFFFu)));
+          j[8 * v + 2 * t + 1] = cb.y + uint32_t(int32_t(w[t]) >> 16);
         }
       }
     }
