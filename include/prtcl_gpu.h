@@ -76,6 +76,20 @@ int prtcl_gpu_field_upload(prtcl_gpu_model *model, const char *group, const char
  * overlap) until the stream reaches the copy. */
 int prtcl_gpu_field_upload_async(prtcl_gpu_model *model, const char *group, const char *field, const void *host,
                                  int64_t count, void *stream);
+/* Upload a varying field like prtcl_gpu_field_upload, but without allocating
+ * device memory.  No counterpart in the reference (its fields live in host
+ * memory).  For callers that cannot allocate when they upload: a host that
+ * hands all free device memory to its own pool, or code that must not enter
+ * the device allocator inside a time-critical section.  real[3] and
+ * real[3][3] fields are staged through one fixed 8 MiB device array of the
+ * library (at most 699,050 vector or 233,016 matrix items per call; larger
+ * counts return PRTCL_GPU_ERROR and change nothing); other fields are copied
+ * directly and have no limit.  The first call on a device looks up the
+ * array's address, so make it before any stream capture.  Synchronous.  The
+ * array is shared by the whole process and keeps the last call's bytes:
+ * calls that overlap in time, from different threads, race on it. */
+int prtcl_gpu_field_upload_noalloc(prtcl_gpu_model *model, const char *group, const char *field, const void *host,
+                                   int64_t count, void *stream);
 /* Copy the field to host memory in the reference layout (synchronous). */
 int prtcl_gpu_field_download(prtcl_gpu_model *model, const char *group, const char *field, void *host, int64_t count,
                              void *stream);

@@ -50,6 +50,7 @@ SIGNATURES = {
     "prtcl_gpu_field_add": [vp, cp, cp, cp, i32, i32p],
     "prtcl_gpu_field_upload": [vp, cp, cp, vp, i64, vp],
     "prtcl_gpu_field_upload_async": [vp, cp, cp, vp, i64, vp],
+    "prtcl_gpu_field_upload_noalloc": [vp, cp, cp, vp, i64, vp],
     "prtcl_gpu_field_download": [vp, cp, cp, vp, i64, vp],
     "prtcl_gpu_field_info": [vp, cp, cp, C.c_char_p, i32p, i32p],
     "prtcl_gpu_uniform_add": [vp, cp, cp, cp, i32, i32p],

@@ -189,6 +189,17 @@ int prtcl_gpu_field_upload_async(prtcl_gpu_model *model, const char *group, cons
     upload_varying(varying(model->m, group, field), g.count, host, size_t(count), model->m.pick(stream), false);
   });
 }
+int prtcl_gpu_field_upload_noalloc(prtcl_gpu_model *model, const char *group, const char *field, const void *host,
+                                   int64_t count, void *stream) {
+  NEED(model);
+  NEED(group);
+  NEED(field);
+  if (count > 0) NEED(host);
+  return guard([&] {
+    Group &g = model->m.group(group);
+    upload_varying_noalloc(varying(model->m, group, field), g.count, host, size_t(count), model->m.pick(stream));
+  });
+}
 int prtcl_gpu_field_download(prtcl_gpu_model *model, const char *group, const char *field, void *host, int64_t count,
                              void *stream) {
   NEED(model);

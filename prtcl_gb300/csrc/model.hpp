@@ -162,6 +162,10 @@ private:
 
 // field kernels (model.cu)
 void upload_varying(VaryingField &f, size_t count, void const *host, size_t n_items, cudaStream_t s, bool sync);
+// upload through a fixed static device array instead of a temporary allocation
+// (noalloc.cu); synchronous, and not safe to overlap with another such call
+void upload_varying_noalloc(VaryingField &f, size_t count, void const *host, size_t n_items, cudaStream_t s);
+size_t noalloc_stage_bytes();
 void download_varying(VaryingField const &f, size_t count, void *host, size_t n_items, cudaStream_t s);
 
 } // namespace prtcl_gpu
