@@ -761,6 +761,13 @@ void *oracle_scene_new(int real_bytes, int fp64_reductions) {
   return s;
 }
 void oracle_scene_free(void *s) { delete static_cast<SceneBase *>(s); }
+// three-way Morton compare of n pairs of int32 triples (a[3 i..], b[3 i..])
+void oracle_morton_compare_many(int32_t const *a, int32_t const *b, int64_t n, int8_t *out) {
+  for (int64_t i = 0; i < n; ++i) {
+    oracle::GI l{a[3 * i], a[3 * i + 1], a[3 * i + 2]}, r{b[3 * i], b[3 * i + 1], b[3 * i + 2]};
+    out[i] = int8_t(oracle::morton_compare(l, r));
+  }
+}
 int oracle_set_threads(int n) {
   if (n > 0) omp_set_num_threads(n);
   return omp_get_max_threads();

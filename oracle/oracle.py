@@ -40,6 +40,8 @@ def lib():
             L.oracle_scene_new.argtypes = [C.c_int, C.c_int]
             L.oracle_scene_free.argtypes = [vp]
             L.oracle_set_threads.argtypes = [C.c_int]
+            L.oracle_morton_compare_many.argtypes = [vp, vp, C.c_int64, vp]
+            L.oracle_morton_compare_many.restype = None
             L.oracle_add_group.argtypes = [vp, cp, cp]
             L.oracle_add_tag.argtypes = [vp, cp, cp]
             L.oracle_resize.argtypes = [vp, cp, i64]
@@ -78,6 +80,16 @@ class OracleError(RuntimeError):
 def _check(rc):
     if rc != 0:
         raise OracleError(lib().oracle_last_error().decode())
+
+
+def morton_compare(a, b):
+    """Three-way Morton compare (-1, 0, 1) of int32 triples a[i] and b[i]."""
+    a = np.ascontiguousarray(a, np.int32).reshape(-1, 3)
+    b = np.ascontiguousarray(b, np.int32).reshape(-1, 3)
+    assert a.shape == b.shape
+    out = np.empty(len(a), np.int8)
+    lib().oracle_morton_compare_many(a.ctypes.data, b.ctypes.data, len(a), out.ctypes.data)
+    return out
 
 
 def set_threads(n=0):
