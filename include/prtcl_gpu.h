@@ -200,6 +200,74 @@ int prtcl_gpu_scheme_procedure_names(prtcl_gpu_scheme *scheme, char *buf, int64_
 int prtcl_gpu_scheme_source(prtcl_gpu_scheme *scheme, char *buf, int64_t size, int64_t *needed_out);
 int prtcl_gpu_registry_scheme_names(char *buf, int64_t size, int64_t *needed_out);
 
+/* ---- batched scenes (no single counterpart in the reference) ----
+ *
+ * A batch keeps many independent dam-break scenes resident on the device and
+ * steps them together: every procedure of the reference's step loop
+ * (share/scripts/prtcl-lua.example.lua:363-461: grid update with a permute
+ * every `permute_every` steps of the scene, density, gravity, velocity
+ * integration, IISPH set-up and relaxed-Jacobi pressure loop, optional WKBB18
+ * implicit viscosity, position integration) runs as one launch over all
+ * scenes.  The relaxed-Jacobi and PCG loops decide convergence per scene, so
+ * each scene stops when its own criterion is met.  A scene's results are the
+ * same, bit for bit, whether it runs alone or beside others, and whenever it
+ * was added.  All scenes of a batch share the parameters below.  Scenes can be
+ * added and removed between steps (continuous batching); added scenes are
+ * set up as the reference's scripts do (update, permute, boundary volumes,
+ * share/scripts/prtcl-lua.example.lua:196-316) at the next step or query. */
+typedef struct prtcl_gpu_batch prtcl_gpu_batch;
+typedef struct prtcl_gpu_batch_params {
+  double smoothing_scale;            /* h; search radius 2 h */
+  double time_step;
+  double rest_density;
+  double gravity[3];
+  double relaxation;                 /* iisph_relaxation (omega) */
+  double max_density_error;          /* eta of the Jacobi loop */
+  int32_t max_iterations;            /* Jacobi cap */
+  int32_t viscosity;                 /* nonzero: WKBB18 implicit viscosity each step */
+  double dynamic_viscosity;          /* fluid */
+  double boundary_dynamic_viscosity;
+  double pcg_max_error;              /* wkbb18_maximum_error */
+  int32_t pcg_max_iterations;        /* wkbb18_maximum_iterations */
+  int32_t permute_every;             /* steps between permutes of a scene (>= 1) */
+} prtcl_gpu_batch_params;
+typedef struct prtcl_gpu_scene_info {
+  int64_t fluid, boundary;           /* particle counts */
+  int64_t steps;                     /* steps taken */
+  int32_t slot;                      /* segment of the scene in the batch */
+  int32_t last_jacobi_iterations;
+  int32_t last_pcg_iterations;
+  int32_t pad;
+  double last_relative_density_error; /* aprde / nprde at the end of the last Jacobi loop */
+  double max_relative_density_error;
+  double jacobi_solves, jacobi_iterations, jacobi_capped; /* accumulated over the scene's steps */
+  double pcg_solves, pcg_iterations, pcg_capped;
+} prtcl_gpu_scene_info;
+
+int prtcl_gpu_batch_create(const prtcl_gpu_batch_params *params, prtcl_gpu_batch **out);
+int prtcl_gpu_batch_destroy(prtcl_gpu_batch *batch);
+/* Add a scene: fluid particles (3 floats each, at rest, mass h^3 rho0) and
+ * static boundary particles.  *scene_id_out is unique within the batch. */
+int prtcl_gpu_batch_add_scene(prtcl_gpu_batch *batch, const float *fluid_xyz, int64_t fluid_count,
+                              const float *boundary_xyz, int64_t boundary_count, int64_t *scene_id_out);
+int prtcl_gpu_batch_remove_scene(prtcl_gpu_batch *batch, int64_t scene_id);
+/* Advance every scene by `steps` steps (queued on the batch's stream; the
+ * grid update synchronises once per step). */
+int prtcl_gpu_batch_step(prtcl_gpu_batch *batch, int32_t steps);
+int prtcl_gpu_batch_synchronize(prtcl_gpu_batch *batch);
+int prtcl_gpu_batch_scene_info(prtcl_gpu_batch *batch, int64_t scene_id, prtcl_gpu_scene_info *out);
+/* Copy a varying field of a scene's fluid particles ("position", "velocity",
+ * "density", "pressure", ...) to host memory in the reference layout;
+ * `count` must equal the scene's fluid count. */
+int prtcl_gpu_batch_download(prtcl_gpu_batch *batch, int64_t scene_id, const char *field, void *host, int64_t count);
+int prtcl_gpu_batch_scene_count(prtcl_gpu_batch *batch, int32_t *count_out);
+int prtcl_gpu_batch_particles(prtcl_gpu_batch *batch, int64_t *fluid_out, int64_t *boundary_out);
+/* Device bytes held by the batch's particle state, grid and neighbour lists. */
+int prtcl_gpu_batch_device_bytes(prtcl_gpu_batch *batch, int64_t *bytes_out);
+int prtcl_gpu_batch_profile_enable(prtcl_gpu_batch *batch, int32_t enable);
+/* Per-kernel timing lines "name launches total_ms", as prtcl_gpu_profile_read. */
+int prtcl_gpu_batch_profile_read(prtcl_gpu_batch *batch, char *buf, int64_t size, int64_t *needed_out);
+
 #ifdef __cplusplus
 }
 #endif

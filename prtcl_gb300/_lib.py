@@ -86,7 +86,38 @@ SIGNATURES = {
     "prtcl_gpu_scheme_procedure_names": [vp, C.c_char_p, i64, i64p],
     "prtcl_gpu_scheme_source": [vp, C.c_char_p, i64, i64p],
     "prtcl_gpu_registry_scheme_names": [C.c_char_p, i64, i64p],
+    "prtcl_gpu_batch_create": [vp, pp],
+    "prtcl_gpu_batch_destroy": [vp],
+    "prtcl_gpu_batch_add_scene": [vp, vp, i64, vp, i64, i64p],
+    "prtcl_gpu_batch_remove_scene": [vp, i64],
+    "prtcl_gpu_batch_step": [vp, i32],
+    "prtcl_gpu_batch_synchronize": [vp],
+    "prtcl_gpu_batch_scene_info": [vp, i64, vp],
+    "prtcl_gpu_batch_download": [vp, i64, cp, vp, i64],
+    "prtcl_gpu_batch_scene_count": [vp, i32p],
+    "prtcl_gpu_batch_particles": [vp, i64p, i64p],
+    "prtcl_gpu_batch_device_bytes": [vp, i64p],
+    "prtcl_gpu_batch_profile_enable": [vp, i32],
+    "prtcl_gpu_batch_profile_read": [vp, C.c_char_p, i64, i64p],
 }
+
+
+class BatchParams(C.Structure):
+    """prtcl_gpu_batch_params"""
+    _fields_ = [("smoothing_scale", C.c_double), ("time_step", C.c_double), ("rest_density", C.c_double),
+                ("gravity", C.c_double * 3), ("relaxation", C.c_double), ("max_density_error", C.c_double),
+                ("max_iterations", C.c_int32), ("viscosity", C.c_int32), ("dynamic_viscosity", C.c_double),
+                ("boundary_dynamic_viscosity", C.c_double), ("pcg_max_error", C.c_double),
+                ("pcg_max_iterations", C.c_int32), ("permute_every", C.c_int32)]
+
+
+class SceneInfo(C.Structure):
+    """prtcl_gpu_scene_info"""
+    _fields_ = [("fluid", C.c_int64), ("boundary", C.c_int64), ("steps", C.c_int64), ("slot", C.c_int32),
+                ("last_jacobi_iterations", C.c_int32), ("last_pcg_iterations", C.c_int32), ("pad", C.c_int32),
+                ("last_relative_density_error", C.c_double), ("max_relative_density_error", C.c_double),
+                ("jacobi_solves", C.c_double), ("jacobi_iterations", C.c_double), ("jacobi_capped", C.c_double),
+                ("pcg_solves", C.c_double), ("pcg_iterations", C.c_double), ("pcg_capped", C.c_double)]
 _RESTYPE = {"prtcl_gpu_last_error": cp, "prtcl_gpu_version": cp, "prtcl_gpu_launch_count": C.c_uint64}
 
 _lock = threading.Lock()

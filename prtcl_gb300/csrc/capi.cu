@@ -1,5 +1,6 @@
 // extern "C" surface of the library (include/prtcl_gpu.h).
 #include "../../include/prtcl_gpu.h"
+#include "batch.hpp"
 #include "schemes.hpp"
 
 #include <atomic>
@@ -17,6 +18,9 @@ struct prtcl_gpu_nhood {
 };
 struct prtcl_gpu_scheme {
   std::unique_ptr<Scheme> s;
+};
+struct prtcl_gpu_batch {
+  std::unique_ptr<Batch> b;
 };
 
 namespace prtcl_gpu {
@@ -450,6 +454,90 @@ int prtcl_gpu_scheme_source(prtcl_gpu_scheme *scheme, char *buf, int64_t size, i
 }
 int prtcl_gpu_registry_scheme_names(char *buf, int64_t size, int64_t *needed_out) {
   return write_str(join(scheme_names()), buf, size, needed_out);
+}
+
+// ---- batched scenes ----
+
+int prtcl_gpu_batch_create(const prtcl_gpu_batch_params *params, prtcl_gpu_batch **out) {
+  NEED(params);
+  NEED(out);
+  *out = nullptr;
+  return guard([&] {
+    auto b = std::make_unique<prtcl_gpu_batch>();
+    b->b = std::make_unique<Batch>(*params);
+    *out = b.release();
+  });
+}
+int prtcl_gpu_batch_destroy(prtcl_gpu_batch *batch) {
+  delete batch;
+  return PRTCL_GPU_OK;
+}
+int prtcl_gpu_batch_add_scene(prtcl_gpu_batch *batch, const float *fluid_xyz, int64_t fluid_count,
+                              const float *boundary_xyz, int64_t boundary_count, int64_t *scene_id_out) {
+  NEED(batch);
+  NEED(scene_id_out);
+  if (fluid_count < 0 || boundary_count < 0) return fail(PRTCL_GPU_INVALID, "invalid argument: negative count");
+  return guard([&] {
+    *scene_id_out = batch->b->add(fluid_xyz, size_t(fluid_count), boundary_xyz, size_t(boundary_count));
+  });
+}
+int prtcl_gpu_batch_remove_scene(prtcl_gpu_batch *batch, int64_t scene_id) {
+  NEED(batch);
+  return guard([&] { batch->b->remove(scene_id); });
+}
+int prtcl_gpu_batch_step(prtcl_gpu_batch *batch, int32_t steps) {
+  NEED(batch);
+  if (steps < 0) return fail(PRTCL_GPU_INVALID, "invalid argument: negative step count");
+  return guard([&] { batch->b->step(steps); });
+}
+int prtcl_gpu_batch_synchronize(prtcl_gpu_batch *batch) {
+  NEED(batch);
+  return guard([&] { batch->b->synchronize(); });
+}
+int prtcl_gpu_batch_scene_info(prtcl_gpu_batch *batch, int64_t scene_id, prtcl_gpu_scene_info *out) {
+  NEED(batch);
+  NEED(out);
+  return guard([&] { *out = batch->b->info(scene_id); });
+}
+int prtcl_gpu_batch_download(prtcl_gpu_batch *batch, int64_t scene_id, const char *field, void *host, int64_t count) {
+  NEED(batch);
+  NEED(field);
+  if (count > 0) NEED(host);
+  if (count < 0) return fail(PRTCL_GPU_INVALID, "invalid argument: negative count");
+  return guard([&] { batch->b->download(scene_id, field, host, size_t(count)); });
+}
+int prtcl_gpu_batch_scene_count(prtcl_gpu_batch *batch, int32_t *count_out) {
+  NEED(batch);
+  NEED(count_out);
+  return guard([&] { *count_out = int32_t(batch->b->scene_count()); });
+}
+int prtcl_gpu_batch_particles(prtcl_gpu_batch *batch, int64_t *fluid_out, int64_t *boundary_out) {
+  NEED(batch);
+  NEED(fluid_out);
+  NEED(boundary_out);
+  return guard([&] { batch->b->particles(*fluid_out, *boundary_out); });
+}
+int prtcl_gpu_batch_device_bytes(prtcl_gpu_batch *batch, int64_t *bytes_out) {
+  NEED(batch);
+  NEED(bytes_out);
+  return guard([&] { *bytes_out = int64_t(batch->b->device_bytes()); });
+}
+int prtcl_gpu_batch_profile_enable(prtcl_gpu_batch *batch, int32_t enable) {
+  NEED(batch);
+  return guard([&] { batch->b->model().prof.enabled = enable != 0; });
+}
+int prtcl_gpu_batch_profile_read(prtcl_gpu_batch *batch, char *buf, int64_t size, int64_t *needed_out) {
+  NEED(batch);
+  std::string text;
+  int rc = guard([&] {
+    for (auto &kv : batch->b->model().prof.read()) {
+      char line[256];
+      std::snprintf(line, sizeof line, "%s %lld %.6f\n", kv.first.c_str(), kv.second.count, kv.second.ms);
+      text += line;
+    }
+  });
+  if (rc != PRTCL_GPU_OK) return rc;
+  return write_str(text, buf, size, needed_out);
 }
 
 } // extern "C"

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 
 namespace prtcl_gpu {
 
@@ -84,6 +85,41 @@ __global__ void k_gather_words(uint32_t const *__restrict__ src, uint32_t *__res
   if (i < n) dst[i * words + w] = src[size_t(perm[i]) * words + w];
 }
 
+// remap gathers: src index 0xFFFFFFFF gives zero
+constexpr uint32_t kNoSrc = 0xFFFFFFFFu;
+template <class V>
+__global__ void k_remap(V const *__restrict__ src, V *__restrict__ dst, uint32_t const *__restrict__ map, size_t n) {
+  size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (i < n) {
+    uint32_t j = map[i];
+    if (j != kNoSrc) dst[i] = src[j];
+  }
+}
+__global__ void k_remap_planar9(float const *__restrict__ src, float *__restrict__ dst, uint32_t const *__restrict__ map,
+                                size_t n, size_t scap, size_t dcap) {
+  size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (i < n) {
+    uint32_t j = map[i];
+    if (j != kNoSrc)
+      for (int k = 0; k < 9; ++k) dst[k * dcap + i] = src[k * scap + j];
+  }
+}
+__global__ void k_remap_words(uint32_t const *__restrict__ src, uint32_t *__restrict__ dst,
+                              uint32_t const *__restrict__ map, size_t n, int words) {
+  size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  size_t i = t / words;
+  int w = int(t % words);
+  if (i < n && map[i] != kNoSrc) dst[i * words + w] = src[size_t(map[i]) * words + w];
+}
+// slot of each item of a segmented group, from the tiles
+__global__ void k_fill_seg(uint4 const *tiles, uint32_t ntiles, uint16_t *seg) {
+  uint32_t t = blockIdx.x;
+  if (t >= ntiles) return;
+  uint4 T = tiles[t];
+  uint32_t i = T.y + threadIdx.x;
+  if (i < T.z) seg[i] = uint16_t(T.x);
+}
+
 // ---------------------------------------------------------------------------
 // storage helpers
 // ---------------------------------------------------------------------------
@@ -129,6 +165,53 @@ void upload_varying(VaryingField &f, size_t count, void const *host, size_t n_it
     PG_CUDA(cudaFreeAsync(stage, s));
   }
   if (sync) PG_CUDA(cudaStreamSynchronize(s));
+}
+
+void upload_varying_range(VaryingField &f, size_t offset, void const *host, size_t n, cudaStream_t s) {
+  if (offset + n > f.cap) throw Error("upload: range beyond the field");
+  f.version++;
+  if (n == 0) return;
+  size_t hbytes = n * f.type.host_item_bytes();
+  if (!f.type.is_vec3() && !f.type.is_mat3()) {
+    PG_CUDA(cudaMemcpyAsync(static_cast<char *>(f.d) + offset * f.type.host_item_bytes(), host, hbytes,
+                            cudaMemcpyHostToDevice, s));
+    return;
+  }
+  void *stage = nullptr;
+  PG_CUDA(cudaMallocAsync(&stage, hbytes, s));
+  PG_CUDA(cudaMemcpyAsync(stage, host, hbytes, cudaMemcpyHostToDevice, s));
+  if (f.type.is_vec3())
+    k_expand_vec3<<<div_up(n, 256), 256, 0, s>>>(static_cast<float *>(stage), static_cast<float4 *>(f.d) + offset, n);
+  else
+    k_to_planar9<<<div_up(n, 256), 256, 0, s>>>(static_cast<float *>(stage), static_cast<float *>(f.d) + offset, n,
+                                                 f.cap);
+  count_launch();
+  PG_LAUNCH_CHECK();
+  PG_CUDA(cudaFreeAsync(stage, s));
+}
+
+void download_varying_range(VaryingField const &f, size_t offset, void *host, size_t n, cudaStream_t s) {
+  if (offset + n > f.cap) throw Error("download: range beyond the field");
+  if (n == 0) return;
+  size_t hbytes = n * f.type.host_item_bytes();
+  if (!f.type.is_vec3() && !f.type.is_mat3()) {
+    PG_CUDA(cudaMemcpyAsync(host, static_cast<char const *>(f.d) + offset * f.type.host_item_bytes(), hbytes,
+                            cudaMemcpyDeviceToHost, s));
+  } else {
+    void *stage = nullptr;
+    PG_CUDA(cudaMallocAsync(&stage, hbytes, s));
+    if (f.type.is_vec3())
+      k_pack_vec3<<<div_up(n, 256), 256, 0, s>>>(static_cast<float4 const *>(f.d) + offset, static_cast<float *>(stage),
+                                                 n);
+    else
+      k_from_planar9<<<div_up(n, 256), 256, 0, s>>>(static_cast<float const *>(f.d) + offset,
+                                                    static_cast<float *>(stage), n, f.cap);
+    count_launch();
+    PG_LAUNCH_CHECK();
+    PG_CUDA(cudaMemcpyAsync(host, stage, hbytes, cudaMemcpyDeviceToHost, s));
+    PG_CUDA(cudaFreeAsync(stage, s));
+  }
+  PG_CUDA(cudaStreamSynchronize(s));
 }
 
 void download_varying(VaryingField const &f, size_t count, void *host, size_t n_items, cudaStream_t s) {
@@ -238,6 +321,138 @@ void Group::permute(uint32_t const *perm, cudaStream_t s) {
   }
 }
 
+void Group::remap(uint32_t const *map, size_t n, cudaStream_t s) {
+  if (n >= (size_t(1) << 28)) throw Error("group '" + name + "' too large: at most 2^28 - 1 items");
+  for (auto &kv : varying) {
+    VaryingField &f = kv.second;
+    void *nd = alloc_field(f.type, n, s); // zeroed
+    unsigned b = 256;
+    if (n) {
+      if (f.type.is_vec3()) {
+        k_remap<float4><<<div_up(n, b), b, 0, s>>>(static_cast<float4 const *>(f.d), static_cast<float4 *>(nd), map, n);
+      } else if (f.type.is_mat3()) {
+        k_remap_planar9<<<div_up(n, b), b, 0, s>>>(static_cast<float const *>(f.d), static_cast<float *>(nd), map, n,
+                                                   f.cap, n);
+      } else if (f.type.host_item_bytes() == 4) {
+        k_remap<uint32_t><<<div_up(n, b), b, 0, s>>>(static_cast<uint32_t const *>(f.d), static_cast<uint32_t *>(nd),
+                                                      map, n);
+      } else {
+        int words = int(f.type.host_item_bytes() / 4);
+        k_remap_words<<<div_up(n * words, b), b, 0, s>>>(static_cast<uint32_t const *>(f.d),
+                                                          static_cast<uint32_t *>(nd), map, n, words);
+      }
+      count_launch();
+      PG_LAUNCH_CHECK();
+    }
+    if (f.d) PG_CUDA(cudaFreeAsync(f.d, s));
+    f.d = nd;
+    f.cap = n;
+    f.version++;
+  }
+  count = n;
+  model_->layout_version++;
+}
+
+// ---------------------------------------------------------------------------
+// segments
+// ---------------------------------------------------------------------------
+
+Segments::~Segments() {
+  for (auto &kv : groups) {
+    if (kv.second.seg) cudaFree(kv.second.seg);
+    if (kv.second.tiles) cudaFree(kv.second.tiles);
+    if (kv.second.slot_tiles) cudaFree(kv.second.slot_tiles);
+  }
+  for (void *p : {(void *)partials, (void *)tickets, (void *)scal, (void *)stat, (void *)stats, (void *)nprde,
+                  (void *)iters, (void *)due})
+    if (p) cudaFree(p);
+}
+
+// Slot state is kept across a change of the slot count (slots that stay keep
+// their statistics); new slots start zeroed.
+void Segments::set_slots(uint32_t n, cudaStream_t s) {
+  if (n > 65536) throw Error("at most 65536 segments");
+  if (n == slots && tickets) return;
+  size_t m = std::max<uint32_t>(n, 1), keep = std::min(n, slots);
+  auto grow = [&](auto *&p, size_t per) {
+    using T = std::remove_reference_t<decltype(*p)>;
+    T *q = nullptr;
+    PG_CUDA(cudaMalloc(&q, m * per * sizeof(T)));
+    PG_CUDA(cudaMemsetAsync(q, 0, m * per * sizeof(T), s));
+    if (p && keep) PG_CUDA(cudaMemcpyAsync(q, p, keep * per * sizeof(T), cudaMemcpyDeviceToDevice, s));
+    if (p) {
+      PG_CUDA(cudaStreamSynchronize(s));
+      PG_CUDA(cudaFree(p));
+    }
+    p = q;
+  };
+  grow(tickets, 1);
+  grow(scal, 16);
+  grow(stat, 8);
+  grow(stats, 8);
+  grow(nprde, 1);
+  grow(iters, 1);
+  grow(due, 1);
+  slots = n;
+}
+
+// zero the state of one slot (a scene that takes the slot over)
+void Segments::reset_slot(uint32_t k, cudaStream_t s) {
+  if (k >= slots) throw Error("segments: slot out of range");
+  PG_CUDA(cudaMemsetAsync(tickets + k, 0, sizeof(unsigned), s));
+  PG_CUDA(cudaMemsetAsync(scal + size_t(k) * 16, 0, 16 * sizeof(double), s));
+  PG_CUDA(cudaMemsetAsync(stat + size_t(k) * 8, 0, 8 * sizeof(int), s));
+  PG_CUDA(cudaMemsetAsync(stats + size_t(k) * 8, 0, 8 * sizeof(double), s));
+  PG_CUDA(cudaMemsetAsync(iters + k, 0, sizeof(int), s));
+  PG_CUDA(cudaMemsetAsync(due + k, 0, 1, s));
+}
+
+void Segments::assign(Group const *g, std::vector<uint32_t> const &count, cudaStream_t s) {
+  if (count.size() != slots) throw Error("segments: one count per slot expected");
+  SegGroup &G = groups[g];
+  G.start.assign(slots + 1, 0);
+  std::vector<uint4> tiles;
+  std::vector<uint32_t> slot_tiles(slots + 1, 0);
+  for (uint32_t k = 0; k < slots; ++k) {
+    G.start[k + 1] = G.start[k] + count[k];
+    slot_tiles[k] = uint32_t(tiles.size());
+    for (uint32_t b = G.start[k]; b < G.start[k + 1]; b += kSegTile)
+      tiles.push_back(make_uint4(k, b, std::min(b + kSegTile, G.start[k + 1]), 0u));
+  }
+  slot_tiles[slots] = uint32_t(tiles.size());
+  size_t n = G.start[slots];
+  if (n != g->count) throw Error("segments of group '" + g->name + "' do not cover its items");
+  if (n > G.seg_cap) {
+    if (G.seg) PG_CUDA(cudaFree(G.seg));
+    G.seg_cap = std::max<size_t>(n + n / 8, 1024);
+    PG_CUDA(cudaMalloc(&G.seg, G.seg_cap * sizeof(uint16_t)));
+  }
+  if (tiles.size() + 1 > G.tile_cap || slots + 1 > G.tile_cap) {
+    if (G.tiles) PG_CUDA(cudaFree(G.tiles));
+    if (G.slot_tiles) PG_CUDA(cudaFree(G.slot_tiles));
+    G.tile_cap = std::max<size_t>(std::max(tiles.size(), size_t(slots)) + 1024, 4096);
+    PG_CUDA(cudaMalloc(&G.tiles, G.tile_cap * sizeof(uint4)));
+    PG_CUDA(cudaMalloc(&G.slot_tiles, G.tile_cap * sizeof(uint32_t)));
+  }
+  G.ntiles = uint32_t(tiles.size());
+  if (!tiles.empty())
+    PG_CUDA(cudaMemcpyAsync(G.tiles, tiles.data(), tiles.size() * sizeof(uint4), cudaMemcpyHostToDevice, s));
+  PG_CUDA(cudaMemcpyAsync(G.slot_tiles, slot_tiles.data(), slot_tiles.size() * sizeof(uint32_t),
+                          cudaMemcpyHostToDevice, s));
+  if (G.ntiles) {
+    k_fill_seg<<<G.ntiles, kSegTile, 0, s>>>(G.tiles, G.ntiles, G.seg);
+    count_launch();
+    PG_LAUNCH_CHECK();
+  }
+  if (G.ntiles > partial_cap) {
+    if (partials) PG_CUDA(cudaFree(partials));
+    partial_cap = size_t(G.ntiles) + G.ntiles / 4 + 1024;
+    PG_CUDA(cudaMalloc(&partials, 3 * partial_cap * sizeof(double)));
+  }
+  // the host copies above read pageable vectors: finish before they go away
+  PG_CUDA(cudaStreamSynchronize(s));
+}
+
 // ---------------------------------------------------------------------------
 // packed neighbour records
 // ---------------------------------------------------------------------------
@@ -321,6 +536,15 @@ float4 const *Model::packed_xmr(Group *g, VaryingField *x, VaryingField *m, Vary
   }
   pack_commit(g, "xmr", key);
   return out;
+}
+
+size_t Model::device_bytes() const {
+  size_t b = arena_cap_;
+  for (auto const &kv : groups_)
+    for (auto const &f : kv.second->varying)
+      b += f.second.cap * (f.second.type.is_vec3() ? 16 : f.second.type.host_item_bytes());
+  for (auto const &kv : packs_) b += kv.second.cap * kv.second.item_bytes;
+  return b;
 }
 
 float *Model::pr_buffer(Group *g, cudaStream_t s) {

@@ -82,6 +82,51 @@ public:
   void resize(size_t n, cudaStream_t s);
   // gather every varying field: new[i] = old[perm[i]] (device perm, uint32)
   void permute(uint32_t const *perm_d, cudaStream_t s);
+  // new count n; every varying field becomes new[i] = old[src[i]], or zero
+  // where src[i] == 0xFFFFFFFF (device src, uint32)
+  void remap(uint32_t const *src_d, size_t n, cudaStream_t s);
+};
+
+// Scene segments of a batched model.  The items of a segmented group are
+// split into consecutive ranges, one per slot (scene); the solvers then take
+// every reduction and loop decision per slot, so that each scene converges
+// on its own and its results do not depend on the other scenes.  Ranges are
+// in slot order; an empty slot has an empty range.
+struct SegGroup {
+  std::vector<uint32_t> start;     // host: range of slot s is [start[s], start[s + 1])
+  uint16_t *seg = nullptr;         // device: slot of each item
+  uint4 *tiles = nullptr;          // device: (slot, begin, end, 0) of each tile of <= kSegTile items
+  uint32_t ntiles = 0;
+  uint32_t *slot_tiles = nullptr;  // device: tiles of slot s are [slot_tiles[s], slot_tiles[s + 1])
+  size_t seg_cap = 0, tile_cap = 0;
+};
+constexpr uint32_t kSegTile = 128; // items per reduction tile (one block)
+struct Segments {
+  uint32_t slots = 0;
+  std::map<Group const *, SegGroup> groups;
+  // per-slot device state
+  double *partials = nullptr; // [3][partial_cap] tile partial sums
+  size_t partial_cap = 0;
+  unsigned *tickets = nullptr; // [slots] finished tiles of the running reduction
+  double *scal = nullptr;      // [slots][16] solver scalars (PCG 0..7, density error 8)
+  int *stat = nullptr;         // [slots][8] loop state (PCG 0..3, Jacobi 4..5)
+  double *stats = nullptr;     // [slots][8] accumulated loop statistics
+  int *nprde = nullptr;        // [slots] fluid items
+  int *iters = nullptr;        // [slots] PCG iterations of the last solve
+  uint8_t *due = nullptr;      // [slots] permute flags
+  Segments() = default;
+  Segments(Segments const &) = delete;
+  Segments &operator=(Segments const &) = delete;
+  ~Segments();
+  SegGroup const *find(Group const *g) const {
+    auto it = groups.find(g);
+    return it == groups.end() ? nullptr : &it->second;
+  }
+  // set the number of slots (state of remaining slots kept, new ones zeroed)
+  void set_slots(uint32_t slots, cudaStream_t s);
+  void reset_slot(uint32_t slot, cudaStream_t s);
+  // ranges of group g: count[s] items in slot s, consecutively in slot order
+  void assign(Group const *g, std::vector<uint32_t> const &count, cudaStream_t s);
 };
 
 class Model {
@@ -128,6 +173,10 @@ public:
   double *stats_d = nullptr;
   void stats_reset(cudaStream_t s);
   Profiler prof;                 // optional per-kernel CUDA-event timing
+  // scene segments (batched models only)
+  std::unique_ptr<Segments> seg;
+  // bytes of the varying fields and packed records
+  size_t device_bytes() const;
 
   // Packed per-particle records gathered by the neighbour sweeps, rebuilt
   // only when one of their source fields changed (keyed on the fields'
@@ -167,5 +216,9 @@ void upload_varying(VaryingField &f, size_t count, void const *host, size_t n_it
 void upload_varying_noalloc(VaryingField &f, size_t count, void const *host, size_t n_items, cudaStream_t s);
 size_t noalloc_stage_bytes();
 void download_varying(VaryingField const &f, size_t count, void *host, size_t n_items, cudaStream_t s);
+// items [offset, offset + n) of a field, in the host layout (stream-ordered;
+// the download synchronises)
+void upload_varying_range(VaryingField &f, size_t offset, void const *host, size_t n, cudaStream_t s);
+void download_varying_range(VaryingField const &f, size_t offset, void *host, size_t n, cudaStream_t s);
 
 } // namespace prtcl_gpu

@@ -79,10 +79,17 @@ __device__ __forceinline__ int3 x_to_gi(float4 x, GridView const &gv) {
                    axis_gi(x.z, gv.rinv, gv.radius));
 }
 
-__device__ __forceinline__ int find_cell(GridView const &gv, int3 gi) {
+__device__ __forceinline__ uint64_t seg_key(GridView const &gv, uint32_t seg) {
+  return gv.seg_shift < 64 ? (uint64_t(seg) << gv.seg_shift) : 0ull;
+}
+__device__ __forceinline__ uint32_t item_seg(GridView const &gv, int g, uint32_t i) {
+  return gv.seg[g] ? uint32_t(gv.seg[g][i]) : 0u;
+}
+
+__device__ __forceinline__ int find_cell(GridView const &gv, int3 gi, uint32_t seg) {
   uint32_t u0 = unsign(gi.x), u1 = unsign(gi.y), u2 = unsign(gi.z);
   if (!key_valid(u0, gv.key) || !key_valid(u1, gv.key) || !key_valid(u2, gv.key)) return -1;
-  uint64_t key = make_key(u0, u1, u2, gv.key.keep);
+  uint64_t key = make_key(u0, u1, u2, gv.key.keep) | seg_key(gv, seg);
   int lo = 0, hi = *gv.ncells;
   while (lo < hi) {
     int mid = (lo + hi) >> 1;
@@ -285,11 +292,12 @@ __global__ void k_cells_u(PosTable pt, GridView gv, int G, size_t N, uint32_t *u
   }
 }
 
-__global__ void k_cells_key(uint32_t const *ukeys, size_t N, uint32_t keep, uint64_t *keys) {
+__global__ void k_cells_key(uint32_t const *ukeys, uint32_t const *vals, size_t N, GridView gv, uint64_t *keys) {
   size_t n = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
   if (n < N) {
     uint4 u = reinterpret_cast<uint4 const *>(ukeys)[n];
-    keys[n] = make_key(u.x, u.y, u.z, keep);
+    uint32_t h = vals[n];
+    keys[n] = make_key(u.x, u.y, u.z, gv.key.keep) | seg_key(gv, item_seg(gv, int(h >> 28), h & 0x0FFFFFFFu));
   }
 }
 
@@ -326,11 +334,12 @@ __global__ void k_cells_adj(GridView gv, int4 const *cell_gi, size_t N, int32_t 
   size_t c = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
   if (c >= N || int(c) >= *gv.ncells) return;
   int4 g = cell_gi[c];
+  uint32_t seg = gv.seg_shift < 64 ? uint32_t(gv.cell_key[c] >> gv.seg_shift) : 0u;
   for (int k = 0; k < 13; ++k) {
     int3 p = make_int3(g.x + c_offsets[k][0], g.y + c_offsets[k][1], g.z + c_offsets[k][2]);
     int3 m = make_int3(g.x - c_offsets[k][0], g.y - c_offsets[k][1], g.z - c_offsets[k][2]);
-    adj[c * 26 + k] = find_cell(gv, p);
-    adj[c * 26 + 25 - k] = find_cell(gv, m);
+    adj[c * 26 + k] = find_cell(gv, p, seg);
+    adj[c * 26 + 25 - k] = find_cell(gv, m, seg);
   }
 }
 
@@ -449,18 +458,19 @@ __global__ void __launch_bounds__(kBuildNT) k_build_lists(GridView gv, float4 co
     cell = gv.s2c[gv.r2s[gv.goff[q] + i]];
   } else {
     gi = x_to_gi(x4, gv);
-    cell = find_cell(gv, gi);
+    cell = find_cell(gv, gi, item_seg(gv, q, i));
     fallback = cell < 0;
   }
   if (!fallback) {
     visit_cell(gv, xs, cell, xi, i, lo, R, K, with_gf, buf);
     for (int k = 0; k < 26; ++k) visit_cell(gv, xs, gv.cell_adj[size_t(cell) * 26 + k], xi, i, lo, R, K, with_gf, buf);
   } else {
+    uint32_t sq = item_seg(gv, q, i);
     for (int k = 0; k < 13; ++k) {
       int3 p = make_int3(gi.x + c_offsets[k][0], gi.y + c_offsets[k][1], gi.z + c_offsets[k][2]);
-      visit_cell(gv, xs, find_cell(gv, p), xi, i, lo, R, K, with_gf, buf);
+      visit_cell(gv, xs, find_cell(gv, p, sq), xi, i, lo, R, K, with_gf, buf);
       int3 m = make_int3(gi.x - c_offsets[k][0], gi.y - c_offsets[k][1], gi.z - c_offsets[k][2]);
-      visit_cell(gv, xs, find_cell(gv, m), xi, i, lo, R, K, with_gf, buf);
+      visit_cell(gv, xs, find_cell(gv, m, sq), xi, i, lo, R, K, with_gf, buf);
     }
   }
 #pragma unroll
@@ -490,6 +500,12 @@ __global__ void k_group_flags(uint32_t const *vals, size_t N, uint32_t g, uint32
 __global__ void k_group_perm(uint32_t const *vals, uint32_t const *flags, uint32_t const *excl, size_t N, uint32_t *perm) {
   size_t s = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
   if (s < N && flags[s]) perm[excl[s]] = vals[s] & 0x0FFFFFFFu;
+}
+
+// items of segments that are not due keep their place
+__global__ void k_perm_keep(uint16_t const *seg, uint8_t const *due, size_t n, uint32_t *perm) {
+  size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (i < n && !due[seg[i]]) perm[i] = uint32_t(i);
 }
 
 } // namespace
@@ -606,7 +622,9 @@ GridView Nhood::view() const {
   v.ncells = ncells_d_;
   for (int g = 0; g <= kMaxGroups; ++g) v.goff[g] = goff_[g];
   for (int g = 0; g < kMaxGroups; ++g) v.in_grid[g] = in_grid_[g];
+  for (int g = 0; g < kMaxGroups; ++g) v.seg[g] = (seg_count_ && g < int(seg_.size())) ? seg_[g] : nullptr;
   v.key = key_;
+  v.seg_shift = seg_count_ ? 3 * key_.bits : 64;
   v.radius = radius_;
   v.r2 = radius_ * radius_;
   v.rinv = float(1.0 / radius_);
@@ -668,14 +686,17 @@ void Nhood::update(cudaStream_t s) {
   if (k.bits > 21)
     throw Error("grid spans too many cells: " + std::to_string(k.bits) +
                 " informative bits per axis (at most 21 are supported)");
+  if (seg_count_ && 3 * k.bits + seg_bits_ > 64)
+    throw Error("grid spans too many cells for " + std::to_string(seg_count_) + " segments: " +
+                std::to_string(k.bits) + " informative bits per axis");
   key_ = k;
-  gv.key = k;
-  // 2. compressed Z-order keys
+  gv = view();
+  // 2. compressed Z-order keys (segment above them)
   model_->prof.begin("grid_sort", s);
-  k_cells_key<<<nb, 256, 0, s>>>(ukeys_, N, k.keep, keys_a_); count_launch();
+  k_cells_key<<<nb, 256, 0, s>>>(ukeys_, vals_a_, N, gv, keys_a_); count_launch();
   PG_LAUNCH_CHECK();
   // 3. stable LSD radix sort over the informative bits
-  int total_bits = 3 * k.bits;
+  int total_bits = 3 * k.bits + (seg_count_ ? seg_bits_ : 0);
   uint64_t *kin = keys_a_, *kout = keys_b_;
   uint32_t *vin = vals_a_, *vout = vals_b_;
   uint32_t tiles = uint32_t((N + kRsTile - 1) / kRsTile);
@@ -850,6 +871,53 @@ void Nhood::permute(Model &m, cudaStream_t s) {
     PG_CUDA(cudaFreeAsync(perm, s));
   }
   update(s);
+}
+
+void Nhood::permute_segments(Model &m, uint8_t const *due_d, cudaStream_t s) {
+  if (&m != model_) throw Error("Neighborhood::Permute with a model that was not loaded");
+  if (!seg_count_) throw Error("permute_segments on an unsegmented neighbourhood");
+  if (!has_grid_) update(s);
+  int G = int(gg_.size());
+  for (int g = 0; g < G; ++g) {
+    if (!in_grid_[g] || gg_[g].g->count == 0) continue;
+    if (g >= int(seg_.size()) || !seg_[g]) throw Error("permute_segments: group without segments");
+    size_t n = gg_[g].g->count;
+    k_group_flags<<<div_up(N_, 256), 256, 0, s>>>(sorted_vals_, N_, uint32_t(g), flags_); count_launch();
+    PG_LAUNCH_CHECK();
+    exclusive_scan(flags_, scan_, N_, block_sums_, block_sums_cap_, s);
+    uint32_t *perm = nullptr;
+    PG_CUDA(cudaMallocAsync(&perm, n * 4, s));
+    k_group_perm<<<div_up(N_, 256), 256, 0, s>>>(sorted_vals_, flags_, scan_, N_, perm); count_launch();
+    k_perm_keep<<<div_up(n, 256), 256, 0, s>>>(seg_[g], due_d, n, perm); count_launch();
+    PG_LAUNCH_CHECK();
+    gg_[g].g->permute(perm, s);
+    PG_CUDA(cudaFreeAsync(perm, s));
+  }
+  update(s);
+}
+
+void Nhood::set_segments(std::vector<uint16_t const *> const &seg, uint32_t count) {
+  if (seg.size() > size_t(kMaxGroups)) throw Error("set_segments: too many groups");
+  if (count > 65536) throw Error("set_segments: at most 65536 segments");
+  seg_ = seg;
+  seg_count_ = count;
+  seg_bits_ = 0;
+  while (count > 1 && (uint32_t(1) << seg_bits_) < count) ++seg_bits_;
+  has_grid_ = false;
+}
+
+size_t Nhood::device_bytes() const {
+  // keys 2x8, values 2x4, ukeys 16, flags 4, scan 4, r2s 4, s2c 4, cell
+  // start 4, adjacency 104, cell key 8, cell index 16, sorted positions 16
+  size_t b = cap_ * (16 + 8 + 16 + 4 + 4 + 4 + 4 + 4 + 104 + 8 + 16 + 16);
+  b += hist_cap_ * 4 + block_sums_cap_ * 4;
+  for (auto const &kv : lists_) {
+    Lists const &L = kv.second;
+    b += L.n * gg_.size() * sizeof(uint2);
+    for (size_t g = 0; g < gg_.size() && g < size_t(kMaxGroups); ++g)
+      b += L.n * (size_t(L.cap[g]) * 4 + size_t(L.cap[g] / kChunk) * kChunkBytes);
+  }
+  return b;
 }
 
 size_t Nhood::cell_count(cudaStream_t s) {

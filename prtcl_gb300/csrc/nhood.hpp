@@ -99,6 +99,11 @@ struct GridView {
   uint32_t goff[kMaxGroups + 1];
   int in_grid[kMaxGroups];
   KeyInfo key;
+  // batched models: per group the segment (scene) of each item, or nullptr
+  // (segment 0); the segment sits above the Z-order bits of the cell key,
+  // at bit seg_shift, so that cells of different segments never meet
+  uint16_t const *seg[kMaxGroups];
+  int seg_shift;
   double radius, r2;
   float rinv;  // 1 / radius rounded to f32 (fast path of the cell index)
   float r2lt;  // d2 < r2lt  <=>  (double) d2 < r2, for every float d2
@@ -116,6 +121,17 @@ public:
   void load(Model &m);
   void update(cudaStream_t s);
   void permute(Model &m, cudaStream_t s);
+  // Permute restricted to the segments whose flag is set in due_d (device,
+  // one byte per segment); the items of other segments keep their order.
+  // Only for segmented groups: segments occupy consecutive index ranges and
+  // the segment is the most significant part of the cell key, so the
+  // permutation never moves an item out of its segment's range.
+  void permute_segments(Model &m, uint8_t const *due_d, cudaStream_t s);
+  // Split the items of every group into segments (scenes of a batched
+  // model): seg[g] gives the segment of each item of group g (device, may
+  // be nullptr for segment 0), `count` segments in all (0: unsegmented).
+  // Invalidates the grid.
+  void set_segments(std::vector<uint16_t const *> const &seg, uint32_t count);
   bool loaded() const { return model_ != nullptr; }
   Model *model() const { return model_; }
 
@@ -134,6 +150,8 @@ public:
   void copy_lists(int q, int ng, int64_t *offsets, uint32_t *idx, size_t cap, cudaStream_t s);
 
   GridView view() const;
+  // bytes of the grid arrays and the neighbour lists
+  size_t device_bytes() const;
   uint64_t epoch() const { return epoch_; }
   // informative-bit overflow and other errors raise; lists growth is handled
   int list_rebuilds = 0;
@@ -169,6 +187,9 @@ private:
   uint32_t goff_[kMaxGroups + 1] = {};
   int in_grid_[kMaxGroups] = {};
   KeyInfo key_{};
+  std::vector<uint16_t const *> seg_;
+  uint32_t seg_count_ = 0;
+  int seg_bits_ = 0;
   uint64_t epoch_ = 0;
   bool has_grid_ = false;
 

@@ -189,6 +189,55 @@ __device__ bool reduce_commit(double const (&v)[NV], Red const &R, double (&out)
 
 unsigned red_grid(size_t n) { return unsigned(std::min<size_t>(div_up(n, kNT), kMaxRedBlocks)); }
 
+// Batched (segmented) models: block b of a tiled launch handles tile b, up to
+// kSegTile consecutive items of one slot (scene).  Reductions are per slot:
+// each tile stores its FP64 block sum; the last tile of the slot to finish
+// sums the slot's tile partials in tile order (one warp, fixed order), so a
+// slot's sums depend only on its own items.
+static_assert(kNT == int(kSegTile), "tiled kernels run one tile per block");
+struct SegArgs {
+  uint4 const *tiles;         // (slot, begin, end, 0)
+  uint32_t const *slot_tiles; // [slots + 1]
+  uint16_t const *seg;        // slot of each item
+  uint32_t ntiles, slots;
+  double *partials;           // [3][pcap]
+  size_t pcap;
+  unsigned *tickets;          // [slots]
+  double *scal;               // [slots][16]
+  int *stat;                  // [slots][8]
+  double *stats;              // [slots][8]
+  int const *nprde;           // [slots]
+  int *iters;                 // [slots]
+};
+constexpr int kSegScal = 16, kSegStat = 8, kSegStats = 8;
+constexpr int kSsAprde = 8;        // scal: density error of the iteration
+constexpr int kStPcgEnded = 3;     // stat: the slot's PCG loop has ended
+
+template <int NV>
+__device__ bool seg_commit(double const (&v)[NV], SegArgs const &S, uint32_t slot, double (&out)[NV]) {
+  __shared__ double sh[32];
+  __shared__ int last;
+  for (int k = 0; k < NV; ++k) {
+    double s = block_sum(v[k], sh);
+    if (threadIdx.x == 0) S.partials[k * S.pcap + blockIdx.x] = s;
+  }
+  __threadfence();
+  uint32_t t0 = S.slot_tiles[slot], t1 = S.slot_tiles[slot + 1];
+  if (threadIdx.x == 0) last = (atomicAdd(&S.tickets[slot], 1u) == t1 - t0 - 1) ? 1 : 0;
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  if (threadIdx.x < 32) {
+    for (int k = 0; k < NV; ++k) {
+      double acc = 0.0;
+      for (uint32_t t = t0 + threadIdx.x; t < t1; t += 32) acc += __ldcg(&S.partials[k * S.pcap + t]);
+      out[k] = warp_sum(acc);
+    }
+  }
+  if (threadIdx.x == 0) S.tickets[slot] = 0u;
+  return true;
+}
+
 // ---------------------------------------------------------------------------
 // density.compute_density (schemes/density.hpp:160-220)
 //   rho_i = sum_f m_j W(x_ij) + sum_b (V_j rho0) W(x_ij)
@@ -378,14 +427,17 @@ __global__ void k_set_i32(int *p, int v) { *p = v; }
 
 // iisph.iteration_pressure_acceleration (schemes/iisph.hpp:358-423).
 // `done` (device-loop mode) skips the work once the loop has converged.
+// Batched models: `segid` / `segstat` skip the items of slots whose loop has
+// ended.
 template <int NF, int NB>
 __global__ void __launch_bounds__(kNT) k_iisph_accel(uint32_t n, float4 const *__restrict__ x, float const *__restrict__ p,
                                                      float const *__restrict__ rho, float4 *__restrict__ a,
                                                      float const *rho0p, Globals G, Nbrs<NF, NB> N,
-                                                     int const *done) {
+                                                     int const *done, uint16_t const *segid, int const *segstat) {
   if (done && *(volatile int const *)done) return;
   uint32_t i = grid_tid();
   if (i >= n) return;
+  if (segid && segstat[segid[i] * kSegStat + kStJacDone]) return;
   KernelParams K = kparams(*G.h);
   bool uc = use_cache(N, K);
   float rho0 = *rho0p;
@@ -421,56 +473,126 @@ __global__ void __launch_bounds__(kNT) k_iisph_accel(uint32_t n, float4 const *_
 // fluid groups of one call: `first` starts it from the global aprde (or
 // from 0 in device-loop mode, where aprde := 0 precedes every iteration),
 // `last_group` stores it.  Also writes p / rho^2 for the next acceleration.
+struct PressureArgs {
+  float4 const *x, *a;
+  float const *rho, *s, *AA;
+  float *p, *pr, *Ap;
+  float const *rho0;
+};
+
+// one item of iteration_pressure; returns its density-error term
 template <int NF, int NB>
-__global__ void __launch_bounds__(kNT) k_iisph_pressure(uint32_t n, float4 const *__restrict__ x,
-                                                        float4 const *__restrict__ a, float const *__restrict__ rho,
-                                                        float const *__restrict__ s, float const *__restrict__ AA,
-                                                        float *__restrict__ p, float *__restrict__ pr,
-                                                        float *__restrict__ Ap, float const *rho0p, Globals G,
-                                                        Nbrs<NF, NB> N, Red R, int first, int last_group,
-                                                        int const *done) {
+__device__ __forceinline__ double iisph_pressure_item(uint32_t i, PressureArgs const &A, KernelParams const &K, bool uc,
+                                                      float rho0, float dt, float omega, Nbrs<NF, NB> const &N) {
+  f3 xi = mk3(A.x[i]), ai = mk3(A.a[i]);
+  float ap = 0.0f;
+#pragma unroll
+  for (int q = 0; q < NF; ++q) {
+    FluidN const &F = N.f[q];
+    for_each_nbr(F.L, i, uc, [&](uint32_t j_, float gf_) {
+      uint32_t j = j_;
+      float4 xm = __ldg(F.xm + j);
+      ap += xm.w * dot3(sub3(ai, mk3(__ldg(F.a + j))), pgrad(uc, gf_, K, sub3(xi, mk3(xm))));
+    });
+  }
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    BoundN const &B = N.b[q];
+    for_each_nbr(B.L, i, uc, [&](uint32_t j_, float gf_) {
+      float4 xv = __ldg(B.xV + j_);
+      ap += (rho0 * xv.w) * dot3(sub3(ai, f3{0.0f, 0.0f, 0.0f}), pgrad(uc, gf_, K, sub3(xi, mk3(xv))));
+    });
+  }
+  float ri = A.rho[i];
+  ap *= (dt * dt) * (rho0 / ri);
+  A.Ap[i] = ap;
+  float si = A.s[i], aai = A.AA[i];
+  float t = A.p[i] + ((omega * (si - ap)) * rcp0(aai, 1e-9f));
+  // std::max({0, t}) returns the first largest element: t only if 0 < t
+  float pn = ((0.0f < t) ? t : 0.0f) * ustep(1e-9f, fabsf(aai));
+  A.p[i] = pn;
+  A.pr[i] = pn / (ri * ri);
+  return double(((ap - si) / rho0) * ustep(1e-9f, pn));
+}
+
+template <int NF, int NB>
+__global__ void __launch_bounds__(kNT) k_iisph_pressure(uint32_t n, PressureArgs A, Globals G, Nbrs<NF, NB> N, Red R,
+                                                        int first, int last_group, int const *done) {
   if (done && *(volatile int const *)done) return;
   KernelParams K = kparams(*G.h);
   bool uc = use_cache(N, K);
-  float rho0 = *rho0p, dt = *G.dt, omega = *G.omega;
+  float rho0 = *A.rho0, dt = *G.dt, omega = *G.omega;
   double part = 0.0;
-  for (uint32_t i = grid_tid(); i < n; i += gridDim.x * blockDim.x) {
-    f3 xi = mk3(x[i]), ai = mk3(a[i]);
-    float ap = 0.0f;
-#pragma unroll
-    for (int q = 0; q < NF; ++q) {
-      FluidN const &F = N.f[q];
-      for_each_nbr(F.L, i, uc, [&](uint32_t j_, float gf_) {
-        uint32_t j = j_;
-        float4 xm = __ldg(F.xm + j);
-        ap += xm.w * dot3(sub3(ai, mk3(__ldg(F.a + j))), pgrad(uc, gf_, K, sub3(xi, mk3(xm))));
-      });
-    }
-#pragma unroll
-    for (int q = 0; q < NB; ++q) {
-      BoundN const &B = N.b[q];
-      for_each_nbr(B.L, i, uc, [&](uint32_t j_, float gf_) {
-        float4 xv = __ldg(B.xV + j_);
-        ap += (rho0 * xv.w) * dot3(sub3(ai, f3{0.0f, 0.0f, 0.0f}), pgrad(uc, gf_, K, sub3(xi, mk3(xv))));
-      });
-    }
-    float ri = rho[i];
-    ap *= (dt * dt) * (rho0 / ri);
-    Ap[i] = ap;
-    float si = s[i], aai = AA[i];
-    float t = p[i] + ((omega * (si - ap)) * rcp0(aai, 1e-9f));
-    // std::max({0, t}) returns the first largest element: t only if 0 < t
-    float pn = ((0.0f < t) ? t : 0.0f) * ustep(1e-9f, fabsf(aai));
-    p[i] = pn;
-    pr[i] = pn / (ri * ri);
-    part += double(((ap - si) / rho0) * ustep(1e-9f, pn));
-  }
+  for (uint32_t i = grid_tid(); i < n; i += gridDim.x * blockDim.x)
+    part += iisph_pressure_item<NF, NB>(i, A, K, uc, rho0, dt, omega, N);
   double v[1] = {part}, out[1];
   if (reduce_commit<1>(v, R, out) && threadIdx.x == 0) {
     double start = first ? (done ? 0.0 : double(*G.aprde)) : R.scalars[kSJacobi];
     double acc = start + out[0];
     R.scalars[kSJacobi] = acc;
     if (last_group) *G.aprde = float(acc);
+  }
+}
+
+// iteration_pressure over the tiles of a batched model: the density error of
+// each slot's iteration goes to scal[slot][kSsAprde]
+template <int NF, int NB>
+__global__ void __launch_bounds__(kNT) k_iisph_pressure_seg(PressureArgs A, Globals G, Nbrs<NF, NB> N, SegArgs S) {
+  uint4 T = S.tiles[blockIdx.x];
+  uint32_t slot = T.x;
+  if (S.stat[slot * kSegStat + kStJacDone]) return; // the whole block: one slot
+  KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
+  float rho0 = *A.rho0, dt = *G.dt, omega = *G.omega;
+  uint32_t i = T.y + threadIdx.x;
+  double part = (i < T.z) ? iisph_pressure_item<NF, NB>(i, A, K, uc, rho0, dt, omega, N) : 0.0;
+  double v[1] = {part}, out[1];
+  if (seg_commit<1>(v, S, slot, out) && threadIdx.x == 0) S.scal[slot * kSegScal + kSsAprde] = out[0];
+}
+
+// per-slot loop start: a slot without fluid items does not iterate
+__global__ void k_seg_jacobi_begin(SegArgs S) {
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < S.slots; k += gridDim.x * blockDim.x) {
+    S.stat[k * kSegStat + kStJacIter] = 0;
+    S.stat[k * kSegStat + kStJacDone] = (S.nprde[k] >= 1) ? 0 : 1;
+  }
+}
+
+// per-slot relaxed-Jacobi control (the rule of k_jacobi_control, per slot);
+// one block; the loop continues while any slot iterates.  stats per slot:
+// 0 solves, 1 iterations, 2 solves stopped at the cap, 3 largest final
+// aprde / nprde, 7 final aprde / nprde of the last solve
+__global__ void k_seg_jacobi_control(Globals G, SegArgs S, cudaGraphConditionalHandle h, int use_handle,
+                                     int kernels, int *all_done) {
+  int any = 0;
+  int maxit = *G.jac_max > 0 ? *G.jac_max : 100;
+  float eta = *G.jac_eta > 0.0f ? *G.jac_eta : 1e-3f;
+  for (uint32_t k = threadIdx.x; k < S.slots; k += blockDim.x) {
+    int *st = S.stat + k * kSegStat;
+    int done = st[kStJacDone];
+    if (!done) {
+      int it = st[kStJacIter] + 1;
+      st[kStJacIter] = it;
+      double rel = S.scal[k * kSegScal + kSsAprde] / double(S.nprde[k]);
+      bool converged = it >= 2 && rel < double(eta);
+      if (converged || it >= maxit || it >= 100000) done = 1;
+      st[kStJacDone] = done;
+      if (done) {
+        double *sv = S.stats + k * kSegStats;
+        sv[0] += 1.0;
+        sv[1] += double(it);
+        if (!converged) sv[2] += 1.0;
+        if (rel > sv[3]) sv[3] = rel;
+        sv[7] = rel;
+      }
+    }
+    any |= !done;
+  }
+  any = __syncthreads_or(any);
+  if (threadIdx.x == 0) {
+    *all_done = any ? 0 : 1;
+    if (kernels) atomicAdd(&g_loop_kernels, (unsigned long long)kernels);
+    if (use_handle) cudaGraphSetConditional(h, any ? 1u : 0u);
   }
 }
 
@@ -661,36 +783,94 @@ __global__ void k_pcg_guess(PcgArgs P) {
 
 // r = A x - b (b = v: the right-hand side's boundary term has v_b = 0),
 // y = M r, p = -y; dots b.b, r.r, r.y (solver/cg_openmp.hpp:48-96)
+// per-item parts of the PCG kernels (shared by the plain and the tiled
+// launches, so both compute the same values)
+template <int NB>
+__device__ __forceinline__ void pcg_init_item(PcgArgs const &P, KernelParams const &K, bool uc, float dt, float rho0,
+                                              float mu, Nbrs<0, NB> const &N, uint32_t i, double &bb, double &rr,
+                                              double &ry) {
+  f3 ax = wkbb18_system<NB>(P, K, uc, dt, rho0, mu, N, P.X, i);
+  f3 b = mk3(P.v[i]);
+  f3 r = sub3(ax, b);
+  f3 y = precond(P.sp, P.cap, i, r);
+  P.Rr[i] = make_float4(r.x, r.y, r.z, 0.0f);
+  P.Y[i] = make_float4(y.x, y.y, y.z, 0.0f);
+  P.P[i] = make_float4(-y.x, -y.y, -y.z, 0.0f);
+  bb += double(dot3(b, b));
+  rr += double(dot3(r, r));
+  ry += double(dot3(r, y));
+}
+template <int NB>
+__device__ __forceinline__ double pcg_q_item(PcgArgs const &P, KernelParams const &K, bool uc, float dt, float rho0,
+                                             float mu, Nbrs<0, NB> const &N, uint32_t i) {
+  f3 q = wkbb18_system<NB>(P, K, uc, dt, rho0, mu, N, P.P, i);
+  P.Q[i] = make_float4(q.x, q.y, q.z, 0.0f);
+  return double(dot3(mk3(P.P[i]), q));
+}
+__device__ __forceinline__ void pcg_update_item(PcgArgs const &P, float alpha, uint32_t i, double &rr, double &ry) {
+  f3 x = mk3(P.X[i]), p = mk3(P.P[i]), r = mk3(P.Rr[i]), q = mk3(P.Q[i]);
+  x = add3(x, scl3(alpha, p));
+  r = add3(r, scl3(alpha, q));
+  f3 y = precond(P.sp, P.cap, i, r);
+  P.X[i] = make_float4(x.x, x.y, x.z, 0.0f);
+  P.Rr[i] = make_float4(r.x, r.y, r.z, 0.0f);
+  P.Y[i] = make_float4(y.x, y.y, y.z, 0.0f);
+  rr += double(dot3(r, r));
+  ry += double(dot3(r, y));
+}
+__device__ __forceinline__ void pcg_p_item(PcgArgs const &P, float beta, uint32_t i) {
+  f3 y = mk3(P.Y[i]), p = mk3(P.P[i]);
+  f3 r = add3(f3{-y.x, -y.y, -y.z}, scl3(beta, p));
+  P.P[i] = make_float4(r.x, r.y, r.z, 0.0f);
+}
+// solver scalars after the initial residual (thr = max(tol^2 |b|^2, FLT_MIN))
+__device__ __forceinline__ void pcg_init_scalars(double *sc, int *st, double const (&out)[3], float tol_f) {
+  double tol = double(tol_f);
+  sc[0] = out[0];
+  double thr = tol * tol * out[0], fmin_ = double(1.17549435082228750797e-38f);
+  sc[1] = (thr < fmin_) ? fmin_ : thr;
+  sc[2] = out[1];
+  sc[3] = out[2];
+  st[kStPcgIter] = 0;
+  st[kStPcgActive] = 1; // iteration 0 always runs (min_k = 1)
+  st[kStPcgBody] = 0;
+}
+// after p.q: alpha, or stop on |p.q| < tol
+__device__ __forceinline__ void pcg_q_scalars(double *sc, int *st, double pq, float tol) {
+  double prev = sc[3];
+  sc[4] = prev;
+  sc[5] = pq;
+  if (fabs(pq) < double(tol)) st[kStPcgActive] = 0;
+  else sc[6] = double(float(prev / pq));
+}
+// after the update: stop on |r.y| < tol, else beta, k + 1 and the loop test
+__device__ __forceinline__ void pcg_update_scalars(double *sc, int *st, double rr, double ry, float tol, int max_k) {
+  double prev = sc[4];
+  sc[2] = rr;
+  sc[3] = ry;
+  if (fabs(prev) < double(tol)) {
+    st[kStPcgActive] = 0;
+  } else {
+    sc[7] = double(float(ry / prev));
+    int k = st[kStPcgIter] + 1;
+    st[kStPcgIter] = k;
+    // loop condition ok(k, r_nsq): k < 1 -> run; k > max_k -> stop;
+    // r_nsq < thr -> stop
+    bool ok = (k < 1) || (!(k > max_k) && !(rr < sc[1]));
+    st[kStPcgActive] = ok ? 1 : 0;
+  }
+}
+
 template <int NB>
 __global__ void __launch_bounds__(kNT) k_pcg_init(PcgArgs P, Globals G, Nbrs<0, NB> N, Red R) {
   KernelParams K = kparams(*G.h);
   bool uc = use_cache(N, K);
   float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
   double bb = 0.0, rr = 0.0, ry = 0.0;
-  for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x) {
-    f3 ax = wkbb18_system<NB>(P, K, uc, dt, rho0, mu, N, P.X, i);
-    f3 b = mk3(P.v[i]);
-    f3 r = sub3(ax, b);
-    f3 y = precond(P.sp, P.cap, i, r);
-    P.Rr[i] = make_float4(r.x, r.y, r.z, 0.0f);
-    P.Y[i] = make_float4(y.x, y.y, y.z, 0.0f);
-    P.P[i] = make_float4(-y.x, -y.y, -y.z, 0.0f);
-    bb += double(dot3(b, b));
-    rr += double(dot3(r, r));
-    ry += double(dot3(r, y));
-  }
+  for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x)
+    pcg_init_item<NB>(P, K, uc, dt, rho0, mu, N, i, bb, rr, ry);
   double v[3] = {bb, rr, ry}, out[3];
-  if (reduce_commit<3>(v, R, out) && threadIdx.x == 0) {
-    double tol = double(*P.tol);
-    R.scalars[kSPcg + 0] = out[0];
-    double thr = tol * tol * out[0], fmin_ = double(1.17549435082228750797e-38f);
-    R.scalars[kSPcg + 1] = (thr < fmin_) ? fmin_ : thr; // max(tol^2 |b|^2, FLT_MIN)
-    R.scalars[kSPcg + 2] = out[1];
-    R.scalars[kSPcg + 3] = out[2];
-    R.status[kStPcgIter] = 0;
-    R.status[kStPcgActive] = 1; // iteration 0 always runs (min_k = 1)
-    R.status[kStPcgBody] = 0;
-  }
+  if (reduce_commit<3>(v, R, out) && threadIdx.x == 0) pcg_init_scalars(R.scalars + kSPcg, R.status, out, *P.tol);
 }
 
 // q = A p; p.q; alpha or break (solver/cg_openmp.hpp:121-151)
@@ -701,19 +881,9 @@ __global__ void __launch_bounds__(kNT) k_pcg_q(PcgArgs P, Globals G, Nbrs<0, NB>
   bool uc = use_cache(N, K);
   float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
   double pq = 0.0;
-  for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x) {
-    f3 q = wkbb18_system<NB>(P, K, uc, dt, rho0, mu, N, P.P, i);
-    P.Q[i] = make_float4(q.x, q.y, q.z, 0.0f);
-    pq += double(dot3(mk3(P.P[i]), q));
-  }
+  for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x) pq += pcg_q_item<NB>(P, K, uc, dt, rho0, mu, N, i);
   double v[1] = {pq}, out[1];
-  if (reduce_commit<1>(v, R, out) && threadIdx.x == 0) {
-    double prev = R.scalars[kSPcg + 3];
-    R.scalars[kSPcg + 4] = prev;
-    R.scalars[kSPcg + 5] = out[0];
-    if (fabs(out[0]) < double(*P.tol)) R.status[kStPcgActive] = 0;
-    else R.scalars[kSPcg + 6] = double(float(prev / out[0]));
-  }
+  if (reduce_commit<1>(v, R, out) && threadIdx.x == 0) pcg_q_scalars(R.scalars + kSPcg, R.status, out[0], *P.tol);
 }
 
 // x += alpha p; r += alpha q; y = M r; r.r; r.y; break / beta
@@ -722,45 +892,17 @@ __global__ void __launch_bounds__(kNT) k_pcg_update(PcgArgs P, Red R) {
   if (!*(volatile int *)&R.status[kStPcgActive]) return;
   float alpha = float(R.scalars[kSPcg + 6]);
   double rr = 0.0, ry = 0.0;
-  for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x) {
-    f3 x = mk3(P.X[i]), p = mk3(P.P[i]), r = mk3(P.Rr[i]), q = mk3(P.Q[i]);
-    x = add3(x, scl3(alpha, p));
-    r = add3(r, scl3(alpha, q));
-    f3 y = precond(P.sp, P.cap, i, r);
-    P.X[i] = make_float4(x.x, x.y, x.z, 0.0f);
-    P.Rr[i] = make_float4(r.x, r.y, r.z, 0.0f);
-    P.Y[i] = make_float4(y.x, y.y, y.z, 0.0f);
-    rr += double(dot3(r, r));
-    ry += double(dot3(r, y));
-  }
+  for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x) pcg_update_item(P, alpha, i, rr, ry);
   double v[2] = {rr, ry}, out[2];
-  if (reduce_commit<2>(v, R, out) && threadIdx.x == 0) {
-    double prev = R.scalars[kSPcg + 4];
-    R.scalars[kSPcg + 2] = out[0];
-    R.scalars[kSPcg + 3] = out[1];
-    if (fabs(prev) < double(*P.tol)) {
-      R.status[kStPcgActive] = 0;
-    } else {
-      R.scalars[kSPcg + 7] = double(float(out[1] / prev));
-      int k = R.status[kStPcgIter] + 1;
-      R.status[kStPcgIter] = k;
-      // loop condition ok(k, r_nsq): k < 1 -> run; k > max_k -> stop;
-      // r_nsq < thr -> stop
-      bool ok = (k < 1) || (!(k > *P.max_k) && !(out[0] < R.scalars[kSPcg + 1]));
-      R.status[kStPcgActive] = ok ? 1 : 0;
-    }
-  }
+  if (reduce_commit<2>(v, R, out) && threadIdx.x == 0)
+    pcg_update_scalars(R.scalars + kSPcg, R.status, out[0], out[1], *P.tol, *P.max_k);
 }
 
 // p = -y + beta p (only when the loop continues)
 __global__ void k_pcg_p(PcgArgs P, Red R) {
   if (!*(volatile int *)&R.status[kStPcgActive]) return;
   float beta = float(R.scalars[kSPcg + 7]);
-  for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x) {
-    f3 y = mk3(P.Y[i]), p = mk3(P.P[i]);
-    f3 r = add3(f3{-y.x, -y.y, -y.z}, scl3(beta, p));
-    P.P[i] = make_float4(r.x, r.y, r.z, 0.0f);
-  }
+  for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x) pcg_p_item(P, beta, i);
 }
 
 // loop control of the device PCG loop: continue while active, and never run
@@ -780,11 +922,111 @@ __global__ void k_pcg_control(PcgArgs P, Red R, cudaGraphConditionalHandle h, in
   if (use_handle) cudaGraphSetConditional(h, cont ? 1u : 0u);
 }
 
+// --- the PCG loop over the tiles of a batched model, per slot -------------
+
+template <int NB>
+__global__ void __launch_bounds__(kNT) k_pcg_init_seg(PcgArgs P, Globals G, Nbrs<0, NB> N, SegArgs S) {
+  uint4 T = S.tiles[blockIdx.x];
+  uint32_t slot = T.x;
+  KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
+  float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
+  double bb = 0.0, rr = 0.0, ry = 0.0;
+  uint32_t i = T.y + threadIdx.x;
+  if (i < T.z) pcg_init_item<NB>(P, K, uc, dt, rho0, mu, N, i, bb, rr, ry);
+  double v[3] = {bb, rr, ry}, out[3];
+  if (seg_commit<3>(v, S, slot, out) && threadIdx.x == 0) {
+    int *st = S.stat + slot * kSegStat;
+    pcg_init_scalars(S.scal + slot * kSegScal, st, out, *P.tol);
+    st[kStPcgEnded] = 0;
+  }
+}
+
+template <int NB>
+__global__ void __launch_bounds__(kNT) k_pcg_q_seg(PcgArgs P, Globals G, Nbrs<0, NB> N, SegArgs S) {
+  uint4 T = S.tiles[blockIdx.x];
+  uint32_t slot = T.x;
+  if (!S.stat[slot * kSegStat + kStPcgActive]) return;
+  KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
+  float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
+  uint32_t i = T.y + threadIdx.x;
+  double v[1] = {(i < T.z) ? pcg_q_item<NB>(P, K, uc, dt, rho0, mu, N, i) : 0.0}, out[1];
+  if (seg_commit<1>(v, S, slot, out) && threadIdx.x == 0)
+    pcg_q_scalars(S.scal + slot * kSegScal, S.stat + slot * kSegStat, out[0], *P.tol);
+}
+
+__global__ void __launch_bounds__(kNT) k_pcg_update_seg(PcgArgs P, SegArgs S) {
+  uint4 T = S.tiles[blockIdx.x];
+  uint32_t slot = T.x;
+  if (!S.stat[slot * kSegStat + kStPcgActive]) return;
+  float alpha = float(S.scal[slot * kSegScal + 6]);
+  double rr = 0.0, ry = 0.0;
+  uint32_t i = T.y + threadIdx.x;
+  if (i < T.z) pcg_update_item(P, alpha, i, rr, ry);
+  double v[2] = {rr, ry}, out[2];
+  if (seg_commit<2>(v, S, slot, out) && threadIdx.x == 0)
+    pcg_update_scalars(S.scal + slot * kSegScal, S.stat + slot * kSegStat, out[0], out[1], *P.tol, *P.max_k);
+}
+
+__global__ void k_pcg_p_seg(PcgArgs P, SegArgs S) {
+  uint32_t i = grid_tid();
+  if (i >= P.n) return;
+  uint32_t slot = S.seg[i];
+  if (!S.stat[slot * kSegStat + kStPcgActive]) return;
+  pcg_p_item(P, float(S.scal[slot * kSegScal + 7]), i);
+}
+
+// per-slot PCG loop control (the rule of k_pcg_control, per slot); one
+// block.  stats per slot: 4 solves, 5 iterations, 6 solves stopped by the
+// iteration limit
+__global__ void k_seg_pcg_control(PcgArgs P, SegArgs S, cudaGraphConditionalHandle h, int use_handle, int kernels,
+                                  int *any_active) {
+  int any = 0;
+  int maxk = *P.max_k;
+  for (uint32_t k = threadIdx.x; k < S.slots; k += blockDim.x) {
+    int *st = S.stat + k * kSegStat;
+    if (st[kStPcgEnded]) continue;
+    int body = st[kStPcgBody] + 1;
+    st[kStPcgBody] = body;
+    bool cont = st[kStPcgActive] && body < (maxk < 0 ? 0 : maxk) + 1 && body < 1000000;
+    if (!cont) {
+      double *sv = S.stats + k * kSegStats;
+      sv[4] += 1.0;
+      sv[5] += double(st[kStPcgIter]);
+      if (st[kStPcgActive]) sv[6] += 1.0;
+      st[kStPcgActive] = 0;
+      st[kStPcgEnded] = 1;
+      S.iters[k] = st[kStPcgIter];
+    }
+    any |= cont ? 1 : 0;
+  }
+  any = __syncthreads_or(any);
+  if (threadIdx.x == 0) {
+    *any_active = any;
+    if (kernels) atomicAdd(&g_loop_kernels, (unsigned long long)kernels);
+    if (use_handle) cudaGraphSetConditional(h, any ? 1u : 0u);
+  }
+}
+
+// slots without fluid items take no part in the loop
+__global__ void k_seg_pcg_begin(SegArgs S) {
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < S.slots; k += gridDim.x * blockDim.x) {
+    int *st = S.stat + k * kSegStat;
+    if (S.slot_tiles[k] == S.slot_tiles[k + 1]) {
+      st[kStPcgActive] = 0;
+      st[kStPcgEnded] = 1;
+      st[kStPcgIter] = 0;
+      S.iters[k] = 0;
+    }
+  }
+}
+
 // apply (schemes/wkbb18.hpp:401-413): vd = (x - v) [0 < (t - t_b) - fade];
 // a = vd / dt
 __global__ void k_pcg_apply(PcgArgs P, Globals G, Red R) {
   uint32_t i = grid_tid();
-  if (i == 0) *P.iterations = R.status[kStPcgIter];
+  if (i == 0 && R.status) *P.iterations = R.status[kStPcgIter];
   if (i >= P.n) return;
   float dt = *G.dt, t = *G.t, fade = *G.fade;
   float u = ustep(0.0f, (t - P.tb[i]) - fade);
@@ -967,6 +1209,29 @@ protected:
   }
   std::vector<FluidG> fluid_;
   std::vector<BoundG> bound_;
+
+  // the per-slot view of a segmented group (batched models), or nullptr
+  bool segmented(Group const *g) const { return model_->seg && model_->seg->find(g); }
+  SegArgs seg_args(Group const *g) {
+    Segments &S = *model_->seg;
+    SegGroup const *G = S.find(g);
+    if (!G) throw Error("group '" + g->name + "' has no segments");
+    SegArgs a{};
+    a.tiles = G->tiles;
+    a.slot_tiles = G->slot_tiles;
+    a.seg = G->seg;
+    a.ntiles = G->ntiles;
+    a.slots = S.slots;
+    a.partials = S.partials;
+    a.pcap = S.partial_cap;
+    a.tickets = S.tickets;
+    a.scal = S.scal;
+    a.stat = S.stat;
+    a.stats = S.stats;
+    a.nprde = S.nprde;
+    a.iters = S.iters;
+    return a;
+  }
 
   static NbrList nl(NbrView const &v, int g) { return NbrList{v.chunks[g], v.idx32[g], v.cb[g], v.cap[g]}; }
   // packed neighbour records of the fluid / boundary groups (made current
@@ -1288,7 +1553,7 @@ public:
   // timing events (never on a capture stream).
   template <int NF, int NB> struct A {
     static void go(Iisph *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s, int const *done, bool prof,
-                   std::string *sig) {
+                   std::string *sig, SegArgs const *SA = nullptr) {
       uint32_t n = uint32_t(F.g->count);
       auto N = S->nbrs<NF, NB>(v, s);
       for (int q = 0; q < NF; ++q) N.f[q].pr = S->model_->packed_pr(S->fluid_[q].g, S->fluid_[q].p, S->fluid_[q].rho, s);
@@ -1304,35 +1569,41 @@ public:
         sig_add(*sig, rho);
         sig_add(*sig, a);
         sig_add(*sig, rho0);
+        if (SA) sig_add(*sig, *SA);
         return;
       }
       if (prof) S->model_->prof.begin("iisph_accel", s);
-      k_iisph_accel<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, x, p, rho, a, rho0, G, N, done); count_launch();
+      k_iisph_accel<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, x, p, rho, a, rho0, G, N, done, SA ? SA->seg : nullptr,
+                                                           SA ? SA->stat : nullptr);
+      count_launch();
       if (prof) S->model_->prof.end(s);
     }
   };
   template <int NF, int NB> struct P {
     static void go(Iisph *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s, int first, int last,
-                   int const *done, bool prof, std::string *sig) {
+                   int const *done, bool prof, std::string *sig, SegArgs const *SA = nullptr) {
       uint32_t n = uint32_t(F.g->count);
       auto N = S->nbrs<NF, NB>(v, s);
       float *pr = S->model_->pr_buffer(F.g, s);
       Red R = S->red(*S->model_, 0);
+      PressureArgs PA{dptr<float4>(F.x), dptr<float4>(F.a), dptr<float>(F.rho), dptr<float>(F.s), dptr<float>(F.AA),
+                      dptr<float>(F.p), pr, dptr<float>(F.Ap), S->u(F.rho0)};
       if (sig) {
         sig_add(*sig, n);
         sig_add(*sig, N);
-        sig_add(*sig, pr);
         sig_add(*sig, R);
-        void const *ptrs[] = {F.x->d, F.a->d, F.rho->d, F.s->d, F.AA->d, F.p->d, F.Ap->d, S->u(F.rho0)};
-        sig_add(*sig, ptrs);
+        sig_add(*sig, PA);
         sig_add(*sig, first);
         sig_add(*sig, last);
+        if (SA) sig_add(*sig, *SA);
         return;
       }
       if (prof) S->model_->prof.begin("iisph_pressure", s);
-      k_iisph_pressure<NF, NB><<<red_grid(n), kNT, 0, s>>>(
-          n, dptr<float4>(F.x), dptr<float4>(F.a), dptr<float>(F.rho), dptr<float>(F.s), dptr<float>(F.AA),
-          dptr<float>(F.p), pr, dptr<float>(F.Ap), S->u(F.rho0), G, N, R, first, last, done);
+      if (SA) {
+        if (SA->ntiles) k_iisph_pressure_seg<NF, NB><<<SA->ntiles, kNT, 0, s>>>(PA, G, N, *SA);
+      } else {
+        k_iisph_pressure<NF, NB><<<red_grid(n), kNT, 0, s>>>(n, PA, G, N, R, first, last, done);
+      }
       count_launch();
       if (prof) S->model_->prof.end(s);
     }
@@ -1376,7 +1647,14 @@ public:
     k_set_i32<<<1, 1, 0, s>>>(G.nprde, int(total)); count_launch();
     PG_LAUNCH_CHECK();
   }
+  void no_segments(char const *what) {
+    for (auto &F : fluid_)
+      if (segmented(F.g))
+        throw Error(std::string(what) + " sums the density error over the whole group; on a batched (segmented) "
+                    "model use solve_pressure, which decides convergence per scene");
+  }
   void accel(Nhood &nh, cudaStream_t s) {
+    no_segments("iteration_pressure_acceleration");
     Globals G = checked_globals();
     int nf = int(fluid_.size()), nb = int(bound_.size());
     for (auto *F : active()) {
@@ -1387,6 +1665,7 @@ public:
     }
   }
   void pressure(Nhood &nh, cudaStream_t s) {
+    no_segments("iteration_pressure");
     Globals G = checked_globals();
     int nf = int(fluid_.size()), nb = int(bound_.size());
     auto act = active();
@@ -1411,6 +1690,16 @@ public:
     auto act = active();
     Red R = red(*model_, 0);
     int const *done = R.status + kStJacDone;
+    // batched model: one segmented fluid group, convergence per slot
+    bool seg = false;
+    for (auto &F : fluid_)
+      if (segmented(F.g)) seg = true;
+    SegArgs SA{};
+    if (seg) {
+      if (fluid_.size() != 1) throw Error("a batched model has exactly one fluid group");
+      SA = seg_args(fluid_[0].g);
+    }
+    SegArgs const *sa = seg ? &SA : nullptr;
     // lists and packed records are made current before the loop, so that
     // building the loop launches nothing else
     std::vector<NbrView const *> views;
@@ -1421,17 +1710,28 @@ public:
     }
     for (auto &B : bound_)
       if (B.g->count) model_->packed_xs(B.g, B.x, B.V, "xV", s);
-    k_jacobi_begin<<<1, 1, 0, s>>>(G, R); count_launch();
+    if (seg) {
+      k_seg_jacobi_begin<<<div_up(std::max<uint32_t>(SA.slots, 1), 256), 256, 0, s>>>(SA); count_launch();
+      k_set_i32<<<1, 1, 0, s>>>(R.status + kStJacDone, 0); count_launch();
+    } else {
+      k_jacobi_begin<<<1, 1, 0, s>>>(G, R); count_launch();
+    }
     PG_LAUNCH_CHECK();
     int kernels = 2 * int(act.size()) + 1;
     auto body = [&](cudaStream_t cs, cudaGraphConditionalHandle h, bool use_handle, bool prof, std::string *sig) {
       for (size_t k = 0; k < act.size(); ++k)
-        dispatch_fb<A>(nf, nb, this, *act[k], *views[k], G, cs, done, prof, sig);
+        dispatch_fb<A>(nf, nb, this, *act[k], *views[k], G, cs, done, prof, sig, sa);
       for (size_t k = 0; k < act.size(); ++k)
         dispatch_fb<P>(nf, nb, this, *act[k], *views[k], G, cs, k == 0 ? 1 : 0, k + 1 == act.size() ? 1 : 0, done,
-                       prof, sig);
+                       prof, sig, sa);
       if (sig) return;
-      k_jacobi_control<<<1, 1, 0, cs>>>(G, R, h, use_handle ? 1 : 0, use_handle ? kernels : 0); count_launch();
+      if (seg) {
+        k_seg_jacobi_control<<<1, 1024, 0, cs>>>(G, SA, h, use_handle ? 1 : 0, use_handle ? kernels : 0,
+                                                 R.status + kStJacDone);
+      } else {
+        k_jacobi_control<<<1, 1, 0, cs>>>(G, R, h, use_handle ? 1 : 0, use_handle ? kernels : 0);
+      }
+      count_launch();
     };
     if (model_->prof.enabled) {
       // host-driven: one iteration per round trip
@@ -1560,23 +1860,50 @@ public:
     auto N = bnbrs<NB>(v, s);
     Red R = red(*model_, 1);
     unsigned rg = red_grid(n), eg = div_up(n, 256);
+    // batched model: one PCG per slot
+    bool seg = segmented(F.g);
+    SegArgs SA = seg ? seg_args(F.g) : SegArgs{};
+    unsigned tg = SA.ntiles;
     k_pcg_guess<<<eg, 256, 0, s>>>(P); count_launch();
     {
       ProfScope ps(model_->prof, "pcg_init", s);
-      k_pcg_init<NB><<<rg, kNT, 0, s>>>(P, G, N, R); count_launch();
+      if (seg) {
+        k_seg_pcg_begin<<<div_up(std::max<uint32_t>(SA.slots, 1), 256), 256, 0, s>>>(SA); count_launch();
+        if (tg) k_pcg_init_seg<NB><<<tg, kNT, 0, s>>>(P, G, N, SA);
+      } else {
+        k_pcg_init<NB><<<rg, kNT, 0, s>>>(P, G, N, R);
+      }
+      count_launch();
     }
     PG_LAUNCH_CHECK();
     auto body = [&](cudaStream_t cs, cudaGraphConditionalHandle h, bool use_handle, bool prof) {
       if (prof) model_->prof.begin("pcg_q", cs);
-      k_pcg_q<NB><<<rg, kNT, 0, cs>>>(P, G, N, R); count_launch();
+      if (seg) {
+        if (tg) k_pcg_q_seg<NB><<<tg, kNT, 0, cs>>>(P, G, N, SA);
+      } else {
+        k_pcg_q<NB><<<rg, kNT, 0, cs>>>(P, G, N, R);
+      }
+      count_launch();
       if (prof) model_->prof.end(cs);
       if (prof) model_->prof.begin("pcg_update", cs);
-      k_pcg_update<<<rg, kNT, 0, cs>>>(P, R); count_launch();
+      if (seg) {
+        if (tg) k_pcg_update_seg<<<tg, kNT, 0, cs>>>(P, SA);
+      } else {
+        k_pcg_update<<<rg, kNT, 0, cs>>>(P, R);
+      }
+      count_launch();
       if (prof) model_->prof.end(cs);
       if (prof) model_->prof.begin("pcg_p", cs);
-      k_pcg_p<<<rg, kNT, 0, cs>>>(P, R); count_launch();
+      if (seg) k_pcg_p_seg<<<eg, 256, 0, cs>>>(P, SA);
+      else k_pcg_p<<<rg, kNT, 0, cs>>>(P, R);
+      count_launch();
       if (prof) model_->prof.end(cs);
-      k_pcg_control<<<1, 1, 0, cs>>>(P, R, h, use_handle ? 1 : 0, use_handle ? 4 : 0); count_launch();
+      if (seg)
+        k_seg_pcg_control<<<1, 1024, 0, cs>>>(P, SA, h, use_handle ? 1 : 0, use_handle ? 4 : 0,
+                                              R.status + kStPcgActive);
+      else
+        k_pcg_control<<<1, 1, 0, cs>>>(P, R, h, use_handle ? 1 : 0, use_handle ? 4 : 0);
+      count_launch();
     };
     if (model_->prof.enabled) {
       // host-driven (timed launches): one iteration per round trip
@@ -1595,10 +1922,13 @@ public:
       sig_add(sig, R);
       sig_add(sig, G);
       sig_add(sig, rg);
+      sig_add(sig, SA);
       loops_[F.g].run(s, sig, [&](cudaStream_t cs, cudaGraphConditionalHandle h) { body(cs, h, true, false); });
       PG_LAUNCH_CHECK();
     }
-    k_pcg_apply<<<eg, 256, 0, s>>>(P, G, R); count_launch();
+    Red RA = R;
+    if (seg) RA.status = nullptr; // per-slot iteration counts are in the segments' state
+    k_pcg_apply<<<eg, 256, 0, s>>>(P, G, RA); count_launch();
     PG_LAUNCH_CHECK();
     F.vd->version++;
     F.a->version++;

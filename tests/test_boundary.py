@@ -62,6 +62,10 @@ def test_no_cpu_fallback(gpu_lib):
     from prtcl_gb300.core import Model
     with pytest.raises(PrtclGpuError):
         Model()
+    from prtcl_gb300 import driver
+    from prtcl_gb300.batch import Batch
+    with pytest.raises(PrtclGpuError):
+        Batch(driver.DAM_BREAK_27K)
 
 
 @pytest.mark.skipif(shutil.which("g++") is None, reason="no C++ compiler")
