@@ -262,10 +262,14 @@ __device__ __forceinline__ int group_of(uint32_t const *goff, int G, uint32_t n)
 
 // pass 1: per item in group-major order, the biased grid indices and the
 // handle; OR-reductions of the bit statistics that select the key bits
-__global__ void k_cells_u(PosTable pt, GridView gv, int G, size_t N, uint32_t *ukeys, uint32_t *vals, uint32_t *stats) {
-  size_t n = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+// (grid-stride; the OR of the block is committed with one atomic per word,
+// so that the atomics on the four shared words do not serialise the pass)
+constexpr int kCellsUNT = 256;
+__global__ void __launch_bounds__(kCellsUNT) k_cells_u(PosTable pt, GridView gv, int G, size_t N, uint32_t *ukeys,
+                                                       uint32_t *vals, uint32_t *stats) {
+  __shared__ uint32_t sh[4][kCellsUNT / 32];
   uint32_t ne = 0, eq = 0, a1 = 0, a0 = 0;
-  if (n < N) {
+  for (size_t n = blockIdx.x * size_t(blockDim.x) + threadIdx.x; n < N; n += size_t(gridDim.x) * blockDim.x) {
     int g = group_of(gv.goff, G, uint32_t(n));
     uint32_t i = uint32_t(n) - gv.goff[g];
     int3 gi = x_to_gi(pt.pos[g][i], gv);
@@ -284,11 +288,18 @@ __global__ void k_cells_u(PosTable pt, GridView gv, int G, size_t N, uint32_t *u
   eq = __reduce_or_sync(kFull, eq);
   a1 = __reduce_or_sync(kFull, a1);
   a0 = __reduce_or_sync(kFull, a0);
+  int w = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0) {
-    if (ne) atomicOr(&stats[0], ne);
-    if (eq) atomicOr(&stats[1], eq);
-    if (a1) atomicOr(&stats[2], a1);
-    if (a0) atomicOr(&stats[3], a0);
+    sh[0][w] = ne;
+    sh[1][w] = eq;
+    sh[2][w] = a1;
+    sh[3][w] = a0;
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    uint32_t v = 0;
+    for (int k = 0; k < kCellsUNT / 32; ++k) v |= sh[threadIdx.x][k];
+    if (v) atomicOr(&stats[threadIdx.x], v);
   }
 }
 
@@ -309,7 +320,7 @@ __global__ void k_cell_flags(uint64_t const *keys, size_t N, uint32_t *flags) {
 // excl = exclusive scan of flags: cell(s) = excl[s] + flag[s] - 1
 __global__ void k_cells_fill(PosTable pt, GridView gv, uint64_t const *keys, uint32_t const *vals, uint32_t const *flags,
                              uint32_t const *excl, size_t N, int32_t *s2c, int32_t *r2s, int32_t *cell_start,
-                             uint64_t *cell_key, int4 *cell_gi, int *ncells) {
+                             uint64_t *cell_key, int4 *cell_gi, int *ncells, int32_t *cell_adj) {
   size_t s = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
   if (s >= N) return;
   uint32_t f = flags[s];
@@ -323,6 +334,10 @@ __global__ void k_cells_fill(PosTable pt, GridView gv, uint64_t const *keys, uin
     cell_key[c] = keys[s];
     int3 gi = x_to_gi(pt.pos[g][i], gv);
     cell_gi[c] = make_int4(gi.x, gi.y, gi.z, 0);
+    // no neighbour yet (k_cells_adj fills the slots it finds)
+    // (a cell's 26 slots start at a multiple of 104 bytes: 8-byte stores)
+    int2 *a = reinterpret_cast<int2 *>(cell_adj + size_t(c) * 26);
+    for (int k = 0; k < 13; ++k) a[k] = make_int2(-1, -1);
   }
   if (s == N - 1) {
     cell_start[c + 1] = int32_t(N);
@@ -330,16 +345,59 @@ __global__ void k_cells_fill(PosTable pt, GridView gv, uint64_t const *keys, uin
   }
 }
 
+// The cell with key kt, searched from cell c (key kc != kt) outwards: a
+// galloping search towards kt, then a binary search in the bracket found.
+// Adjacent cells are mostly near in Z-order, so the probes stay close to c.
+__device__ __forceinline__ int find_from(uint64_t const *__restrict__ keys, int C, int c, uint64_t kc, uint64_t kt) {
+  int lo, hi;
+  if (kt > kc) {
+    lo = c + 1;
+    int step = 1, probe = c + 1;
+    while (probe < C && keys[probe] < kt) {
+      lo = probe + 1;
+      step <<= 1;
+      probe = c + step;
+    }
+    hi = min(probe, C);
+  } else {
+    hi = c;
+    int step = 1, probe = c - 1;
+    while (probe >= 0 && keys[probe] > kt) {
+      hi = probe;
+      step <<= 1;
+      probe = c - step;
+    }
+    lo = max(probe, 0);
+  }
+  while (lo < hi) { // first index in [lo, hi) with key >= kt
+    int mid = (lo + hi) >> 1;
+    if (keys[mid] < kt) lo = mid + 1;
+    else hi = mid;
+  }
+  return (lo < C && keys[lo] == kt) ? lo : -1;
+}
+
+// 26-cell adjacency (util/grouped_uniform_grid.hpp:312-337): cell c searches
+// the cells at +offset[k] only and writes both mirror slots, adj[c][k] = d
+// and adj[d][25 - k] = c, so every slot is written by exactly one thread
+// (adj starts at -1)
 __global__ void k_cells_adj(GridView gv, int4 const *cell_gi, size_t N, int32_t *adj) {
   size_t c = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
-  if (c >= N || int(c) >= *gv.ncells) return;
+  int C = *gv.ncells;
+  if (c >= N || int(c) >= C) return;
   int4 g = cell_gi[c];
-  uint32_t seg = gv.seg_shift < 64 ? uint32_t(gv.cell_key[c] >> gv.seg_shift) : 0u;
+  uint64_t kc = gv.cell_key[c];
+  uint64_t sk = seg_key(gv, gv.seg_shift < 64 ? uint32_t(kc >> gv.seg_shift) : 0u);
   for (int k = 0; k < 13; ++k) {
     int3 p = make_int3(g.x + c_offsets[k][0], g.y + c_offsets[k][1], g.z + c_offsets[k][2]);
-    int3 m = make_int3(g.x - c_offsets[k][0], g.y - c_offsets[k][1], g.z - c_offsets[k][2]);
-    adj[c * 26 + k] = find_cell(gv, p, seg);
-    adj[c * 26 + 25 - k] = find_cell(gv, m, seg);
+    uint32_t u0 = unsign(p.x), u1 = unsign(p.y), u2 = unsign(p.z);
+    if (!key_valid(u0, gv.key) || !key_valid(u1, gv.key) || !key_valid(u2, gv.key)) continue;
+    uint64_t kt = make_key(u0, u1, u2, gv.key.keep) | sk;
+    int d = find_from(gv.cell_key, C, int(c), kc, kt);
+    if (d >= 0) {
+      adj[c * 26 + k] = d;
+      adj[size_t(d) * 26 + 25 - k] = int32_t(c);
+    }
   }
 }
 
@@ -670,7 +728,8 @@ void Nhood::update(cudaStream_t s) {
   unsigned nb = div_up(N, 256);
   {
     ProfScope ps(model_->prof, "grid_keys", s);
-    k_cells_u<<<nb, 256, 0, s>>>(pt, gv, G, N, ukeys_, vals_a_, stats_d_); count_launch();
+    unsigned ub = std::min<unsigned>(div_up(N, kCellsUNT), 152u * 8u);
+    k_cells_u<<<ub, kCellsUNT, 0, s>>>(pt, gv, G, N, ukeys_, vals_a_, stats_d_); count_launch();
   }
   PG_LAUNCH_CHECK();
   PG_CUDA(cudaMemcpyAsync(stats_h_, stats_d_, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -724,9 +783,9 @@ void Nhood::update(cudaStream_t s) {
   PG_LAUNCH_CHECK();
   exclusive_scan(flags_, scan_, N, block_sums_, block_sums_cap_, s);
   k_cells_fill<<<nb, 256, 0, s>>>(pt, gv, kin, vin, flags_, scan_, N, s2c_, r2s_, cell_start_, cell_key_, cell_gi_,
-                                  ncells_d_); count_launch();
+                                  ncells_d_, cell_adj_); count_launch();
   PG_LAUNCH_CHECK();
-  // 5. adjacency
+  // 5. adjacency (cells <= N; slots without a neighbour stay -1)
   k_cells_adj<<<nb, 256, 0, s>>>(gv, cell_gi_, N, cell_adj_); count_launch();
   model_->prof.end(s); // grid_cells
   PG_LAUNCH_CHECK();
