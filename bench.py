@@ -21,6 +21,14 @@ Arms:
                      procedures, f32 reductions, per-procedure neighbour
                      re-query) on all host threads, same scene and metric.
 
+Extra measurements in the same line (rank 0, one GPU; --no-extras skips them):
+  search    neighbour search only, 4M points (uniform / 64 Gaussian blobs),
+            radius for 40 mean neighbours, GB/s of algorithmic bytes vs HBM
+  batched   256 mixed-size dam-break scenes stepped together by one batch,
+            against the same scenes through the plain single-scene path
+  serving   Poisson arrivals of dam-break requests, continuous batching,
+            throughput and p50 / p99 latency
+
 Prints one JSON line (rank 0).  Inputs are larger than L2 (the 1.36M-particle
 working set is ~270 MB), so no explicit L2 flush is done between steps.
 """
@@ -49,8 +57,7 @@ UNIT = "particle-steps/s"
 # boundary item)
 ALGO_BYTES = {
     "density": (20, 16),        # x, m -> rho ; boundary x, V
-    "iisph_c": (32, 16),        # x, m, rho -> c
-    "iisph_s_aa": (56, 16),     # x, v, c, m, rho -> p, s, AA
+    "iisph_setup": (88, 32),    # x, v, m, rho -> c, p, s, AA ; boundary x, V (both passes)
     "iisph_accel": (36, 16),    # x, m, p, rho -> a
     "iisph_pressure": (52, 16),  # x, m, a, rho, s, AA, p -> Ap, p
     "wkbb18_diag": (56, 16),    # x, m, rho -> sp
@@ -240,6 +247,12 @@ def run_ours(args, rank, world, dist):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(sc, p, nf, steps=args.cpu_steps)
 
+    extras = {}
+    if rank == 0 and world == 1 and not args.no_extras:
+        extras["search"] = run_search(peak)
+        extras["batched"] = run_batched()
+        extras["serving"] = run_serving()
+
     solves = max(st["jacobi_solves"], 1.0)
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -259,6 +272,7 @@ def run_ours(args, rank, world, dist):
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": int(launches),
         "kernels": {k: {"launches": c, "ms": round(m, 3), "us_per_launch": round(1e3 * m / c, 2)}
                     for k, (c, m) in prof.items()},
+        **extras,
     }
     if rank == 0:
         print(json.dumps(line))
@@ -325,6 +339,132 @@ def cpu_baseline(sc, p, nf, steps=2, threads=0):
             "sample": f"{steps} steps of the same scene after set-up and one warm step ({secs:.1f} s)"}
 
 
+def run_search(peak, n=4_000_000, reps=5, target=40.0):
+    """Neighbour search only (4M points in the unit cube, uniform and 64
+    Gaussian blobs): grid update + the neighbour sets of every point, radius
+    calibrated on the device to a mean of `target` neighbours (self
+    included).  Algorithmic bytes per point: 32 + 4 n (positions in and
+    sorted out, permutation, one 4-byte index per neighbour, CSR offset)."""
+    import torch
+    from prtcl_gb300.core import DeviceScene
+    out = {}
+    for dist, seed in (("uniform", 1), ("blobs", 2)):
+        pts = scenes.search_points(n, dist, seed=seed)
+        d = DeviceScene()
+        d.add_group("p", "fluid")
+        d.resize("p", n)
+        d.set_varying("p", "position", pts)
+
+        def mean_nbrs(r):
+            d.set_radius(r)
+            d.update()
+            return d.nhood.query(0, count_pairs=True) / n
+
+        lo, hi = 0.2 * scenes.uniform_radius_for_mean_neighbours(n, target), \
+            scenes.uniform_radius_for_mean_neighbours(n, target)
+        while mean_nbrs(hi) < target:
+            lo, hi = hi, 2.0 * hi
+        for _ in range(14):
+            mid = 0.5 * (lo + hi)
+            if mean_nbrs(mid) < target:
+                lo = mid
+            else:
+                hi = mid
+        r = float(np.float32(hi))
+        nbar = mean_nbrs(r)
+        s = torch.cuda.ExternalStream(d.model.stream_handle())
+        for _ in range(2):
+            d.update()
+            d.nhood.query(0)
+        d.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            d.update()
+            d.nhood.query(0)
+        e1.record(s)
+        e1.synchronize()
+        sec = e0.elapsed_time(e1) / 1e3 / reps
+        algo = (32 + 4 * nbar) * n
+        out[dist] = {"points": n, "radius": r, "mean_neighbours": round(nbar, 3),
+                     "ms_per_search": round(sec * 1e3, 3), "points_per_s": round(n / sec, 1),
+                     "achieved_GBps": round(algo / sec / 1e9, 1), "frac_of_hbm_peak": round(algo / sec / 1e9 / peak, 4),
+                     "algorithmic_bytes": int(algo)}
+        del d
+    return out
+
+
+def run_batched(count=256, steps=10, warmup=3, plain_steps=5):
+    """256 dam-break scenes, fluid counts log-uniform in 2,000-200,000,
+    aspect ratios uniform in [0.5, 2], boxes 2x the fluid extent, parameters
+    of the 27k dam break: all scenes stepped together by one batch, against
+    the same scenes stepped one after another through the plain
+    single-scene path.  Wall time with a device synchronise on both sides
+    (the batch step includes its per-step host synchronisations)."""
+    from prtcl_gb300.batch import Batch
+    from prtcl_gb300.core import DeviceScene
+    p = dict(driver.DAM_BREAK_27K)
+    sc = scenes.mixed_batch(count=count)
+    nf = sum(len(x["fluid"]) for x in sc)
+    nb = sum(len(x["boundary"]) for x in sc)
+    bt = Batch(p)
+    ids = [bt.add_scene(x["fluid"], x["boundary"]) for x in sc]
+    bt.step(warmup)
+    bt.synchronize()
+    before = [bt.info(i) for i in ids]
+    t0 = time.perf_counter()
+    bt.step(steps)
+    bt.synchronize()
+    secs = time.perf_counter() - t0
+    after = [bt.info(i) for i in ids]
+    gb = bt.device_bytes() / 1e9
+    solves = sum(a["jacobi_solves"] - b["jacobi_solves"] for a, b in zip(after, before))
+    iters = sum(a["jacobi_iterations"] - b["jacobi_iterations"] for a, b in zip(after, before))
+    capped = sum(a["jacobi_capped"] - b["jacobi_capped"] for a, b in zip(after, before))
+    del bt
+    tp, work = 0.0, 0
+    for x in sc:
+        d = DeviceScene()
+        driver.setup_dam_break(d, x, p)
+        loop = driver.StepLoop(d, p, device_loop=True)
+        for _ in range(warmup):
+            loop.step(quiet=True)
+        d.synchronize()
+        t1 = time.perf_counter()
+        for _ in range(plain_steps):
+            loop.step(quiet=True)
+        d.synchronize()
+        tp += time.perf_counter() - t1
+        work += len(x["fluid"]) * plain_steps
+        del loop, d
+    v, vp = nf * steps / secs, work / tp
+    return {"workload": f"{count} dam-break scenes, fluid log-uniform 2k-200k (seed 3), IISPH dt 1e-3 s",
+            "fluid_particles": nf, "boundary_particles": nb, "steps": steps, "warmup": warmup,
+            "value": round(v, 1), "unit": UNIT, "ms_per_step": round(secs * 1e3 / steps, 3),
+            "plain_value": round(vp, 1), "plain_sample": f"{plain_steps} steps of each scene after {warmup} warm-up",
+            "batched_over_plain": round(v / vp, 2), "jacobi_iterations_mean": round(iters / max(solves, 1), 3),
+            "jacobi_capped_steps": int(capped), "device_GB": round(gb, 2)}
+
+
+def run_serving(count=48, rate=4.0):
+    """Poisson arrivals (rate/s, seed 4) of dam-break requests, fluid
+    log-uniform 5k-500k, steps uniform 100-1000, IISPH + WKBB18 viscosity;
+    continuous batching under a 120 GB device budget."""
+    from prtcl_gb300.batch import Batch
+    from prtcl_gb300.serve import Server, poisson_requests, report
+    p = dict(driver.DAM_BREAK_27K, viscosity=True)
+    reqs = poisson_requests(count, rate, seed=4)
+    for r in reqs:
+        r.scene()  # requests arrive with their particles
+    srv = Server(Batch, p, budget_bytes=120e9, keep_results=False)
+    done = srv.run(reqs)
+    rep = report(done, srv.makespan, srv.particle_steps, eta=p["eta"])
+    rep.update({"workload": f"{count} requests, Poisson {rate}/s, fluid log-uniform 5k-500k, "
+                            "steps uniform 100-1000, IISPH + WKBB18", "unit": UNIT, "batch_steps": srv.steps_run,
+                "budget_GB": 120})
+    return rep
+
+
 def run_reference(args, rank, world, dist):
     """Reference arm: the CPU restatement of the reference's OpenMP path on
     all host threads (the reference itself does not build here: Eigen,
@@ -373,6 +513,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--profile-steps", type=int, default=3)
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the neighbour-search, batched-scenes and serving measurements")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

@@ -159,6 +159,13 @@ int prtcl_gpu_nhood_update(prtcl_gpu_nhood *nhood, void *stream);
 /* Neighborhood::Permute (util/neighborhood.cpp:106-154): reorders every
  * varying field of each neighbour-capable group into cell order, then Update */
 int prtcl_gpu_nhood_permute(prtcl_gpu_nhood *nhood, prtcl_gpu_model *model, void *stream);
+/* The neighbour sets of every item of `query_group` (grouped_uniform_grid::
+ * neighbors, util/grouped_uniform_grid.hpp:407-422, for all items at once):
+ * builds the device lists the procedures read, without copying them out.
+ * No counterpart as an entry point in the reference, which queries per item
+ * inside each procedure.  *pairs_out (optional) receives the number of
+ * (item, neighbour) pairs over all neighbour groups; it synchronises. */
+int prtcl_gpu_nhood_query(prtcl_gpu_nhood *nhood, int32_t query_group, int64_t *pairs_out, void *stream);
 /* Neighborhood::CopyNeighbors (util/neighborhood.cpp:156-166): neighbours of
  * item `index` of group `group`; counts_out[g] receives the number of
  * neighbours in group g (group-count entries), indices_out the raw indices

@@ -318,6 +318,14 @@ class Neighborhood:
     def permute(self, model, stream=None):
         check(load().prtcl_gpu_nhood_permute(self._h, model._h, _stream(stream)))
 
+    def query(self, group_index, count_pairs=False, stream=None):
+        """Build the neighbour sets of every item of a group on the device;
+        with count_pairs, return the number of (item, neighbour) pairs."""
+        n = C.c_int64(0)
+        check(load().prtcl_gpu_nhood_query(self._h, int(group_index), C.byref(n) if count_pairs else None,
+                                           _stream(stream)))
+        return n.value if count_pairs else None
+
     def copy_neighbors(self, group_index, index):
         """Neighbours of (group, index): one int64 array per group."""
         G = self._model.group_count

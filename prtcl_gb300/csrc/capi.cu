@@ -368,6 +368,15 @@ int prtcl_gpu_nhood_update(prtcl_gpu_nhood *nhood, void *stream) {
     nhood->n.update(nhood->n.model()->pick(stream));
   });
 }
+int prtcl_gpu_nhood_query(prtcl_gpu_nhood *nhood, int32_t query_group, int64_t *pairs_out, void *stream) {
+  NEED(nhood);
+  return guard([&] {
+    if (!nhood->n.loaded()) throw Error("Neighborhood::Query before Load");
+    cudaStream_t s = nhood->n.model()->pick(stream);
+    if (pairs_out) *pairs_out = int64_t(nhood->n.pair_count(query_group, s));
+    else nhood->n.lists(query_group, s);
+  });
+}
 int prtcl_gpu_nhood_permute(prtcl_gpu_nhood *nhood, prtcl_gpu_model *model, void *stream) {
   NEED(nhood);
   NEED(model);

@@ -475,6 +475,7 @@ __device__ __forceinline__ void row_add(ListOut const &lo, int g, uint32_t i, Ro
   if (slot == kChunk - 1) flush_chunk(lo, g, i, k / kChunk, buf);
 }
 
+template <int NG>
 __device__ __forceinline__ void visit_cell(GridView const &gv, float4 const *__restrict__ xs, int cell, f3 xi,
                                            uint32_t i, ListOut const &lo, RowState *R, KernelParams const &K,
                                            bool with_gf, uint32_t *buf) {
@@ -488,25 +489,53 @@ __device__ __forceinline__ void visit_cell(GridView const &gv, float4 const *__r
       uint32_t g = h >> 28, j = h & 0x0FFFFFFFu;
       float f = with_gf ? kgrad_factor(K, d2) : 0.0f;
 #pragma unroll
-      for (int q = 0; q < kMaxListGroups; ++q)
+      for (int q = 0; q < NG; ++q)
         if (q == int(g)) row_add(lo, q, i, R[q], j, f, buf);
     }
   }
 }
 
+// Lower bounds, in units of the cell edge (= the radius), of the distance
+// from a point to the faces of its own cell: lo to the lower face (the cells
+// at offset -1 along the axis), hi to the upper face (offset +1).  t = x / r
+// in FP32 is within |t| 2^-22.4 of the exact quotient; where that error could
+// put the point on the other side of a face, both bounds are 0.
+// Returns false (bounds 0) unless the point lies, beyond that error, inside
+// the cell of index `gi` along the axis (the cell the grid assigned to it).
+__device__ __forceinline__ bool face_bounds(float x, float rinv, int gi, float &lo, float &hi) {
+  float t = x * rinv;
+  float f = floorf(t);
+  float d = t - f;
+  float err = fabsf(t) * 4.8e-7f + 1e-6f;
+  lo = 0.0f;
+  hi = 0.0f;
+  if (!(fminf(d, 1.0f - d) > 2.0f * err) || !(fabsf(f) < 2.0e9f) || int(f) != gi) return false;
+  lo = fmaxf(d - err, 0.0f);
+  hi = fmaxf((1.0f - d) - err, 0.0f);
+  return true;
+}
+
 // neighbour lists of one query group (grid query of util/grouped_uniform_grid.hpp:407-531)
+// `order` (optional): thread t builds the row of item order[t] (the group's
+// items in grid order), so that the threads of a warp walk nearby cells.
+// Adjacent cells whose box is farther than the radius from the query (with a
+// margin of 1e-4 of the radius, far above the rounding of the exact test)
+// cannot hold a neighbour and are not scanned; the lists are unchanged.
+template <int NG>
 __global__ void __launch_bounds__(kBuildNT) k_build_lists(GridView gv, float4 const *__restrict__ xs,
                                                           float4 const *__restrict__ qpos, int q, ListOut lo,
-                                                          float const *hp, float *hcache) {
+                                                          float const *hp, float *hcache,
+                                                          uint32_t const *__restrict__ order) {
   extern __shared__ uint32_t buf[];
-  uint32_t i = blockIdx.x * kBuildNT + threadIdx.x;
+  uint32_t t = blockIdx.x * kBuildNT + threadIdx.x;
   bool with_gf = hp != nullptr;
   KernelParams K = kparams(with_gf ? *hp : 1.0f);
-  if (i == 0) *hcache = with_gf ? K.h : __int_as_float(0x7fc00000);
-  if (i >= lo.n) return;
-  RowState R[kMaxListGroups];
+  if (t == 0) *hcache = with_gf ? K.h : __int_as_float(0x7fc00000);
+  if (t >= lo.n) return;
+  uint32_t i = order ? order[t] : t;
+  RowState R[NG];
 #pragma unroll
-  for (int g = 0; g < kMaxListGroups; ++g) R[g] = RowState{0u, 0u, false};
+  for (int g = 0; g < NG; ++g) R[g] = RowState{0u, 0u, false};
   float4 x4 = qpos[i];
   f3 xi = mk3(x4);
   int cell = -1;
@@ -520,19 +549,39 @@ __global__ void __launch_bounds__(kBuildNT) k_build_lists(GridView gv, float4 co
     fallback = cell < 0;
   }
   if (!fallback) {
-    visit_cell(gv, xs, cell, xi, i, lo, R, K, with_gf, buf);
-    for (int k = 0; k < 26; ++k) visit_cell(gv, xs, gv.cell_adj[size_t(cell) * 26 + k], xi, i, lo, R, K, with_gf, buf);
+    float lo3[3], hi3[3];
+    int4 cg = gv.cell_gi[cell];
+    bool inside = face_bounds(x4.x, gv.rinv, cg.x, lo3[0], hi3[0]);
+    inside = face_bounds(x4.y, gv.rinv, cg.y, lo3[1], hi3[1]) && inside;
+    inside = face_bounds(x4.z, gv.rinv, cg.z, lo3[2], hi3[2]) && inside;
+    if (!inside)
+      for (int a = 0; a < 3; ++a) lo3[a] = hi3[a] = 0.0f;
+    visit_cell<NG>(gv, xs, cell, xi, i, lo, R, K, with_gf, buf);
+    for (int k = 0; k < 26; ++k) {
+      // slot k < 13: +offset[k]; slot 25 - k: -offset[k]
+      int kk = k < 13 ? k : 25 - k;
+      int sg = k < 13 ? 1 : -1;
+      float lb = 0.0f;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        int o = sg * c_offsets[kk][a];
+        float b = o > 0 ? hi3[a] : (o < 0 ? lo3[a] : 0.0f);
+        lb += b * b;
+      }
+      if (lb > 1.0001f) continue;
+      visit_cell<NG>(gv, xs, gv.cell_adj[size_t(cell) * 26 + k], xi, i, lo, R, K, with_gf, buf);
+    }
   } else {
     uint32_t sq = item_seg(gv, q, i);
     for (int k = 0; k < 13; ++k) {
       int3 p = make_int3(gi.x + c_offsets[k][0], gi.y + c_offsets[k][1], gi.z + c_offsets[k][2]);
-      visit_cell(gv, xs, find_cell(gv, p, sq), xi, i, lo, R, K, with_gf, buf);
+      visit_cell<NG>(gv, xs, find_cell(gv, p, sq), xi, i, lo, R, K, with_gf, buf);
       int3 m = make_int3(gi.x - c_offsets[k][0], gi.y - c_offsets[k][1], gi.z - c_offsets[k][2]);
-      visit_cell(gv, xs, find_cell(gv, m, sq), xi, i, lo, R, K, with_gf, buf);
+      visit_cell<NG>(gv, xs, find_cell(gv, m, sq), xi, i, lo, R, K, with_gf, buf);
     }
   }
 #pragma unroll
-  for (int g = 0; g < kMaxListGroups; ++g) {
+  for (int g = 0; g < NG; ++g) {
     if (g >= lo.G) break;
     uint32_t n = R[g].c;
     lo.cb[size_t(g) * lo.n + i] = make_uint2(n | (R[g].wide ? kWide : 0u), R[g].j0);
@@ -548,6 +597,21 @@ __global__ void __launch_bounds__(kBuildNT) k_build_lists(GridView gv, float4 co
       flush_chunk(lo, g, i, n / kChunk, buf);
     }
   }
+}
+
+template <int NG>
+void launch_build_lists(size_t n, size_t smem, cudaStream_t s, GridView const &gv, float4 const *xs,
+                        float4 const *qpos, int q, ListOut const &lo, float const *h, float *hcache,
+                        uint32_t const *order) {
+  PG_CUDA(cudaFuncSetAttribute(k_build_lists<NG>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  k_build_lists<NG><<<div_up(n, kBuildNT), kBuildNT, smem, s>>>(gv, xs, qpos, q, lo, h, hcache, order);
+}
+
+__global__ void k_pair_count(uint2 const *cb, size_t n, unsigned long long *total) {
+  size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  unsigned long long c = (i < n) ? (cb[i].x & ~kWide) : 0u;
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(kFull, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(total, c);
 }
 
 __global__ void k_group_flags(uint32_t const *vals, size_t N, uint32_t g, uint32_t *flags) {
@@ -602,7 +666,7 @@ static void free_all(std::initializer_list<void *> ps) {
 Nhood::~Nhood() {
   for (auto &kv : lists_) free_lists(kv.second);
   free_all({keys_a_, keys_b_, vals_a_, vals_b_, ukeys_, flags_, scan_, r2s_, s2c_, cell_start_, cell_adj_, cell_key_,
-            cell_gi_, xsorted_, hist_, block_sums_, stats_d_, ncells_d_});
+            cell_gi_, xsorted_, hist_, block_sums_, stats_d_, ncells_d_, order_});
   cudaFreeHost(stats_h_);
 }
 
@@ -642,6 +706,7 @@ void Nhood::load(Model &m) {
   gg_ = ng;
   if (!same) {
     has_grid_ = false;
+    for (auto &c : permuted_count_) c = 0;
     for (auto &kv : lists_) free_lists(kv.second);
     lists_.clear();
   }
@@ -677,6 +742,7 @@ GridView Nhood::view() const {
   v.cell_start = cell_start_;
   v.cell_key = cell_key_;
   v.cell_adj = cell_adj_;
+  v.cell_gi = cell_gi_;
   v.ncells = ncells_d_;
   for (int g = 0; g <= kMaxGroups; ++g) v.goff[g] = goff_[g];
   for (int g = 0; g < kMaxGroups; ++g) v.in_grid[g] = in_grid_[g];
@@ -812,6 +878,21 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
     k_xsorted<<<div_up(N_, 256), 256, 0, s>>>(pt, sorted_vals_, N_, xsorted_); count_launch();
     PG_LAUNCH_CHECK();
   }
+  // a group that is not in cell order (never permuted, or resized since) is
+  // walked in grid order
+  uint32_t const *order = nullptr;
+  if (in_grid_[q] && n > 0 && permuted_count_[q] != n) {
+    if (n > order_cap_) {
+      if (order_) PG_CUDA(cudaFree(order_));
+      order_cap_ = n + n / 8;
+      PG_CUDA(cudaMalloc(&order_, order_cap_ * 4));
+    }
+    k_group_flags<<<div_up(N_, 256), 256, 0, s>>>(sorted_vals_, N_, uint32_t(q), flags_); count_launch();
+    exclusive_scan(flags_, scan_, N_, block_sums_, block_sums_cap_, s);
+    k_group_perm<<<div_up(N_, 256), 256, 0, s>>>(sorted_vals_, flags_, scan_, N_, order_); count_launch();
+    PG_LAUNCH_CHECK();
+    order = order_;
+  }
   auto alloc_slots = [&](int g, uint32_t want) {
     if (L.idx32[g]) PG_CUDA(cudaFree(L.idx32[g]));
     if (L.chunks[g]) PG_CUDA(cudaFree(L.chunks[g]));
@@ -842,7 +923,6 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
       lo.cap[g] = L.cap[g];
     }
     size_t smem = size_t(G) * 24 * kBuildNT * 4;
-    PG_CUDA(cudaFuncSetAttribute(k_build_lists, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     lo.cb = L.cb;
     lo.maxcnt = stats_d_ + 8;
     lo.n = uint32_t(n);
@@ -852,7 +932,14 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
     float4 const *qpos = static_cast<float4 const *>(gg_[q].pos->d);
     {
       ProfScope ps(model_->prof, "nhood_lists", s);
-      k_build_lists<<<div_up(n, kBuildNT), kBuildNT, smem, s>>>(gv, xsorted_, qpos, q, lo, h, L.hcache); count_launch();
+      switch (G) {
+      case 1: launch_build_lists<1>(n, smem, s, gv, xsorted_, qpos, q, lo, h, L.hcache, order); break;
+      case 2: launch_build_lists<2>(n, smem, s, gv, xsorted_, qpos, q, lo, h, L.hcache, order); break;
+      case 3: launch_build_lists<3>(n, smem, s, gv, xsorted_, qpos, q, lo, h, L.hcache, order); break;
+      case 4: launch_build_lists<4>(n, smem, s, gv, xsorted_, qpos, q, lo, h, L.hcache, order); break;
+      default: launch_build_lists<kMaxListGroups>(n, smem, s, gv, xsorted_, qpos, q, lo, h, L.hcache, order);
+      }
+      count_launch();
     }
     PG_LAUNCH_CHECK();
     PG_CUDA(cudaMemcpyAsync(stats_h_ + 8, stats_d_ + 8, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -928,6 +1015,7 @@ void Nhood::permute(Model &m, cudaStream_t s) {
     PG_LAUNCH_CHECK();
     gg_[g].g->permute(perm, s);
     PG_CUDA(cudaFreeAsync(perm, s));
+    permuted_count_[g] = n;
   }
   update(s);
 }
@@ -951,6 +1039,7 @@ void Nhood::permute_segments(Model &m, uint8_t const *due_d, cudaStream_t s) {
     PG_LAUNCH_CHECK();
     gg_[g].g->permute(perm, s);
     PG_CUDA(cudaFreeAsync(perm, s));
+    permuted_count_[g] = n;
   }
   update(s);
 }
@@ -963,6 +1052,24 @@ void Nhood::set_segments(std::vector<uint16_t const *> const &seg, uint32_t coun
   seg_bits_ = 0;
   while (count > 1 && (uint32_t(1) << seg_bits_) < count) ++seg_bits_;
   has_grid_ = false;
+}
+
+uint64_t Nhood::pair_count(int q, cudaStream_t s) {
+  NbrView const &v = lists(q, s);
+  unsigned long long *d = nullptr;
+  PG_CUDA(cudaMallocAsync(&d, sizeof *d, s));
+  PG_CUDA(cudaMemsetAsync(d, 0, sizeof *d, s));
+  for (size_t g = 0; g < gg_.size(); ++g)
+    if (v.n && v.cb[g]) {
+      k_pair_count<<<div_up(v.n, 256), 256, 0, s>>>(v.cb[g], v.n, d);
+      count_launch();
+    }
+  PG_LAUNCH_CHECK();
+  unsigned long long h = 0;
+  PG_CUDA(cudaMemcpyAsync(&h, d, sizeof h, cudaMemcpyDeviceToHost, s));
+  PG_CUDA(cudaFreeAsync(d, s));
+  PG_CUDA(cudaStreamSynchronize(s));
+  return uint64_t(h);
 }
 
 size_t Nhood::device_bytes() const {

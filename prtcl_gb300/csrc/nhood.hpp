@@ -95,6 +95,7 @@ struct GridView {
   int32_t const *cell_start; // cell -> first sorted (C + 1 entries)
   uint64_t const *cell_key; // cell -> compressed key
   int32_t const *cell_adj;  // cell -> 26 adjacent cells (-1 none)
+  int4 const *cell_gi;      // cell -> grid index
   int const *ncells;        // number of cells (device)
   uint32_t goff[kMaxGroups + 1];
   int in_grid[kMaxGroups];
@@ -146,6 +147,8 @@ public:
   void copy_grid(uint32_t *sorted, int32_t *cell_gi, int32_t *cell_range, int32_t *cell_adj, cudaStream_t s);
   // neighbours of one item, per group, like Neighborhood::CopyNeighbors
   size_t copy_neighbors(int g, size_t i, int64_t *counts, int64_t *out, size_t cap, cudaStream_t s);
+  // total neighbour count of the lists of query group q (synchronises)
+  uint64_t pair_count(int q, cudaStream_t s);
   // CSR copy of the lists of query group q to neighbour group ng
   void copy_lists(int q, int ng, int64_t *offsets, uint32_t *idx, size_t cap, cudaStream_t s);
 
@@ -187,6 +190,11 @@ private:
   uint32_t goff_[kMaxGroups + 1] = {};
   int in_grid_[kMaxGroups] = {};
   KeyInfo key_{};
+  // item count of each group when it was last permuted into cell order (the
+  // list build walks a group that was not in grid order instead)
+  size_t permuted_count_[kMaxGroups] = {};
+  uint32_t *order_ = nullptr; // group items in grid order (list build)
+  size_t order_cap_ = 0;
   std::vector<uint16_t const *> seg_;
   uint32_t seg_count_ = 0;
   int seg_bits_ = 0;

@@ -32,6 +32,10 @@ __device__ unsigned long long g_loop_kernels = 0;
 namespace {
 
 constexpr int kNT = 128;            // threads per block for particle kernels
+// resident blocks per SM the neighbour sweeps are compiled for (caps their
+// registers at 64): the sweeps wait on gathers, and more resident warps hide
+// more of that latency
+constexpr int kMinBlocks = 8;
 constexpr int kMaxRedBlocks = 4096; // block partials per reduced value
 
 // model scratch layout
@@ -244,7 +248,7 @@ __device__ bool seg_commit(double const (&v)[NV], SegArgs const &S, uint32_t slo
 // ---------------------------------------------------------------------------
 
 template <int NF, int NB>
-__global__ void __launch_bounds__(kNT) k_density(uint32_t n, float4 const *__restrict__ x, float *__restrict__ rho,
+__global__ void __launch_bounds__(kNT, kMinBlocks) k_density(uint32_t n, float4 const *__restrict__ x, float *__restrict__ rho,
                                                  float const *rho0p, Globals G, Nbrs<NF, NB> N) {
   uint32_t i = grid_tid();
   if (i >= n) return;
@@ -273,7 +277,7 @@ __global__ void __launch_bounds__(kNT) k_density(uint32_t n, float4 const *__res
 
 // aiast12.compute_volume (schemes/aiast12.hpp:125-175): V_i = 1 / sum_b W
 template <int NB>
-__global__ void __launch_bounds__(kNT) k_volume(uint32_t n, float4 const *__restrict__ x, float *__restrict__ V,
+__global__ void __launch_bounds__(kNT, kMinBlocks) k_volume(uint32_t n, float4 const *__restrict__ x, float *__restrict__ V,
                                                 Globals G, Nbrs<0, NB> N) {
   uint32_t i = grid_tid();
   if (i >= n) return;
@@ -341,19 +345,29 @@ __global__ void k_max_speed_begin(Globals G, unsigned *maxord) { *maxord = f2ord
 __global__ void k_max_speed_end(Globals G, unsigned const *maxord) { *G.max_speed = ord2f(*maxord); }
 
 // ---------------------------------------------------------------------------
-// iisph.setup pass 1 (schemes/iisph.hpp:197-249)
-//   c_i = -sum_f (m_j / rho_i^2) gradW - sum_b ((0.7*2) rho0 (V_j / rho_i^2)) gradW
+// iisph.setup (schemes/iisph.hpp:188-354)
+//   pass 1: c_i = -sum_f (m_j / rho_i^2) gradW - sum_b ((0.7*2) rho0 (V_j / rho_i^2)) gradW
+//   pass 2: p = 0, source term s and diagonal element AA; also p / rho^2
+//           (= 0) for the pressure acceleration
 // ---------------------------------------------------------------------------
 
+// Passes 1 and 2 in one sweep: pass 2 reads only the item's own c, so each
+// thread computes c over its neighbours, stores it, then walks the same (now
+// cached) neighbour rows again for s and AA, with the operations of the
+// generated passes.
 template <int NF, int NB>
-__global__ void __launch_bounds__(kNT) k_iisph_c(uint32_t n, float4 const *__restrict__ x, float const *__restrict__ rho,
-                                                 float4 *__restrict__ cout, float const *rho0p, Globals G,
-                                                 Nbrs<NF, NB> N) {
+__global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_setup(uint32_t n, float4 const *__restrict__ x,
+                                                                 float4 const *__restrict__ v,
+                                                                 float4 *__restrict__ cout, float const *__restrict__ m,
+                                                                 float const *__restrict__ rho, float *__restrict__ p,
+                                                                 float *__restrict__ pr, float *__restrict__ s,
+                                                                 float *__restrict__ AA, float const *rho0p, Globals G,
+                                                                 Nbrs<NF, NB> N) {
   uint32_t i = grid_tid();
   if (i >= n) return;
   KernelParams K = kparams(*G.h);
   bool uc = use_cache(N, K);
-  float rho0 = *rho0p;
+  float rho0 = *rho0p, dt = *G.dt;
   f3 xi = mk3(x[i]);
   float ri = rho[i];
   f3 c = {0.0f, 0.0f, 0.0f};
@@ -374,24 +388,8 @@ __global__ void __launch_bounds__(kNT) k_iisph_c(uint32_t n, float4 const *__res
     });
   }
   cout[i] = make_float4(c.x, c.y, c.z, 0.0f);
-}
-
-// iisph.setup pass 2 (schemes/iisph.hpp:254-354): p = 0, source term s and
-// diagonal element AA; also p / rho^2 (= 0) for the pressure acceleration
-template <int NF, int NB>
-__global__ void __launch_bounds__(kNT) k_iisph_s_aa(uint32_t n, float4 const *__restrict__ x, float4 const *__restrict__ v,
-                                                    float4 const *__restrict__ cf, float const *__restrict__ m,
-                                                    float const *__restrict__ rho, float *__restrict__ p,
-                                                    float *__restrict__ pr, float *__restrict__ s,
-                                                    float *__restrict__ AA, float const *rho0p, Globals G,
-                                                    Nbrs<NF, NB> N) {
-  uint32_t i = grid_tid();
-  if (i >= n) return;
-  KernelParams K = kparams(*G.h);
-  bool uc = use_cache(N, K);
-  float rho0 = *rho0p, dt = *G.dt;
-  f3 xi = mk3(x[i]), vi = mk3(v[i]), ci = mk3(cf[i]);
-  float mi = m[i], ri = rho[i];
+  f3 vi = mk3(v[i]), ci = c;
+  float mi = m[i];
   float sa = 0.0f, aa = 0.0f;
 #pragma unroll
   for (int q = 0; q < NF; ++q) {
@@ -430,7 +428,7 @@ __global__ void k_set_i32(int *p, int v) { *p = v; }
 // Batched models: `segid` / `segstat` skip the items of slots whose loop has
 // ended.
 template <int NF, int NB>
-__global__ void __launch_bounds__(kNT) k_iisph_accel(uint32_t n, float4 const *__restrict__ x, float const *__restrict__ p,
+__global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_accel(uint32_t n, float4 const *__restrict__ x, float const *__restrict__ p,
                                                      float const *__restrict__ rho, float4 *__restrict__ a,
                                                      float const *rho0p, Globals G, Nbrs<NF, NB> N,
                                                      int const *done, uint16_t const *segid, int const *segstat) {
@@ -516,7 +514,7 @@ __device__ __forceinline__ double iisph_pressure_item(uint32_t i, PressureArgs c
 }
 
 template <int NF, int NB>
-__global__ void __launch_bounds__(kNT) k_iisph_pressure(uint32_t n, PressureArgs A, Globals G, Nbrs<NF, NB> N, Red R,
+__global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_pressure(uint32_t n, PressureArgs A, Globals G, Nbrs<NF, NB> N, Red R,
                                                         int first, int last_group, int const *done) {
   if (done && *(volatile int const *)done) return;
   KernelParams K = kparams(*G.h);
@@ -537,7 +535,7 @@ __global__ void __launch_bounds__(kNT) k_iisph_pressure(uint32_t n, PressureArgs
 // iteration_pressure over the tiles of a batched model: the density error of
 // each slot's iteration goes to scal[slot][kSsAprde]
 template <int NF, int NB>
-__global__ void __launch_bounds__(kNT) k_iisph_pressure_seg(PressureArgs A, Globals G, Nbrs<NF, NB> N, SegArgs S) {
+__global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_pressure_seg(PressureArgs A, Globals G, Nbrs<NF, NB> N, SegArgs S) {
   uint4 T = S.tiles[blockIdx.x];
   uint32_t slot = T.x;
   if (S.stat[slot * kSegStat + kStJacDone]) return; // the whole block: one slot
@@ -661,7 +659,7 @@ __device__ __forceinline__ M3 minv3(M3 const &A) {
 // runs over the particle's own group (`foreach _ neighbor`); xmr holds
 // (x, m / rho).
 template <int NB>
-__global__ void __launch_bounds__(kNT) k_wkbb18_diag(uint32_t n, uint32_t cap, float4 const *__restrict__ xmr,
+__global__ void __launch_bounds__(kNT, kMinBlocks) k_wkbb18_diag(uint32_t n, uint32_t cap, float4 const *__restrict__ xmr,
                                                      float const *__restrict__ rho, float *__restrict__ sp,
                                                      float const *rho0p, float const *mup, Globals G, NbrList self,
                                                      Nbrs<0, NB> N) {
@@ -862,7 +860,7 @@ __device__ __forceinline__ void pcg_update_scalars(double *sc, int *st, double r
 }
 
 template <int NB>
-__global__ void __launch_bounds__(kNT) k_pcg_init(PcgArgs P, Globals G, Nbrs<0, NB> N, Red R) {
+__global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_init(PcgArgs P, Globals G, Nbrs<0, NB> N, Red R) {
   KernelParams K = kparams(*G.h);
   bool uc = use_cache(N, K);
   float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
@@ -875,7 +873,7 @@ __global__ void __launch_bounds__(kNT) k_pcg_init(PcgArgs P, Globals G, Nbrs<0, 
 
 // q = A p; p.q; alpha or break (solver/cg_openmp.hpp:121-151)
 template <int NB>
-__global__ void __launch_bounds__(kNT) k_pcg_q(PcgArgs P, Globals G, Nbrs<0, NB> N, Red R) {
+__global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_q(PcgArgs P, Globals G, Nbrs<0, NB> N, Red R) {
   if (!*(volatile int *)&R.status[kStPcgActive]) return;
   KernelParams K = kparams(*G.h);
   bool uc = use_cache(N, K);
@@ -888,7 +886,7 @@ __global__ void __launch_bounds__(kNT) k_pcg_q(PcgArgs P, Globals G, Nbrs<0, NB>
 
 // x += alpha p; r += alpha q; y = M r; r.r; r.y; break / beta
 // (solver/cg_openmp.hpp:153-191)
-__global__ void __launch_bounds__(kNT) k_pcg_update(PcgArgs P, Red R) {
+__global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_update(PcgArgs P, Red R) {
   if (!*(volatile int *)&R.status[kStPcgActive]) return;
   float alpha = float(R.scalars[kSPcg + 6]);
   double rr = 0.0, ry = 0.0;
@@ -925,7 +923,7 @@ __global__ void k_pcg_control(PcgArgs P, Red R, cudaGraphConditionalHandle h, in
 // --- the PCG loop over the tiles of a batched model, per slot -------------
 
 template <int NB>
-__global__ void __launch_bounds__(kNT) k_pcg_init_seg(PcgArgs P, Globals G, Nbrs<0, NB> N, SegArgs S) {
+__global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_init_seg(PcgArgs P, Globals G, Nbrs<0, NB> N, SegArgs S) {
   uint4 T = S.tiles[blockIdx.x];
   uint32_t slot = T.x;
   KernelParams K = kparams(*G.h);
@@ -943,7 +941,7 @@ __global__ void __launch_bounds__(kNT) k_pcg_init_seg(PcgArgs P, Globals G, Nbrs
 }
 
 template <int NB>
-__global__ void __launch_bounds__(kNT) k_pcg_q_seg(PcgArgs P, Globals G, Nbrs<0, NB> N, SegArgs S) {
+__global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_q_seg(PcgArgs P, Globals G, Nbrs<0, NB> N, SegArgs S) {
   uint4 T = S.tiles[blockIdx.x];
   uint32_t slot = T.x;
   if (!S.stat[slot * kSegStat + kStPcgActive]) return;
@@ -956,7 +954,7 @@ __global__ void __launch_bounds__(kNT) k_pcg_q_seg(PcgArgs P, Globals G, Nbrs<0,
     pcg_q_scalars(S.scal + slot * kSegScal, S.stat + slot * kSegStat, out[0], *P.tol);
 }
 
-__global__ void __launch_bounds__(kNT) k_pcg_update_seg(PcgArgs P, SegArgs S) {
+__global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_update_seg(PcgArgs P, SegArgs S) {
   uint4 T = S.tiles[blockIdx.x];
   uint32_t slot = T.x;
   if (!S.stat[slot * kSegStat + kStPcgActive]) return;
@@ -1524,25 +1522,16 @@ public:
     bind(m);
     loop_.reset();
   }
-  template <int NF, int NB> struct C {
-    static void go(Iisph *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
-      uint32_t n = uint32_t(F.g->count);
-      auto N = S->nbrs<NF, NB>(v, s);
-      ProfScope ps(S->model_->prof, "iisph_c", s);
-      k_iisph_c<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(F.x), dptr<float>(F.rho), dptr<float4>(F.c),
-                                                        S->u(F.rho0), G, N);
-      count_launch();
-    }
-  };
-  template <int NF, int NB> struct SAA {
+  template <int NF, int NB> struct SETUP {
     static void go(Iisph *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
       uint32_t n = uint32_t(F.g->count);
       auto N = S->nbrs<NF, NB>(v, s);
       float *pr = S->model_->pr_buffer(F.g, s);
-      ProfScope ps(S->model_->prof, "iisph_s_aa", s);
-      k_iisph_s_aa<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(F.x), dptr<float4>(F.v), dptr<float4>(F.c),
-                                                           dptr<float>(F.m), dptr<float>(F.rho), dptr<float>(F.p), pr,
-                                                           dptr<float>(F.s), dptr<float>(F.AA), S->u(F.rho0), G, N);
+      ProfScope ps(S->model_->prof, "iisph_setup", s);
+      k_iisph_setup<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(F.x), dptr<float4>(F.v), dptr<float4>(F.c),
+                                                            dptr<float>(F.m), dptr<float>(F.rho), dptr<float>(F.p),
+                                                            pr, dptr<float>(F.s), dptr<float>(F.AA), S->u(F.rho0), G,
+                                                            N);
       count_launch();
     }
   };
@@ -1629,16 +1618,13 @@ public:
   void setup(Nhood &nh, cudaStream_t s) {
     Globals G = checked_globals();
     int nf = int(fluid_.size()), nb = int(bound_.size());
-    for (auto *F : active()) {
-      dispatch_fb<C>(nf, nb, this, *F, lists(nh, F->g, G, s), G, s);
-      PG_LAUNCH_CHECK();
-      F->c->version++;
-    }
+    // one fused sweep per group (pass 2 of a group reads only its own c)
     long long total = 0;
     for (auto *F : active()) {
       total += (long long)F->g->count;
-      dispatch_fb<SAA>(nf, nb, this, *F, lists(nh, F->g, G, s), G, s);
+      dispatch_fb<SETUP>(nf, nb, this, *F, lists(nh, F->g, G, s), G, s);
       PG_LAUNCH_CHECK();
+      F->c->version++;
       F->s->version++;
       F->AA->version++;
       wrote_pressure(*F);

@@ -46,6 +46,8 @@ def test_random_points(oracle_mod, dist):
     groups = [("p", "fluid", pts, [])]
     d, o = make(oracle_mod, groups, r)
     compare(d, o, groups)
+    offs, _ = o.neighbor_lists(0, 0, n)
+    assert d.nhood.query(0, count_pairs=True) == int(offs[-1])
 
 
 def test_negative_coordinates_and_exact_radius(oracle_mod):
