@@ -141,7 +141,8 @@ def dist_setup(n):
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        if torch.cuda.is_available():
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
         return rank, world, dist
     return 0, 1, None
