@@ -59,8 +59,10 @@ struct NbrList {
 // of 16 entries is fetched with six 16-byte streaming loads (evict-first:
 // the lists are read once per sweep, the gathered particle records should
 // stay in L2), so that its 16 gathers can be in flight together.
+// (keep_l2: plain L2-cached loads instead, for a row that is walked again
+// right after)
 template <class F>
-__device__ __forceinline__ void for_each_nbr(NbrList const &L, uint32_t i, bool with_gf, F &&f) {
+__device__ __forceinline__ void for_each_nbr(NbrList const &L, uint32_t i, bool with_gf, F &&f, bool keep_l2 = false) {
   uint2 cb = __ldg(L.cb + i);
   uint32_t c = min(cb.x & ~kWide, L.cap);
   bool wide = (cb.x & kWide) != 0;
@@ -81,7 +83,7 @@ __device__ __forceinline__ void for_each_nbr(NbrList const &L, uint32_t i, bool 
     } else {
 #pragma unroll
       for (int v = 0; v < 2; ++v) {
-        uint4 a = __ldcs(ch + v);
+        uint4 a = keep_l2 ? __ldcg(ch + v) : __ldcs(ch + v);
         uint32_t w[4] = {a.x, a.y, a.z, a.w};
 #pragma unroll
         for (int t = 0; t < 4; ++t) {
@@ -95,7 +97,7 @@ __device__ __forceinline__ void for_each_nbr(NbrList const &L, uint32_t i, bool 
     if (with_gf) {
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
-        uint4 a = __ldcs(ch + 2 + v);
+        uint4 a = keep_l2 ? __ldcg(ch + 2 + v) : __ldcs(ch + 2 + v);
         g[4 * v] = __uint_as_float(a.x);
         g[4 * v + 1] = __uint_as_float(a.y);
         g[4 * v + 2] = __uint_as_float(a.z);
@@ -377,7 +379,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_setup(uint32_t n, flo
     for_each_nbr(F.L, i, uc, [&](uint32_t j_, float gf_) {
       float4 xm = __ldg(F.xm + j_);
       c = sub3(c, scl3(xm.w / (ri * ri), pgrad(uc, gf_, K, sub3(xi, mk3(xm)))));
-    });
+    }, true);
   }
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
@@ -385,7 +387,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_setup(uint32_t n, flo
     for_each_nbr(B.L, i, uc, [&](uint32_t j_, float gf_) {
       float4 xv = __ldg(B.xV + j_);
       c = sub3(c, scl3(((0.7f * 2.0f) * rho0) * (xv.w / (ri * ri)), pgrad(uc, gf_, K, sub3(xi, mk3(xv)))));
-    });
+    }, true);
   }
   cout[i] = make_float4(c.x, c.y, c.z, 0.0f);
   f3 vi = mk3(v[i]), ci = c;
