@@ -63,6 +63,9 @@ int prtcl_gpu_group_resize(prtcl_gpu_model *model, const char *group, int64_t co
 int prtcl_gpu_group_count(prtcl_gpu_model *model, const char *group, int64_t *count_out);
 int prtcl_gpu_group_index(prtcl_gpu_model *model, const char *group, int32_t *index_out);
 int prtcl_gpu_model_group_count(prtcl_gpu_model *model, int32_t *count_out);
+/* Model::GetGroups: the group names in index order, '\n'-separated (written
+ * to `buf` as prtcl_gpu_scheme_full_name does). */
+int prtcl_gpu_model_group_names(prtcl_gpu_model *model, char *buf, int64_t size, int64_t *needed_out);
 
 /* VaryingManager::AddFieldImpl (data/varying_manager.hpp:33-46): adds a
  * field (or checks the type of an existing one).  rank 0..2, extents[rank]. */
@@ -121,6 +124,14 @@ int prtcl_gpu_global_set_async(prtcl_gpu_model *model, const char *field, const 
  * iterations, [6] PCG solves stopped by the iteration limit.  Waits for the
  * model's stream; `reset` != 0 zeroes them afterwards. */
 int prtcl_gpu_model_stats(prtcl_gpu_model *model, double *out, int32_t n, int32_t reset);
+
+/* Model::Save / Model::Load (data/model.cpp:54-75) in the reference's native
+ * binary archive format (util/archive.cpp:5-40): global fields, then per
+ * group its name, type, tags, varying fields and uniform fields.  Load adds
+ * the groups and fields it finds (resizing the groups to the archive's item
+ * counts) and uploads the values; f32 and s32 components only.  Synchronous. */
+int prtcl_gpu_model_save(prtcl_gpu_model *model, const char *path);
+int prtcl_gpu_model_load(prtcl_gpu_model *model, const char *path);
 
 /* Types of uniform and global fields (ctype_out >= 4 bytes, extents_out[2]). */
 int prtcl_gpu_uniform_info(prtcl_gpu_model *model, const char *group, const char *field, char *ctype_out,

@@ -87,6 +87,9 @@ SIGNATURES = {
     "prtcl_gpu_scheme_source": [vp, C.c_char_p, i64, i64p],
     "prtcl_gpu_registry_scheme_names": [C.c_char_p, i64, i64p],
     "prtcl_gpu_nhood_query": [vp, i32, i64p, vp],
+    "prtcl_gpu_model_group_names": [vp, C.c_char_p, i64, i64p],
+    "prtcl_gpu_model_save": [vp, cp],
+    "prtcl_gpu_model_load": [vp, cp],
     "prtcl_gpu_batch_create": [vp, pp],
     "prtcl_gpu_batch_destroy": [vp],
     "prtcl_gpu_batch_add_scene": [vp, vp, i64, vp, i64, i64p],

@@ -247,6 +247,20 @@ class Model:
     def group_count(self):
         return len(self._groups)
 
+    def save(self, path):
+        """Model::Save in the reference's native binary archive format."""
+        check(load().prtcl_gpu_model_save(self._h, b(str(path))))
+
+    def load(self, path):
+        """Model::Load from a native binary archive (adds groups and fields)."""
+        check(load().prtcl_gpu_model_load(self._h, b(str(path))))
+        for name in read_str(load().prtcl_gpu_model_group_names, self._h).splitlines():
+            self._groups.setdefault(name, Group(self, name))
+        self._dirty = True
+
+    Save = save
+    Load = load
+
     def synchronize(self, stream=None):
         check(load().prtcl_gpu_model_synchronize(self._h, _stream(stream)))
 

@@ -322,6 +322,22 @@ int prtcl_gpu_model_synchronize(prtcl_gpu_model *model, void *stream) {
   });
 }
 
+int prtcl_gpu_model_group_names(prtcl_gpu_model *model, char *buf, int64_t size, int64_t *needed_out) {
+  NEED(model);
+  std::vector<std::string> names;
+  for (Group *g : model->m.groups_by_index()) names.push_back(g->name);
+  return write_str(join(names), buf, size, needed_out);
+}
+int prtcl_gpu_model_save(prtcl_gpu_model *model, const char *path) {
+  NEED(model);
+  NEED(path);
+  return guard([&] { save_model(model->m, path, model->m.stream()); });
+}
+int prtcl_gpu_model_load(prtcl_gpu_model *model, const char *path) {
+  NEED(model);
+  NEED(path);
+  return guard([&] { load_model(model->m, path, model->m.stream()); });
+}
 int prtcl_gpu_profile_enable(prtcl_gpu_model *model, int32_t enable) {
   NEED(model);
   return guard([&] { model->m.prof.enabled = enable != 0; });

@@ -144,6 +144,7 @@ public:
 
   SmallField &add_global(std::string const &name, FieldType const &t);
   SmallField *find_global(std::string const &name);
+  std::map<std::string, SmallField> const &globals() const { return global_; }
 
   // arena access
   SmallField &alloc_small(SmallField &f, FieldType const &t);
@@ -216,6 +217,9 @@ void upload_varying(VaryingField &f, size_t count, void const *host, size_t n_it
 void upload_varying_noalloc(VaryingField &f, size_t count, void const *host, size_t n_items, cudaStream_t s);
 size_t noalloc_stage_bytes();
 void download_varying(VaryingField const &f, size_t count, void *host, size_t n_items, cudaStream_t s);
+// the model in the reference's native binary archive format (archive.cu)
+void save_model(Model &m, std::string const &path, cudaStream_t s);
+void load_model(Model &m, std::string const &path, cudaStream_t s);
 // items [offset, offset + n) of a field, in the host layout (stream-ordered;
 // the download synchronises)
 void upload_varying_range(VaryingField &f, size_t offset, void const *host, size_t n, cudaStream_t s);

@@ -99,3 +99,53 @@ def test_device_grid_cell_order_matches_reference(name):
     point_scene(d, groups, r)
     d.update()
     assert_bitwise(d.nhood.grid()["cell_gi"], gi, f"{name} cell order")
+
+
+def test_archive_fixture_is_consistent():
+    """model_small.bin (the reference's native format, read back by the
+    reference's own reader when it was made) against its values."""
+    import struct
+    data = open(os.path.join(GOLDEN, "model_small.bin"), "rb").read()
+    exp = dict(np.load(os.path.join(GOLDEN, "model_small.npz")))
+    pos = [0]
+
+    def size():
+        v = struct.unpack_from("<Q", data, pos[0])[0]
+        pos[0] += 8
+        return v
+
+    def string():
+        n = size()
+        s = data[pos[0]:pos[0] + n].decode()
+        pos[0] += n
+        return s
+
+    def ttype():
+        ct = string()
+        shape = [size() for _ in range(size())]
+        return {"f32": np.float32, "s32": np.int32}[ct], shape
+
+    def values(dt, n):
+        a = np.frombuffer(data, dt, n, pos[0])
+        pos[0] += a.nbytes
+        return a
+
+    for _ in range(size()):
+        name = string()
+        dt, shape = ttype()
+        np.testing.assert_array_equal(values(dt, int(np.prod(shape))), np.ravel(exp["global/" + name]))
+    for _ in range(size()):
+        g, _type = string(), string()
+        [string() for _ in range(size())]
+        count = size()
+        for _ in range(size()):
+            name = string()
+            dt, shape = ttype()
+            assert size() == count
+            v = values(dt, count * int(np.prod(shape)))
+            np.testing.assert_array_equal(v, np.ravel(exp[f"{g}/varying/{name}"]))
+        for _ in range(size()):
+            name = string()
+            dt, shape = ttype()
+            np.testing.assert_array_equal(values(dt, int(np.prod(shape))), np.ravel(exp[f"{g}/uniform/{name}"]))
+    assert pos[0] == len(data)
