@@ -133,6 +133,11 @@ int prtcl_gpu_model_stats(prtcl_gpu_model *model, double *out, int32_t n, int32_
 int prtcl_gpu_model_save(prtcl_gpu_model *model, const char *path);
 int prtcl_gpu_model_load(prtcl_gpu_model *model, const char *path);
 
+/* SaveVTK (util/save_vtk.cpp:57-128): one group as a legacy ASCII VTK
+ * polydata file (points from "position"; velocity, acceleration, mass,
+ * volume, density, pressure, time_of_birth ... where present).  Synchronous. */
+int prtcl_gpu_group_save_vtk(prtcl_gpu_model *model, const char *group, const char *path);
+
 /* Types of uniform and global fields (ctype_out >= 4 bytes, extents_out[2]). */
 int prtcl_gpu_uniform_info(prtcl_gpu_model *model, const char *group, const char *field, char *ctype_out,
                            int32_t *rank_out, int32_t *extents_out);

@@ -560,6 +560,54 @@ template <class T> struct Scene : SceneBase {
     });
   }
 
+  // viscosity.accumulate_acceleration (share/schemes/viscosity.prtcl:31-66,
+  // generated schemes/viscosity.hpp:171-240): explicit viscosity added to a,
+  // over the neighbours of every fluid group, then of every boundary group
+  // (boundary velocity zero)
+  void viscosity_accumulate_acceleration() {
+    for (auto *g : of_type("fluid")) {
+      for (auto n : {"position", "velocity", "acceleration"}) g->vf(n, 3);
+      for (auto n : {"density", "mass"}) g->vf(n, 1);
+    }
+    for (auto *g : of_type("boundary")) { g->vf("position", 3); g->vf("volume", 1); }
+    auto fl = of_type("fluid"), bd = of_type("boundary");
+    Kernel<T> K(gr("smoothing_scale"));
+    T h = K.h;
+    foreach_with_neighbors(fl, [&](Group<T> *p, size_t i, auto &nb) {
+      auto *x = p->v3("position");
+      auto *v = p->v3("velocity");
+      auto *a = p->v3("acceleration");
+      T *rho = p->s1("density");
+      T rho0 = ur(*p, "rest_density"), mu = ur(*p, "dynamic_viscosity");
+      V3<T> ai = a[i];
+      for (auto *n : fl) {
+        auto *nx = n->v3("position");
+        auto *nv = n->v3("velocity");
+        T *nm = n->s1("mass");
+        T *nrho = n->s1("density");
+        for (size_t j : nb[gidx(n)]) {
+          V3<T> xij = vsub(x[i], nx[j]);
+          T coef = (((T(10) * (mu / rho[i])) * (nm[j] / nrho[j])) * vdot(vsub(v[i], nv[j]), xij)) /
+                   (vnsq(xij) + ((T(0.01) * h) * h));
+          ai = vadd(ai, vscale(coef, K.gradW(xij)));
+        }
+      }
+      for (auto *n : bd) {
+        auto *nx = n->v3("position");
+        T *nV = n->s1("volume");
+        T nmu = ur(*n, "dynamic_viscosity");
+        for (size_t j : nb[gidx(n)]) {
+          V3<T> xij = vsub(x[i], nx[j]);
+          V3<T> zero{T(0), T(0), T(0)};
+          T coef = (((T(10) * (nmu / rho[i])) * ((rho0 * nV[j]) / rho[i])) * vdot(vsub(v[i], zero), xij)) /
+                   (vnsq(xij) + ((T(0.01) * h) * h));
+          ai = vadd(ai, vscale(coef, K.gradW(xij)));
+        }
+      }
+      a[i] = ai;
+    });
+  }
+
   // dot over a vector of 3-vectors: per item a0*b0 + (a1*b1 + a2*b2) in T,
   // accumulated in T (reference mode) or sequentially in double (FP64 mode)
   double cg_dot(std::vector<V3<T>> const &a, std::vector<V3<T>> const &b) const {
@@ -722,6 +770,7 @@ template <class T> struct Scene : SceneBase {
     if (scheme == "iisph" && proc == "iteration_pressure") return iisph_iteration_pressure();
     if (scheme == "iisph" && proc == "solve_pressure") return iisph_solve_pressure();
     if (scheme == "wkbb18" && proc == "compute_diagonal") return wkbb18_compute_diagonal();
+    if (scheme == "viscosity" && proc == "accumulate_acceleration") return viscosity_accumulate_acceleration();
     if (scheme == "wkbb18" && proc == "accumulate_acceleration") return wkbb18_accumulate_acceleration();
     throw std::runtime_error("procedure does not exist: " + scheme + "." + proc);
   }

@@ -89,6 +89,7 @@ SIGNATURES = {
     "prtcl_gpu_nhood_query": [vp, i32, i64p, vp],
     "prtcl_gpu_model_group_names": [vp, C.c_char_p, i64, i64p],
     "prtcl_gpu_model_save": [vp, cp],
+    "prtcl_gpu_group_save_vtk": [vp, cp, cp],
     "prtcl_gpu_model_load": [vp, cp],
     "prtcl_gpu_batch_create": [vp, pp],
     "prtcl_gpu_batch_destroy": [vp],

@@ -192,6 +192,10 @@ class Group:
         check(load().prtcl_gpu_group_resize(self._m._h, b(self.name), int(n)))
         self._m._dirty = True
 
+    def save_vtk(self, path):
+        """SaveVTK: the group as a legacy ASCII VTK polydata file."""
+        check(load().prtcl_gpu_group_save_vtk(self._m._h, b(self.name), b(str(path))))
+
     AddTag = add_tag
     Resize = resize
     GetItemCount = lambda self: self.item_count  # noqa: E731

@@ -328,6 +328,12 @@ int prtcl_gpu_model_group_names(prtcl_gpu_model *model, char *buf, int64_t size,
   for (Group *g : model->m.groups_by_index()) names.push_back(g->name);
   return write_str(join(names), buf, size, needed_out);
 }
+int prtcl_gpu_group_save_vtk(prtcl_gpu_model *model, const char *group, const char *path) {
+  NEED(model);
+  NEED(group);
+  NEED(path);
+  return guard([&] { save_vtk(model->m.group(group), path, model->m.stream()); });
+}
 int prtcl_gpu_model_save(prtcl_gpu_model *model, const char *path) {
   NEED(model);
   NEED(path);

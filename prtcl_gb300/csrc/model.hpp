@@ -220,6 +220,8 @@ void download_varying(VaryingField const &f, size_t count, void *host, size_t n_
 // the model in the reference's native binary archive format (archive.cu)
 void save_model(Model &m, std::string const &path, cudaStream_t s);
 void load_model(Model &m, std::string const &path, cudaStream_t s);
+// a group as a legacy ASCII VTK file, the reference's SaveVTK format (vtk.cu)
+void save_vtk(Group &g, std::string const &path, cudaStream_t s);
 // items [offset, offset + n) of a field, in the host layout (stream-ordered;
 // the download synchronises)
 void upload_varying_range(VaryingField &f, size_t offset, void const *host, size_t n, cudaStream_t s);

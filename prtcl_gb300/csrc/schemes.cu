@@ -36,6 +36,10 @@ constexpr int kNT = 128;            // threads per block for particle kernels
 // registers at 64): the sweeps wait on gathers, and more resident warps hide
 // more of that latency
 constexpr int kMinBlocks = 8;
+// neighbour entries a sweep thread holds at a time (16 or 8; measured on
+// the 1M dam break: 16 for every sweep but the IISPH setup, whose two walks
+// over a row run faster with 8)
+constexpr uint32_t kNbrBatchDefault = 16;
 constexpr int kMaxRedBlocks = 4096; // block partials per reduced value
 
 // model scratch layout
@@ -61,19 +65,22 @@ struct NbrList {
 // stay in L2), so that its 16 gathers can be in flight together.
 // (keep_l2: plain L2-cached loads instead, for a row that is walked again
 // right after)
-template <class F>
+template <uint32_t kNbrBatch = kNbrBatchDefault, class F>
 __device__ __forceinline__ void for_each_nbr(NbrList const &L, uint32_t i, bool with_gf, F &&f, bool keep_l2 = false) {
   uint2 cb = __ldg(L.cb + i);
   uint32_t c = min(cb.x & ~kWide, L.cap);
   bool wide = (cb.x & kWide) != 0;
   unsigned char const *row = L.chunks + size_t(i) * (L.cap / kChunk) * kChunkBytes;
-  for (uint32_t kb = 0; kb < c; kb += kChunk) {
+  // entries are taken kNbrBatch at a time (16: a whole chunk; 8: half a
+  // chunk, fewer registers held per thread)
+  for (uint32_t kb = 0; kb < c; kb += kNbrBatch) {
+    uint32_t h = (kb % kChunk) / kNbrBatch; // batch within the chunk
     uint4 const *ch = reinterpret_cast<uint4 const *>(row + size_t(kb / kChunk) * kChunkBytes);
-    uint32_t j[kChunk];
+    uint32_t j[kNbrBatch];
     if (wide) {
       uint4 const *w32 = reinterpret_cast<uint4 const *>(L.idx32 + size_t(i) * L.cap + kb);
 #pragma unroll
-      for (int v = 0; v < 4; ++v) {
+      for (int v = 0; v < int(kNbrBatch / 4); ++v) {
         uint4 a = __ldcs(w32 + v);
         j[4 * v] = a.x;
         j[4 * v + 1] = a.y;
@@ -82,8 +89,8 @@ __device__ __forceinline__ void for_each_nbr(NbrList const &L, uint32_t i, bool 
       }
     } else {
 #pragma unroll
-      for (int v = 0; v < 2; ++v) {
-        uint4 a = keep_l2 ? __ldcg(ch + v) : __ldcs(ch + v);
+      for (int v = 0; v < int(kNbrBatch / 8); ++v) {
+        uint4 a = keep_l2 ? __ldcg(ch + h * (kNbrBatch / 8) + v) : __ldcs(ch + h * (kNbrBatch / 8) + v);
         uint32_t w[4] = {a.x, a.y, a.z, a.w};
 #pragma unroll
         for (int t = 0; t < 4; ++t) {
@@ -93,11 +100,12 @@ __device__ __forceinline__ void for_each_nbr(NbrList const &L, uint32_t i, bool 
         }
       }
     }
-    float g[kChunk];
+    float g[kNbrBatch];
     if (with_gf) {
 #pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        uint4 a = keep_l2 ? __ldcg(ch + 2 + v) : __ldcs(ch + 2 + v);
+      for (int v = 0; v < int(kNbrBatch / 4); ++v) {
+        uint4 const *gp = ch + 2 + h * (kNbrBatch / 4) + v;
+        uint4 a = keep_l2 ? __ldcg(gp) : __ldcs(gp);
         g[4 * v] = __uint_as_float(a.x);
         g[4 * v + 1] = __uint_as_float(a.y);
         g[4 * v + 2] = __uint_as_float(a.z);
@@ -105,10 +113,10 @@ __device__ __forceinline__ void for_each_nbr(NbrList const &L, uint32_t i, bool 
       }
     } else {
 #pragma unroll
-      for (int t = 0; t < int(kChunk); ++t) g[t] = 0.0f;
+      for (int t = 0; t < int(kNbrBatch); ++t) g[t] = 0.0f;
     }
 #pragma unroll
-    for (int t = 0; t < int(kChunk); ++t)
+    for (int t = 0; t < int(kNbrBatch); ++t)
       if (kb + t < c) f(j[t], g[t]);
   }
 }
@@ -376,7 +384,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_setup(uint32_t n, flo
 #pragma unroll
   for (int q = 0; q < NF; ++q) {
     FluidN const &F = N.f[q];
-    for_each_nbr(F.L, i, uc, [&](uint32_t j_, float gf_) {
+    for_each_nbr<8>(F.L, i, uc, [&](uint32_t j_, float gf_) {
       float4 xm = __ldg(F.xm + j_);
       c = sub3(c, scl3(xm.w / (ri * ri), pgrad(uc, gf_, K, sub3(xi, mk3(xm)))));
     }, true);
@@ -384,7 +392,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_setup(uint32_t n, flo
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
-    for_each_nbr(B.L, i, uc, [&](uint32_t j_, float gf_) {
+    for_each_nbr<8>(B.L, i, uc, [&](uint32_t j_, float gf_) {
       float4 xv = __ldg(B.xV + j_);
       c = sub3(c, scl3(((0.7f * 2.0f) * rho0) * (xv.w / (ri * ri)), pgrad(uc, gf_, K, sub3(xi, mk3(xv)))));
     }, true);
@@ -396,7 +404,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_setup(uint32_t n, flo
 #pragma unroll
   for (int q = 0; q < NF; ++q) {
     FluidN const &F = N.f[q];
-    for_each_nbr(F.L, i, uc, [&](uint32_t j_, float gf_) {
+    for_each_nbr<8>(F.L, i, uc, [&](uint32_t j_, float gf_) {
       uint32_t j = j_;
       float4 xm = __ldg(F.xm + j);
       f3 g = pgrad(uc, gf_, K, sub3(xi, mk3(xm)));
@@ -409,7 +417,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_setup(uint32_t n, flo
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
-    for_each_nbr(B.L, i, uc, [&](uint32_t j_, float gf_) {
+    for_each_nbr<8>(B.L, i, uc, [&](uint32_t j_, float gf_) {
       float4 xv = __ldg(B.xV + j_);
       f3 g = pgrad(uc, gf_, K, sub3(xi, mk3(xv)));
       float w = rho0 * xv.w;
@@ -624,6 +632,56 @@ __global__ void k_jacobi_control(Globals G, Red R, cudaGraphConditionalHandle h,
     }
   }
   if (use_handle) cudaGraphSetConditional(h, done ? 0u : 1u);
+}
+
+// ---------------------------------------------------------------------------
+// viscosity.accumulate_acceleration (share/schemes/viscosity.prtcl:31-66,
+// generated schemes/viscosity.hpp:171-240): explicit viscosity added to a.
+//   a_i += ((10 (mu_i / rho_i)) (m_j / rho_j) (v_i - v_j).x_ij / (|x_ij|^2 + 0.01 h^2)) gradW
+//   a_i += ((10 (mu_b / rho_i)) (rho0 V_b / rho_i) v_i.x_ib / (|x_ib|^2 + 0.01 h^2)) gradW
+// over the neighbours of every fluid group, then of every boundary group.
+// The fluid records are (x, m / rho) (the packed xmr records: m_j / rho_j is
+// the generated code's division).
+// ---------------------------------------------------------------------------
+
+template <int NF, int NB>
+__global__ void __launch_bounds__(kNT, kMinBlocks) k_viscosity(uint32_t n, float4 const *__restrict__ x,
+                                                               float4 const *__restrict__ v,
+                                                               float const *__restrict__ rho, float4 *__restrict__ a,
+                                                               float const *rho0p, float const *mup, Globals G,
+                                                               Nbrs<NF, NB> N) {
+  uint32_t i = grid_tid();
+  if (i >= n) return;
+  KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
+  float h = K.h, rho0 = *rho0p, mu = *mup;
+  float hh = (0.01f * h) * h;
+  f3 xi = mk3(x[i]), vi = mk3(v[i]);
+  float ri = rho[i];
+  f3 ai = mk3(a[i]);
+#pragma unroll
+  for (int q = 0; q < NF; ++q) {
+    FluidN const &F = N.f[q];
+    for_each_nbr(F.L, i, uc, [&](uint32_t j_, float gf_) {
+      float4 xr = __ldg(F.xm + j_);
+      f3 xij = sub3(xi, mk3(xr));
+      float coef = (((10.0f * (mu / ri)) * xr.w) * dot3(sub3(vi, mk3(__ldg(F.v + j_))), xij)) / (nsq3(xij) + hh);
+      ai = add3(ai, scl3(coef, pgrad(uc, gf_, K, xij)));
+    });
+  }
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    BoundN const &B = N.b[q];
+    float bmu = *B.mu;
+    for_each_nbr(B.L, i, uc, [&](uint32_t j_, float gf_) {
+      float4 xv = __ldg(B.xV + j_);
+      f3 xij = sub3(xi, mk3(xv));
+      float coef = (((10.0f * (bmu / ri)) * ((rho0 * xv.w) / ri)) * dot3(sub3(vi, f3{0.0f, 0.0f, 0.0f}), xij)) /
+                   (nsq3(xij) + hh);
+      ai = add3(ai, scl3(coef, pgrad(uc, gf_, K, xij)));
+    });
+  }
+  a[i] = make_float4(ai.x, ai.y, ai.z, 0.0f);
 }
 
 // ---------------------------------------------------------------------------
@@ -1959,6 +2017,68 @@ private:
   }
 };
 
+// ---------------------------------------------------------------------------
+// viscosity (explicit)
+// ---------------------------------------------------------------------------
+
+class Viscosity : public SchemeCommon {
+public:
+  Viscosity() {
+    reg("accumulate_acceleration", [this](Nhood &nh, cudaStream_t s) { accumulate(nh, s); });
+  }
+  std::string name() const override { return "viscosity"; }
+  std::string source() const override {
+    return "procedure accumulate_acceleration: a_f += 10 (mu_f / rho_f) (m_f' / rho_f') (v_f - v_f').x_ff' / "
+           "(|x_ff'|^2 + 0.01 h^2) gradW + boundary term with v_b = 0";
+  }
+  void load(Model &m) override {
+    m.add_global("smoothing_scale", ft_real());
+    collect(m, true, true);
+    for (auto &F : fluid_) {
+      F.rho0 = &F.g->add_uniform("rest_density", ft_real());
+      F.mu = &F.g->add_uniform("dynamic_viscosity", ft_real());
+      F.x = &F.g->add_varying("position", ft_vec3());
+      F.v = &F.g->add_varying("velocity", ft_vec3());
+      F.a = &F.g->add_varying("acceleration", ft_vec3());
+      F.rho = &F.g->add_varying("density", ft_real());
+      F.m = &F.g->add_varying("mass", ft_real());
+    }
+    for (auto &B : bound_) {
+      B.mu = &B.g->add_uniform("dynamic_viscosity", ft_real());
+      B.x = &B.g->add_varying("position", ft_vec3());
+      B.V = &B.g->add_varying("volume", ft_real());
+    }
+    bind(m);
+  }
+  template <int NF, int NB> struct L {
+    static void go(Viscosity *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
+      uint32_t n = uint32_t(F.g->count);
+      auto N = S->nbrs<NF, NB>(v, s);
+      // fluid neighbour records (x, m / rho)
+      for (int q = 0; q < NF; ++q) {
+        FluidG &Q = S->fluid_[q];
+        N.f[q].xm = S->model_->packed_xmr(Q.g, Q.x, Q.m, Q.rho, s);
+      }
+      ProfScope ps(S->model_->prof, "viscosity", s);
+      k_viscosity<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(F.x), dptr<float4>(F.v), dptr<float>(F.rho),
+                                                          dptr<float4>(F.a), S->u(F.rho0), S->u(F.mu), G, N);
+      count_launch();
+    }
+  };
+  void accumulate(Nhood &nh, cudaStream_t s) {
+    Globals G = globals(*model_);
+    need({{G.h, "smoothing_scale"}});
+    // every group's sums read the accelerations of no neighbour: groups in turn
+    for (auto &F : fluid_) {
+      if (!F.g->count) continue;
+      NbrView const &v = lists(nh, F.g, G, s);
+      dispatch_fb<L>(int(fluid_.size()), int(bound_.size()), this, F, v, G, s);
+      PG_LAUNCH_CHECK();
+      F.a->version++;
+    }
+  }
+};
+
 using Factory = std::unique_ptr<Scheme> (*)();
 
 template <class S> std::unique_ptr<Scheme> make() { return std::unique_ptr<Scheme>(new S()); }
@@ -1973,6 +2093,7 @@ std::map<std::string, Factory> const &registry() {
     add(&make<Iisph>);
     add(&make<SymplecticEuler>);
     add(&make<Wkbb18>);
+    add(&make<Viscosity>);
     return m;
   }();
   return r;

@@ -74,6 +74,13 @@ def test_step_procedures_bitwise(pair):
         m.run("symplectic_euler", "integrate_position")
     assert_bitwise(fld(d, "f", "position", 3), fld(o, "f", "position", 3), "position")
     assert d.get_global("maximum_speed") == np.float32(o.get_global("maximum_speed"))
+    # explicit viscosity (viscosity.accumulate_acceleration) on top of gravity
+    for m in (d, o):
+        m.update()
+        m.run("density", "compute_density")
+        m.run("gravity", "initialize_acceleration")
+        m.run("viscosity", "accumulate_acceleration")
+    assert_bitwise(fld(d, "f", "acceleration", 3), fld(o, "f", "acceleration", 3), "explicit viscosity")
 
 
 def test_unknown_procedure_and_scheme(pair):
