@@ -522,12 +522,17 @@ template <class T> struct Scene : SceneBase {
     for (auto *g : of_type("boundary")) { g->vf("position", 3); g->vf("volume", 1); }
   }
 
-  void wkbb18_compute_diagonal() {
+  // gc: wkbb18_gc (share/schemes/wkbb18_gc.prtcl), every kernel gradient
+  // premultiplied by the item's gradient correction L_i
+  void wkbb18_compute_diagonal(bool gc = false) {
     wkbb18_fields();
     auto fl = of_type("fluid"), bd = of_type("boundary");
+    if (gc)
+      for (auto *g : fl) g->vf("gradient_correction", 9);
     Kernel<T> K(gr("smoothing_scale"));
     T h = K.h, dt = gr("time_step");
     foreach_with_neighbors(fl, [&](Group<T> *p, size_t i, auto &nb) {
+      auto grad = [&](V3<T> const &xij) { return gc ? mvmul(p->m3("gradient_correction")[i], K.gradW(xij)) : K.gradW(xij); };
       auto *x = p->v3("position");
       T *m = p->s1("mass");
       T *rho = p->s1("density");
@@ -541,7 +546,7 @@ template <class T> struct Scene : SceneBase {
       for (size_t j : nb[gidx(p)]) {
         V3<T> xij = vsub(x[i], x[j]);
         T coef = ((T(10) * (mu / rho[i])) * (m[j] / rho[j])) / (vnsq(xij) + ((T(0.01) * h) * h));
-        acc_outer(coef, K.gradW(xij), xij);
+        acc_outer(coef, grad(xij), xij);
       }
       for (auto *n : bd) {
         auto *nx = n->v3("position");
@@ -550,13 +555,54 @@ template <class T> struct Scene : SceneBase {
         for (size_t j : nb[gidx(n)]) {
           V3<T> xij = vsub(x[i], nx[j]);
           T coef = ((T(10) * (nmu / rho[i])) * ((rho0 * nV[j]) / rho[i])) / (vnsq(xij) + ((T(0.01) * h) * h));
-          acc_outer(coef, K.gradW(xij), xij);
+          acc_outer(coef, grad(xij), xij);
         }
       }
       M3<T> A;
       for (int c = 0; c < 3; ++c)
         for (int r = 0; r < 3; ++r) A[3 * c + r] = (r == c ? T(1) : T(0)) - dt * S[3 * c + r];
       p->m3("wkbb18_system_diagonal")[i] = minv(A);
+    });
+  }
+
+  // correction.identity_gradient_correction / compute_gradient_correction
+  // (share/schemes/correction.prtcl:14-43, schemes/correction.hpp:134-230):
+  //   L_f = invert_pm(sum_{fluid neighbours} (m_j / rho_i) gradW(x_ij) (x_j - x_i)^T)
+  void correction_identity() {
+    for (auto *g : of_type("fluid")) {
+      g->vf("gradient_correction", 9);
+      auto *L = g->m3("gradient_correction");
+      for (size_t i = 0; i < g->count; ++i) {
+        L[i].fill(T(0));
+        L[i][0] = L[i][4] = L[i][8] = T(1);
+      }
+    }
+  }
+  void correction_compute() {
+    auto fl = of_type("fluid");
+    for (auto *g : fl) {
+      g->vf("position", 3);
+      for (auto n : {"density", "mass"}) g->vf(n, 1);
+      g->vf("gradient_correction", 9);
+    }
+    Kernel<T> K(gr("smoothing_scale"));
+    foreach_with_neighbors(fl, [&](Group<T> *p, size_t i, auto &nb) {
+      auto *x = p->v3("position");
+      T *rho = p->s1("density");
+      M3<T> Lf;
+      Lf.fill(T(0));
+      for (auto *n : fl) {
+        auto *nx = n->v3("position");
+        T *nm = n->s1("mass");
+        for (size_t j : nb[gidx(n)]) {
+          V3<T> g = K.gradW(vsub(x[i], nx[j]));
+          V3<T> d = vsub(nx[j], x[i]);
+          T sc = nm[j] / rho[i];
+          for (int c = 0; c < 3; ++c)
+            for (int r = 0; r < 3; ++r) Lf[3 * c + r] = Lf[3 * c + r] + sc * (g[r] * d[c]);
+        }
+      }
+      p->m3("gradient_correction")[i] = pinv3(Lf);
     });
   }
 
@@ -623,9 +669,11 @@ template <class T> struct Scene : SceneBase {
     return double(acc);
   }
 
-  void wkbb18_accumulate_acceleration() {
+  void wkbb18_accumulate_acceleration(bool gc = false) {
     wkbb18_fields();
     auto fl = of_type("fluid"), bd = of_type("boundary");
+    if (gc)
+      for (auto *g : fl) g->vf("gradient_correction", 9);
     Kernel<T> K(gr("smoothing_scale"));
     T h = K.h, dt = gr("time_step"), t = gr("current_time"), fade = gr("fade_duration");
     size_t Gn = groups.size();
@@ -643,6 +691,7 @@ template <class T> struct Scene : SceneBase {
       T tol = ur(*p, "wkbb18_maximum_error");
       int64_t max_k = int64_t(p->uf("wkbb18_maximum_iterations", 1)[0]);
       auto *sp = p->m3("wkbb18_system_diagonal");
+      M3<T> const *Lc = gc ? p->m3("gradient_correction") : nullptr;
       size_t pi = gidx(p);
       std::vector<V3<T>> X(n), Y(n), Rr(n), P(n), Q(n), B(n);
       // system product: into = with - dt * a_f(with)  (wkbb18.hpp:339-396)
@@ -659,7 +708,7 @@ template <class T> struct Scene : SceneBase {
               V3<T> xij = vsub(x[i], x[j]);
               T coef = (((T(10) * (mu / rho[i])) * (m[j] / rho[j])) * vdot(vsub(with[i], with[j]), xij)) /
                        (vnsq(xij) + ((T(0.01) * h) * h));
-              af = vadd(af, vscale(coef, K.gradW(xij)));
+              af = vadd(af, vscale(coef, Lc ? mvmul(Lc[i], K.gradW(xij)) : K.gradW(xij)));
             }
             for (auto *nn : bd) {
               auto *nx = nn->v3("position");
@@ -669,7 +718,7 @@ template <class T> struct Scene : SceneBase {
                 V3<T> xij = vsub(x[i], nx[j]);
                 T coef = (((T(10) * (nmu / rho[i])) * ((rho0 * nV[j]) / rho[i])) * vdot(with[i], xij)) /
                          (vnsq(xij) + ((T(0.01) * h) * h));
-                af = vadd(af, vscale(coef, K.gradW(xij)));
+                af = vadd(af, vscale(coef, Lc ? mvmul(Lc[i], K.gradW(xij)) : K.gradW(xij)));
               }
             }
             into[i] = vsub(with[i], vscale(dt, af));
@@ -771,6 +820,10 @@ template <class T> struct Scene : SceneBase {
     if (scheme == "iisph" && proc == "solve_pressure") return iisph_solve_pressure();
     if (scheme == "wkbb18" && proc == "compute_diagonal") return wkbb18_compute_diagonal();
     if (scheme == "viscosity" && proc == "accumulate_acceleration") return viscosity_accumulate_acceleration();
+    if (scheme == "wkbb18_gc" && proc == "compute_diagonal") return wkbb18_compute_diagonal(true);
+    if (scheme == "wkbb18_gc" && proc == "accumulate_acceleration") return wkbb18_accumulate_acceleration(true);
+    if (scheme == "correction" && proc == "identity_gradient_correction") return correction_identity();
+    if (scheme == "correction" && proc == "compute_gradient_correction") return correction_compute();
     if (scheme == "wkbb18" && proc == "accumulate_acceleration") return wkbb18_accumulate_acceleration();
     throw std::runtime_error("procedure does not exist: " + scheme + "." + proc);
   }
@@ -815,6 +868,15 @@ void oracle_morton_compare_many(int32_t const *a, int32_t const *b, int64_t n, i
   for (int64_t i = 0; i < n; ++i) {
     oracle::GI l{a[3 * i], a[3 * i + 1], a[3 * i + 2]}, r{b[3 * i], b[3 * i + 1], b[3 * i + 2]};
     out[i] = int8_t(oracle::morton_compare(l, r));
+  }
+}
+// pseudo-inverses of n column-major 3x3 matrices (f32), for tests
+void oracle_pinv3_many(float const *a, int64_t n, float *out) {
+  for (int64_t k = 0; k < n; ++k) {
+    oracle::M3<float> m;
+    for (int e = 0; e < 9; ++e) m[e] = a[9 * k + e];
+    oracle::M3<float> r = oracle::pinv3(m);
+    for (int e = 0; e < 9; ++e) out[9 * k + e] = r[e];
   }
 }
 int oracle_set_threads(int n) {

@@ -102,6 +102,58 @@ template <class T> inline V3<T> mvmul(M3<T> const &m, V3<T> const &v) {
 }
 
 // unit_step_l (math/impl/eigen.hpp:307-314): 1 if eps < x else 0
+// Moore-Penrose pseudo-inverse of a 3x3 matrix (column-major m[3 c + r]):
+// one-sided Jacobi SVD (Hestenes) with a fixed 8 sweeps over the column pairs
+// (0,1), (0,2), (1,2); A V = W with orthogonal columns w_i = sigma_i u_i, so
+// A+ = sum_i v_i w_i^T / sigma_i^2 over the sigma_i > 3 eps sigma_max (the
+// rank threshold of a complete orthogonal decomposition of a 3x3 matrix).
+// Stands in for the reference's invert_pm (math/impl/eigen.hpp:266-276,
+// Eigen's completeOrthogonalDecomposition().pseudoInverse()); agrees with it
+// to rounding where the rank is clear.
+template <class T> inline T dot3r(T const *a, T const *b) { return a[0] * b[0] + (a[1] * b[1] + a[2] * b[2]); }
+template <class T> inline M3<T> pinv3(M3<T> const &A) {
+  T w[3][3], v[3][3];
+  for (int c = 0; c < 3; ++c)
+    for (int r = 0; r < 3; ++r) {
+      w[c][r] = A[3 * c + r];
+      v[c][r] = (r == c) ? T(1) : T(0);
+    }
+  static constexpr int pairs[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+  for (int sweep = 0; sweep < 8; ++sweep)
+    for (auto const &pq : pairs) {
+      int p = pq[0], q = pq[1];
+      T alpha = dot3r(w[p], w[p]), beta = dot3r(w[q], w[q]), gamma = dot3r(w[p], w[q]);
+      if (gamma == T(0)) continue;
+      T zeta = (beta - alpha) / (T(2) * gamma);
+      T t = std::copysign(T(1), zeta) / (std::fabs(zeta) + std::sqrt(T(1) + zeta * zeta));
+      T c = T(1) / std::sqrt(T(1) + t * t);
+      T s = c * t;
+      for (int r = 0; r < 3; ++r) {
+        T wp = w[p][r], wq = w[q][r];
+        w[p][r] = c * wp - s * wq;
+        w[q][r] = s * wp + c * wq;
+        T vp = v[p][r], vq = v[q][r];
+        v[p][r] = c * vp - s * vq;
+        v[q][r] = s * vp + c * vq;
+      }
+    }
+  T s2[3], smax = T(0);
+  for (int i = 0; i < 3; ++i) {
+    s2[i] = dot3r(w[i], w[i]);
+    T si = std::sqrt(s2[i]);
+    if (si > smax) smax = si;
+  }
+  T thr = T(3) * std::numeric_limits<T>::epsilon() * smax;
+  M3<T> R;
+  R.fill(T(0));
+  for (int i = 0; i < 3; ++i) {
+    if (!(std::sqrt(s2[i]) > thr)) continue;
+    for (int c = 0; c < 3; ++c)
+      for (int r = 0; r < 3; ++r) R[3 * c + r] = R[3 * c + r] + (v[i][r] * w[i][c]) / s2[i];
+  }
+  return R;
+}
+
 template <class T> inline T ustep(T eps, T x) { return (eps < x) ? T(1) : T(0); }
 // reciprocal_or_zero (math/impl/eigen.hpp:293-300)
 template <class T> inline T rcp0(T x, T eps) {

@@ -41,6 +41,8 @@ def lib():
             L.oracle_scene_free.argtypes = [vp]
             L.oracle_set_threads.argtypes = [C.c_int]
             L.oracle_morton_compare_many.argtypes = [vp, vp, C.c_int64, vp]
+            L.oracle_pinv3_many.argtypes = [vp, C.c_int64, vp]
+            L.oracle_pinv3_many.restype = None
             L.oracle_morton_compare_many.restype = None
             L.oracle_add_group.argtypes = [vp, cp, cp]
             L.oracle_add_tag.argtypes = [vp, cp, cp]
@@ -90,6 +92,15 @@ def morton_compare(a, b):
     out = np.empty(len(a), np.int8)
     lib().oracle_morton_compare_many(a.ctypes.data, b.ctypes.data, len(a), out.ctypes.data)
     return out
+
+
+def pinv3(a):
+    """Pseudo-inverses (f32) of 3x3 matrices a[k] (row-major numpy input)."""
+    a = np.asarray(a, np.float32).reshape(-1, 3, 3)
+    cm = np.ascontiguousarray(np.transpose(a, (0, 2, 1)))  # column-major items
+    out = np.empty_like(cm)
+    lib().oracle_pinv3_many(cm.ctypes.data, len(cm), out.ctypes.data)
+    return np.transpose(out, (0, 2, 1))
 
 
 def set_threads(n=0):

@@ -714,19 +714,133 @@ __device__ __forceinline__ M3 minv3(M3 const &A) {
   return r;
 }
 
-// wkbb18.compute_diagonal (schemes/wkbb18.hpp:194-270): block-Jacobi
-// preconditioner sp_i = (I - dt S_i)^-1, stored as 9 planes.  The fluid sum
-// runs over the particle's own group (`foreach _ neighbor`); xmr holds
-// (x, m / rho).
-template <int NB>
-__global__ void __launch_bounds__(kNT, kMinBlocks) k_wkbb18_diag(uint32_t n, uint32_t cap, float4 const *__restrict__ xmr,
-                                                     float const *__restrict__ rho, float *__restrict__ sp,
-                                                     float const *rho0p, float const *mup, Globals G, NbrList self,
-                                                     Nbrs<0, NB> N) {
+// Moore-Penrose pseudo-inverse of a 3x3 matrix: one-sided Jacobi SVD
+// (Hestenes), 8 sweeps over the column pairs (0,1), (0,2), (1,2); A V = W
+// with orthogonal columns w_i = sigma_i u_i, A+ = sum_i v_i w_i^T / sigma_i^2
+// over the sigma_i > 3 eps sigma_max.  Stands in for the reference's
+// invert_pm (math/impl/eigen.hpp:266-276, Eigen's complete orthogonal
+// decomposition); the oracle runs the same operations.
+__device__ __forceinline__ float dot3r(float const *a, float const *b) { return a[0] * b[0] + (a[1] * b[1] + a[2] * b[2]); }
+__device__ M3 pinv3(M3 const &A) {
+  float w[3][3], v[3][3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      w[c][r] = A.m[3 * c + r];
+      v[c][r] = (r == c) ? 1.0f : 0.0f;
+    }
+  for (int sweep = 0; sweep < 8; ++sweep)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      int p = k < 2 ? 0 : 1, q = k == 0 ? 1 : 2;
+      float alpha = dot3r(w[p], w[p]), beta = dot3r(w[q], w[q]), gamma = dot3r(w[p], w[q]);
+      if (gamma == 0.0f) continue;
+      float zeta = (beta - alpha) / (2.0f * gamma);
+      float t = copysignf(1.0f, zeta) / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
+      float c = 1.0f / sqrtf(1.0f + t * t);
+      float sn = c * t;
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        float wp = w[p][r], wq = w[q][r];
+        w[p][r] = c * wp - sn * wq;
+        w[q][r] = sn * wp + c * wq;
+        float vp = v[p][r], vq = v[q][r];
+        v[p][r] = c * vp - sn * vq;
+        v[q][r] = sn * vp + c * vq;
+      }
+    }
+  float s2[3], smax = 0.0f;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    s2[i] = dot3r(w[i], w[i]);
+    float si = sqrtf(s2[i]);
+    if (si > smax) smax = si;
+  }
+  float thr = 3.0f * 1.1920928955078125e-07f * smax;
+  M3 R;
+#pragma unroll
+  for (int e = 0; e < 9; ++e) R.m[e] = 0.0f;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    if (!(sqrtf(s2[i]) > thr)) continue;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int r = 0; r < 3; ++r) R.m[3 * c + r] = R.m[3 * c + r] + (v[i][r] * w[i][c]) / s2[i];
+  }
+  return R;
+}
+
+// L g for a column-major 3x3 L (row . vector, a0 + (a1 + a2))
+__device__ __forceinline__ f3 mv3(float const (&L)[9], f3 g) {
+  return {L[0] * g.x + (L[3] * g.y + L[6] * g.z), L[1] * g.x + (L[4] * g.y + L[7] * g.z),
+          L[2] * g.x + (L[5] * g.y + L[8] * g.z)};
+}
+
+// correction.compute_gradient_correction (share/schemes/correction.prtcl:
+// 25-43, schemes/correction.hpp:162-230):
+//   L_f = invert_pm(sum_{fluid neighbours} (m_j / rho_i) gradW(x_ij) (x_j - x_i)^T)
+template <int NF, int NB>
+__global__ void __launch_bounds__(kNT, kMinBlocks) k_correction(uint32_t n, uint32_t cap, float4 const *__restrict__ x,
+                                                                float const *__restrict__ rho, float *__restrict__ L,
+                                                                Globals G, Nbrs<NF, NB> N) {
   uint32_t i = grid_tid();
   if (i >= n) return;
   KernelParams K = kparams(*G.h);
   bool uc = use_cache(N, K);
+  f3 xi = mk3(x[i]);
+  float ri = rho[i];
+  M3 A;
+#pragma unroll
+  for (int e = 0; e < 9; ++e) A.m[e] = 0.0f;
+#pragma unroll
+  for (int q = 0; q < NF; ++q) {
+    FluidN const &F = N.f[q];
+    for_each_nbr(F.L, i, uc, [&](uint32_t j_, float gf_) {
+      float4 xm = __ldg(F.xm + j_);
+      f3 xj = mk3(xm);
+      f3 g = pgrad(uc, gf_, K, sub3(xi, xj));
+      f3 d = sub3(xj, xi);
+      float sc = xm.w / ri;
+      float gv[3] = {g.x, g.y, g.z}, dv[3] = {d.x, d.y, d.z};
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int r = 0; r < 3; ++r) A.m[3 * c + r] = A.m[3 * c + r] + sc * (gv[r] * dv[c]);
+    });
+  }
+  M3 R = pinv3(A);
+#pragma unroll
+  for (int e = 0; e < 9; ++e) L[size_t(e) * cap + i] = R.m[e];
+}
+
+__global__ void k_identity9(uint32_t n, uint32_t cap, float *L) {
+  uint32_t i = grid_tid();
+  if (i < n)
+#pragma unroll
+    for (int e = 0; e < 9; ++e) L[size_t(e) * cap + i] = (e % 4 == 0) ? 1.0f : 0.0f;
+}
+
+// wkbb18.compute_diagonal (schemes/wkbb18.hpp:194-270): block-Jacobi
+// preconditioner sp_i = (I - dt S_i)^-1, stored as 9 planes.  The fluid sum
+// runs over the particle's own group (`foreach _ neighbor`); xmr holds
+// (x, m / rho).
+// GC (wkbb18_gc, share/schemes/wkbb18_gc.prtcl): every kernel gradient
+// premultiplied by the item's gradient correction L_i (planar, capacity lcap)
+template <int NB, bool GC = false>
+__global__ void __launch_bounds__(kNT, kMinBlocks) k_wkbb18_diag(uint32_t n, uint32_t cap, float4 const *__restrict__ xmr,
+                                                     float const *__restrict__ rho, float *__restrict__ sp,
+                                                     float const *rho0p, float const *mup, Globals G, NbrList self,
+                                                     Nbrs<0, NB> N, float const *__restrict__ Lc, uint32_t lcap) {
+  uint32_t i = grid_tid();
+  if (i >= n) return;
+  KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
+  float Li[9];
+  if (GC)
+#pragma unroll
+    for (int e = 0; e < 9; ++e) Li[e] = Lc[size_t(e) * lcap + i];
   float h = K.h, dt = *G.dt, rho0 = *rho0p, mu = *mup;
   f3 xi = mk3(xmr[i]);
   float ri = rho[i];
@@ -740,6 +854,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_wkbb18_diag(uint32_t n, uin
     f3 xij = sub3(xi, mk3(xj));
     float coef = (cmu * xj.w) / (nsq3(xij) + hh);
     f3 g = pgrad(uc, gf_, K, xij);
+    if (GC) g = mv3(Li, g);
     float gv[3] = {g.x, g.y, g.z}, xv[3] = {xij.x, xij.y, xij.z};
 #pragma unroll
     for (int c = 0; c < 3; ++c)
@@ -756,6 +871,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_wkbb18_diag(uint32_t n, uin
       f3 xij = sub3(xi, mk3(xv));
       float coef = ((10.0f * (bmu / ri)) * ((rho0 * xv.w) / ri)) / (nsq3(xij) + hh);
       f3 g = pgrad(uc, gf_, K, xij);
+      if (GC) g = mv3(Li, g);
       float gv[3] = {g.x, g.y, g.z}, xw[3] = {xij.x, xij.y, xij.z};
 #pragma unroll
       for (int c = 0; c < 3; ++c)
@@ -796,13 +912,19 @@ struct PcgArgs {
   int const *max_k;
   int *iterations; // uniform wkbb18_iterations
   NbrList self;
+  float const *L;  // gradient correction (wkbb18_gc), planar with capacity lcap
+  uint32_t lcap;
 };
 
 // system product of wkbb18.accumulate_acceleration (schemes/wkbb18.hpp:
 // 339-396): (A w)_i = w_i - dt * a_f(w)_i
-template <int NB>
+template <int NB, bool GC>
 __device__ __forceinline__ f3 wkbb18_system(PcgArgs const &P, KernelParams const &K, bool uc, float dt, float rho0,
                                             float mu, Nbrs<0, NB> const &N, float4 const *__restrict__ w, uint32_t i) {
+  float Li[9];
+  if (GC)
+#pragma unroll
+    for (int e = 0; e < 9; ++e) Li[e] = P.L[size_t(e) * P.lcap + i];
   float h = K.h;
   float hh = (0.01f * h) * h;
   f3 xi = mk3(P.xmr[i]), wi = mk3(w[i]);
@@ -814,7 +936,9 @@ __device__ __forceinline__ f3 wkbb18_system(PcgArgs const &P, KernelParams const
     float4 xj = __ldg(P.xmr + j);
     f3 xij = sub3(xi, mk3(xj));
     float coef = ((cmu * xj.w) * dot3(sub3(wi, mk3(__ldg(w + j))), xij)) / (nsq3(xij) + hh);
-    af = add3(af, scl3(coef, pgrad(uc, gf_, K, xij)));
+    f3 g = pgrad(uc, gf_, K, xij);
+    if (GC) g = mv3(Li, g);
+    af = add3(af, scl3(coef, g));
     });
 
 #pragma unroll
@@ -826,7 +950,9 @@ __device__ __forceinline__ f3 wkbb18_system(PcgArgs const &P, KernelParams const
       float4 xv = __ldg(B.xV + j_);
       f3 xij = sub3(xi, mk3(xv));
       float coef = ((cb_mu * ((rho0 * xv.w) / ri)) * dot3(wi, xij)) / (nsq3(xij) + hh);
-      af = add3(af, scl3(coef, pgrad(uc, gf_, K, xij)));
+      f3 g = pgrad(uc, gf_, K, xij);
+      if (GC) g = mv3(Li, g);
+      af = add3(af, scl3(coef, g));
     });
   }
   return sub3(wi, scl3(dt, af));
@@ -843,11 +969,11 @@ __global__ void k_pcg_guess(PcgArgs P) {
 // y = M r, p = -y; dots b.b, r.r, r.y (solver/cg_openmp.hpp:48-96)
 // per-item parts of the PCG kernels (shared by the plain and the tiled
 // launches, so both compute the same values)
-template <int NB>
+template <int NB, bool GC>
 __device__ __forceinline__ void pcg_init_item(PcgArgs const &P, KernelParams const &K, bool uc, float dt, float rho0,
                                               float mu, Nbrs<0, NB> const &N, uint32_t i, double &bb, double &rr,
                                               double &ry) {
-  f3 ax = wkbb18_system<NB>(P, K, uc, dt, rho0, mu, N, P.X, i);
+  f3 ax = wkbb18_system<NB, GC>(P, K, uc, dt, rho0, mu, N, P.X, i);
   f3 b = mk3(P.v[i]);
   f3 r = sub3(ax, b);
   f3 y = precond(P.sp, P.cap, i, r);
@@ -858,10 +984,10 @@ __device__ __forceinline__ void pcg_init_item(PcgArgs const &P, KernelParams con
   rr += double(dot3(r, r));
   ry += double(dot3(r, y));
 }
-template <int NB>
+template <int NB, bool GC>
 __device__ __forceinline__ double pcg_q_item(PcgArgs const &P, KernelParams const &K, bool uc, float dt, float rho0,
                                              float mu, Nbrs<0, NB> const &N, uint32_t i) {
-  f3 q = wkbb18_system<NB>(P, K, uc, dt, rho0, mu, N, P.P, i);
+  f3 q = wkbb18_system<NB, GC>(P, K, uc, dt, rho0, mu, N, P.P, i);
   P.Q[i] = make_float4(q.x, q.y, q.z, 0.0f);
   return double(dot3(mk3(P.P[i]), q));
 }
@@ -919,27 +1045,27 @@ __device__ __forceinline__ void pcg_update_scalars(double *sc, int *st, double r
   }
 }
 
-template <int NB>
+template <int NB, bool GC = false>
 __global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_init(PcgArgs P, Globals G, Nbrs<0, NB> N, Red R) {
   KernelParams K = kparams(*G.h);
   bool uc = use_cache(N, K);
   float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
   double bb = 0.0, rr = 0.0, ry = 0.0;
   for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x)
-    pcg_init_item<NB>(P, K, uc, dt, rho0, mu, N, i, bb, rr, ry);
+    pcg_init_item<NB, GC>(P, K, uc, dt, rho0, mu, N, i, bb, rr, ry);
   double v[3] = {bb, rr, ry}, out[3];
   if (reduce_commit<3>(v, R, out) && threadIdx.x == 0) pcg_init_scalars(R.scalars + kSPcg, R.status, out, *P.tol);
 }
 
 // q = A p; p.q; alpha or break (solver/cg_openmp.hpp:121-151)
-template <int NB>
+template <int NB, bool GC = false>
 __global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_q(PcgArgs P, Globals G, Nbrs<0, NB> N, Red R) {
   if (!*(volatile int *)&R.status[kStPcgActive]) return;
   KernelParams K = kparams(*G.h);
   bool uc = use_cache(N, K);
   float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
   double pq = 0.0;
-  for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x) pq += pcg_q_item<NB>(P, K, uc, dt, rho0, mu, N, i);
+  for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x) pq += pcg_q_item<NB, GC>(P, K, uc, dt, rho0, mu, N, i);
   double v[1] = {pq}, out[1];
   if (reduce_commit<1>(v, R, out) && threadIdx.x == 0) pcg_q_scalars(R.scalars + kSPcg, R.status, out[0], *P.tol);
 }
@@ -982,7 +1108,7 @@ __global__ void k_pcg_control(PcgArgs P, Red R, cudaGraphConditionalHandle h, in
 
 // --- the PCG loop over the tiles of a batched model, per slot -------------
 
-template <int NB>
+template <int NB, bool GC = false>
 __global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_init_seg(PcgArgs P, Globals G, Nbrs<0, NB> N, SegArgs S) {
   uint4 T = S.tiles[blockIdx.x];
   uint32_t slot = T.x;
@@ -991,7 +1117,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_init_seg(PcgArgs P, Glo
   float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
   double bb = 0.0, rr = 0.0, ry = 0.0;
   uint32_t i = T.y + threadIdx.x;
-  if (i < T.z) pcg_init_item<NB>(P, K, uc, dt, rho0, mu, N, i, bb, rr, ry);
+  if (i < T.z) pcg_init_item<NB, GC>(P, K, uc, dt, rho0, mu, N, i, bb, rr, ry);
   double v[3] = {bb, rr, ry}, out[3];
   if (seg_commit<3>(v, S, slot, out) && threadIdx.x == 0) {
     int *st = S.stat + slot * kSegStat;
@@ -1000,7 +1126,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_init_seg(PcgArgs P, Glo
   }
 }
 
-template <int NB>
+template <int NB, bool GC = false>
 __global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_q_seg(PcgArgs P, Globals G, Nbrs<0, NB> N, SegArgs S) {
   uint4 T = S.tiles[blockIdx.x];
   uint32_t slot = T.x;
@@ -1009,7 +1135,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_q_seg(PcgArgs P, Global
   bool uc = use_cache(N, K);
   float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
   uint32_t i = T.y + threadIdx.x;
-  double v[1] = {(i < T.z) ? pcg_q_item<NB>(P, K, uc, dt, rho0, mu, N, i) : 0.0}, out[1];
+  double v[1] = {(i < T.z) ? pcg_q_item<NB, GC>(P, K, uc, dt, rho0, mu, N, i) : 0.0}, out[1];
   if (seg_commit<1>(v, S, slot, out) && threadIdx.x == 0)
     pcg_q_scalars(S.scal + slot * kSegScal, S.stat + slot * kSegStat, out[0], *P.tol);
 }
@@ -1225,7 +1351,7 @@ namespace {
 // groups of a model selected by type / tag, with their fields
 struct FluidG {
   Group *g;
-  VaryingField *x, *v, *a, *rho, *p, *m, *c, *s, *AA, *Ap, *tb, *vd, *sp;
+  VaryingField *x, *v, *a, *rho, *p, *m, *c, *s, *AA, *Ap, *tb, *vd, *sp, *L;
   SmallField *rho0, *mu, *tol, *max_k, *iters;
 };
 struct BoundG {
@@ -1812,17 +1938,21 @@ private:
 // wkbb18
 // ---------------------------------------------------------------------------
 
+// gc: wkbb18_gc (share/schemes/wkbb18_gc.prtcl), the same procedures with
+// every kernel gradient premultiplied by the item's gradient correction
 class Wkbb18 : public SchemeCommon {
 public:
-  Wkbb18() {
+  explicit Wkbb18(bool gc = false) : gc_(gc) {
     reg("compute_diagonal", [this](Nhood &nh, cudaStream_t s) { diag(nh, s); });
     reg("accumulate_acceleration", [this](Nhood &nh, cudaStream_t s) { pcg(nh, s); });
   }
   ~Wkbb18() override { free_vectors(); }
-  std::string name() const override { return "wkbb18"; }
+  std::string name() const override { return gc_ ? "wkbb18_gc" : "wkbb18"; }
   std::string source() const override {
-    return "procedures compute_diagonal (sp = (I - dt S)^-1), accumulate_acceleration (PCG over fluid velocities "
-           "with the implicit viscosity system, Jacobi block preconditioner sp, apply vd and a = vd / dt)";
+    return std::string("procedures compute_diagonal (sp = (I - dt S)^-1), accumulate_acceleration (PCG over fluid "
+                       "velocities with the implicit viscosity system, Jacobi block preconditioner sp, apply vd and "
+                       "a = vd / dt)") +
+           (gc_ ? "; every kernel gradient premultiplied by gradient_correction" : "");
   }
   void load(Model &m) override {
     m.add_global("smoothing_scale", ft_real());
@@ -1844,6 +1974,7 @@ public:
       F.vd = &F.g->add_varying("wkbb18_velocity_delta", ft_vec3());
       F.sp = &F.g->add_varying("wkbb18_system_diagonal", ft_mat3());
       F.tb = &F.g->add_varying("time_of_birth", ft_real());
+      F.L = gc_ ? &F.g->add_varying("gradient_correction", ft_mat3()) : nullptr;
     }
     for (auto &B : bound_) {
       B.mu = &B.g->add_uniform("dynamic_viscosity", ft_real());
@@ -1858,8 +1989,15 @@ public:
     auto N = bnbrs<NB>(v, s);
     float4 const *xmr = model_->packed_xmr(F.g, F.x, F.m, F.rho, s);
     ProfScope ps(model_->prof, "wkbb18_diag", s);
-    k_wkbb18_diag<NB><<<div_up(n, kNT), kNT, 0, s>>>(n, uint32_t(F.sp->cap), xmr, dptr<float>(F.rho),
-                                                      dptr<float>(F.sp), u(F.rho0), u(F.mu), G, nl(v, F.g->index), N);
+    if (gc_)
+      k_wkbb18_diag<NB, true><<<div_up(n, kNT), kNT, 0, s>>>(n, uint32_t(F.sp->cap), xmr, dptr<float>(F.rho),
+                                                              dptr<float>(F.sp), u(F.rho0), u(F.mu), G,
+                                                              nl(v, F.g->index), N, dptr<float>(F.L),
+                                                              uint32_t(F.L->cap));
+    else
+      k_wkbb18_diag<NB, false><<<div_up(n, kNT), kNT, 0, s>>>(n, uint32_t(F.sp->cap), xmr, dptr<float>(F.rho),
+                                                               dptr<float>(F.sp), u(F.rho0), u(F.mu), G,
+                                                               nl(v, F.g->index), N, nullptr, 0u);
     count_launch();
   }
   void diag(Nhood &nh, cudaStream_t s) {
@@ -1880,6 +2018,10 @@ public:
   // solver/cg_openmp.hpp:35-215 on the device: guess and initial residual,
   // then a device loop of [q = A p, update, p update, control], then apply
   template <int NB> void pcg_group(FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
+    if (gc_) pcg_group_t<NB, true>(F, v, G, s);
+    else pcg_group_t<NB, false>(F, v, G, s);
+  }
+  template <int NB, bool GC> void pcg_group_t(FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
     uint32_t n = uint32_t(F.g->count);
     ensure_vectors(n);
     PcgArgs P{};
@@ -1903,6 +2045,8 @@ public:
     P.max_k = static_cast<int const *>(model_->small_ptr(*F.max_k));
     P.iterations = static_cast<int *>(model_->small_ptr(*F.iters));
     P.self = nl(v, F.g->index);
+    P.L = GC ? dptr<float>(F.L) : nullptr;
+    P.lcap = GC ? uint32_t(F.L->cap) : 0u;
     auto N = bnbrs<NB>(v, s);
     Red R = red(*model_, 1);
     unsigned rg = red_grid(n), eg = div_up(n, 256);
@@ -1915,9 +2059,9 @@ public:
       ProfScope ps(model_->prof, "pcg_init", s);
       if (seg) {
         k_seg_pcg_begin<<<div_up(std::max<uint32_t>(SA.slots, 1), 256), 256, 0, s>>>(SA); count_launch();
-        if (tg) k_pcg_init_seg<NB><<<tg, kNT, 0, s>>>(P, G, N, SA);
+        if (tg) k_pcg_init_seg<NB, GC><<<tg, kNT, 0, s>>>(P, G, N, SA);
       } else {
-        k_pcg_init<NB><<<rg, kNT, 0, s>>>(P, G, N, R);
+        k_pcg_init<NB, GC><<<rg, kNT, 0, s>>>(P, G, N, R);
       }
       count_launch();
     }
@@ -1925,9 +2069,9 @@ public:
     auto body = [&](cudaStream_t cs, cudaGraphConditionalHandle h, bool use_handle, bool prof) {
       if (prof) model_->prof.begin("pcg_q", cs);
       if (seg) {
-        if (tg) k_pcg_q_seg<NB><<<tg, kNT, 0, cs>>>(P, G, N, SA);
+        if (tg) k_pcg_q_seg<NB, GC><<<tg, kNT, 0, cs>>>(P, G, N, SA);
       } else {
-        k_pcg_q<NB><<<rg, kNT, 0, cs>>>(P, G, N, R);
+        k_pcg_q<NB, GC><<<rg, kNT, 0, cs>>>(P, G, N, R);
       }
       count_launch();
       if (prof) model_->prof.end(cs);
@@ -1997,6 +2141,7 @@ public:
   }
 
 private:
+  bool gc_;
   float4 *vec_[5] = {};
   size_t vec_cap_ = 0;
   std::map<Group *, WhileLoop> loops_;
@@ -2079,7 +2224,68 @@ public:
   }
 };
 
+// ---------------------------------------------------------------------------
+// correction (gradient correction for wkbb18_gc)
+// ---------------------------------------------------------------------------
+
+class Correction : public SchemeCommon {
+public:
+  Correction() {
+    reg("identity_gradient_correction", [this](Nhood &, cudaStream_t s) {
+      for (auto &F : fluid_) {
+        uint32_t n = uint32_t(F.g->count);
+        if (!n) continue;
+        k_identity9<<<div_up(n, 256), 256, 0, s>>>(n, uint32_t(F.L->cap), dptr<float>(F.L));
+        count_launch();
+        PG_LAUNCH_CHECK();
+        F.L->version++;
+      }
+    });
+    reg("compute_gradient_correction", [this](Nhood &nh, cudaStream_t s) { compute(nh, s); });
+  }
+  std::string name() const override { return "correction"; }
+  std::string source() const override {
+    return "procedures identity_gradient_correction (L = I), compute_gradient_correction (L_f = invert_pm(sum_fluid "
+           "(m_f' / rho_f) gradW(x_ff') (x_f' - x_f)^T))";
+  }
+  void load(Model &m) override {
+    m.add_global("smoothing_scale", ft_real());
+    collect(m, true, false);
+    for (auto &F : fluid_) {
+      F.x = &F.g->add_varying("position", ft_vec3());
+      F.rho = &F.g->add_varying("density", ft_real());
+      F.m = &F.g->add_varying("mass", ft_real());
+      F.L = &F.g->add_varying("gradient_correction", ft_mat3());
+    }
+    bind(m);
+  }
+  template <int NF, int NB> struct L {
+    static void go(Correction *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
+      uint32_t n = uint32_t(F.g->count);
+      auto N = S->nbrs<NF, 0>(v, s);
+      ProfScope ps(S->model_->prof, "correction", s);
+      k_correction<NF, 0><<<div_up(n, kNT), kNT, 0, s>>>(n, uint32_t(F.L->cap), dptr<float4>(F.x), dptr<float>(F.rho),
+                                                          dptr<float>(F.L), G, N);
+      count_launch();
+    }
+  };
+  void compute(Nhood &nh, cudaStream_t s) {
+    Globals G = globals(*model_);
+    need({{G.h, "smoothing_scale"}});
+    // every group's sums read positions, masses and densities only
+    for (auto &F : fluid_) {
+      if (!F.g->count) continue;
+      NbrView const &v = lists(nh, F.g, G, s);
+      dispatch_fb<L>(int(fluid_.size()), 0, this, F, v, G, s);
+      PG_LAUNCH_CHECK();
+      F.L->version++;
+    }
+  }
+};
+
 using Factory = std::unique_ptr<Scheme> (*)();
+
+std::unique_ptr<Scheme> make_wkbb18_gc() { return std::unique_ptr<Scheme>(new Wkbb18(true)); }
 
 template <class S> std::unique_ptr<Scheme> make() { return std::unique_ptr<Scheme>(new S()); }
 
@@ -2094,6 +2300,8 @@ std::map<std::string, Factory> const &registry() {
     add(&make<SymplecticEuler>);
     add(&make<Wkbb18>);
     add(&make<Viscosity>);
+    add(&make<Correction>);
+    add(&make_wkbb18_gc);
     return m;
   }();
   return r;

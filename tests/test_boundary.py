@@ -34,7 +34,8 @@ def test_registry_and_errors_without_device(gpu_lib):
     from prtcl_gb300 import PrtclNotFound
     from prtcl_gb300.core import get_scheme_names, make_scheme
     names = get_scheme_names()
-    for s in ("aiast12", "density", "gravity", "iisph", "symplectic_euler", "wkbb18"):
+    for s in ("aiast12", "correction", "density", "gravity", "iisph", "symplectic_euler", "viscosity", "wkbb18",
+              "wkbb18_gc"):
         assert f"prtcl::schemes::{s}[T=f32, N=3, K=Cubic Spline]" in names
     with pytest.raises(PrtclNotFound, match="scheme is not registered"):
         make_scheme("prtcl::schemes::sesph[T=f32, N=3, K=Cubic Spline]")

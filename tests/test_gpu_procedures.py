@@ -81,6 +81,22 @@ def test_step_procedures_bitwise(pair):
         m.run("gravity", "initialize_acceleration")
         m.run("viscosity", "accumulate_acceleration")
     assert_bitwise(fld(d, "f", "acceleration", 3), fld(o, "f", "acceleration", 3), "explicit viscosity")
+    # gradient correction (pseudo-inverse) and the gradient-corrected WKBB18
+    for m in (d, o):
+        m.run("correction", "identity_gradient_correction")
+    eye = np.tile(np.eye(3, dtype=np.float32).reshape(1, 9), (fld(d, "f", "density", 1).shape[0], 1))
+    assert_bitwise(fld(d, "f", "gradient_correction", 9), eye, "identity L")
+    for m in (d, o):
+        m.run("correction", "compute_gradient_correction")
+    assert_bitwise(fld(d, "f", "gradient_correction", 9), fld(o, "f", "gradient_correction", 9), "L")
+    for m in (d, o):
+        m.run("wkbb18_gc", "compute_diagonal")
+    assert_bitwise(fld(d, "f", "wkbb18_system_diagonal", 9), fld(o, "f", "wkbb18_system_diagonal", 9), "sp gc")
+    for m in (d, o):
+        m.run("wkbb18_gc", "accumulate_acceleration")
+    assert d.get_uniform("f", "wkbb18_iterations") == int(o.get_uniform("f", "wkbb18_iterations"))
+    assert_bitwise(fld(d, "f", "wkbb18_velocity_delta", 3), fld(o, "f", "wkbb18_velocity_delta", 3), "vd gc")
+    assert_bitwise(fld(d, "f", "acceleration", 3), fld(o, "f", "acceleration", 3), "viscous accel gc")
 
 
 def test_unknown_procedure_and_scheme(pair):

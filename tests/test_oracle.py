@@ -224,3 +224,27 @@ def test_pcg_matches_dense_solve(oracle_mod):
     assert res < 1e-6
     assert np.abs(x - xs).max() < 1e-4 * max(1.0, np.abs(xs).max())
     assert int(o.get_uniform("f", "wkbb18_iterations")) >= 1
+
+
+def test_pseudo_inverse_matches_numpy(oracle_mod):
+    """The 3x3 pseudo-inverse standing in for invert_pm (Eigen's complete
+    orthogonal decomposition): full rank, rank 2, rank 1 and zero matrices
+    against numpy's SVD-based pinv in float64."""
+    rng = np.random.default_rng(8)
+    full = rng.standard_normal((200, 3, 3))
+    u = rng.standard_normal((100, 3, 2))
+    r2 = u @ rng.standard_normal((100, 2, 3))
+    r1 = rng.standard_normal((50, 3, 1)) @ rng.standard_normal((50, 1, 3))
+    mats = np.concatenate([full, r2, r1, np.zeros((2, 3, 3)), np.eye(3)[None] * 1e-3]).astype(np.float32)
+    got = oracle_mod.pinv3(mats).astype(np.float64)
+    ref = np.linalg.pinv(mats.astype(np.float64), rcond=1e-5)
+    scale = np.maximum(np.abs(ref).max(axis=(1, 2)), 1e-30)
+    cond = np.linalg.cond(mats.astype(np.float64)[:200])
+    err = np.abs(got - ref).max(axis=(1, 2)) / scale
+    assert (err[:200] <= 2e-6 * np.maximum(cond, 1.0)).all()
+    assert (err[200:] <= 1e-4).all()
+    assert not got[350:352].any()  # pinv(0) = 0
+    # Moore-Penrose conditions A A+ A = A and A+ A A+ = A+
+    a = mats.astype(np.float64)
+    np.testing.assert_allclose(a @ got @ a, a, atol=1e-4 * np.abs(a).max())
+    np.testing.assert_allclose(got @ a @ got, got, atol=1e-3 * np.abs(got).max())
