@@ -68,6 +68,10 @@ public:
   void GetUniform(std::string_view name, void *value) const {
     check(prtcl_gpu_uniform_get(m_, name_.c_str(), std::string(name).c_str(), value));
   }
+  // SaveVTK (util/save_vtk.cpp:57-128)
+  void SaveVTK(std::string const &path) const {
+    check(prtcl_gpu_group_save_vtk(m_, name_.c_str(), path.c_str()));
+  }
 
 private:
   prtcl_gpu_model *m_;
@@ -102,6 +106,33 @@ public:
     check(prtcl_gpu_global_get(m_, std::string(name).c_str(), value));
   }
   void Synchronize() { check(prtcl_gpu_model_synchronize(m_, nullptr)); }
+  // Model::Save / Model::Load in the reference's native binary archive format
+  void Save(std::string const &path) { check(prtcl_gpu_model_save(m_, path.c_str())); }
+  void Load(std::string const &path) { check(prtcl_gpu_model_load(m_, path.c_str())); }
+  std::vector<std::string> GetGroupNames() const {
+    int64_t need = 0;
+    check(prtcl_gpu_model_group_names(m_, nullptr, 0, &need));
+    std::string out(size_t(need), '\0');
+    check(prtcl_gpu_model_group_names(m_, out.data(), need, &need));
+    out.resize(out.size() ? out.size() - 1 : 0);
+    std::vector<std::string> r;
+    size_t a = 0;
+    while (a < out.size()) {
+      size_t b = out.find('\n', a);
+      if (b == std::string::npos) b = out.size();
+      if (b > a) r.push_back(out.substr(a, b - a));
+      a = b + 1;
+    }
+    return r;
+  }
+  // device-loop statistics (prtcl_gpu_model_stats): Jacobi solves,
+  // iterations, capped solves, largest aprde / nprde, PCG solves, iterations,
+  // capped solves
+  std::array<double, 7> Stats(bool reset = false) {
+    std::array<double, 7> st{};
+    check(prtcl_gpu_model_stats(m_, st.data(), 7, reset ? 1 : 0));
+    return st;
+  }
   prtcl_gpu_model *handle() const { return m_; }
 
 private:

@@ -32,11 +32,12 @@ def nvcc():
 
 def _deps():
     return [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [
-        os.path.join(HERE, "..", "include", "prtcl_gpu.h"), __file__]
+        os.path.join(HERE, "..", "include", "prtcl_gpu.h"), os.path.join(HERE, "..", "include", "prtcl_gpu.hpp"),
+        os.path.join(HERE, "host", "prtcl_gpu_run.cpp"), __file__]
 
 
 def up_to_date():
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(os.path.join(HERE, "bin", "prtcl_gpu_run")):
         return False
     t = os.path.getmtime(LIB)
     return all(os.path.getmtime(d) <= t for d in _deps())
@@ -66,7 +67,27 @@ def build(force=False, verbose=False, extra=()):
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_driver()
     return LIB
+
+
+DRIVER_SRC = os.path.join(HERE, "host", "prtcl_gpu_run.cpp")
+DRIVER = os.path.join(HERE, "bin", "prtcl_gpu_run")
+
+
+def build_driver():
+    """The native driver (host C++ over the C++ facade), linked against the
+    library with an rpath to it."""
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        raise RuntimeError("no C++ compiler for the native driver")
+    os.makedirs(os.path.dirname(DRIVER), exist_ok=True)
+    cmd = [cxx, "-O2", "-std=c++17", "-I", os.path.join(HERE, "..", "include"), DRIVER_SRC,
+           "-L", HERE, "-lprtcl_gpu", "-Wl,-rpath,$ORIGIN/..", "-o", DRIVER]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{r.stderr}")
+    return DRIVER
 
 
 if __name__ == "__main__":
