@@ -421,6 +421,7 @@ struct ListOut {
   uint32_t *maxcnt; // [kMaxListGroups]
   uint32_t n;
   int G;
+  int with_gf; // factors are written (lists built without them never read them)
 };
 
 // State of one item's list towards one neighbour group.  The current chunk
@@ -442,8 +443,10 @@ __device__ __forceinline__ uint32_t &bufw(uint32_t *buf, int g, int w) {
 __device__ __forceinline__ void flush_chunk(ListOut const &lo, int g, uint32_t i, uint32_t chunk, uint32_t *buf) {
   size_t nch = lo.cap[g] / kChunk;
   uint4 *dst = reinterpret_cast<uint4 *>(lo.chunks[g] + (size_t(i) * nch + chunk) * kChunkBytes);
-#pragma unroll
-  for (int v = 0; v < 6; ++v)
+  // offsets (2 vectors), then the factors (4 vectors) when the lists carry
+  // them: sweeps read factors only from lists built with a smoothing scale
+  int nv = lo.with_gf ? 6 : 2;
+  for (int v = 0; v < nv; ++v)
     dst[v] = make_uint4(bufw(buf, g, 4 * v), bufw(buf, g, 4 * v + 1), bufw(buf, g, 4 * v + 2), bufw(buf, g, 4 * v + 3));
 }
 
@@ -927,6 +930,7 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
     lo.maxcnt = stats_d_ + 8;
     lo.n = uint32_t(n);
     lo.G = G;
+    lo.with_gf = h != nullptr ? 1 : 0;
     PG_CUDA(cudaMemsetAsync(stats_d_ + 8, 0, 8 * sizeof(uint32_t), s));
     GridView gv = view();
     float4 const *qpos = static_cast<float4 const *>(gg_[q].pos->d);
