@@ -184,37 +184,43 @@ __global__ void k_scan_apply(uint32_t const *in, size_t n, uint32_t const *sums,
 
 constexpr int kRsNT = 256, kRsWarps = kRsNT / 32, kRsWarpItems = 512, kRsTile = kRsWarps * kRsWarpItems;
 
+// One pass over the digit of B bits at `shift`: per tile of kRsTile keys a
+// histogram (bucket-major, hist[d * tiles + tile]), then after its exclusive
+// scan a stable scatter that ranks equal digits within each warp by lane.
+template <int B>
 __global__ void k_rs_hist(uint64_t const *__restrict__ keys, size_t n, int shift, uint32_t *hist, uint32_t tiles) {
-  __shared__ uint32_t h[256];
-  h[threadIdx.x] = 0;
+  constexpr uint32_t NB = 1u << B;
+  __shared__ uint32_t h[NB];
+  for (uint32_t d = threadIdx.x; d < NB; d += kRsNT) h[d] = 0;
   __syncthreads();
   size_t base = size_t(blockIdx.x) * kRsTile;
   for (int k = 0; k < kRsTile / kRsNT; ++k) {
     size_t i = base + size_t(k) * kRsNT + threadIdx.x;
-    if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+    if (i < n) atomicAdd(&h[(keys[i] >> shift) & (NB - 1u)], 1u);
   }
   __syncthreads();
-  hist[size_t(threadIdx.x) * tiles + blockIdx.x] = h[threadIdx.x];
+  for (uint32_t d = threadIdx.x; d < NB; d += kRsNT) hist[size_t(d) * tiles + blockIdx.x] = h[d];
 }
 
+template <int B>
 __global__ void k_rs_scatter(uint64_t const *__restrict__ kin, uint32_t const *__restrict__ vin,
                              uint64_t *__restrict__ kout, uint32_t *__restrict__ vout, size_t n, int shift,
                              uint32_t const *__restrict__ offs, uint32_t tiles) {
-  __shared__ uint32_t cnt[kRsWarps][256];
+  constexpr uint32_t NB = 1u << B;
+  __shared__ uint32_t cnt[kRsWarps][NB];
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int d = threadIdx.x; d < kRsWarps * 256; d += kRsNT) cnt[d / 256][d % 256] = 0;
+  for (uint32_t d = threadIdx.x; d < kRsWarps * NB; d += kRsNT) cnt[d / NB][d % NB] = 0;
   __syncthreads();
   size_t base = size_t(blockIdx.x) * kRsTile + size_t(w) * kRsWarpItems;
   for (int step = 0; step < kRsWarpItems / 32; ++step) {
     size_t i = base + size_t(step) * 32 + lane;
-    uint32_t d = i < n ? uint32_t((kin[i] >> shift) & 255u) : 256u;
+    uint32_t d = i < n ? uint32_t((kin[i] >> shift) & (NB - 1u)) : NB;
     uint32_t peers = __match_any_sync(kFull, d);
-    if (d != 256u && lane == __ffs(peers) - 1) cnt[w][d] += __popc(peers);
+    if (d != NB && lane == __ffs(peers) - 1) cnt[w][d] += __popc(peers);
     __syncwarp();
   }
   __syncthreads();
-  {
-    int d = threadIdx.x;
+  for (uint32_t d = threadIdx.x; d < NB; d += kRsNT) {
     uint32_t run = offs[size_t(d) * tiles + blockIdx.x];
     for (int ww = 0; ww < kRsWarps; ++ww) {
       uint32_t c = cnt[ww][d];
@@ -227,16 +233,16 @@ __global__ void k_rs_scatter(uint64_t const *__restrict__ kin, uint32_t const *_
   for (int step = 0; step < kRsWarpItems / 32; ++step) {
     size_t i = base + size_t(step) * 32 + lane;
     uint64_t key = 0;
-    uint32_t val = 0, d = 256u;
+    uint32_t val = 0, d = NB;
     if (i < n) {
       key = kin[i];
       val = vin[i];
-      d = uint32_t((key >> shift) & 255u);
+      d = uint32_t((key >> shift) & (NB - 1u));
     }
     uint32_t peers = __match_any_sync(kFull, d);
-    uint32_t pos = (d != 256u) ? cnt[w][d] : 0u;
+    uint32_t pos = (d != NB) ? cnt[w][d] : 0u;
     __syncwarp();
-    if (d != 256u) {
+    if (d != NB) {
       uint32_t dst = pos + __popc(peers & lt);
       kout[dst] = key;
       vout[dst] = val;
@@ -828,16 +834,25 @@ void Nhood::update(cudaStream_t s) {
   uint64_t *kin = keys_a_, *kout = keys_b_;
   uint32_t *vin = vals_a_, *vout = vals_b_;
   uint32_t tiles = uint32_t((N + kRsTile - 1) / kRsTile);
-  size_t hl = size_t(tiles) * 256;
+  // the fewest passes of at most 10-bit digits, the digits as even as possible
+  int passes = std::max(1, (total_bits + 9) / 10);
+  int dbits = std::max(8, (total_bits + passes - 1) / passes);
+  size_t hl = size_t(tiles) << dbits;
   if (hl > hist_cap_) {
     if (hist_) PG_CUDA(cudaFree(hist_));
     hist_cap_ = hl + hl / 4;
     PG_CUDA(cudaMalloc(&hist_, hist_cap_ * 4));
   }
-  for (int shift = 0; shift < total_bits; shift += 8) {
-    k_rs_hist<<<tiles, kRsNT, 0, s>>>(kin, N, shift, hist_, tiles); count_launch();
+  for (int shift = 0; shift < total_bits; shift += dbits) {
+    if (dbits == 8) k_rs_hist<8><<<tiles, kRsNT, 0, s>>>(kin, N, shift, hist_, tiles);
+    else if (dbits == 9) k_rs_hist<9><<<tiles, kRsNT, 0, s>>>(kin, N, shift, hist_, tiles);
+    else k_rs_hist<10><<<tiles, kRsNT, 0, s>>>(kin, N, shift, hist_, tiles);
+    count_launch();
     exclusive_scan(hist_, hist_, hl, block_sums_, block_sums_cap_, s);
-    k_rs_scatter<<<tiles, kRsNT, 0, s>>>(kin, vin, kout, vout, N, shift, hist_, tiles); count_launch();
+    if (dbits == 8) k_rs_scatter<8><<<tiles, kRsNT, 0, s>>>(kin, vin, kout, vout, N, shift, hist_, tiles);
+    else if (dbits == 9) k_rs_scatter<9><<<tiles, kRsNT, 0, s>>>(kin, vin, kout, vout, N, shift, hist_, tiles);
+    else k_rs_scatter<10><<<tiles, kRsNT, 0, s>>>(kin, vin, kout, vout, N, shift, hist_, tiles);
+    count_launch();
     PG_LAUNCH_CHECK();
     std::swap(kin, kout);
     std::swap(vin, vout);
