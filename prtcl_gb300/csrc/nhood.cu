@@ -387,7 +387,46 @@ __device__ __forceinline__ int find_from(uint64_t const *__restrict__ keys, int 
 // the cells at +offset[k] only and writes both mirror slots, adj[c][k] = d
 // and adj[d][25 - k] = c, so every slot is written by exactly one thread
 // (adj starts at -1)
-__global__ void k_cells_adj(GridView gv, int4 const *cell_gi, size_t N, int32_t *adj) {
+// Hash table of the cell keys (open addressing, linear probing) for the
+// adjacency lookups: a power-of-two table larger than the item count, so it
+// always has an empty slot (every probe loop ends); the slot of a key does
+// not depend on the order of insertion, so the lookups are exact.
+// kEmptyKey marks an empty slot; no cell key equals it while the keys use
+// fewer than 64 bits (the host falls back to the searches otherwise).
+constexpr uint64_t kEmptyKey = ~0ull;
+__device__ __forceinline__ uint32_t key_hash(uint64_t k, uint32_t mask) {
+  return uint32_t((k * 0x9E3779B97F4A7C15ull) >> 32) & mask;
+}
+__global__ void k_hash_insert(GridView gv, size_t N, uint64_t *hk, int32_t *hv, uint32_t mask) {
+  size_t c = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  int C = *gv.ncells;
+  if (c >= N || int(c) >= C) return;
+  uint64_t key = gv.cell_key[c];
+  uint32_t h = key_hash(key, mask);
+  for (uint32_t probe = 0; probe <= mask; ++probe) {
+    unsigned long long prev = atomicCAS(reinterpret_cast<unsigned long long *>(hk + h), kEmptyKey, key);
+    if (prev == kEmptyKey) {
+      hv[h] = int32_t(c);
+      return;
+    }
+    h = (h + 1) & mask;
+  }
+}
+__device__ __forceinline__ int hash_find(uint64_t const *__restrict__ hk, int32_t const *__restrict__ hv, uint32_t mask,
+                                         uint64_t key) {
+  uint32_t h = key_hash(key, mask);
+  for (uint32_t probe = 0; probe <= mask; ++probe) {
+    uint64_t k = hk[h];
+    if (k == key) return hv[h];
+    if (k == kEmptyKey) return -1;
+    h = (h + 1) & mask;
+  }
+  return -1;
+}
+
+// (hk == nullptr: galloping searches over the sorted cell keys instead)
+__global__ void k_cells_adj(GridView gv, int4 const *cell_gi, size_t N, int32_t *adj, uint64_t const *hk,
+                            int32_t const *hv, uint32_t mask) {
   size_t c = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
   int C = *gv.ncells;
   if (c >= N || int(c) >= C) return;
@@ -399,7 +438,7 @@ __global__ void k_cells_adj(GridView gv, int4 const *cell_gi, size_t N, int32_t 
     uint32_t u0 = unsign(p.x), u1 = unsign(p.y), u2 = unsign(p.z);
     if (!key_valid(u0, gv.key) || !key_valid(u1, gv.key) || !key_valid(u2, gv.key)) continue;
     uint64_t kt = make_key(u0, u1, u2, gv.key.keep) | sk;
-    int d = find_from(gv.cell_key, C, int(c), kc, kt);
+    int d = hk ? hash_find(hk, hv, mask, kt) : find_from(gv.cell_key, C, int(c), kc, kt);
     if (d >= 0) {
       adj[c * 26 + k] = d;
       adj[size_t(d) * 26 + 25 - k] = int32_t(c);
@@ -675,7 +714,7 @@ static void free_all(std::initializer_list<void *> ps) {
 Nhood::~Nhood() {
   for (auto &kv : lists_) free_lists(kv.second);
   free_all({keys_a_, keys_b_, vals_a_, vals_b_, ukeys_, flags_, scan_, r2s_, s2c_, cell_start_, cell_adj_, cell_key_,
-            cell_gi_, xsorted_, hist_, block_sums_, stats_d_, ncells_d_, order_});
+            cell_gi_, xsorted_, hist_, block_sums_, stats_d_, ncells_d_, order_, hkeys_, hvals_});
   cudaFreeHost(stats_h_);
 }
 
@@ -870,7 +909,26 @@ void Nhood::update(cudaStream_t s) {
                                   ncells_d_, cell_adj_); count_launch();
   PG_LAUNCH_CHECK();
   // 5. adjacency (cells <= N; slots without a neighbour stay -1)
-  k_cells_adj<<<nb, 256, 0, s>>>(gv, cell_gi_, N, cell_adj_); count_launch();
+  uint64_t *hk = nullptr;
+  int32_t *hv = nullptr;
+  uint32_t mask = 0;
+  if (total_bits < 64 && N < (size_t(1) << 30)) {
+    size_t hs = 1;
+    while (hs <= N) hs <<= 1; // > N >= cells: an empty slot always remains
+    if (hs > hash_cap_) {
+      if (hkeys_) PG_CUDA(cudaFree(hkeys_));
+      if (hvals_) PG_CUDA(cudaFree(hvals_));
+      PG_CUDA(cudaMalloc(&hkeys_, hs * sizeof(uint64_t)));
+      PG_CUDA(cudaMalloc(&hvals_, hs * sizeof(int32_t)));
+      hash_cap_ = hs;
+    }
+    PG_CUDA(cudaMemsetAsync(hkeys_, 0xFF, hs * sizeof(uint64_t), s));
+    mask = uint32_t(hs - 1);
+    hk = hkeys_;
+    hv = hvals_;
+    k_hash_insert<<<nb, 256, 0, s>>>(gv, N, hk, hv, mask); count_launch();
+  }
+  k_cells_adj<<<nb, 256, 0, s>>>(gv, cell_gi_, N, cell_adj_, hk, hv, mask); count_launch();
   model_->prof.end(s); // grid_cells
   PG_LAUNCH_CHECK();
 }

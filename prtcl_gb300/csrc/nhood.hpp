@@ -194,6 +194,9 @@ private:
   // list build walks a group that was not in grid order instead)
   size_t permuted_count_[kMaxGroups] = {};
   uint32_t *order_ = nullptr; // group items in grid order (list build)
+  uint64_t *hkeys_ = nullptr;  // cell-key hash table (adjacency lookups)
+  int32_t *hvals_ = nullptr;
+  size_t hash_cap_ = 0;
   size_t order_cap_ = 0;
   std::vector<uint16_t const *> seg_;
   uint32_t seg_count_ = 0;
