@@ -22,6 +22,7 @@ Arms:
                      re-query) on all host threads, same scene and metric.
 
 Extra measurements in the same line (rank 0, one GPU; --no-extras skips them):
+  plain_27k the reference's plain 27k dam break (IISPH), beside the CPU oracle
   search    neighbour search only, 4M points (uniform / 64 Gaussian blobs),
             radius for 40 mean neighbours, GB/s of algorithmic bytes vs HBM
   batched   256 mixed-size dam-break scenes stepped together by one batch,
@@ -269,6 +270,7 @@ def run_ours(args, rank, world, dist):
 
     extras = {}
     if rank == 0 and world == 1 and not args.no_extras:
+        extras["plain_27k"] = run_plain_27k(args.no_cpu_baseline)
         extras["search"] = run_search(peak)
         extras["batched"] = run_batched()
         extras["serving"] = run_serving()
@@ -357,6 +359,46 @@ def cpu_baseline(sc, p, nf, steps=2, threads=0):
     secs = time.perf_counter() - t0
     return {"value": round(nf * steps / secs, 1), "unit": UNIT, "cores": th, "kind": "port",
             "sample": f"{steps} steps of the same scene after set-up and one warm step ({secs:.1f} s)"}
+
+
+def run_plain_27k(no_cpu=False, steps=100, warmup=3, cpu_steps=10):
+    """The reference's plain configuration: the 27,000-particle dam break
+    (spacing 0.025 m, 2 x 1 x 1 m box, dt 1e-3 s, IISPH to 0.1 % or 100
+    iterations), `steps` timed steps of the device step loop after `warmup`,
+    beside the CPU oracle (reference mode, all host threads) on `cpu_steps`
+    steps of the same scene."""
+    from prtcl_gb300.core import DeviceScene
+    sc, p = scenes.dam_break(), dict(driver.DAM_BREAK_27K)
+    nf = len(sc["fluid"])
+    d = DeviceScene()
+    driver.setup_dam_break(d, sc, p)
+    loop = driver.StepLoop(d, p, device_loop=True)
+    for _ in range(warmup):
+        loop.step(quiet=True)
+    d.model.stats(reset=True)
+    secs, wall, _ = timed_steps(d, loop, steps)
+    st = d.model.stats(reset=True)
+    out = {"workload": "dam break 27k fluid + %d boundary, IISPH, dt 1e-3 s" % len(sc["boundary"]),
+           "steps": steps, "warmup": warmup, "value": round(nf * steps / secs, 1), "unit": UNIT,
+           "ms_per_step": round(secs * 1e3 / steps, 4),
+           "jacobi_iterations_mean": round(st["jacobi_iterations"] / max(st["jacobi_solves"], 1.0), 3),
+           "jacobi_capped_steps": int(st["jacobi_capped"]), "max_relative_density_error": st["max_relative_aprde"]}
+    if not no_cpu:
+        from oracle import oracle as O
+        O.build()
+        th = O.set_threads(0)
+        o = O.Scene(np.float32, fp64_reductions=False)
+        driver.setup_dam_break(o, sc, p)
+        for _ in range(warmup):
+            o.step(permute=False, max_iters=p["max_iters"], eta=p["eta"], viscosity=False)
+        t0 = time.perf_counter()
+        for k in range(cpu_steps):
+            o.step(permute=((k + 1) % p["permute_every"] == 0), max_iters=p["max_iters"], eta=p["eta"],
+                   viscosity=False)
+        cs = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round(nf * cpu_steps / cs, 1), "unit": UNIT, "cores": th, "kind": "port",
+                               "sample": f"{cpu_steps} steps after {warmup} warm-up steps"}
+    return out
 
 
 def run_search(peak, n=4_000_000, reps=5, target=40.0):
