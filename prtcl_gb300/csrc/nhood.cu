@@ -476,6 +476,11 @@ struct ListOut {
 // Deltas are signed, relative to the row's first neighbour j0 (the row's
 // base); a row whose neighbours do not all fit becomes "wide": its indices
 // then go to idx32 (the entries already written are converted on the spot).
+// A wide row's offset words are never read, so the 8 words hold its 32-bit
+// indices instead, one half-chunk at a time, written to idx32 as two 16-byte
+// stores when the half is full: one whole sector per 8 entries rather than a
+// sector per entry (neighbours of an unpermuted group make nearly every row
+// wide).
 struct RowState {
   uint32_t c, j0;
   bool wide;
@@ -485,14 +490,24 @@ __device__ __forceinline__ uint32_t &bufw(uint32_t *buf, int g, int w) {
   return buf[(size_t(g) * 24 + w) * kBuildNT + threadIdx.x];
 }
 
-__device__ __forceinline__ void flush_chunk(ListOut const &lo, int g, uint32_t i, uint32_t chunk, uint32_t *buf) {
+__device__ __forceinline__ void flush_chunk(ListOut const &lo, int g, uint32_t i, uint32_t chunk, bool wide,
+                                            uint32_t *buf) {
   size_t nch = lo.cap[g] / kChunk;
   uint4 *dst = reinterpret_cast<uint4 *>(lo.chunks[g] + (size_t(i) * nch + chunk) * kChunkBytes);
-  // offsets (2 vectors), then the factors (4 vectors) when the lists carry
-  // them: sweeps read factors only from lists built with a smoothing scale
-  int nv = lo.with_gf ? 6 : 2;
-  for (int v = 0; v < nv; ++v)
+  // offsets (2 vectors, not for a wide row), then the factors (4 vectors)
+  // when the lists carry them: sweeps read factors only from lists built
+  // with a smoothing scale
+  int v0 = wide ? 2 : 0, nv = lo.with_gf ? 6 : 2;
+  for (int v = v0; v < nv; ++v)
     dst[v] = make_uint4(bufw(buf, g, 4 * v), bufw(buf, g, 4 * v + 1), bufw(buf, g, 4 * v + 2), bufw(buf, g, 4 * v + 3));
+}
+
+// the 8 buffered indices of a wide row's entries e0..e0+7 (e0 % 8 == 0) to
+// idx32: 32 aligned bytes (cap is a multiple of 16)
+__device__ __forceinline__ void flush_wide_half(ListOut const &lo, int g, uint32_t i, uint32_t e0, uint32_t *buf) {
+  uint4 *dst = reinterpret_cast<uint4 *>(lo.idx32[g] + size_t(i) * lo.cap[g] + e0);
+  dst[0] = make_uint4(bufw(buf, g, 0), bufw(buf, g, 1), bufw(buf, g, 2), bufw(buf, g, 3));
+  dst[1] = make_uint4(bufw(buf, g, 4), bufw(buf, g, 5), bufw(buf, g, 6), bufw(buf, g, 7));
 }
 
 __device__ __forceinline__ void row_add(ListOut const &lo, int g, uint32_t i, RowState &R, uint32_t j, float f,
@@ -514,13 +529,20 @@ __device__ __forceinline__ void row_add(ListOut const &lo, int g, uint32_t i, Ro
       int32_t de = int32_t(int16_t((e & 1) ? (w >> 16) : (w & 0xFFFFu)));
       lo.idx32[g][size_t(i) * lo.cap[g] + e] = R.j0 + uint32_t(de);
     }
+    // the current half-chunk's entries back into the buffer as indices (the
+    // packed words they came from are no longer needed)
+    for (uint32_t e = k - slot % 8; e < k; ++e) bufw(buf, g, int(e % 8)) = lo.idx32[g][size_t(i) * lo.cap[g] + e];
   }
-  if (R.wide) lo.idx32[g][size_t(i) * lo.cap[g] + k] = j;
-  uint32_t &w = bufw(buf, g, int(slot / 2));
-  uint32_t h = R.wide ? 0u : (uint32_t(d) & 0xFFFFu);
-  w = (slot & 1) ? ((w & 0xFFFFu) | (h << 16)) : h;
+  if (R.wide) {
+    bufw(buf, g, int(slot % 8)) = j;
+  } else {
+    uint32_t &w = bufw(buf, g, int(slot / 2));
+    uint32_t h = uint32_t(d) & 0xFFFFu;
+    w = (slot & 1) ? ((w & 0xFFFFu) | (h << 16)) : h;
+  }
   bufw(buf, g, 8 + int(slot)) = __float_as_uint(f);
-  if (slot == kChunk - 1) flush_chunk(lo, g, i, k / kChunk, buf);
+  if (R.wide && slot % 8 == 7) flush_wide_half(lo, g, i, k - 7, buf);
+  if (slot == kChunk - 1) flush_chunk(lo, g, i, k / kChunk, R.wide, buf);
 }
 
 template <int NG>
@@ -636,13 +658,20 @@ __global__ void __launch_bounds__(kBuildNT) k_build_lists(GridView gv, float4 co
     if (n > lo.cap[g]) {
       atomicMax(&lo.maxcnt[g], n);
     } else if (n % kChunk) {
-      // the partial last chunk, zero-filled
+      // the partial last chunk (and half-chunk of a wide row), zero-filled
+      bool wide = R[g].wide;
+      if (wide && n % 8) {
+        for (uint32_t e = n % 8; e < 8; ++e) bufw(buf, g, int(e)) = 0u;
+        flush_wide_half(lo, g, i, n - n % 8, buf);
+      }
       for (uint32_t slot = n % kChunk; slot < kChunk; ++slot) {
-        uint32_t &w = bufw(buf, g, int(slot / 2));
-        w = (slot & 1) ? (w & 0xFFFFu) : 0u;
+        if (!wide) {
+          uint32_t &w = bufw(buf, g, int(slot / 2));
+          w = (slot & 1) ? (w & 0xFFFFu) : 0u;
+        }
         bufw(buf, g, 8 + int(slot)) = 0u;
       }
-      flush_chunk(lo, g, i, n / kChunk, buf);
+      flush_chunk(lo, g, i, n / kChunk, wide, buf);
     }
   }
 }

@@ -127,3 +127,21 @@ def test_full_size_search_properties():
         assert (d2 < r * r * 1.0001).all()
         for j in js[:8]:
             assert i in idx[offs[j]:offs[j + 1]]
+
+
+def test_rows_turning_wide_mid_list(oracle_mod):
+    """A lattice in storage order (neighbour deltas fit 16 bits) with 1 % of
+    its points swapped with points 100,000 indices away: rows become wide at
+    every position of the list (first, mid-chunk, in a later chunk), and the
+    entries written before are converted; lists must match the oracle."""
+    m = 56
+    ax = np.arange(m, dtype=np.float32) * np.float32(0.01)
+    pts = np.stack(np.meshgrid(ax, ax, ax, indexing="ij"), -1).reshape(-1, 3).copy()
+    n = len(pts)
+    rng = np.random.default_rng(5)
+    for a in rng.choice(n, n // 100, replace=False):
+        b = (a + 100_000) % n
+        pts[[a, b]] = pts[[b, a]]
+    groups = [("p", "fluid", pts, [])]
+    d, o = make(oracle_mod, groups, 0.0205)
+    compare(d, o, groups)
