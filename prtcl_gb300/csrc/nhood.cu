@@ -536,11 +536,11 @@ __device__ __forceinline__ void row_add(ListOut const &lo, int g, uint32_t i, Ro
   if (R.wide) {
     bufw(buf, g, int(slot % 8)) = j;
   } else {
-    uint32_t &w = bufw(buf, g, int(slot / 2));
-    uint32_t h = uint32_t(d) & 0xFFFFu;
-    w = (slot & 1) ? ((w & 0xFFFFu) | (h << 16)) : h;
+    // the slot's half-word (little-endian: even slots low); a stale upper
+    // half past the row's end is cleared when the last chunk is written
+    reinterpret_cast<uint16_t *>(&bufw(buf, g, int(slot / 2)))[slot & 1] = uint16_t(uint32_t(d) & 0xFFFFu);
   }
-  bufw(buf, g, 8 + int(slot)) = __float_as_uint(f);
+  if (lo.with_gf) bufw(buf, g, 8 + int(slot)) = __float_as_uint(f);
   if (R.wide && slot % 8 == 7) flush_wide_half(lo, g, i, k - 7, buf);
   if (slot == kChunk - 1) flush_chunk(lo, g, i, k / kChunk, R.wide, buf);
 }
