@@ -492,8 +492,7 @@ __device__ __forceinline__ uint32_t &bufw(uint32_t *buf, int g, int w) {
 
 __device__ __forceinline__ void flush_chunk(ListOut const &lo, int g, uint32_t i, uint32_t chunk, bool wide,
                                             uint32_t *buf) {
-  size_t nch = lo.cap[g] / kChunk;
-  uint4 *dst = reinterpret_cast<uint4 *>(lo.chunks[g] + (size_t(i) * nch + chunk) * kChunkBytes);
+  uint4 *dst = reinterpret_cast<uint4 *>(lo.chunks[g] + (size_t(chunk) * lo.n + i) * kChunkBytes);
   // offsets (2 vectors, not for a wide row), then the factors (4 vectors)
   // when the lists carry them: sweeps read factors only from lists built
   // with a smoothing scale
@@ -521,11 +520,10 @@ __device__ __forceinline__ void row_add(ListOut const &lo, int g, uint32_t i, Ro
     // becomes wide: entries 0..k-1 to idx32 (full chunks from global memory,
     // the current one from the buffer)
     R.wide = true;
-    size_t nch = lo.cap[g] / kChunk;
     for (uint32_t e = 0; e < k; ++e) {
       uint32_t w;
       if (e / kChunk == k / kChunk) w = bufw(buf, g, int((e % kChunk) / 2));
-      else w = reinterpret_cast<uint32_t const *>(lo.chunks[g] + (size_t(i) * nch + e / kChunk) * kChunkBytes)[(e % kChunk) / 2];
+      else w = reinterpret_cast<uint32_t const *>(lo.chunks[g] + (size_t(e / kChunk) * lo.n + i) * kChunkBytes)[(e % kChunk) / 2];
       int32_t de = int32_t(int16_t((e & 1) ? (w >> 16) : (w & 0xFFFFu)));
       lo.idx32[g][size_t(i) * lo.cap[g] + e] = R.j0 + uint32_t(de);
     }
@@ -1235,14 +1233,16 @@ size_t Nhood::copy_neighbors(int g, size_t i, int64_t *counts, int64_t *out, siz
     uint32_t cn = cb.x & ~kWide;
     counts[ng] = cn;
     if (!cn) continue;
-    size_t rowbytes = size_t(v.cap[ng] / kChunk) * kChunkBytes;
-    std::vector<unsigned char> row(rowbytes);
+    // the item's chunks, one per chunk plane, packed on the host
+    size_t nch = v.cap[ng] / kChunk;
+    std::vector<unsigned char> row(nch * kChunkBytes);
     std::vector<uint32_t> e32(v.cap[ng]);
-    PG_CUDA(cudaMemcpyAsync(row.data(), v.chunks[ng] + i * rowbytes, rowbytes, cudaMemcpyDeviceToHost, s));
+    PG_CUDA(cudaMemcpy2DAsync(row.data(), kChunkBytes, v.chunks[ng] + i * kChunkBytes, size_t(v.n) * kChunkBytes,
+                              kChunkBytes, nch, cudaMemcpyDeviceToHost, s));
     PG_CUDA(cudaMemcpyAsync(e32.data(), v.idx32[ng] + i * v.cap[ng], v.cap[ng] * 4, cudaMemcpyDeviceToHost, s));
     PG_CUDA(cudaStreamSynchronize(s));
     for (uint32_t slot = 0; slot < cn; ++slot) {
-      if (k < cap) out[k] = nbr_host_decode(cb, row.data(), e32.data(), slot);
+      if (k < cap) out[k] = nbr_host_decode(cb, row.data(), 1, 0, e32.data(), slot);
       ++k;
     }
   }
@@ -1270,7 +1270,7 @@ void Nhood::copy_lists(int q, int ng, int64_t *offsets, uint32_t *idx, size_t ca
   if (size_t(offsets[n]) > cap) throw Error("copy_lists: capacity too small");
   for (size_t i = 0; i < n; ++i)
     for (uint32_t k = 0; k < (cb[i].x & ~kWide); ++k)
-      idx[offsets[i] + k] = nbr_host_decode(cb[i], ch.data() + i * rowbytes, e32.data() + i * v.cap[ng], k);
+      idx[offsets[i] + k] = nbr_host_decode(cb[i], ch.data(), n, i, e32.data() + i * v.cap[ng], k);
 }
 
 } // namespace prtcl_gpu

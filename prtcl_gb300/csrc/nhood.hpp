@@ -43,12 +43,15 @@
 namespace prtcl_gpu {
 
 // Device view of the neighbour lists of one query group, one set per
-// neighbour group g.  Row-major in 16-entry chunks: item i owns cap / 16
-// consecutive 96-byte chunks; chunk c holds entries 16c..16c+15 as
+// neighbour group g.  In 96-byte chunks of 16 entries: chunk c of item i
+// holds its entries 16c..16c+15 as
 //   16 x uint16  j - base   (32 bytes)
 //   16 x float   the pair's kernel-gradient factor (64 bytes)
 // so a chunk is exactly three 32-byte sectors and every fetched sector is
-// used once (offsets are signed 16-bit: j = base + offset).  Also per item:
+// used once (offsets are signed 16-bit: j = base + offset).  Chunk-major:
+// chunk c of item i sits at chunks[(c * n + i) * 96], so that the threads
+// of a warp, walking consecutive items, read their chunk c from one
+// contiguous 3 KB span.  Also per item:
 //   cb[g][i]    (count | kWide if "wide", base = the first neighbour's index)
 //   idx32[g]    j as 32-bit indices at [i * cap + k], written and read for
 //               "wide" items only (neighbours spanning >= 65536 indices)
@@ -68,12 +71,13 @@ struct NbrView {
 
 constexpr uint32_t kWide = 0x80000000u;
 
-// host decode of entry k of an item whose row of chunks is `row`: the
-// 16-bit entries are signed offsets from the row's base (its first
-// neighbour)
-inline uint32_t nbr_host_decode(uint2 cb, unsigned char const *row, uint32_t const *idx32row, uint32_t k) {
+// host decode of entry k of item i, with `chunks` a host copy of the
+// chunk-major array of n items: the 16-bit entries are signed offsets from
+// the row's base (its first neighbour)
+inline uint32_t nbr_host_decode(uint2 cb, unsigned char const *chunks, size_t n, size_t i, uint32_t const *idx32row,
+                                uint32_t k) {
   if (cb.x & kWide) return idx32row[k];
-  unsigned char const *p = row + size_t(k / kChunk) * kChunkBytes + (k % kChunk) * 2;
+  unsigned char const *p = chunks + (size_t(k / kChunk) * n + i) * kChunkBytes + (k % kChunk) * 2;
   int16_t d = int16_t(uint16_t(p[0] | (p[1] << 8)));
   return cb.y + uint32_t(int32_t(d));
 }

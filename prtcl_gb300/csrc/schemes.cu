@@ -53,10 +53,11 @@ constexpr int kStJacIter = 4, kStJacDone = 5;
 // ---------------------------------------------------------------------------
 
 struct NbrList {
-  unsigned char const *chunks; // rows of 96-byte chunks (16 offsets + 16 factors)
+  unsigned char const *chunks; // 96-byte chunks (16 offsets + 16 factors), chunk c of item i at (c * n + i)
   uint32_t const *idx32;       // [i * cap + k]: j (read for wide items only)
   uint2 const *cb;             // per item: (count | kWide, base)
   uint32_t cap;                // row length in entries, a multiple of 16
+  uint32_t n;                  // rows
 };
 
 // Calls f(j, factor) for the neighbours of item i, in list order.  A chunk
@@ -70,12 +71,12 @@ __device__ __forceinline__ void for_each_nbr(NbrList const &L, uint32_t i, bool 
   uint2 cb = __ldg(L.cb + i);
   uint32_t c = min(cb.x & ~kWide, L.cap);
   bool wide = (cb.x & kWide) != 0;
-  unsigned char const *row = L.chunks + size_t(i) * (L.cap / kChunk) * kChunkBytes;
+  unsigned char const *row = L.chunks + size_t(i) * kChunkBytes;
   // entries are taken kNbrBatch at a time (16: a whole chunk; 8: half a
   // chunk, fewer registers held per thread)
   for (uint32_t kb = 0; kb < c; kb += kNbrBatch) {
     uint32_t h = (kb % kChunk) / kNbrBatch; // batch within the chunk
-    uint4 const *ch = reinterpret_cast<uint4 const *>(row + size_t(kb / kChunk) * kChunkBytes);
+    uint4 const *ch = reinterpret_cast<uint4 const *>(row + size_t(kb / kChunk) * L.n * kChunkBytes);
     uint32_t j[kNbrBatch];
     if (wide) {
       uint4 const *w32 = reinterpret_cast<uint4 const *>(L.idx32 + size_t(i) * L.cap + kb);
@@ -1417,7 +1418,7 @@ protected:
     return a;
   }
 
-  static NbrList nl(NbrView const &v, int g) { return NbrList{v.chunks[g], v.idx32[g], v.cb[g], v.cap[g]}; }
+  static NbrList nl(NbrView const &v, int g) { return NbrList{v.chunks[g], v.idx32[g], v.cb[g], v.cap[g], v.n}; }
   // packed neighbour records of the fluid / boundary groups (made current
   // here: may launch a pack kernel on `s`)
   FluidN fn(FluidG const &F, NbrView const &v, cudaStream_t s) {
