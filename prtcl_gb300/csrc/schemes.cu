@@ -73,7 +73,9 @@ __device__ __forceinline__ void for_each_nbr(NbrList const &L, uint32_t i, bool 
   bool wide = (cb.x & kWide) != 0;
   unsigned char const *row = L.chunks + size_t(i) * kChunkBytes;
   // entries are taken kNbrBatch at a time (16: a whole chunk; 8: half a
-  // chunk, fewer registers held per thread)
+  // chunk, fewer registers held per thread).  Measured per sweep on the 1M
+  // dam break: 8 is faster for the pressure acceleration, the WKBB18
+  // diagonal and system product; 16 for the density and pressure sweeps.
   for (uint32_t kb = 0; kb < c; kb += kNbrBatch) {
     uint32_t h = (kb % kChunk) / kNbrBatch; // batch within the chunk
     uint4 const *ch = reinterpret_cast<uint4 const *>(row + size_t(kb / kChunk) * L.n * kChunkBytes);
@@ -457,7 +459,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_accel(uint32_t n, flo
 #pragma unroll
   for (int q = 0; q < NF; ++q) {
     FluidN const &F = N.f[q];
-    for_each_nbr(F.L, i, uc, [&](uint32_t j_, float gf_) {
+    for_each_nbr<8>(F.L, i, uc, [&](uint32_t j_, float gf_) {
       uint32_t j = j_;
       float4 xm = __ldg(F.xm + j);
       float coef = xm.w * (pri + __ldg(F.pr + j));
@@ -468,7 +470,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_accel(uint32_t n, flo
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
-    for_each_nbr(B.L, i, uc, [&](uint32_t j_, float gf_) {
+    for_each_nbr<8>(B.L, i, uc, [&](uint32_t j_, float gf_) {
       float4 xv = __ldg(B.xV + j_);
       float coef = ((0.7f * rho0) * xv.w) * bterm;
       acc = sub3(acc, scl3(coef, pgrad(uc, gf_, K, sub3(xi, mk3(xv)))));
@@ -850,7 +852,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_wkbb18_diag(uint32_t n, uin
   for (int k = 0; k < 9; ++k) S[k] = 0.0f;
   float hh = (0.01f * h) * h;
   float cmu = 10.0f * (mu / ri);
-  for_each_nbr(self, i, uc, [&](uint32_t j_, float gf_) {
+  for_each_nbr<8>(self, i, uc, [&](uint32_t j_, float gf_) {
     float4 xj = __ldg(xmr + j_);
     f3 xij = sub3(xi, mk3(xj));
     float coef = (cmu * xj.w) / (nsq3(xij) + hh);
@@ -867,7 +869,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_wkbb18_diag(uint32_t n, uin
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
     float bmu = *B.mu;
-    for_each_nbr(B.L, i, uc, [&](uint32_t j_, float gf_) {
+    for_each_nbr<8>(B.L, i, uc, [&](uint32_t j_, float gf_) {
       float4 xv = __ldg(B.xV + j_);
       f3 xij = sub3(xi, mk3(xv));
       float coef = ((10.0f * (bmu / ri)) * ((rho0 * xv.w) / ri)) / (nsq3(xij) + hh);
@@ -932,7 +934,7 @@ __device__ __forceinline__ f3 wkbb18_system(PcgArgs const &P, KernelParams const
   float ri = P.rho[i];
   float cmu = 10.0f * (mu / ri);
   f3 af = {0.0f, 0.0f, 0.0f};
-  for_each_nbr(P.self, i, uc, [&](uint32_t j_, float gf_) {
+  for_each_nbr<8>(P.self, i, uc, [&](uint32_t j_, float gf_) {
     uint32_t j = j_;
     float4 xj = __ldg(P.xmr + j);
     f3 xij = sub3(xi, mk3(xj));
@@ -947,7 +949,7 @@ __device__ __forceinline__ f3 wkbb18_system(PcgArgs const &P, KernelParams const
     BoundN const &B = N.b[q];
     float bmu = *B.mu;
     float cb_mu = 10.0f * (bmu / ri);
-    for_each_nbr(B.L, i, uc, [&](uint32_t j_, float gf_) {
+    for_each_nbr<8>(B.L, i, uc, [&](uint32_t j_, float gf_) {
       float4 xv = __ldg(B.xV + j_);
       f3 xij = sub3(xi, mk3(xv));
       float coef = ((cb_mu * ((rho0 * xv.w) / ri)) * dot3(wi, xij)) / (nsq3(xij) + hh);
