@@ -47,8 +47,19 @@ __host__ __device__ __forceinline__ uint64_t spread3(uint32_t x) {
   return v;
 }
 
-__host__ __device__ __forceinline__ uint64_t make_key(uint32_t u0, uint32_t u1, uint32_t u2, uint32_t keep) {
-  return (spread3(pext32(u0, keep)) << 2) | (spread3(pext32(u1, keep)) << 1) | spread3(pext32(u2, keep));
+// pext32(u, k.keep) from the runs of `keep` (the same bits; a run's bits
+// keep their order and the runs are packed from bit 0 up)
+__device__ __forceinline__ uint32_t key_pext(uint32_t u, KeyInfo const &k) {
+  if (k.nruns == 0) return pext32(u, k.keep);
+  uint32_t r = 0;
+#pragma unroll
+  for (int t = 0; t < kKeyRuns; ++t)
+    if (t < k.nruns) r |= (u & k.run_mask[t]) >> k.run_shift[t];
+  return r;
+}
+
+__device__ __forceinline__ uint64_t make_key(uint32_t u0, uint32_t u1, uint32_t u2, KeyInfo const &k) {
+  return (spread3(key_pext(u0, k)) << 2) | (spread3(key_pext(u1, k)) << 1) | spread3(key_pext(u2, k));
 }
 
 // is u consistent with the deleted bit positions (could a cell have it?)
@@ -89,7 +100,7 @@ __device__ __forceinline__ uint32_t item_seg(GridView const &gv, int g, uint32_t
 __device__ __forceinline__ int find_cell(GridView const &gv, int3 gi, uint32_t seg) {
   uint32_t u0 = unsign(gi.x), u1 = unsign(gi.y), u2 = unsign(gi.z);
   if (!key_valid(u0, gv.key) || !key_valid(u1, gv.key) || !key_valid(u2, gv.key)) return -1;
-  uint64_t key = make_key(u0, u1, u2, gv.key.keep) | seg_key(gv, seg);
+  uint64_t key = make_key(u0, u1, u2, gv.key) | seg_key(gv, seg);
   int lo = 0, hi = *gv.ncells;
   while (lo < hi) {
     int mid = (lo + hi) >> 1;
@@ -314,7 +325,7 @@ __global__ void k_cells_key(uint32_t const *ukeys, uint32_t const *vals, size_t 
   if (n < N) {
     uint4 u = reinterpret_cast<uint4 const *>(ukeys)[n];
     uint32_t h = vals[n];
-    keys[n] = make_key(u.x, u.y, u.z, gv.key.keep) | seg_key(gv, item_seg(gv, int(h >> 28), h & 0x0FFFFFFFu));
+    keys[n] = make_key(u.x, u.y, u.z, gv.key) | seg_key(gv, item_seg(gv, int(h >> 28), h & 0x0FFFFFFFu));
   }
 }
 
@@ -437,7 +448,7 @@ __global__ void k_cells_adj(GridView gv, int4 const *cell_gi, size_t N, int32_t 
     int3 p = make_int3(g.x + c_offsets[k][0], g.y + c_offsets[k][1], g.z + c_offsets[k][2]);
     uint32_t u0 = unsign(p.x), u1 = unsign(p.y), u2 = unsign(p.z);
     if (!key_valid(u0, gv.key) || !key_valid(u1, gv.key) || !key_valid(u2, gv.key)) continue;
-    uint64_t kt = make_key(u0, u1, u2, gv.key.keep) | sk;
+    uint64_t kt = make_key(u0, u1, u2, gv.key) | sk;
     int d = hk ? hash_find(hk, hv, mask, kt) : find_from(gv.cell_key, C, int(c), kc, kt);
     if (d >= 0) {
       adj[c * 26 + k] = d;
@@ -883,6 +894,7 @@ void Nhood::update(cudaStream_t s) {
   if (a1 && a0) k.keep |= 0x80000000u;
   else k.b31_const = a1 ? 0x80000000u : 0u;
   k.bits = __builtin_popcount(k.keep);
+  key_runs(k);
   if (k.bits > 21)
     throw Error("grid spans too many cells: " + std::to_string(k.bits) +
                 " informative bits per axis (at most 21 are supported)");

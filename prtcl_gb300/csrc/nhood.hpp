@@ -84,13 +84,43 @@ inline uint32_t nbr_host_decode(uint2 cb, unsigned char const *chunks, size_t n,
 
 constexpr int kMaxListGroups = 8; // groups a neighbour-list build supports
 
+constexpr int kKeyRuns = 4; // runs of kept bits gathered without a bit loop
+
 struct KeyInfo {
   uint32_t keep = 0;   // informative bit positions of u
   uint32_t rel_eq = 0; // deleted low positions always equal to bit 31
   uint32_t rel_ne = 0; // deleted low positions always unequal to bit 31
   uint32_t b31_const = 0; // value of bit 31 if deleted (0 or 0x80000000)
   int bits = 0;        // informative bits per axis
+  // `keep` as runs of consecutive bits, when it has at most kKeyRuns of
+  // them (nruns = 0 otherwise): the gather of run r is
+  // (u & run_mask[r]) >> run_shift[r]
+  int nruns = 0;
+  uint32_t run_mask[kKeyRuns] = {};
+  uint32_t run_shift[kKeyRuns] = {};
 };
+
+// split `keep` into runs of consecutive set bits (at most kKeyRuns)
+inline void key_runs(KeyInfo &k) {
+  k.nruns = 0;
+  uint32_t m = k.keep;
+  int out = 0; // output position of the next run
+  while (m) {
+    if (k.nruns == kKeyRuns) {
+      k.nruns = 0;
+      return;
+    }
+    int lo = __builtin_ctz(m);
+    uint32_t low = m >> lo;
+    int len = (low == 0xFFFFFFFFu) ? 32 : __builtin_ctz(~low);
+    uint32_t rm = (len == 32 ? 0xFFFFFFFFu : ((1u << len) - 1u)) << lo;
+    k.run_mask[k.nruns] = rm;
+    k.run_shift[k.nruns] = uint32_t(lo - out);
+    ++k.nruns;
+    out += len;
+    m &= ~rm;
+  }
+}
 
 struct GridView {
   uint32_t const *sorted;   // sorted -> handle (group << 28 | index)

@@ -145,3 +145,30 @@ def test_rows_turning_wide_mid_list(oracle_mod):
     groups = [("p", "fluid", pts, [])]
     d, o = make(oracle_mod, groups, 0.0205)
     compare(d, o, groups)
+
+
+@pytest.mark.parametrize("levels,near", [
+    ((0, 2, 8, 10), True),          # informative key bits in two runs
+    ((0, -3, 70, -70), True),       # three runs, negative indices
+    ((1, 11, 33, 513), False),      # four runs
+    ((1, 683, 547, 137), False),    # five runs: the general bit gather
+])
+def test_scattered_grid_indices(oracle_mod, levels, near):
+    """Small clusters at grid indices whose bit patterns leave one to more
+    than four runs of informative key bits (`near`: with a cluster in the
+    next cell along x of each, so adjacency is not empty): cells, adjacency
+    and lists must match the oracle."""
+    r = 0.1
+    rng = np.random.default_rng(sum(abs(v) for v in levels))
+    pts = []
+    for a in levels:
+        for b in levels[:3]:
+            for c in levels[::-1][:3]:
+                centre = (np.array([a, b, c], np.float64) + 0.5) * r
+                pts.append(centre + rng.uniform(-0.45 * r, 0.45 * r, (12, 3)))
+                if near:
+                    pts.append(centre + np.array([r, 0.0, 0.0]) + rng.uniform(-0.45 * r, 0.45 * r, (3, 3)))
+    pts = np.concatenate(pts).astype(np.float32)
+    groups = [("p", "fluid", pts, [])]
+    d, o = make(oracle_mod, groups, r)
+    compare(d, o, groups)
