@@ -70,6 +70,8 @@ ALGO_BYTES = {
     "integrate_position": (36, 0),  # x, v -> x
     "gravity": (12, 0),
 }
+# list build (nhood_lists): per fluid query and per listed pair
+LIST_BYTES_PER_QUERY, LIST_BYTES_PER_PAIR = 16, 8
 
 
 def load_peaks():
@@ -250,6 +252,13 @@ def run_ours(args, rank, world, dist):
         name, (cnt, ms) = top
         bf, bb = ALGO_BYTES.get(name, (0, 0))
         per_launch = bf * nf + bb * nb
+        if name == "nhood_lists":
+            # per fluid query its position and count (16 B), per listed pair
+            # (fluid and boundary neighbours) an index and a gradient factor
+            # (8 B); the pairs of the lists as they stand after the pass
+            d.update()
+            pairs = d.nhood.query(d.model.get_group("f").index, count_pairs=True)
+            per_launch = LIST_BYTES_PER_QUERY * nf + LIST_BYTES_PER_PAIR * pairs
         avg_s = ms / 1e3 / cnt
         ach = per_launch / avg_s / 1e9
         tr = load_traffic().get(name)

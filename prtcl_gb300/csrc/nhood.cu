@@ -193,7 +193,7 @@ __global__ void k_scan_apply(uint32_t const *in, size_t n, uint32_t const *sums,
 // stable LSD radix sort of (uint64 key, uint32 value), 8-bit digits
 // ---------------------------------------------------------------------------
 
-constexpr int kRsNT = 256, kRsWarps = kRsNT / 32, kRsWarpItems = 512, kRsTile = kRsWarps * kRsWarpItems;
+constexpr int kRsNT = 256, kRsWarps = kRsNT / 32, kRsWarpItems = 256, kRsTile = kRsWarps * kRsWarpItems;
 
 // One pass over the digit of B bits at `shift`: per tile of kRsTile keys a
 // histogram (bucket-major, hist[d * tiles + tile]), then after its exclusive
