@@ -221,6 +221,13 @@ int prtcl_gpu_scheme_run(prtcl_gpu_scheme *scheme, const char *procedure, prtcl_
 int prtcl_gpu_scheme_full_name(prtcl_gpu_scheme *scheme, char *buf, int64_t size, int64_t *needed_out);
 int prtcl_gpu_scheme_procedure_names(prtcl_gpu_scheme *scheme, char *buf, int64_t size, int64_t *needed_out);
 int prtcl_gpu_scheme_source(prtcl_gpu_scheme *scheme, char *buf, int64_t size, int64_t *needed_out);
+/* Load a scheme plugin: a shared library generated from the scheme language
+ * (share/schemes/*.prtcl, compiled by prtcl_gb300.dsl), whose exported
+ * prtcl_gpu_plugin_init registers its schemes by full name, after which
+ * prtcl_gpu_scheme_new creates them like the built-in ones.  Counterpart of
+ * the reference's generated scheme headers (lua/prtcl/generate/
+ * cxx_openmp_impl_hpp.lua) compiled into the library. */
+int prtcl_gpu_scheme_load_plugin(const char *path);
 int prtcl_gpu_registry_scheme_names(char *buf, int64_t size, int64_t *needed_out);
 
 /* ---- batched scenes (no single counterpart in the reference) ----

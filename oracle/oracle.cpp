@@ -3,6 +3,8 @@
 //
 // Procedures restated here, each following the reference's generated code:
 //   density.compute_density            schemes/density.hpp:160-220
+//   sesph.compute_density_and_pressure schemes/sesph.hpp:171-237
+//   sesph.accumulate_acceleration      schemes/sesph.hpp:240-302
 //   aiast12.compute_volume             schemes/aiast12.hpp:125-175
 //   gravity.initialize_acceleration    schemes/gravity.hpp:133-158
 //   symplectic_euler.integrate_velocity_with_hard_fade
@@ -294,6 +296,72 @@ template <class T> struct Scene : SceneBase {
         for (size_t j : nb[gidx(n)]) acc += (nV[j] * rho0) * K.W(vsub(x[i], nx[j]));
       }
       rho[i] = acc;
+    });
+  }
+
+  // sesph.compute_density_and_pressure (schemes/sesph.hpp, generated from
+  // share/schemes/sesph.prtcl): the density as density.compute_density,
+  // then p = kappa max(0, rho / rho0 - 1), max as std::max({0, x})
+  void sesph_compute_density_and_pressure() {
+    auto fl = of_type("fluid"), bd = of_type("boundary");
+    Kernel<T> K(gr("smoothing_scale"));
+    for (auto *g : fl) {
+      g->vf("position", 3); g->vf("density", 1); g->vf("mass", 1); g->vf("pressure", 1);
+    }
+    for (auto *g : bd) { g->vf("position", 3); g->vf("volume", 1); }
+    foreach_with_neighbors(fl, [&](Group<T> *p, size_t i, auto &nb) {
+      auto *x = p->v3("position");
+      T rho0 = ur(*p, "rest_density"), kappa = ur(*p, "compressibility");
+      T acc = 0;
+      for (auto *n : fl) {
+        auto *nx = n->v3("position");
+        T *nm = n->s1("mass");
+        for (size_t j : nb[gidx(n)]) acc += nm[j] * K.W(vsub(x[i], nx[j]));
+      }
+      for (auto *n : bd) {
+        auto *nx = n->v3("position");
+        T *nV = n->s1("volume");
+        for (size_t j : nb[gidx(n)]) acc += (nV[j] * rho0) * K.W(vsub(x[i], nx[j]));
+      }
+      p->s1("density")[i] = acc;
+      T t = acc / rho0 - T(1);
+      p->s1("pressure")[i] = kappa * ((T(0) < t) ? t : T(0));
+    });
+  }
+
+  // sesph.accumulate_acceleration: a -= m_j (p_i / rho_i^2 + p_j / rho_j^2)
+  // gradW - (0.7 V_b rho0) (2 p_i / rho_i^2) gradW, into the existing a
+  void sesph_accumulate_acceleration() {
+    auto fl = of_type("fluid"), bd = of_type("boundary");
+    Kernel<T> K(gr("smoothing_scale"));
+    for (auto *g : fl) {
+      g->vf("position", 3); g->vf("acceleration", 3); g->vf("density", 1); g->vf("mass", 1);
+      g->vf("pressure", 1);
+    }
+    for (auto *g : bd) { g->vf("position", 3); g->vf("volume", 1); }
+    foreach_with_neighbors(fl, [&](Group<T> *p, size_t i, auto &nb) {
+      auto *x = p->v3("position");
+      T *pr = p->s1("pressure");
+      T *rho = p->s1("density");
+      T rho0 = ur(*p, "rest_density");
+      V3<T> a = p->v3("acceleration")[i];
+      for (auto *n : fl) {
+        auto *nx = n->v3("position");
+        T *nm = n->s1("mass");
+        T *np = n->s1("pressure");
+        T *nrho = n->s1("density");
+        for (size_t j : nb[gidx(n)])
+          a = vsub(a, vscale(nm[j] * ((pr[i] / (rho[i] * rho[i])) + (np[j] / (nrho[j] * nrho[j]))),
+                             K.gradW(vsub(x[i], nx[j]))));
+      }
+      for (auto *n : bd) {
+        auto *nx = n->v3("position");
+        T *nV = n->s1("volume");
+        for (size_t j : nb[gidx(n)])
+          a = vsub(a, vscale(((T(0.7) * nV[j]) * rho0) * ((T(2) * pr[i]) / (rho[i] * rho[i])),
+                             K.gradW(vsub(x[i], nx[j]))));
+      }
+      p->v3("acceleration")[i] = a;
     });
   }
 
@@ -809,6 +877,8 @@ template <class T> struct Scene : SceneBase {
 
   void run(std::string const &scheme, std::string const &proc) override {
     if (scheme == "density" && proc == "compute_density") return density_compute_density();
+    if (scheme == "sesph" && proc == "compute_density_and_pressure") return sesph_compute_density_and_pressure();
+    if (scheme == "sesph" && proc == "accumulate_acceleration") return sesph_accumulate_acceleration();
     if (scheme == "aiast12" && proc == "compute_volume") return aiast12_compute_volume();
     if (scheme == "gravity" && proc == "initialize_acceleration") return gravity_initialize_acceleration();
     if (scheme == "symplectic_euler" && proc == "integrate_velocity_with_hard_fade")

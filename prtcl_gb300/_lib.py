@@ -86,6 +86,7 @@ SIGNATURES = {
     "prtcl_gpu_scheme_procedure_names": [vp, C.c_char_p, i64, i64p],
     "prtcl_gpu_scheme_source": [vp, C.c_char_p, i64, i64p],
     "prtcl_gpu_registry_scheme_names": [C.c_char_p, i64, i64p],
+    "prtcl_gpu_scheme_load_plugin": [C.c_char_p],
     "prtcl_gpu_nhood_query": [vp, i32, i64p, vp],
     "prtcl_gpu_model_group_names": [vp, C.c_char_p, i64, i64p],
     "prtcl_gpu_model_save": [vp, cp],

@@ -62,7 +62,7 @@ def build(force=False, verbose=False, extra=()):
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB + ".tmp"
-    cmd = [cc, *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs]
+    cmd = [cc, *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs, "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")

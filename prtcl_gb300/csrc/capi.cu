@@ -4,6 +4,7 @@
 #include "schemes.hpp"
 
 #include <atomic>
+#include <dlfcn.h>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -485,6 +486,18 @@ int prtcl_gpu_scheme_source(prtcl_gpu_scheme *scheme, char *buf, int64_t size, i
 }
 int prtcl_gpu_registry_scheme_names(char *buf, int64_t size, int64_t *needed_out) {
   return write_str(join(scheme_names()), buf, size, needed_out);
+}
+int prtcl_gpu_scheme_load_plugin(const char *path) {
+  NEED(path);
+  return guard([&] {
+    // kept open for the life of the process: the schemes it registered
+    // point into it
+    void *h = dlopen(path, RTLD_NOW | RTLD_LOCAL);
+    if (!h) throw Error(std::string("cannot load scheme plugin: ") + dlerror());
+    auto init = reinterpret_cast<void (*)()>(dlsym(h, "prtcl_gpu_plugin_init"));
+    if (!init) throw Error("scheme plugin has no prtcl_gpu_plugin_init: " + std::string(path));
+    init();
+  });
 }
 
 // ---- batched scenes ----

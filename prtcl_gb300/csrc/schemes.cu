@@ -18,6 +18,8 @@
 // the last block of the launch sums the block partials.  The relaxed-Jacobi
 // loop (iisph.solve_pressure) and the PCG loop run on the device as CUDA
 // graphs with a conditional while node: no host round trip per iteration.
+#include "mat3.cuh"
+#include "nbr_walk.cuh"
 #include "schemes.hpp"
 
 #include <algorithm>
@@ -36,10 +38,6 @@ constexpr int kNT = 128;            // threads per block for particle kernels
 // registers at 64): the sweeps wait on gathers, and more resident warps hide
 // more of that latency
 constexpr int kMinBlocks = 8;
-// neighbour entries a sweep thread holds at a time (16 or 8; measured on
-// the 1M dam break: 16 for every sweep but the IISPH setup, whose two walks
-// over a row run faster with 8)
-constexpr uint32_t kNbrBatchDefault = 16;
 constexpr int kMaxRedBlocks = 4096; // block partials per reduced value
 
 // model scratch layout
@@ -51,78 +49,6 @@ constexpr int kStJacIter = 4, kStJacDone = 5;
 // ---------------------------------------------------------------------------
 // argument structs
 // ---------------------------------------------------------------------------
-
-struct NbrList {
-  unsigned char const *chunks; // 96-byte chunks (16 offsets + 16 factors), chunk c of item i at (c * n + i)
-  uint32_t const *idx32;       // [i * cap + k]: j (read for wide items only)
-  uint2 const *cb;             // per item: (count | kWide, base)
-  uint32_t cap;                // row length in entries, a multiple of 16
-  uint32_t n;                  // rows
-};
-
-// Calls f(j, factor) for the neighbours of item i, in list order.  A chunk
-// of 16 entries is fetched with six 16-byte streaming loads (evict-first:
-// the lists are read once per sweep, the gathered particle records should
-// stay in L2), so that its 16 gathers can be in flight together.
-// (keep_l2: plain L2-cached loads instead, for a row that is walked again
-// right after)
-template <uint32_t kNbrBatch = kNbrBatchDefault, class F>
-__device__ __forceinline__ void for_each_nbr(NbrList const &L, uint32_t i, bool with_gf, F &&f, bool keep_l2 = false) {
-  uint2 cb = __ldg(L.cb + i);
-  uint32_t c = min(cb.x & ~kWide, L.cap);
-  bool wide = (cb.x & kWide) != 0;
-  unsigned char const *row = L.chunks + size_t(i) * kChunkBytes;
-  // entries are taken kNbrBatch at a time (16: a whole chunk; 8: half a
-  // chunk, fewer registers held per thread).  Measured per sweep on the 1M
-  // dam break: 8 is faster for the pressure acceleration, the WKBB18
-  // diagonal and system product; 16 for the density and pressure sweeps.
-  for (uint32_t kb = 0; kb < c; kb += kNbrBatch) {
-    uint32_t h = (kb % kChunk) / kNbrBatch; // batch within the chunk
-    uint4 const *ch = reinterpret_cast<uint4 const *>(row + size_t(kb / kChunk) * L.n * kChunkBytes);
-    uint32_t j[kNbrBatch];
-    if (wide) {
-      uint4 const *w32 = reinterpret_cast<uint4 const *>(L.idx32 + size_t(i) * L.cap + kb);
-#pragma unroll
-      for (int v = 0; v < int(kNbrBatch / 4); ++v) {
-        uint4 a = __ldcs(w32 + v);
-        j[4 * v] = a.x;
-        j[4 * v + 1] = a.y;
-        j[4 * v + 2] = a.z;
-        j[4 * v + 3] = a.w;
-      }
-    } else {
-#pragma unroll
-      for (int v = 0; v < int(kNbrBatch / 8); ++v) {
-        uint4 a = keep_l2 ? __ldcg(ch + h * (kNbrBatch / 8) + v) : __ldcs(ch + h * (kNbrBatch / 8) + v);
-        uint32_t w[4] = {a.x, a.y, a.z, a.w};
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-          // signed 16-bit offsets from the row's base
-          j[8 * v + 2 * t] = cb.y + uint32_t(int32_t(int16_t(w[t] & 0xFFFFu)));
-          j[8 * v + 2 * t + 1] = cb.y + uint32_t(int32_t(w[t]) >> 16);
-        }
-      }
-    }
-    float g[kNbrBatch];
-    if (with_gf) {
-#pragma unroll
-      for (int v = 0; v < int(kNbrBatch / 4); ++v) {
-        uint4 const *gp = ch + 2 + h * (kNbrBatch / 4) + v;
-        uint4 a = keep_l2 ? __ldcg(gp) : __ldcs(gp);
-        g[4 * v] = __uint_as_float(a.x);
-        g[4 * v + 1] = __uint_as_float(a.y);
-        g[4 * v + 2] = __uint_as_float(a.z);
-        g[4 * v + 3] = __uint_as_float(a.w);
-      }
-    } else {
-#pragma unroll
-      for (int t = 0; t < int(kNbrBatch); ++t) g[t] = 0.0f;
-    }
-#pragma unroll
-    for (int t = 0; t < int(kNbrBatch); ++t)
-      if (kb + t < c) f(j[t], g[t]);
-  }
-}
 
 // the pair's kernel gradient: from the cached factor (bit-identical to
 // kgradW) when the lists were built with the current smoothing scale
@@ -690,96 +616,6 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_viscosity(uint32_t n, float
 // ---------------------------------------------------------------------------
 // WKBB18 (schemes/wkbb18.hpp)
 // ---------------------------------------------------------------------------
-
-struct M3 {
-  float m[9]; // column-major
-};
-
-__device__ __forceinline__ float cof3(M3 const &A, int i, int j) {
-  int i1 = (i + 1) % 3, i2 = (i + 2) % 3, j1 = (j + 1) % 3, j2 = (j + 2) % 3;
-  return A.m[3 * j1 + i1] * A.m[3 * j2 + i2] - A.m[3 * j2 + i1] * A.m[3 * j1 + i2];
-}
-// inverse by the adjugate (cofactors, determinant along column 0)
-__device__ __forceinline__ M3 minv3(M3 const &A) {
-  float c00 = cof3(A, 0, 0), c10 = cof3(A, 1, 0), c20 = cof3(A, 2, 0);
-  float det = c00 * A.m[0] + (c10 * A.m[1] + c20 * A.m[2]);
-  float inv = 1.0f / det;
-  M3 r;
-  r.m[0] = c00 * inv;           // (0,0)
-  r.m[3] = c10 * inv;           // (0,1)
-  r.m[6] = c20 * inv;           // (0,2)
-  r.m[1] = cof3(A, 0, 1) * inv; // (1,0)
-  r.m[4] = cof3(A, 1, 1) * inv; // (1,1)
-  r.m[7] = cof3(A, 2, 1) * inv; // (1,2)
-  r.m[2] = cof3(A, 0, 2) * inv; // (2,0)
-  r.m[5] = cof3(A, 1, 2) * inv; // (2,1)
-  r.m[8] = cof3(A, 2, 2) * inv; // (2,2)
-  return r;
-}
-
-// Moore-Penrose pseudo-inverse of a 3x3 matrix: one-sided Jacobi SVD
-// (Hestenes), 8 sweeps over the column pairs (0,1), (0,2), (1,2); A V = W
-// with orthogonal columns w_i = sigma_i u_i, A+ = sum_i v_i w_i^T / sigma_i^2
-// over the sigma_i > 3 eps sigma_max.  Stands in for the reference's
-// invert_pm (math/impl/eigen.hpp:266-276, Eigen's complete orthogonal
-// decomposition); the oracle runs the same operations.
-__device__ __forceinline__ float dot3r(float const *a, float const *b) { return a[0] * b[0] + (a[1] * b[1] + a[2] * b[2]); }
-__device__ M3 pinv3(M3 const &A) {
-  float w[3][3], v[3][3];
-#pragma unroll
-  for (int c = 0; c < 3; ++c)
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-      w[c][r] = A.m[3 * c + r];
-      v[c][r] = (r == c) ? 1.0f : 0.0f;
-    }
-  for (int sweep = 0; sweep < 8; ++sweep)
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      int p = k < 2 ? 0 : 1, q = k == 0 ? 1 : 2;
-      float alpha = dot3r(w[p], w[p]), beta = dot3r(w[q], w[q]), gamma = dot3r(w[p], w[q]);
-      if (gamma == 0.0f) continue;
-      float zeta = (beta - alpha) / (2.0f * gamma);
-      float t = copysignf(1.0f, zeta) / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
-      float c = 1.0f / sqrtf(1.0f + t * t);
-      float sn = c * t;
-#pragma unroll
-      for (int r = 0; r < 3; ++r) {
-        float wp = w[p][r], wq = w[q][r];
-        w[p][r] = c * wp - sn * wq;
-        w[q][r] = sn * wp + c * wq;
-        float vp = v[p][r], vq = v[q][r];
-        v[p][r] = c * vp - sn * vq;
-        v[q][r] = sn * vp + c * vq;
-      }
-    }
-  float s2[3], smax = 0.0f;
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    s2[i] = dot3r(w[i], w[i]);
-    float si = sqrtf(s2[i]);
-    if (si > smax) smax = si;
-  }
-  float thr = 3.0f * 1.1920928955078125e-07f * smax;
-  M3 R;
-#pragma unroll
-  for (int e = 0; e < 9; ++e) R.m[e] = 0.0f;
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    if (!(sqrtf(s2[i]) > thr)) continue;
-#pragma unroll
-    for (int c = 0; c < 3; ++c)
-#pragma unroll
-      for (int r = 0; r < 3; ++r) R.m[3 * c + r] = R.m[3 * c + r] + (v[i][r] * w[i][c]) / s2[i];
-  }
-  return R;
-}
-
-// L g for a column-major 3x3 L (row . vector, a0 + (a1 + a2))
-__device__ __forceinline__ f3 mv3(float const (&L)[9], f3 g) {
-  return {L[0] * g.x + (L[3] * g.y + L[6] * g.z), L[1] * g.x + (L[4] * g.y + L[7] * g.z),
-          L[2] * g.x + (L[5] * g.y + L[8] * g.z)};
-}
 
 // correction.compute_gradient_correction (share/schemes/correction.prtcl:
 // 25-43, schemes/correction.hpp:162-230):
@@ -2312,16 +2148,32 @@ std::map<std::string, Factory> const &registry() {
 
 } // namespace
 
+namespace {
+std::map<std::string, SchemeFactory> &added() {
+  static std::map<std::string, SchemeFactory> m;
+  return m;
+}
+} // namespace
+
+void register_scheme(std::string const &full_name, SchemeFactory f) {
+  if (registry().count(full_name) || added().count(full_name))
+    throw Error("scheme is already registered: " + full_name);
+  added()[full_name] = std::move(f);
+}
+
 std::unique_ptr<Scheme> new_scheme(std::string const &full_name) {
   auto const &r = registry();
   auto it = r.find(full_name);
-  if (it == r.end()) throw Error("scheme is not registered");
-  return it->second();
+  if (it != r.end()) return it->second();
+  auto jt = added().find(full_name);
+  if (jt != added().end()) return jt->second();
+  throw Error("scheme is not registered");
 }
 
 std::vector<std::string> scheme_names() {
   std::vector<std::string> v;
   for (auto &kv : registry()) v.push_back(kv.first);
+  for (auto &kv : added()) v.push_back(kv.first);
   return v;
 }
 

@@ -47,4 +47,10 @@ private:
 std::unique_ptr<Scheme> new_scheme(std::string const &full_name);
 std::vector<std::string> scheme_names();
 
+// Schemes added at run time: the generated plugins (schemes compiled from
+// the scheme language) register a factory per scheme when they are loaded.
+// A name already taken is an error.
+using SchemeFactory = std::function<std::unique_ptr<Scheme>()>;
+void register_scheme(std::string const &full_name, SchemeFactory f);
+
 } // namespace prtcl_gpu
