@@ -310,6 +310,144 @@ __device__ __forceinline__ double block_reduce_max(double v, double *sh) {
 }
 __device__ __forceinline__ double block_reduce_min(double v, double *sh) { return -block_reduce_max(-v, sh); }
 
+// ---- solve pcg: the generic preconditioned CG of the reference
+// (solver/cg_openmp.hpp:35-215) over the particles of one group, values of
+// type float (real) or f3 (real[], stored as float4).  The per-item dots
+// are f32 (a0 b0 + (a1 b1 + a2 b2)); their sums, the threshold and the
+// breaks are FP64 and alpha, beta the FP64 quotients rounded to f32, as the
+// hand-written WKBB18 solver and the oracle's FP64 mode.
+struct PcgState {
+  double thr, r_nsq, prev_rdy, next_rdy, tol;
+  float alpha, beta;
+  int iter, stop, max_k;
+};
+
+__device__ __forceinline__ float vdot(float a, float b) { return a * b; }
+__device__ __forceinline__ float vdot(f3 a, f3 b) { return dot(a, b); }
+__device__ __forceinline__ float vld(float const *a, uint32_t i) { return a[i]; }
+__device__ __forceinline__ f3 vld(float4 const *a, uint32_t i) { return mk3(a[i]); }
+__device__ __forceinline__ void vst(float *a, uint32_t i, float v) { a[i] = v; }
+__device__ __forceinline__ void vst(float4 *a, uint32_t i, f3 v) { a[i] = make_float4(v.x, v.y, v.z, 0.0f); }
+
+constexpr int kPcgNT = 128;
+
+__device__ __forceinline__ void pcg_commit(double v, double *part) {
+  __shared__ double sh[32];
+  double b = block_sum(v, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = b;
+}
+// r = r - b; sum b.b
+template <class S> __global__ void k_pcg_residual(uint32_t n, S *r, S const *b, double *part) {
+  uint32_t i = blockIdx.x * kPcgNT + threadIdx.x;
+  double v = 0.0;
+  if (i < n) {
+    auto bi = vld(b, i);
+    vst(r, i, vld(r, i) - bi);
+    v = double(vdot(bi, bi));
+  }
+  pcg_commit(v, part);
+}
+// p = -y; sums r.r and r.y
+template <class S> __global__ void k_pcg_start(uint32_t n, S *p, S const *y, S const *r, double *part_rr,
+                                               double *part_ry) {
+  uint32_t i = blockIdx.x * kPcgNT + threadIdx.x;
+  double rr = 0.0, ry = 0.0;
+  if (i < n) {
+    auto yi = vld(y, i), ri = vld(r, i);
+    vst(p, i, -yi);
+    rr = double(vdot(ri, ri));
+    ry = double(vdot(ri, yi));
+  }
+  pcg_commit(rr, part_rr);
+  pcg_commit(ry, part_ry);
+}
+// sum a.b
+template <class S> __global__ void k_pcg_dot(uint32_t n, S const *a, S const *b, double *part) {
+  uint32_t i = blockIdx.x * kPcgNT + threadIdx.x;
+  double v = 0.0;
+  if (i < n) v = double(vdot(vld(a, i), vld(b, i)));
+  pcg_commit(v, part);
+}
+// x += alpha p; r += alpha q; sum r.r (nothing once the loop has stopped)
+template <class S> __global__ void k_pcg_update(uint32_t n, S *x, S *r, S const *p, S const *q, PcgState const *st,
+                                                double *part_rr) {
+  uint32_t i = blockIdx.x * kPcgNT + threadIdx.x;
+  double rr = 0.0;
+  if (i < n && !st->stop) {
+    float alpha = st->alpha;
+    vst(x, i, vld(x, i) + alpha * vld(p, i));
+    auto ri = vld(r, i) + alpha * vld(q, i);
+    vst(r, i, ri);
+    rr = double(vdot(ri, ri));
+  }
+  pcg_commit(rr, part_rr);
+}
+// p = -y + beta p
+template <class S> __global__ void k_pcg_direction(uint32_t n, S *p, S const *y, PcgState const *st) {
+  uint32_t i = blockIdx.x * kPcgNT + threadIdx.x;
+  if (i < n && !st->stop) vst(p, i, -vld(y, i) + st->beta * vld(p, i));
+}
+__device__ __forceinline__ double pcg_sum(double const *part, uint32_t nb) {
+  double a = 0.0;
+  for (uint32_t b = 0; b < nb; ++b) a += part[b];
+  return a;
+}
+__device__ __forceinline__ bool pcg_ok(PcgState const &s, int k, double r_nsq) {
+  if (k < 1) return true;
+  if (k > s.max_k) return false;
+  return !(r_nsq < s.thr);
+}
+// after the initial residual and preconditioned iterate
+__global__ void k_pcg_begin(PcgState *st, SReal tol, SInt max_k, double const *part_bb, double const *part_rr,
+                            double const *part_ry, uint32_t nb) {
+  PcgState s{};
+  s.tol = double(rd(tol));
+  s.max_k = rd(max_k);
+  double b_nsq = pcg_sum(part_bb, nb);
+  double thr = s.tol * s.tol * b_nsq;
+  double fmin = double(1.17549435082228750797e-38f); // smallest positive normal f32
+  s.thr = thr < fmin ? fmin : thr;
+  s.r_nsq = pcg_sum(part_rr, nb);
+  s.next_rdy = pcg_sum(part_ry, nb);
+  s.iter = 0;
+  s.stop = pcg_ok(s, 0, s.r_nsq) ? 0 : 1;
+  *st = s;
+}
+// after q = A p: the first break test and alpha
+__global__ void k_pcg_step(PcgState *st, double const *part_pq, uint32_t nb) {
+  PcgState s = *st;
+  if (s.stop) return;
+  s.prev_rdy = s.next_rdy;
+  double pdq = pcg_sum(part_pq, nb);
+  if (fabs(pdq) < s.tol) {
+    s.stop = 1;
+  } else {
+    s.alpha = float(s.prev_rdy / pdq);
+  }
+  *st = s;
+}
+// after y = T r: the second break test, beta, the iteration count and the
+// loop condition
+__global__ void k_pcg_next(PcgState *st, double const *part_rr, double const *part_ry, uint32_t nb) {
+  PcgState s = *st;
+  if (s.stop) return;
+  s.r_nsq = pcg_sum(part_rr, nb);
+  s.next_rdy = pcg_sum(part_ry, nb);
+  if (fabs(s.prev_rdy) < s.tol) {
+    s.stop = 1;
+  } else {
+    s.beta = float(s.next_rdy / s.prev_rdy);
+    s.iter += 1;
+    // the loop condition; the direction update is skipped once the loop is
+    // over (the direction is not read after it)
+    if (!pcg_ok(s, s.iter, s.r_nsq)) s.stop = 1;
+  }
+  *st = s;
+}
+__global__ void k_pcg_end(PcgState const *st, SInt iterations) { wr(iterations, st->iter); }
+// an empty group: the solve returns 0 iterations
+__global__ void k_pcg_zero(SInt iterations) { wr(iterations, 0); }
+
 // the lists of a query group to neighbour group g
 __device__ __forceinline__ NbrList nbr_list(NbrView const &v, int g) {
   return NbrList{v.chunks[g], v.idx32[g], v.cb[g], v.cap[g], v.n};

@@ -17,6 +17,7 @@ from __future__ import annotations
 import hashlib
 import os
 import subprocess
+import threading
 
 from .. import build as libbuild
 from .cuda import full_name, generate_all
@@ -24,6 +25,7 @@ from .parser import parse
 
 CACHE = os.path.join(libbuild.HERE, "_dsl_cache")
 _loaded = {}
+_lib_lock = threading.Lock()  # one library build at a time
 
 
 def plugin_source(source: str, prefix: str = ""):
@@ -34,7 +36,8 @@ def plugin_source(source: str, prefix: str = ""):
 
 
 def _compile(name: str, cu: str) -> str:
-    lib = libbuild.build()
+    with _lib_lock:
+        lib = libbuild.build()
     key = hashlib.sha1((cu + str(os.path.getmtime(lib))).encode()).hexdigest()[:16]
     d = os.path.join(CACHE, key)
     so = os.path.join(d, "plugin.so")

@@ -22,6 +22,12 @@ Execution (one GPU stream, no host round trip inside a procedure):
   in a small device frame, so that particle loops can read and reduce them.
 * ``foreach dimension index d`` at procedure level -> a host loop over the
   N = 3 dimensions; ``d`` is a kernel argument.
+* ``solve pcg`` -> per selected group, a kernel per part (guess, right-hand
+  side, system and preconditioner products, apply) over the solver's
+  vectors, driven by the reference's CG (solver/cg_openmp.hpp:35-215) with
+  its state on the device and one 4-byte read per iteration for the stop
+  decision; dots, threshold and breaks in FP64 as the hand-written WKBB18
+  solver (csrc/dsl_device.cuh).
 
 Arithmetic follows the reference's generated expressions: every binary
 operation as written, folded left, with literals cast to f32 and the
@@ -141,7 +147,8 @@ class Emitter:
 
     def field_read(self, e, ctx):
         if isinstance(e.ref, SolveRef):
-            raise DslError("solve pcg is not supported by the CUDA backend yet")
+            _, idx = self.binding(e, ctx)
+            return f"vld({e.ref.kind}_, {idx})"
         var, idx = self.binding(e, ctx)
         f = e.ref
         if f.kind == "varying":
@@ -207,9 +214,9 @@ class Emitter:
             tgt = tgt.subject
         ty = ctype(self.info.types[id(tgt)])
         # read-modify-write through a temporary of the target's type
-        if isinstance(tgt, FieldAccess):
-            if isinstance(tgt.ref, SolveRef):
-                raise DslError("solve pcg is not supported by the CUDA backend yet")
+        if isinstance(tgt, FieldAccess) and isinstance(tgt.ref, SolveRef):
+            read, write = "vld(into_, i)", "vst(into_, i, {});"
+        elif isinstance(tgt, FieldAccess):
             var, idx = self.binding(tgt, ctx)
             f = tgt.ref
             if f.kind == "varying":
@@ -313,7 +320,8 @@ class Emitter:
                 self.body(proc, st.body, host, dims + [st.index], ind + 1)
                 host.append(f"{pad}}}")
             elif isinstance(st, Solve):
-                raise DslError(f"scheme {self.s.name}: solve pcg is not supported by the CUDA backend yet")
+                flush()
+                self.solve(proc, st, host, dims, ind)
             else:
                 scalar.append(st)
         flush()
@@ -363,19 +371,105 @@ class Emitter:
             host.append(f"{pad}  count_launch();")
         host.append(f"{pad}}}")
 
+    def solve(self, proc, st, host, dims, ind):
+        pad = "  " * ind
+        t = norm_type(st.type)
+        if t.base != "real" or t.rank > 1:
+            raise DslError(f"solve pcg over {t} (the CUDA backend takes real and real[])")
+        S = "float" if t.rank == 0 else "float4"
+        g = self.groups[st.groups]
+        aliases = {f.alias: f for f in g.fields if f.kind == "uniform"}
+        for a, base in (("pcg_max_error", "real"), ("pcg_max_iters", "integer"), ("pcg_iterations", "integer")):
+            if a not in aliases or norm_type(aliases[a].type) != NDType(base):
+                raise DslError(f"solve pcg over groups {st.groups!r} needs a uniform field {a} of type {base}")
+        parts = {}
+        for part in st.parts:
+            key = getattr(part, "name", "apply")
+            k = _Kernel(f"k_{_ident(proc.name)}_v{self.pidx}_{key}", st)
+            k.dims = list(dims)
+            k.solve_storage = S
+            for x in part.body:
+                self.stmt(x, k, None, 2)
+            self.kernels.append(k)
+            parts[key] = k
+        self.pidx += 1
+        gsn = _ident(st.groups)
+        dargs = "".join(f", d_{_ident(d)}" for d in dims)
+        uses_nb = any(k.nb_groups or "nbr_list(" in "\n".join(k.lines) for k in parts.values())
+
+        def launch(key, into, with_):
+            k = parts[key]
+            nb_args = "".join(f", all_{_ident(gn)}()" for gn in k.nb_groups)
+            return (f"{pad}    {k.name}<<<nb_, kGenNT, 0, s>>>(pp_{nb_args}, glob(), lv_, frame_{dargs}, "
+                    f"{into}, {with_});")
+
+        h = host.append
+        h(f"{pad}{{ // solve pcg {t} over {st.groups} particle {st.index}")
+        h(f"{pad}  for (Group *pg : sel_{gsn}) {{")
+        h(f"{pad}    {self.gs(st.groups)} pp_ = mk_{gsn}(pg);")
+        h(f"{pad}    uint32_t n_ = uint32_t(pg->count);")
+        h(f"{pad}    if (n_ == 0) {{ k_pcg_zero<<<1, 1, 0, s>>>(pp_.u_pcg_iterations); count_launch(); continue; }}")
+        h(f"{pad}    uint32_t nb_ = (n_ + kGenNT - 1) / kGenNT;")
+        h(f"{pad}    ensure_pcg(n_ * sizeof({S}), nb_);")
+        h(f"{pad}    {S} *x_ = pcg_vec<{S}>(0, n_), *b_ = pcg_vec<{S}>(1, n_), *r_ = pcg_vec<{S}>(2, n_);")
+        h(f"{pad}    {S} *p_ = pcg_vec<{S}>(3, n_), *q_ = pcg_vec<{S}>(4, n_), *y_ = pcg_vec<{S}>(5, n_);")
+        h(f"{pad}    double *c0_ = pcg_part_, *c1_ = pcg_part_ + pcg_part_cap_, *c2_ = pcg_part_ + 2 * pcg_part_cap_;")
+        if uses_nb:
+            h(f"{pad}    NbrView const &lv_ = nh.lists(pg->index, s);")
+        else:
+            h(f"{pad}    NbrView lv_{{}};")
+        h(f"{pad}    {S} *none_ = nullptr;")
+        # x = guess; b = rhs; r = A x - b; y = T r; p = -y
+        h(launch("guess", "x_", "none_"))
+        h(launch("right_hand_side", "b_", "none_"))
+        h(launch("system", "r_", "x_"))
+        h(f"{pad}    k_pcg_residual<{S}><<<nb_, kPcgNT, 0, s>>>(n_, r_, b_, c0_);")
+        h(launch("preconditioner", "y_", "r_"))
+        h(f"{pad}    k_pcg_start<{S}><<<nb_, kPcgNT, 0, s>>>(n_, p_, y_, r_, c1_, c2_);")
+        h(f"{pad}    k_pcg_begin<<<1, 1, 0, s>>>(pcg_state_, pp_.u_pcg_max_error, pp_.u_pcg_max_iters, c0_, c1_, c2_, nb_);")
+        h(f"{pad}    for (int k = 0; k < 7; ++k) count_launch();")
+        h(f"{pad}    for (long it_ = 0;; ++it_) {{")
+        h(f"{pad}      // q = A p; alpha; x += alpha p, r += alpha q; y = T r; beta; p = -y + beta p")
+        h("  " + launch("system", "q_", "p_"))
+        h(f"{pad}      k_pcg_dot<{S}><<<nb_, kPcgNT, 0, s>>>(n_, p_, q_, c0_);")
+        h(f"{pad}      k_pcg_step<<<1, 1, 0, s>>>(pcg_state_, c0_, nb_);")
+        h(f"{pad}      k_pcg_update<{S}><<<nb_, kPcgNT, 0, s>>>(n_, x_, r_, p_, q_, pcg_state_, c1_);")
+        h("  " + launch("preconditioner", "y_", "r_"))
+        h(f"{pad}      k_pcg_dot<{S}><<<nb_, kPcgNT, 0, s>>>(n_, r_, y_, c2_);")
+        h(f"{pad}      k_pcg_next<<<1, 1, 0, s>>>(pcg_state_, c1_, c2_, nb_);")
+        h(f"{pad}      k_pcg_direction<{S}><<<nb_, kPcgNT, 0, s>>>(n_, p_, y_, pcg_state_);")
+        h(f"{pad}      for (int k = 0; k < 8; ++k) count_launch();")
+        h(f"{pad}      PG_CUDA(cudaMemcpyAsync(pcg_stop_h_, &pcg_state_->stop, sizeof(int), cudaMemcpyDeviceToHost, s));")
+        h(f"{pad}      PG_CUDA(cudaStreamSynchronize(s));")
+        h(f"{pad}      if (*pcg_stop_h_) break;")
+        h(f"{pad}      if (it_ > (1L << 30)) throw Error(\"solve pcg did not stop\");")
+        h(f"{pad}    }}")
+        h(launch("apply", f"none_", "x_"))
+        h(f"{pad}    k_pcg_end<<<1, 1, 0, s>>>(pcg_state_, pp_.u_pcg_iterations);")
+        h(f"{pad}    count_launch();")
+        h(f"{pad}    count_launch();")
+        h(f"{pad}  }}")
+        for fname in self.written_fields(st):
+            h(f'{pad}  for (Group *pg : sel_{gsn}) pg->varying.at("{fname}").version++;')
+        h(f"{pad}}}")
+        self.uses_pcg = True
+
     def written_fields(self, loop):
         names = []
 
         def walk(stmts):
             for st in stmts:
-                if isinstance(st, Compute):
+                if hasattr(st, "body") and not isinstance(st, (ForeachNeighbor, Compute)) and \
+                        type(st).__name__.startswith("Solve"):
+                    walk(st.body)
+                elif isinstance(st, Compute):
                     t = st.target.subject if isinstance(st.target, Slice) else st.target
                     if isinstance(t, FieldAccess) and isinstance(t.ref, FieldDef) and t.ref.kind == "varying" \
                             and t.loop is loop and t.ref.name not in names:
                         names.append(t.ref.name)
                 elif isinstance(st, ForeachNeighbor):
                     walk(st.body)
-        walk(loop.body)
+        walk(loop.parts if isinstance(loop, Solve) else loop.body)
         return names
 
     def finalize_kernel(self, fk, k):
@@ -471,6 +565,19 @@ class Emitter:
             return
         gsn = self.gs(k.loop.groups)
         nb = "".join(f", {self.gs(gname)}_all nb_{_ident(gname)}" for gname in k.nb_groups)
+        if isinstance(k.loop, Solve):
+            S = k.solve_storage
+            w(f"__global__ void __launch_bounds__(kGenNT) {k.name}({gsn} p{nb}, Glob g, NbrView L, float *fr{dparams}, "
+              f"{S} *into_, {S} const *with_) {{")
+            w("  uint32_t i = blockIdx.x * kGenNT + threadIdx.x;")
+            w("  if (i >= p.n) return;")
+            w("  (void)into_;")
+            w("  (void)with_;")
+            for line in k.lines:
+                w(line)
+            w("}")
+            w("")
+            return
         w(f"__global__ void __launch_bounds__(kGenNT) {k.name}({gsn} p{nb}, Glob g, NbrView L, float *fr{dparams}, "
           f"double *red, uint32_t red_cap, uint32_t red_off) {{")
         w("  uint32_t i = blockIdx.x * kGenNT + threadIdx.x;")
@@ -504,6 +611,10 @@ class Emitter:
         w("  ~Scheme_() override {")
         w("    if (frame_) cudaFree(frame_);")
         w("    if (red_) cudaFree(red_);")
+        w("    if (pcg_buf_) cudaFree(pcg_buf_);")
+        w("    if (pcg_part_) cudaFree(pcg_part_);")
+        w("    if (pcg_state_) cudaFree(pcg_state_);")
+        w("    if (pcg_stop_h_) cudaFreeHost(pcg_stop_h_);")
         w("  }")
         w(f'  std::string name() const override {{ return "{self.full_short}"; }}')
         delim = "prtcl_source"
@@ -547,6 +658,31 @@ class Emitter:
         w("    red_cap_ = parts + parts / 4 + 64;")
         w(f"    PG_CUDA(cudaMalloc(&red_, size_t({max(1, self.max_red)}) * red_cap_ * sizeof(double)));")
         w("    (void)nred;")
+        w("  }")
+        w("  void *pcg_buf_ = nullptr;")
+        w("  size_t pcg_vec_bytes_ = 0;")
+        w("  double *pcg_part_ = nullptr;")
+        w("  uint32_t pcg_part_cap_ = 0;")
+        w("  PcgState *pcg_state_ = nullptr;")
+        w("  int *pcg_stop_h_ = nullptr;")
+        w("  // six solver vectors of `bytes` each, three partial-sum arrays of `parts` blocks")
+        w("  void ensure_pcg(size_t bytes, uint32_t parts) {")
+        w("    bytes = (bytes + 255) / 256 * 256;")
+        w("    if (bytes > pcg_vec_bytes_) {")
+        w("      if (pcg_buf_) PG_CUDA(cudaFree(pcg_buf_));")
+        w("      pcg_vec_bytes_ = bytes + bytes / 4;")
+        w("      PG_CUDA(cudaMalloc(&pcg_buf_, 6 * pcg_vec_bytes_));")
+        w("    }")
+        w("    if (parts > pcg_part_cap_) {")
+        w("      if (pcg_part_) PG_CUDA(cudaFree(pcg_part_));")
+        w("      pcg_part_cap_ = parts + parts / 4 + 64;")
+        w("      PG_CUDA(cudaMalloc(&pcg_part_, 3 * size_t(pcg_part_cap_) * sizeof(double)));")
+        w("    }")
+        w("    if (!pcg_state_) PG_CUDA(cudaMalloc(&pcg_state_, sizeof(PcgState)));")
+        w("    if (!pcg_stop_h_) PG_CUDA(cudaMallocHost(&pcg_stop_h_, sizeof(int)));")
+        w("  }")
+        w("  template <class S> S *pcg_vec(int k, uint32_t) const {")
+        w("    return reinterpret_cast<S *>(static_cast<char *>(pcg_buf_) + size_t(k) * pcg_vec_bytes_);")
         w("  }")
         w("  Glob glob() const {")
         w("    Glob r{};")

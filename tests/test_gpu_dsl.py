@@ -21,7 +21,7 @@ SRC = os.path.join(os.path.dirname(__file__), "dsl", "sph_test_schemes.prtcl")
 def generated(gpu_lib):
     from prtcl_gb300.dsl.build import compile_file
     names = compile_file(SRC)
-    assert len(names) == 9
+    assert len(names) == 11
     return names
 
 
@@ -148,6 +148,38 @@ def test_group_selectors(pair):
     d.run("t_selectors", "mark")
     np.testing.assert_array_equal(fld(d, "b", "volume", 1), v0 * np.float32(2))
     assert (fld(d, "b", "marker", 1) == 1).all()
+
+
+def test_wkbb18_pcg(pair):
+    """A generated solve pcg: WKBB18's implicit viscosity against the
+    oracle's FP64-mode solver, fields and iteration count exact."""
+    d, o, _ = pair
+    for m in (d, o):
+        m.run("density", "compute_density")
+        m.run("gravity", "initialize_acceleration")
+        m.run("symplectic_euler", "integrate_velocity_with_hard_fade")
+    d.run("t_wkbb18", "compute_diagonal")
+    o.run("wkbb18", "compute_diagonal")
+    assert_bitwise(fld(d, "f", "wkbb18_system_diagonal", 9), fld(o, "f", "wkbb18_system_diagonal", 9), "sp")
+    d.run("t_wkbb18", "accumulate_acceleration")
+    o.run("wkbb18", "accumulate_acceleration")
+    it = int(d.get_uniform("f", "wkbb18_iterations"))
+    assert it == int(o.get_uniform("f", "wkbb18_iterations")) and it >= 1
+    assert_bitwise(fld(d, "f", "wkbb18_velocity_delta", 3), fld(o, "f", "wkbb18_velocity_delta", 3), "vd")
+    assert_bitwise(fld(d, "f", "acceleration", 3), fld(o, "f", "acceleration", 3), "viscous accel")
+
+
+def test_scalar_pcg(pair):
+    d, _, sc = pair
+    n = len(sc["fluid"])
+    src = np.random.default_rng(2).standard_normal(n).astype(np.float32)
+    d.scheme("t_scalar_pcg")
+    d.set_varying("f", "scalar_source", src)
+    d.set_uniform("f", "scalar_pcg_error", 1e-6)
+    d.set_uniform("f", "scalar_pcg_iterations_max", 10)
+    d.run("t_scalar_pcg", "solve")
+    np.testing.assert_array_equal(fld(d, "f", "scalar_solution", 1), src * np.float32(0.5))
+    assert int(d.get_uniform("f", "scalar_pcg_iterations")) == 1
 
 
 def test_unknown_generated_procedure(generated, gpu_lib):
