@@ -56,6 +56,24 @@ def ctype(t: NDType) -> str:
     return "f3" if t.rank == 1 else "M3"
 
 
+def device_type_ok(t: NDType) -> bool:
+    try:
+        ctype(t)
+        return True
+    except DslError:
+        return False
+
+
+def _field_type_expr_any(t: NDType) -> str:
+    """FieldType of any declared type (fields the kernels cannot read are
+    still created at load, as the reference's Load does)."""
+    ct = "i32" if t.base == "integer" else "f32"
+    if t.rank == 0:
+        return f'parse_field_type("{ct}", 0, nullptr)'
+    ext = ", ".join(str(e or 3) for e in t.extents)
+    return f'[] {{ static int const e[] = {{{ext}}}; return parse_field_type("{ct}", {t.rank}, e); }}()'
+
+
 def _varying_member(t: NDType) -> str:
     c = ctype(t)
     return {"float": "float *", "int": "int *", "f3": "float4 *", "M3": "Planar9 "}[c]
@@ -124,6 +142,7 @@ class Emitter:
                     return f"frd<{ctype(r.type)}>(fr, {slot})"
                 return f"l_{_ident(r.name)}"
             if isinstance(r, FieldDef):
+                self.usable(r)
                 return f"rd(g.g_{_ident(r.alias)})"
             if isinstance(r, ForeachDimension):
                 return f"d_{_ident(r.index)}"
@@ -151,9 +170,15 @@ class Emitter:
             return f"vld({e.ref.kind}_, {idx})"
         var, idx = self.binding(e, ctx)
         f = e.ref
+        self.usable(f)
         if f.kind == "varying":
             return f"rd({var}.v_{_ident(f.alias)}, {idx})"
         return f"rd({var}.u_{_ident(f.alias)})"
+
+    def usable(self, f):
+        if not device_type_ok(f.type):
+            raise DslError(f"field {f.name} of type {f.type} cannot be used by the CUDA backend "
+                           "(it takes real, real[], real[][] and integer)")
 
     def binding(self, e, ctx):
         lp = e.loop
@@ -219,6 +244,7 @@ class Emitter:
         elif isinstance(tgt, FieldAccess):
             var, idx = self.binding(tgt, ctx)
             f = tgt.ref
+            self.usable(f)
             if f.kind == "varying":
                 read, write = f"rd({var}.v_{_ident(f.alias)}, {idx})", f"wr({var}.v_{_ident(f.alias)}, {idx}, {{}});"
             else:
@@ -231,6 +257,7 @@ class Emitter:
             else:
                 read, write = f"frd<{ty}>(fr, {slot})", f"fwr(fr, {slot}, {{}});"
         elif isinstance(tgt, NameRef) and isinstance(tgt.ref, FieldDef):
+            self.usable(tgt.ref)
             name = f"g.g_{_ident(tgt.ref.alias)}"
             read, write = f"rd({name})", f"wr({name}, {{}});"
         else:
@@ -523,6 +550,8 @@ class Emitter:
             w("  uint32_t n;")
             w("  int index;")
             for f in g.fields:
+                if not device_type_ok(f.type):
+                    continue  # created at load; no procedure may use it
                 if f.kind == "varying":
                     w(f"  {_varying_member(f.type)}v_{_ident(f.alias)};")
                 else:
@@ -534,7 +563,8 @@ class Emitter:
             w("};")
         w("struct Glob {")
         for f in self.s.globals:
-            w(f"  {_small_member(f.type)} g_{_ident(f.alias)};")
+            if device_type_ok(f.type):
+                w(f"  {_small_member(f.type)} g_{_ident(f.alias)};")
         w("  int unused_;")
         w("};")
         w("")
@@ -623,7 +653,7 @@ class Emitter:
         w(f'  std::string source() const override {{ return R"{delim}({src}){delim}"; }}')
         w("  void load(Model &m) override {")
         for f in self.s.globals:
-            w(f'    glob_{_ident(f.alias)}_ = &m.add_global("{f.name}", {_field_type_expr(f.type)});')
+            w(f'    glob_{_ident(f.alias)}_ = &m.add_global("{f.name}", {_field_type_expr_any(f.type)});')
         for g in self.s.groups:
             gs = _ident(g.name)
             w(f"    sel_{gs}.clear();")
@@ -635,7 +665,7 @@ class Emitter:
             w(f"        sel_{gs}.push_back(grp);")
             for f in g.fields:
                 fn = "add_varying" if f.kind == "varying" else "add_uniform"
-                w(f'        grp->{fn}("{f.name}", {_field_type_expr(f.type)});')
+                w(f'        grp->{fn}("{f.name}", {_field_type_expr_any(f.type)});')
             w("      }")
         w("    }")
         nslots = max(1, self.info.frame_slots)
@@ -687,6 +717,8 @@ class Emitter:
         w("  Glob glob() const {")
         w("    Glob r{};")
         for f in self.s.globals:
+            if not device_type_ok(f.type):
+                continue
             c = _small_member(f.type)
             base = "int" if c == "SInt" else "float"
             w(f"    r.g_{_ident(f.alias)} = {c}{{static_cast<{base} *>(model_->small_ptr(*glob_{_ident(f.alias)}_))}};")
@@ -701,6 +733,8 @@ class Emitter:
             w("    r.index = grp->index;")
             for f in g.fields:
                 a = _ident(f.alias)
+                if not device_type_ok(f.type):
+                    continue
                 if f.kind == "varying":
                     c = ctype(f.type)
                     w(f'    VaryingField &f_{a} = grp->varying.at("{f.name}");')
