@@ -560,13 +560,24 @@ __device__ __forceinline__ void visit_cell(GridView const &gv, float4 const *__r
                                            bool with_gf, uint32_t *buf) {
   if (cell < 0) return;
   int s0 = gv.cell_start[cell], s1 = gv.cell_start[cell + 1];
-  for (int s = s0; s < s1; ++s) {
-    float4 xj = xs[s];
-    float d2 = nsq3(sub3(xi, mk3(xj)));
-    if (d2 < gv.r2lt) { // == (double) d2 < r^2
+  // the distance tests of up to 32 candidates into a mask, then the
+  // accepted ones appended in candidate order: the append code runs once
+  // per hit of the lane with the most hits in the cell, not once per
+  // candidate on which any lane of the warp hits
+  for (int base = s0; base < s1; base += 32) {
+    int e = min(s1 - base, 32);
+    uint32_t mask = 0;
+    for (int t = 0; t < e; ++t) {
+      float d2 = nsq3(sub3(xi, mk3(xs[base + t])));
+      if (d2 < gv.r2lt) mask |= 1u << t; // == (double) d2 < r^2
+    }
+    while (mask) {
+      int t = __ffs(int(mask)) - 1;
+      mask &= mask - 1u;
+      float4 xj = xs[base + t];
       uint32_t h = __float_as_uint(xj.w);
       uint32_t g = h >> 28, j = h & 0x0FFFFFFFu;
-      float f = with_gf ? kgrad_factor(K, d2) : 0.0f;
+      float f = with_gf ? kgrad_factor(K, nsq3(sub3(xi, mk3(xj)))) : 0.0f;
 #pragma unroll
       for (int q = 0; q < NG; ++q)
         if (q == int(g)) row_add(lo, q, i, R[q], j, f, buf);
