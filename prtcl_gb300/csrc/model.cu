@@ -362,6 +362,8 @@ Segments::~Segments() {
     if (kv.second.seg) cudaFree(kv.second.seg);
     if (kv.second.tiles) cudaFree(kv.second.tiles);
     if (kv.second.slot_tiles) cudaFree(kv.second.slot_tiles);
+    if (kv.second.active) cudaFree(kv.second.active);
+    if (kv.second.nactive) cudaFree(kv.second.nactive);
   }
   for (void *p : {(void *)partials, (void *)tickets, (void *)scal, (void *)stat, (void *)stats, (void *)nprde,
                   (void *)iters, (void *)due})
@@ -430,9 +432,12 @@ void Segments::assign(Group const *g, std::vector<uint32_t> const &count, cudaSt
   if (tiles.size() + 1 > G.tile_cap || slots + 1 > G.tile_cap) {
     if (G.tiles) PG_CUDA(cudaFree(G.tiles));
     if (G.slot_tiles) PG_CUDA(cudaFree(G.slot_tiles));
+    if (G.active) PG_CUDA(cudaFree(G.active));
     G.tile_cap = std::max<size_t>(std::max(tiles.size(), size_t(slots)) + 1024, 4096);
     PG_CUDA(cudaMalloc(&G.tiles, G.tile_cap * sizeof(uint4)));
     PG_CUDA(cudaMalloc(&G.slot_tiles, G.tile_cap * sizeof(uint32_t)));
+    PG_CUDA(cudaMalloc(&G.active, G.tile_cap * sizeof(uint32_t)));
+    if (!G.nactive) PG_CUDA(cudaMalloc(&G.nactive, sizeof(uint32_t)));
   }
   G.ntiles = uint32_t(tiles.size());
   if (!tiles.empty())

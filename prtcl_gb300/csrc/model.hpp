@@ -98,6 +98,10 @@ struct SegGroup {
   uint4 *tiles = nullptr;          // device: (slot, begin, end, 0) of each tile of <= kSegTile items
   uint32_t ntiles = 0;
   uint32_t *slot_tiles = nullptr;  // device: tiles of slot s are [slot_tiles[s], slot_tiles[s + 1])
+  // device: the tiles of the slots whose solver loop still iterates (the
+  // first nactive[0] entries), rebuilt after each loop decision
+  uint32_t *active = nullptr;
+  uint32_t *nactive = nullptr;
   size_t seg_cap = 0, tile_cap = 0;
 };
 constexpr uint32_t kSegTile = 128; // items per reduction tile (one block)

@@ -151,18 +151,24 @@ struct SegArgs {
   double *stats;              // [slots][8]
   int const *nprde;           // [slots]
   int *iters;                 // [slots]
+  uint32_t *active;           // tiles of the slots still iterating ([nactive[0]])
+  uint32_t *nactive;
 };
 constexpr int kSegScal = 16, kSegStat = 8, kSegStats = 8;
+// blocks of the kernels that walk the active tiles (a multiple of the SM
+// count times the blocks resident per SM)
+constexpr uint32_t kActiveBlocks = 152 * 8;
 constexpr int kSsAprde = 8;        // scal: density error of the iteration
 constexpr int kStPcgEnded = 3;     // stat: the slot's PCG loop has ended
 
 template <int NV>
-__device__ bool seg_commit(double const (&v)[NV], SegArgs const &S, uint32_t slot, double (&out)[NV]) {
+__device__ bool seg_commit(double const (&v)[NV], SegArgs const &S, uint32_t slot, double (&out)[NV],
+                           uint32_t tile) {
   __shared__ double sh[32];
   __shared__ int last;
   for (int k = 0; k < NV; ++k) {
     double s = block_sum(v[k], sh);
-    if (threadIdx.x == 0) S.partials[k * S.pcap + blockIdx.x] = s;
+    if (threadIdx.x == 0) S.partials[k * S.pcap + tile] = s;
   }
   __threadfence();
   uint32_t t0 = S.slot_tiles[slot], t1 = S.slot_tiles[slot + 1];
@@ -180,6 +186,47 @@ __device__ bool seg_commit(double const (&v)[NV], SegArgs const &S, uint32_t slo
   if (threadIdx.x == 0) S.tickets[slot] = 0u;
   return true;
 }
+
+// The tiles of the slots whose Jacobi loop still iterates, in slot order
+// (one block, all threads): the Jacobi sweeps of a batched model walk this
+// list, so that the slots that have converged cost nothing in the
+// iterations that follow.
+__device__ void seg_list_active(SegArgs const &S) {
+  __shared__ uint32_t warp_tot[32];
+  __shared__ uint32_t base;
+  if (threadIdx.x == 0) base = 0;
+  __syncthreads();
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (uint32_t s0 = 0; s0 < S.slots; s0 += blockDim.x) {
+    uint32_t sl = s0 + threadIdx.x;
+    uint32_t t0 = 0, cnt = 0;
+    if (sl < S.slots && !S.stat[sl * kSegStat + kStJacDone]) {
+      t0 = S.slot_tiles[sl];
+      cnt = S.slot_tiles[sl + 1] - t0;
+    }
+    // block-exclusive prefix of the counts
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    if (lane == 31) warp_tot[w] = incl;
+    __syncthreads();
+    uint32_t wbase = 0, total = 0;
+    for (int k = 0; k < nw; ++k) {
+      if (k < w) wbase += warp_tot[k];
+      total += warp_tot[k];
+    }
+    uint32_t off = base + wbase + incl - cnt;
+    for (uint32_t j = 0; j < cnt; ++j) S.active[off + j] = t0 + j;
+    __syncthreads();
+    if (threadIdx.x == 0) base += total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *S.nactive = base;
+}
+__global__ void k_seg_active(SegArgs S) { seg_list_active(S); }
 
 // ---------------------------------------------------------------------------
 // density.compute_density (schemes/density.hpp:160-220)
@@ -364,20 +411,10 @@ __global__ void k_set_i32(int *p, int v) { *p = v; }
 
 // iisph.iteration_pressure_acceleration (schemes/iisph.hpp:358-423).
 // `done` (device-loop mode) skips the work once the loop has converged.
-// Batched models: `segid` / `segstat` skip the items of slots whose loop has
-// ended.
 template <int NF, int NB>
-__global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_accel(uint32_t n, float4 const *__restrict__ x, float const *__restrict__ p,
-                                                     float const *__restrict__ rho, float4 *__restrict__ a,
-                                                     float const *rho0p, Globals G, Nbrs<NF, NB> N,
-                                                     int const *done, uint16_t const *segid, int const *segstat) {
-  if (done && *(volatile int const *)done) return;
-  uint32_t i = grid_tid();
-  if (i >= n) return;
-  if (segid && segstat[segid[i] * kSegStat + kStJacDone]) return;
-  KernelParams K = kparams(*G.h);
-  bool uc = use_cache(N, K);
-  float rho0 = *rho0p;
+__device__ __forceinline__ void iisph_accel_item(uint32_t i, float4 const *__restrict__ x, float const *__restrict__ p,
+                                                 float const *__restrict__ rho, float4 *__restrict__ a,
+                                                 KernelParams const &K, bool uc, float rho0, Nbrs<NF, NB> const &N) {
   f3 xi = mk3(x[i]);
   float pi = p[i], ri = rho[i];
   float pri = pi / (ri * ri);
@@ -403,6 +440,31 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_accel(uint32_t n, flo
     });
   }
   a[i] = make_float4(acc.x, acc.y, acc.z, 0.0f);
+}
+template <int NF, int NB>
+__global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_accel(uint32_t n, float4 const *__restrict__ x, float const *__restrict__ p,
+                                                     float const *__restrict__ rho, float4 *__restrict__ a,
+                                                     float const *rho0p, Globals G, Nbrs<NF, NB> N, int const *done) {
+  if (done && *(volatile int const *)done) return;
+  uint32_t i = grid_tid();
+  if (i >= n) return;
+  KernelParams K = kparams(*G.h);
+  iisph_accel_item<NF, NB>(i, x, p, rho, a, K, use_cache(N, K), *rho0p, N);
+}
+// batched models: the tiles of the slots still iterating
+template <int NF, int NB>
+__global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_accel_seg(float4 const *__restrict__ x, float const *__restrict__ p,
+                                                         float const *__restrict__ rho, float4 *__restrict__ a,
+                                                         float const *rho0p, Globals G, Nbrs<NF, NB> N, SegArgs S) {
+  KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
+  float rho0 = *rho0p;
+  uint32_t na = *S.nactive;
+  for (uint32_t t = blockIdx.x; t < na; t += gridDim.x) {
+    uint4 T = S.tiles[S.active[t]];
+    uint32_t i = T.y + threadIdx.x;
+    if (i < T.z) iisph_accel_item<NF, NB>(i, x, p, rho, a, K, uc, rho0, N);
+  }
 }
 
 // iisph.iteration_pressure (schemes/iisph.hpp:426-516) with the FP64
@@ -475,16 +537,19 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_pressure(uint32_t n, 
 // each slot's iteration goes to scal[slot][kSsAprde]
 template <int NF, int NB>
 __global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_pressure_seg(PressureArgs A, Globals G, Nbrs<NF, NB> N, SegArgs S) {
-  uint4 T = S.tiles[blockIdx.x];
-  uint32_t slot = T.x;
-  if (S.stat[slot * kSegStat + kStJacDone]) return; // the whole block: one slot
+  // one active tile per block (the hardware's block scheduling balances the
+  // tiles' uneven costs); the blocks past the active tiles exit at once
+  if (blockIdx.x >= *S.nactive) return;
   KernelParams K = kparams(*G.h);
   bool uc = use_cache(N, K);
   float rho0 = *A.rho0, dt = *G.dt, omega = *G.omega;
+  uint32_t t = S.active[blockIdx.x];
+  uint4 T = S.tiles[t];
+  uint32_t slot = T.x;
   uint32_t i = T.y + threadIdx.x;
   double part = (i < T.z) ? iisph_pressure_item<NF, NB>(i, A, K, uc, rho0, dt, omega, N) : 0.0;
   double v[1] = {part}, out[1];
-  if (seg_commit<1>(v, S, slot, out) && threadIdx.x == 0) S.scal[slot * kSegScal + kSsAprde] = out[0];
+  if (seg_commit<1>(v, S, slot, out, t) && threadIdx.x == 0) S.scal[slot * kSegScal + kSsAprde] = out[0];
 }
 
 // per-slot loop start: a slot without fluid items does not iterate
@@ -526,6 +591,7 @@ __global__ void k_seg_jacobi_control(Globals G, SegArgs S, cudaGraphConditionalH
     any |= !done;
   }
   any = __syncthreads_or(any);
+  if (any) seg_list_active(S);
   if (threadIdx.x == 0) {
     *all_done = any ? 0 : 1;
     if (kernels) atomicAdd(&g_loop_kernels, (unsigned long long)kernels);
@@ -958,7 +1024,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_init_seg(PcgArgs P, Glo
   uint32_t i = T.y + threadIdx.x;
   if (i < T.z) pcg_init_item<NB, GC>(P, K, uc, dt, rho0, mu, N, i, bb, rr, ry);
   double v[3] = {bb, rr, ry}, out[3];
-  if (seg_commit<3>(v, S, slot, out) && threadIdx.x == 0) {
+  if (seg_commit<3>(v, S, slot, out, blockIdx.x) && threadIdx.x == 0) {
     int *st = S.stat + slot * kSegStat;
     pcg_init_scalars(S.scal + slot * kSegScal, st, out, *P.tol);
     st[kStPcgEnded] = 0;
@@ -975,7 +1041,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_q_seg(PcgArgs P, Global
   float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
   uint32_t i = T.y + threadIdx.x;
   double v[1] = {(i < T.z) ? pcg_q_item<NB, GC>(P, K, uc, dt, rho0, mu, N, i) : 0.0}, out[1];
-  if (seg_commit<1>(v, S, slot, out) && threadIdx.x == 0)
+  if (seg_commit<1>(v, S, slot, out, blockIdx.x) && threadIdx.x == 0)
     pcg_q_scalars(S.scal + slot * kSegScal, S.stat + slot * kSegStat, out[0], *P.tol);
 }
 
@@ -988,7 +1054,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_update_seg(PcgArgs P, S
   uint32_t i = T.y + threadIdx.x;
   if (i < T.z) pcg_update_item(P, alpha, i, rr, ry);
   double v[2] = {rr, ry}, out[2];
-  if (seg_commit<2>(v, S, slot, out) && threadIdx.x == 0)
+  if (seg_commit<2>(v, S, slot, out, blockIdx.x) && threadIdx.x == 0)
     pcg_update_scalars(S.scal + slot * kSegScal, S.stat + slot * kSegStat, out[0], out[1], *P.tol, *P.max_k);
 }
 
@@ -1253,6 +1319,8 @@ protected:
     a.stats = S.stats;
     a.nprde = S.nprde;
     a.iters = S.iters;
+    a.active = G->active;
+    a.nactive = G->nactive;
     return a;
   }
 
@@ -1587,8 +1655,12 @@ public:
         return;
       }
       if (prof) S->model_->prof.begin("iisph_accel", s);
-      k_iisph_accel<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, x, p, rho, a, rho0, G, N, done, SA ? SA->seg : nullptr,
-                                                           SA ? SA->stat : nullptr);
+      if (SA) {
+        if (SA->ntiles)
+          k_iisph_accel_seg<NF, NB><<<std::min(SA->ntiles, kActiveBlocks), kNT, 0, s>>>(x, p, rho, a, rho0, G, N, *SA);
+      } else {
+        k_iisph_accel<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, x, p, rho, a, rho0, G, N, done);
+      }
       count_launch();
       if (prof) S->model_->prof.end(s);
     }
@@ -1723,6 +1795,7 @@ public:
       if (B.g->count) model_->packed_xs(B.g, B.x, B.V, "xV", s);
     if (seg) {
       k_seg_jacobi_begin<<<div_up(std::max<uint32_t>(SA.slots, 1), 256), 256, 0, s>>>(SA); count_launch();
+      k_seg_active<<<1, 1024, 0, s>>>(SA); count_launch();
       k_set_i32<<<1, 1, 0, s>>>(R.status + kStJacDone, 0); count_launch();
     } else {
       k_jacobi_begin<<<1, 1, 0, s>>>(G, R); count_launch();
