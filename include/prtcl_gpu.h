@@ -298,6 +298,76 @@ int prtcl_gpu_batch_profile_enable(prtcl_gpu_batch *batch, int32_t enable);
 /* Per-kernel timing lines "name launches total_ms", as prtcl_gpu_profile_read. */
 int prtcl_gpu_batch_profile_read(prtcl_gpu_batch *batch, char *buf, int64_t size, int64_t *needed_out);
 
+/* ---- Serving: continuous batching of simulation requests ----------------
+ * The reference runs one scene per process (share/scripts/prtcl-lua.example.lua);
+ * a server keeps every admitted request resident in one batch and advances
+ * them together, one step per turn.  A turn:
+ *   1. admits the submitted requests whose arrival time has come, in arrival
+ *      order (ties in submission order), while a scene slot is free and the
+ *      batch's device bytes plus the request's estimate (its particles times
+ *      the largest bytes per particle seen so far) stay within the budget; a
+ *      request is always admitted when nothing is resident;
+ *   2. steps every resident scene once;
+ *   3. retires, in admission order, the requests that have taken all their
+ *      steps: their scene information and (keep_results) final fluid
+ *      positions are kept until read with prtcl_gpu_server_next_result.
+ * Every scene converges on its own, so a request's result is the same, bit
+ * for bit, alone and in the mix.  Times are seconds on the server's clock. */
+typedef struct prtcl_gpu_server prtcl_gpu_server;
+typedef double (*prtcl_gpu_clock_fn)(void *user);
+typedef struct prtcl_gpu_server_params {
+  double budget_bytes;               /* admission limit on the batch's device bytes */
+  int32_t max_scenes;                /* resident requests at most (>= 1) */
+  int32_t keep_results;              /* nonzero: keep each request's final fluid positions */
+  double bytes_per_particle;         /* admission estimate until the batch holds a scene */
+  prtcl_gpu_clock_fn clock;          /* NULL: a steady clock started at creation */
+  void *clock_user;
+} prtcl_gpu_server_params;
+/* The batch a server drives, supplied by the caller
+ * (prtcl_gpu_server_create_custom): each operation returns 0 on success. */
+typedef struct prtcl_gpu_server_batch_ops {
+  int (*add_scene)(void *user, const float *fluid_xyz, int64_t fluid_count, const float *boundary_xyz,
+                   int64_t boundary_count, int64_t *scene_id_out);
+  int (*remove_scene)(void *user, int64_t scene_id);
+  int (*step)(void *user, int32_t steps);
+  int (*synchronize)(void *user);
+  int (*device_bytes)(void *user, int64_t *bytes_out);
+  int (*scene_info)(void *user, int64_t scene_id, prtcl_gpu_scene_info *out);
+  int (*download_positions)(void *user, int64_t scene_id, float *host_xyz, int64_t count);
+} prtcl_gpu_server_batch_ops;
+typedef struct prtcl_gpu_request_result {
+  int64_t request_id;
+  int64_t fluid, boundary, steps;
+  double arrival, admitted, finished;
+  prtcl_gpu_scene_info info;         /* the scene's information at retirement */
+} prtcl_gpu_request_result;
+typedef struct prtcl_gpu_server_status {
+  int64_t pending, running, results; /* submitted, resident, retired and not yet read */
+  int64_t steps_run, particle_steps; /* turns that stepped; fluid particles x steps */
+  int64_t held_bytes;                /* the batch's device bytes at the last admission or retirement */
+  double next_arrival;               /* of the first pending request; +inf when none */
+} prtcl_gpu_server_status;
+
+/* A server over a batch of its own (prtcl_gpu_batch_create with `batch`). */
+int prtcl_gpu_server_create(const prtcl_gpu_batch_params *batch, const prtcl_gpu_server_params *params,
+                            prtcl_gpu_server **out);
+/* A server over a caller's batch; `ops` and `user` must outlive the server. */
+int prtcl_gpu_server_create_custom(const prtcl_gpu_server_batch_ops *ops, void *user,
+                                   const prtcl_gpu_server_params *params, prtcl_gpu_server **out);
+int prtcl_gpu_server_destroy(prtcl_gpu_server *server);
+/* Queue a request (its particles are copied); request ids are the caller's. */
+int prtcl_gpu_server_submit(prtcl_gpu_server *server, int64_t request_id, double arrival, const float *fluid_xyz,
+                            int64_t fluid_count, const float *boundary_xyz, int64_t boundary_count, int64_t steps);
+/* One turn; *stepped_out = 1 if the resident scenes were stepped, 0 if
+ * nothing was resident (wait for status.next_arrival). */
+int prtcl_gpu_server_turn(prtcl_gpu_server *server, int32_t *stepped_out);
+int prtcl_gpu_server_status_get(prtcl_gpu_server *server, prtcl_gpu_server_status *out);
+/* The oldest unread result (*has_out = 0 when there is none).  Its final
+ * fluid positions are copied to `positions_xyz` (NULL: not copied; otherwise
+ * `capacity` >= the request's fluid count, in particles). */
+int prtcl_gpu_server_next_result(prtcl_gpu_server *server, prtcl_gpu_request_result *out, float *positions_xyz,
+                                 int64_t capacity, int32_t *has_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -11,6 +11,7 @@
 
 #include "prtcl_gpu.h"
 
+#include <algorithm>
 #include <array>
 #include <cstdint>
 #include <memory>
@@ -242,6 +243,93 @@ inline SchemeRegistry &GetSchemeRegistry() {
   static SchemeRegistry r;
   return r;
 }
+
+// Batched scenes (prtcl_gpu_batch_*): no reference counterpart; the
+// reference runs one scene per process.
+class Batch {
+public:
+  explicit Batch(prtcl_gpu_batch_params const &p) { check(prtcl_gpu_batch_create(&p, &b_)); }
+  ~Batch() { prtcl_gpu_batch_destroy(b_); }
+  Batch(Batch const &) = delete;
+  Batch &operator=(Batch const &) = delete;
+
+  int64_t AddScene(std::vector<float> const &fluid_xyz, std::vector<float> const &boundary_xyz) {
+    int64_t id = 0;
+    check(prtcl_gpu_batch_add_scene(b_, fluid_xyz.data(), int64_t(fluid_xyz.size() / 3), boundary_xyz.data(),
+                                    int64_t(boundary_xyz.size() / 3), &id));
+    return id;
+  }
+  void RemoveScene(int64_t id) { check(prtcl_gpu_batch_remove_scene(b_, id)); }
+  void Step(int32_t steps = 1) { check(prtcl_gpu_batch_step(b_, steps)); }
+  void Synchronize() { check(prtcl_gpu_batch_synchronize(b_)); }
+  prtcl_gpu_scene_info Info(int64_t id) {
+    prtcl_gpu_scene_info s{};
+    check(prtcl_gpu_batch_scene_info(b_, id, &s));
+    return s;
+  }
+  std::vector<float> Positions(int64_t id) {
+    prtcl_gpu_scene_info s = Info(id);
+    std::vector<float> x(size_t(s.fluid) * 3);
+    check(prtcl_gpu_batch_download(b_, id, "position", x.data(), s.fluid));
+    return x;
+  }
+  prtcl_gpu_batch *handle() { return b_; }
+
+private:
+  prtcl_gpu_batch *b_ = nullptr;
+};
+
+// The serving loop (prtcl_gpu_server_*) over a batch of its own.
+class Server {
+public:
+  struct Result {
+    prtcl_gpu_request_result r;
+    std::vector<float> positions; // empty unless keep_results
+  };
+  Server(prtcl_gpu_batch_params const &batch, prtcl_gpu_server_params const &p) : keep_(p.keep_results != 0) {
+    check(prtcl_gpu_server_create(&batch, &p, &s_));
+  }
+  ~Server() { prtcl_gpu_server_destroy(s_); }
+  Server(Server const &) = delete;
+  Server &operator=(Server const &) = delete;
+
+  void Submit(int64_t request_id, double arrival, std::vector<float> const &fluid_xyz,
+              std::vector<float> const &boundary_xyz, int64_t steps) {
+    check(prtcl_gpu_server_submit(s_, request_id, arrival, fluid_xyz.data(), int64_t(fluid_xyz.size() / 3),
+                                  boundary_xyz.data(), int64_t(boundary_xyz.size() / 3), steps));
+    max_fluid_ = std::max<int64_t>(max_fluid_, int64_t(fluid_xyz.size() / 3));
+  }
+  // one turn; false when nothing was resident
+  bool Turn() {
+    int32_t stepped = 0;
+    check(prtcl_gpu_server_turn(s_, &stepped));
+    return stepped != 0;
+  }
+  prtcl_gpu_server_status Status() {
+    prtcl_gpu_server_status st{};
+    check(prtcl_gpu_server_status_get(s_, &st));
+    return st;
+  }
+  // the retired requests not yet read, oldest first
+  std::vector<Result> TakeResults() {
+    std::vector<Result> out;
+    std::vector<float> buf(keep_ ? size_t(max_fluid_) * 3 : 0);
+    for (;;) {
+      Result r{};
+      int32_t has = 0;
+      check(prtcl_gpu_server_next_result(s_, &r.r, keep_ ? buf.data() : nullptr, keep_ ? max_fluid_ : 0, &has));
+      if (!has) break;
+      if (keep_) r.positions.assign(buf.begin(), buf.begin() + size_t(r.r.fluid) * 3);
+      out.push_back(std::move(r));
+    }
+    return out;
+  }
+
+private:
+  prtcl_gpu_server *s_ = nullptr;
+  bool keep_;
+  int64_t max_fluid_ = 0;
+};
 
 } // namespace prtcl_gpu
 

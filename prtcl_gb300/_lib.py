@@ -105,6 +105,13 @@ SIGNATURES = {
     "prtcl_gpu_batch_device_bytes": [vp, i64p],
     "prtcl_gpu_batch_profile_enable": [vp, i32],
     "prtcl_gpu_batch_profile_read": [vp, C.c_char_p, i64, i64p],
+    "prtcl_gpu_server_create": [vp, vp, pp],
+    "prtcl_gpu_server_create_custom": [vp, vp, vp, pp],
+    "prtcl_gpu_server_destroy": [vp],
+    "prtcl_gpu_server_submit": [vp, i64, dbl, vp, i64, vp, i64, i64],
+    "prtcl_gpu_server_turn": [vp, i32p],
+    "prtcl_gpu_server_status_get": [vp, vp],
+    "prtcl_gpu_server_next_result": [vp, vp, vp, i64, i32p],
 }
 
 
@@ -124,6 +131,43 @@ class SceneInfo(C.Structure):
                 ("last_relative_density_error", C.c_double), ("max_relative_density_error", C.c_double),
                 ("jacobi_solves", C.c_double), ("jacobi_iterations", C.c_double), ("jacobi_capped", C.c_double),
                 ("pcg_solves", C.c_double), ("pcg_iterations", C.c_double), ("pcg_capped", C.c_double)]
+
+
+CLOCK_FN = C.CFUNCTYPE(C.c_double, C.c_void_p)
+
+
+class ServerParams(C.Structure):
+    """prtcl_gpu_server_params"""
+    _fields_ = [("budget_bytes", C.c_double), ("max_scenes", C.c_int32), ("keep_results", C.c_int32),
+                ("bytes_per_particle", C.c_double), ("clock", CLOCK_FN), ("clock_user", C.c_void_p)]
+
+
+class ServerBatchOps(C.Structure):
+    """prtcl_gpu_server_batch_ops"""
+    _fields_ = [
+        ("add_scene", C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_float), C.c_int64, C.POINTER(C.c_float),
+                                  C.c_int64, C.POINTER(C.c_int64))),
+        ("remove_scene", C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int64)),
+        ("step", C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int32)),
+        ("synchronize", C.CFUNCTYPE(C.c_int, C.c_void_p)),
+        ("device_bytes", C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_int64))),
+        ("scene_info", C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int64, C.POINTER(SceneInfo))),
+        ("download_positions", C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int64, C.POINTER(C.c_float), C.c_int64)),
+    ]
+
+
+class RequestResult(C.Structure):
+    """prtcl_gpu_request_result"""
+    _fields_ = [("request_id", C.c_int64), ("fluid", C.c_int64), ("boundary", C.c_int64), ("steps", C.c_int64),
+                ("arrival", C.c_double), ("admitted", C.c_double), ("finished", C.c_double), ("info", SceneInfo)]
+
+
+class ServerStatus(C.Structure):
+    """prtcl_gpu_server_status"""
+    _fields_ = [("pending", C.c_int64), ("running", C.c_int64), ("results", C.c_int64), ("steps_run", C.c_int64),
+                ("particle_steps", C.c_int64), ("held_bytes", C.c_int64), ("next_arrival", C.c_double)]
+
+
 _RESTYPE = {"prtcl_gpu_last_error": cp, "prtcl_gpu_version": cp, "prtcl_gpu_launch_count": C.c_uint64}
 
 _lock = threading.Lock()

@@ -17,7 +17,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libprtcl_gpu.so")
-SOURCES = ["model.cu", "nhood.cu", "schemes.cu", "capi.cu", "noalloc.cu", "batch.cu", "archive.cu", "vtk.cu"]
+SOURCES = ["model.cu", "nhood.cu", "schemes.cu", "capi.cu", "noalloc.cu", "batch.cu", "server.cu", "archive.cu",
+           "vtk.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
          "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]

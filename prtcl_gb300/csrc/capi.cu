@@ -2,6 +2,7 @@
 #include "../../include/prtcl_gpu.h"
 #include "batch.hpp"
 #include "schemes.hpp"
+#include "server.hpp"
 
 #include <atomic>
 #include <dlfcn.h>
@@ -22,6 +23,9 @@ struct prtcl_gpu_scheme {
 };
 struct prtcl_gpu_batch {
   std::unique_ptr<Batch> b;
+};
+struct prtcl_gpu_server {
+  std::unique_ptr<Server> s;
 };
 
 namespace prtcl_gpu {
@@ -582,6 +586,65 @@ int prtcl_gpu_batch_profile_read(prtcl_gpu_batch *batch, char *buf, int64_t size
   });
   if (rc != PRTCL_GPU_OK) return rc;
   return write_str(text, buf, size, needed_out);
+}
+
+int prtcl_gpu_server_create(const prtcl_gpu_batch_params *batch, const prtcl_gpu_server_params *params,
+                            prtcl_gpu_server **out) {
+  NEED(batch);
+  NEED(params);
+  NEED(out);
+  *out = nullptr;
+  return guard([&] {
+    auto s = std::make_unique<prtcl_gpu_server>();
+    s->s = std::make_unique<Server>(device_serve_batch(*batch), *params);
+    *out = s.release();
+  });
+}
+int prtcl_gpu_server_create_custom(const prtcl_gpu_server_batch_ops *ops, void *user,
+                                   const prtcl_gpu_server_params *params, prtcl_gpu_server **out) {
+  NEED(ops);
+  NEED(params);
+  NEED(out);
+  *out = nullptr;
+  return guard([&] {
+    auto s = std::make_unique<prtcl_gpu_server>();
+    s->s = std::make_unique<Server>(callback_serve_batch(*ops, user), *params);
+    *out = s.release();
+  });
+}
+int prtcl_gpu_server_destroy(prtcl_gpu_server *server) {
+  delete server;
+  return PRTCL_GPU_OK;
+}
+int prtcl_gpu_server_submit(prtcl_gpu_server *server, int64_t request_id, double arrival, const float *fluid_xyz,
+                            int64_t fluid_count, const float *boundary_xyz, int64_t boundary_count, int64_t steps) {
+  NEED(server);
+  if (fluid_count < 0 || boundary_count < 0) return fail(PRTCL_GPU_INVALID, "invalid argument: negative count");
+  if (steps < 1) return fail(PRTCL_GPU_INVALID, "invalid argument: a request needs at least one step");
+  return guard([&] {
+    server->s->submit(request_id, arrival, fluid_xyz, size_t(fluid_count), boundary_xyz, size_t(boundary_count),
+                      steps);
+  });
+}
+int prtcl_gpu_server_turn(prtcl_gpu_server *server, int32_t *stepped_out) {
+  NEED(server);
+  return guard([&] {
+    bool stepped = server->s->turn();
+    if (stepped_out) *stepped_out = stepped ? 1 : 0;
+  });
+}
+int prtcl_gpu_server_status_get(prtcl_gpu_server *server, prtcl_gpu_server_status *out) {
+  NEED(server);
+  NEED(out);
+  return guard([&] { *out = server->s->status(); });
+}
+int prtcl_gpu_server_next_result(prtcl_gpu_server *server, prtcl_gpu_request_result *out, float *positions_xyz,
+                                 int64_t capacity, int32_t *has_out) {
+  NEED(server);
+  NEED(out);
+  NEED(has_out);
+  if (capacity < 0) return fail(PRTCL_GPU_INVALID, "invalid argument: negative capacity");
+  return guard([&] { *has_out = server->s->next_result(*out, positions_xyz, size_t(capacity)) ? 1 : 0; });
 }
 
 } // extern "C"

@@ -10,11 +10,14 @@ a slot is free, and retires the requests that have taken all their steps
 scene converges on its own and its neighbour order does not depend on the
 other scenes, a request's result is the same alone and in the mix.
 
-The batch is injected (``batch_factory``), so the scheduling logic runs on
-the CPU against a stand-in in the tests.
+The loop itself is native (``prtcl_gpu_server_*``, csrc/server.cu); this
+module submits requests as they arrive, turns the server and collects the
+results.  The batch is injected (``batch_factory``), so the scheduling logic
+runs on the CPU against a stand-in in the tests.
 """
 from __future__ import annotations
 
+import ctypes as C
 import math
 import time
 from collections import deque
@@ -77,75 +80,170 @@ def poisson_requests(count, rate, seed=4, lo=5000, hi=500000, steps=(100, 1000))
 
 
 class Server:
-    """``budget_bytes``: device bytes the batch may hold (admission limit);
-    ``bytes_per_particle``: estimate for a request not yet admitted, replaced
-    by the batch's measured bytes per particle once it holds scenes."""
+    """The native serving loop (``prtcl_gpu_server_*``) driven from Python.
+
+    ``batch_factory``: ``prtcl_gb300.batch.Batch`` (or None) serves on the
+    device through the server's own batch; any other factory's object (the
+    batch interface: add_scene, remove_scene, step, synchronize,
+    device_bytes, info, download) is driven through callbacks, so the
+    scheduling runs on the CPU against a stand-in in the tests.
+    ``budget_bytes``: device bytes the batch may hold (admission limit);
+    ``bytes_per_particle``: estimate for a request not yet admitted,
+    replaced by the batch's measured bytes per particle once it holds
+    scenes.  ``clock`` / ``sleep`` give the server its time (seconds)."""
 
     def __init__(self, batch_factory, params, budget_bytes=120e9, max_scenes=4096, bytes_per_particle=1000.0,
                  clock=time.perf_counter, sleep=time.sleep, keep_results=True):
-        self.batch = batch_factory(params)
-        self.budget = float(budget_bytes)
-        self.max_scenes = int(max_scenes)
-        self.bpp = float(bytes_per_particle)
+        from ._lib import CLOCK_FN, ServerParams, check, load
+        from .batch import Batch, params_struct
         self.clock, self.sleep = clock, sleep
         self.keep_results = keep_results
         self.steps_run = 0
         self.particle_steps = 0
+        self.makespan = 0.0
+        self._t0 = clock()
+        self._error = None
+        self._clock_fn = CLOCK_FN(lambda _user: self.clock() - self._t0)
+        sp = ServerParams()
+        sp.budget_bytes = float(budget_bytes)
+        sp.max_scenes = int(max_scenes)
+        sp.keep_results = 1 if keep_results else 0
+        sp.bytes_per_particle = float(bytes_per_particle)
+        sp.clock = self._clock_fn
+        sp.clock_user = None
+        h = C.c_void_p()
+        if batch_factory is None or batch_factory is Batch:
+            self.batch = None
+            check(load().prtcl_gpu_server_create(C.byref(params_struct(params)), C.byref(sp), C.byref(h)))
+        else:
+            self.batch = batch_factory(params)
+            self._ops = self._callback_ops(self.batch)
+            check(load().prtcl_gpu_server_create_custom(C.byref(self._ops), None, C.byref(sp), C.byref(h)))
+        self._h = h
 
-    def _estimate(self, req, scene):
-        return (len(scene["fluid"]) + len(scene["boundary"])) * self.bpp
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            from ._lib import load
+            load().prtcl_gpu_server_destroy(h)
+            self._h = None
+
+    def _callback_ops(self, bt):
+        """prtcl_gpu_server_batch_ops over a Python batch object; an exception
+        in a callback fails the operation and is raised after the call."""
+        from ._lib import SceneInfo, ServerBatchOps
+
+        def guarded(fn):
+            def call(*a):
+                try:
+                    fn(*a)
+                    return 0
+                except BaseException as e:  # re-raised by _call
+                    self._error = e
+                    return 1
+            return call
+
+        def xyz(ptr, n):
+            return np.ctypeslib.as_array(ptr, shape=(n, 3)).copy() if n else np.zeros((0, 3), np.float32)
+
+        def add_scene(_u, f, nf, b, nb, out):
+            out[0] = int(bt.add_scene(xyz(f, nf), xyz(b, nb)))
+
+        def scene_info(_u, sid, out):
+            d = bt.info(sid)
+            for k, t in SceneInfo._fields_:
+                if k in d:
+                    setattr(out.contents, k, int(d[k]) if t in (C.c_int32, C.c_int64) else float(d[k]))
+
+        def download(_u, sid, host, n):
+            if n:
+                np.ctypeslib.as_array(host, shape=(n, 3))[:] = bt.download(sid, "position")
+
+        def device_bytes(_u, out):
+            out[0] = int(bt.device_bytes())
+
+        T = dict(ServerBatchOps._fields_)
+        return ServerBatchOps(
+            add_scene=T["add_scene"](guarded(add_scene)),
+            remove_scene=T["remove_scene"](guarded(lambda _u, sid: bt.remove_scene(sid))),
+            step=T["step"](guarded(lambda _u, k: bt.step(k))),
+            synchronize=T["synchronize"](guarded(lambda _u: bt.synchronize())),
+            device_bytes=T["device_bytes"](guarded(device_bytes)),
+            scene_info=T["scene_info"](guarded(scene_info)),
+            download_positions=T["download_positions"](guarded(download)))
+
+    def _call(self, fn, *args):
+        from ._lib import check
+        self._error = None
+        rc = fn(self._h, *args)
+        if self._error is not None:
+            e, self._error = self._error, None
+            raise e
+        check(rc)
+
+    def _status(self):
+        from ._lib import ServerStatus, load
+        st = ServerStatus()
+        self._call(load().prtcl_gpu_server_status_get, C.byref(st))
+        return st
 
     def run(self, requests):
+        """Serve ``requests`` (each submitted when its arrival time has come)
+        until all are done; returns them in retirement order."""
+        from ._lib import RequestResult, load
+        L = load()
+        self._t0 = self.clock()
         pending = deque(sorted(requests, key=lambda r: r.arrival))
-        running = {}
+        inflight = {}
         done = []
-        held = 0.0
-        t0 = self.clock()
-        while pending or running:
-            now = self.clock() - t0
-            # admit in arrival order while the budget and the slots allow
-            while pending and pending[0].arrival <= now and len(running) < self.max_scenes:
-                req = pending[0]
+        buf = np.empty((0, 3), np.float32)
+        res = RequestResult()
+        has = C.c_int32(0)
+        stepped = C.c_int32(0)
+        while True:
+            now = self.clock() - self._t0
+            while pending and pending[0].arrival <= now:
+                req = pending.popleft()
                 sc = req.scene()
-                need = self._estimate(req, sc)
-                # (a request alone is always admitted, even above the budget)
-                if running and held + need > self.budget:
-                    break
-                pending.popleft()
-                sid = self.batch.add_scene(sc["fluid"], sc["boundary"])
+                f = np.ascontiguousarray(sc["fluid"], np.float32).reshape(-1, 3)
+                bd = np.ascontiguousarray(sc["boundary"], np.float32).reshape(-1, 3)
+                key = len(done) + len(inflight)
+                while key in inflight:
+                    key += 1
+                self._call(L.prtcl_gpu_server_submit, key, float(req.arrival), f.ctypes.data, len(f),
+                           bd.ctypes.data, len(bd), int(req.steps))
+                req.fluid, req.boundary = len(f), len(bd)
                 req.release()
-                req.admitted = now
-                req.fluid, req.boundary = len(sc["fluid"]), len(sc["boundary"])
-                running[sid] = req
-                held = float(self.batch.device_bytes())
-                nparts = sum(r.fluid + r.boundary for r in running.values())
-                if nparts:
-                    self.bpp = max(self.bpp, held / nparts)
-            if not running:
-                if pending:
-                    self.sleep(max(0.0, pending[0].arrival - (self.clock() - t0)))
-                continue
-            self.batch.step(1)
-            self.steps_run += 1
-            self.particle_steps += sum(r.fluid for r in running.values())
-            finished = []
-            for sid, req in running.items():
-                req.done_steps += 1
-                if req.done_steps >= req.steps:
-                    finished.append(sid)
-            for sid in finished:
-                req = running.pop(sid)
-                req.info = self.batch.info(sid)
+                inflight[key] = req
+            st = self._status()
+            if not pending and st.pending == 0 and st.running == 0 and st.results == 0:
+                break
+            self._call(L.prtcl_gpu_server_turn, C.byref(stepped))
+            if self.keep_results and inflight:
+                need = max(r.fluid for r in inflight.values())
+                if len(buf) < need:
+                    buf = np.empty((need, 3), np.float32)
+            while True:
+                self._call(L.prtcl_gpu_server_next_result, C.byref(res),
+                           buf.ctypes.data if self.keep_results else None, len(buf), C.byref(has))
+                if not has.value:
+                    break
+                req = inflight.pop(res.request_id)
+                req.admitted, req.finished = res.admitted, res.finished
+                req.done_steps = int(res.steps)
+                req.info = {k: getattr(res.info, k) for k, _ in res.info._fields_ if k != "pad"}
                 if self.keep_results:
-                    req.result = self.batch.download(sid, "position")
-                else:
-                    self.batch.synchronize()
-                req.finished = self.clock() - t0
-                self.batch.remove_scene(sid)
+                    req.result = buf[:req.fluid].copy()
                 done.append(req)
-            if finished:
-                held = float(self.batch.device_bytes()) if running else 0.0
-        self.makespan = self.clock() - t0
+            if not stepped.value:
+                # nothing resident: wait for the next arrival
+                st = self._status()
+                nxt = min(st.next_arrival, pending[0].arrival if pending else math.inf)
+                if math.isfinite(nxt):
+                    self.sleep(max(0.0, nxt - (self.clock() - self._t0)))
+        st = self._status()
+        self.steps_run, self.particle_steps = int(st.steps_run), int(st.particle_steps)
+        self.makespan = self.clock() - self._t0
         return done
 
 

@@ -1,11 +1,20 @@
-"""Serving loop: scheduling on the CPU against a stand-in batch (arrival
-order, HBM budget, completion); on the GPU, every served request's result is
-the same as the request run alone."""
+"""Serving loop (the native ``prtcl_gpu_server_*``): scheduling on the CPU
+against a stand-in batch driven through callbacks (arrival order, HBM
+budget, scene slots, completion, errors); on the GPU, every served request's
+result is the same as the request run alone."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
 from prtcl_gb300 import driver
-from prtcl_gb300.serve import Server, poisson_requests, report
+from prtcl_gb300.serve import Request, Server, poisson_requests, report
+
+
+@pytest.fixture(autouse=True)
+def _library(gpu_lib):
+    """The server is native: build / load the library (no GPU needed)."""
+    return gpu_lib
 
 
 class Clock:
@@ -33,7 +42,8 @@ class FakeBatch:
         sid = self.next
         self.next += 1
         self.scenes[sid] = [len(f), len(b), 0]
-        self.log.append(("add", sid))
+        self.log.append(("add", sid, len(f)))
+        self.max_resident = max(getattr(self, "max_resident", 0), len(self.scenes))
         return sid
 
     def remove_scene(self, sid):
@@ -59,16 +69,16 @@ class FakeBatch:
         pass
 
 
-def serve(reqs, budget):
+def serve(reqs, budget, batch=FakeBatch, **kw):
     clock = Clock()
     holder = {}
 
     def factory(p):
-        holder["b"] = FakeBatch(clock)
+        holder["b"] = batch(clock)
         return holder["b"]
 
     srv = Server(factory, driver.DAM_BREAK_27K, budget_bytes=budget, clock=clock, sleep=clock.sleep,
-                 bytes_per_particle=1000.0)
+                 bytes_per_particle=1000.0, **kw)
     done = srv.run(reqs)
     return srv, done, holder["b"]
 
@@ -94,7 +104,7 @@ def test_every_request_completes_in_arrival_order_of_admission():
         assert r.admitted >= r.arrival - 1e-12 and r.finished > r.admitted
         # at least one 10 ms step per requested step
         assert r.latency >= 0.01 * r.steps - 1e-9
-    order = [sid for op, sid in fb.log if op == "add"]
+    order = [e[1] for e in fb.log if e[0] == "add"]
     assert order == sorted(order)
     rep = report(done, srv.makespan, srv.particle_steps)
     assert rep["requests"] == 12 and rep["latency_p99_s"] >= rep["latency_p50_s"] > 0
@@ -108,6 +118,54 @@ def test_budget_limits_resident_bytes():
     srv, done, fb = serve(reqs, budget=budget)
     assert len(done) == 10
     assert fb.max_held <= budget
+
+
+def test_scene_slots_limit_resident_requests():
+    reqs = poisson_requests(9, rate=1000.0, seed=8, lo=200, hi=800, steps=(4, 9))
+    srv, done, fb = serve(reqs, budget=1e12, max_scenes=2)
+    assert len(done) == 9 and fb.max_resident == 2
+    assert sum(r.fluid * r.steps for r in done) == srv.particle_steps
+
+
+def test_ties_in_arrival_keep_submission_order_and_results():
+    reqs = [Request(rid=k, arrival=0.5, fluid_cells=(2 + k, 2, 2), steps=3) for k in range(4)]
+    srv, done, fb = serve(reqs, budget=1e12)
+    assert [e[2] for e in fb.log if e[0] == "add"] == [8 * (2 + k) // 2 for k in range(4)]
+    assert [r.rid for r in done] == [0, 1, 2, 3]  # same step count: retired in admission order
+    for r in done:
+        assert r.result.shape == (r.fluid, 3) and r.admitted == 0.5
+    _, done, _ = serve([Request(rid=0, arrival=0.0, fluid_cells=(2, 2, 2), steps=2)], budget=1e12,
+                       keep_results=False)
+    assert done[0].result is None
+
+
+class FailingBatch(FakeBatch):
+    def step(self, k):
+        if sum(v[2] for v in self.scenes.values()) > 5:
+            raise RuntimeError("stand-in step failed")
+        super().step(k)
+
+
+def test_batch_errors_reach_the_caller():
+    reqs = poisson_requests(3, rate=1000.0, seed=9, lo=200, hi=400, steps=(10, 12))
+    with pytest.raises(RuntimeError, match="stand-in step failed"):
+        serve(reqs, budget=1e12, batch=FailingBatch)
+
+
+def test_server_rejects_invalid_requests(gpu_lib):
+    from prtcl_gb300 import PrtclGpuError
+    from prtcl_gb300._lib import ServerParams, check
+    srv = Server(lambda p: FakeBatch(Clock()), driver.DAM_BREAK_27K, budget_bytes=1e9)
+    x = np.zeros((4, 3), np.float32)
+    with pytest.raises(PrtclGpuError, match="at least one step"):
+        check(gpu_lib.prtcl_gpu_server_submit(srv._h, 0, 0.0, x.ctypes.data, 4, x.ctypes.data, 4, 0))
+    with pytest.raises(PrtclGpuError, match="not finite"):
+        check(gpu_lib.prtcl_gpu_server_submit(srv._h, 0, float("nan"), x.ctypes.data, 4, x.ctypes.data, 4, 1))
+    sp = ServerParams()
+    sp.max_scenes = 0
+    h = C.c_void_p()
+    with pytest.raises(PrtclGpuError, match="max_scenes"):
+        check(gpu_lib.prtcl_gpu_server_create_custom(C.byref(srv._ops), None, C.byref(sp), C.byref(h)))
 
 
 @pytest.mark.gpu
