@@ -40,6 +40,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -96,7 +97,7 @@ class Clocks:
 
     def __init__(self):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"prtcl_gb300_clocks_{os.getpid()}.csv")
 
     def start(self):
         try:
@@ -135,6 +136,10 @@ class Clocks:
                 for n, v in zip(names, c[5:9]):
                     if v.lower().startswith("active"):
                         reasons.add(n)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
                 "reasons": sorted(reasons), "samples": len(sm)}
 
