@@ -38,9 +38,9 @@ def compare(d, o, groups):
             assert_bitwise(idd, ido, f"indices {q}->{ng}")
 
 
-@pytest.mark.parametrize("dist", ["uniform", "blobs"])
-def test_random_points(oracle_mod, dist):
-    n = 60000
+# 150k points: sorts and scans of several tiles per pass
+@pytest.mark.parametrize("dist,n", [("uniform", 60000), ("blobs", 60000), ("uniform", 150000)])
+def test_random_points(oracle_mod, dist, n):
     pts = scenes.search_points(n, dist, seed=1 if dist == "uniform" else 2)
     r = scenes.uniform_radius_for_mean_neighbours(n, 40.0) * (0.4 if dist == "blobs" else 1.0)
     groups = [("p", "fluid", pts, [])]
