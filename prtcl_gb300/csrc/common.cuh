@@ -36,6 +36,41 @@ constexpr int kMaxNbrGroups = 4;  // fluid / boundary groups a procedure sums ov
 
 inline unsigned div_up(size_t a, size_t b) { return unsigned((a + b - 1) / b); }
 
+// float -> double from the two IEEE-754 binary formats, on the integer pipe:
+// the conversion is exact, so the value equals the hardware conversion's
+// (a NaN keeps its payload bits).  The FP64 reductions convert one float per
+// item; GB300's FP64 pipe is narrow, so it is kept for the additions.
+__host__ __device__ __forceinline__ double f2d(float f) {
+#ifdef __CUDA_ARCH__
+  uint32_t u = __float_as_uint(f);
+#else
+  uint32_t u;
+  __builtin_memcpy(&u, &f, 4);
+#endif
+  uint64_t bits = uint64_t(u & 0x80000000u) << 32;
+  uint32_t e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
+  if (e == 0xFFu) {
+    bits |= 0x7FF0000000000000ull | (uint64_t(m) << 29);
+  } else if (e != 0u) {
+    bits |= (uint64_t(e + (1023u - 127u)) << 52) | (uint64_t(m) << 29);
+  } else if (m != 0u) {
+    // subnormal m * 2^-149, leading one at bit p: a normal double
+#ifdef __CUDA_ARCH__
+    int p = 31 - __clz(int(m));
+#else
+    int p = 31 - __builtin_clz(m);
+#endif
+    bits |= (uint64_t(p + (1023 - 149)) << 52) | ((uint64_t(m) << (52 - p)) & 0x000FFFFFFFFFFFFFull);
+  }
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)bits);
+#else
+  double d;
+  __builtin_memcpy(&d, &bits, 8);
+  return d;
+#endif
+}
+
 // number of kernels this library has launched from the host (process-wide)
 uint64_t launch_count();
 void count_launch();

@@ -511,7 +511,7 @@ __device__ __forceinline__ double iisph_pressure_item(uint32_t i, PressureArgs c
   float pn = ((0.0f < t) ? t : 0.0f) * ustep(1e-9f, fabsf(aai));
   A.p[i] = pn;
   A.pr[i] = pn / (ri * ri);
-  return double(((ap - si) / rho0) * ustep(1e-9f, pn));
+  return f2d(((ap - si) / rho0) * ustep(1e-9f, pn));
 }
 
 template <int NF, int NB>
@@ -885,16 +885,16 @@ __device__ __forceinline__ void pcg_init_item(PcgArgs const &P, KernelParams con
   P.Rr[i] = make_float4(r.x, r.y, r.z, 0.0f);
   P.Y[i] = make_float4(y.x, y.y, y.z, 0.0f);
   P.P[i] = make_float4(-y.x, -y.y, -y.z, 0.0f);
-  bb += double(dot3(b, b));
-  rr += double(dot3(r, r));
-  ry += double(dot3(r, y));
+  bb += f2d(dot3(b, b));
+  rr += f2d(dot3(r, r));
+  ry += f2d(dot3(r, y));
 }
 template <int NB, bool GC>
 __device__ __forceinline__ double pcg_q_item(PcgArgs const &P, KernelParams const &K, bool uc, float dt, float rho0,
                                              float mu, Nbrs<0, NB> const &N, uint32_t i) {
   f3 q = wkbb18_system<NB, GC>(P, K, uc, dt, rho0, mu, N, P.P, i);
   P.Q[i] = make_float4(q.x, q.y, q.z, 0.0f);
-  return double(dot3(mk3(P.P[i]), q));
+  return f2d(dot3(mk3(P.P[i]), q));
 }
 __device__ __forceinline__ void pcg_update_item(PcgArgs const &P, float alpha, uint32_t i, double &rr, double &ry) {
   f3 x = mk3(P.X[i]), p = mk3(P.P[i]), r = mk3(P.Rr[i]), q = mk3(P.Q[i]);
@@ -904,8 +904,8 @@ __device__ __forceinline__ void pcg_update_item(PcgArgs const &P, float alpha, u
   P.X[i] = make_float4(x.x, x.y, x.z, 0.0f);
   P.Rr[i] = make_float4(r.x, r.y, r.z, 0.0f);
   P.Y[i] = make_float4(y.x, y.y, y.z, 0.0f);
-  rr += double(dot3(r, r));
-  ry += double(dot3(r, y));
+  rr += f2d(dot3(r, r));
+  ry += f2d(dot3(r, y));
 }
 __device__ __forceinline__ void pcg_p_item(PcgArgs const &P, float beta, uint32_t i) {
   f3 y = mk3(P.Y[i]), p = mk3(P.P[i]);
@@ -1991,7 +1991,9 @@ public:
       if (seg) {
         if (tg) k_pcg_update_seg<<<tg, kNT, 0, cs>>>(P, SA);
       } else {
-        k_pcg_update<<<rg, kNT, 0, cs>>>(P, R);
+        // one resident wave: each thread folds several items before the
+        // block's FP64 tree (the FP64 pipe is narrow on this GPU)
+        k_pcg_update<<<std::min(rg, unsigned(152 * kMinBlocks)), kNT, 0, cs>>>(P, R);
       }
       count_launch();
       if (prof) model_->prof.end(cs);
