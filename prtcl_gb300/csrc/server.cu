@@ -113,9 +113,11 @@ bool Server::turn() {
     Request &q = pending_.front();
     double need = double(q.nf + q.nb) * bpp_;
     if (!running_.empty() && held_ + need > p_.budget_bytes) break;
+    // the request leaves the queue only once the batch holds it
+    int64_t sid = b_->add(q.xf.data(), q.nf, q.xb.data(), q.nb);
     Request r = std::move(q);
     pending_.pop_front();
-    r.sid = b_->add(r.xf.data(), r.nf, r.xb.data(), r.nb);
+    r.sid = sid;
     r.admitted = t;
     std::vector<float>().swap(r.xf);
     std::vector<float>().swap(r.xb);
@@ -133,13 +135,13 @@ bool Server::turn() {
     particle_steps_ += int64_t(x.nf);
     x.done++;
   }
-  // 3. retirements, in admission order
+  // 3. retirements, in admission order; a request leaves the resident set
+  // only once its result is stored and its scene removed
   bool retired = false;
-  std::vector<Request> keep;
-  keep.reserve(running_.size());
-  for (auto &x : running_) {
+  for (size_t k = 0; k < running_.size();) {
+    Request &x = running_[k];
     if (x.done < x.steps) {
-      keep.push_back(std::move(x));
+      ++k;
       continue;
     }
     Result res;
@@ -159,9 +161,9 @@ bool Server::turn() {
     res.r.finished = now();
     b_->remove(x.sid);
     results_.push_back(std::move(res));
+    running_.erase(running_.begin() + std::ptrdiff_t(k));
     retired = true;
   }
-  running_.swap(keep);
   if (retired) held_ = running_.empty() ? 0.0 : double(b_->device_bytes());
   return true;
 }

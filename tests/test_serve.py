@@ -152,6 +152,21 @@ def test_batch_errors_reach_the_caller():
         serve(reqs, budget=1e12, batch=FailingBatch)
 
 
+class RefusingBatch(FakeBatch):
+    def add_scene(self, f, b):
+        raise MemoryError("stand-in batch is full")
+
+
+def test_a_refused_admission_keeps_the_request_queued():
+    clock = Clock()
+    srv = Server(lambda p: RefusingBatch(clock), driver.DAM_BREAK_27K, budget_bytes=1e12, clock=clock,
+                 sleep=clock.sleep)
+    with pytest.raises(MemoryError):
+        srv.run([Request(rid=0, arrival=0.0, fluid_cells=(2, 2, 2), steps=2)])
+    st = srv._status()
+    assert (st.pending, st.running, st.results) == (1, 0, 0)
+
+
 def test_server_rejects_invalid_requests(gpu_lib):
     from prtcl_gb300 import PrtclGpuError
     from prtcl_gb300._lib import ServerParams, check
