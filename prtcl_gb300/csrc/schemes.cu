@@ -159,6 +159,7 @@ constexpr int kSegScal = 16, kSegStat = 8, kSegStats = 8;
 // count times the blocks resident per SM)
 constexpr uint32_t kActiveBlocks = 152 * 8;
 constexpr int kSsAprde = 8;        // scal: density error of the iteration
+constexpr int kSegUpdateNT = 32;   // threads of a tiled PCG update block
 constexpr int kStPcgEnded = 3;     // stat: the slot's PCG loop has ended
 
 template <int NV>
@@ -1051,8 +1052,9 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_update_seg(PcgArgs P, S
   if (!S.stat[slot * kSegStat + kStPcgActive]) return;
   float alpha = float(S.scal[slot * kSegScal + 6]);
   double rr = 0.0, ry = 0.0;
-  uint32_t i = T.y + threadIdx.x;
-  if (i < T.z) pcg_update_item(P, alpha, i, rr, ry);
+  // one warp per tile (kSegUpdateNT): each lane folds four items before the
+  // FP64 tree, which this GPU's narrow FP64 pipe makes the costly part
+  for (uint32_t i = T.y + threadIdx.x; i < T.z; i += blockDim.x) pcg_update_item(P, alpha, i, rr, ry);
   double v[2] = {rr, ry}, out[2];
   if (seg_commit<2>(v, S, slot, out, blockIdx.x) && threadIdx.x == 0)
     pcg_update_scalars(S.scal + slot * kSegScal, S.stat + slot * kSegStat, out[0], out[1], *P.tol, *P.max_k);
@@ -1989,7 +1991,7 @@ public:
       if (prof) model_->prof.end(cs);
       if (prof) model_->prof.begin("pcg_update", cs);
       if (seg) {
-        if (tg) k_pcg_update_seg<<<tg, kNT, 0, cs>>>(P, SA);
+        if (tg) k_pcg_update_seg<<<tg, kSegUpdateNT, 0, cs>>>(P, SA);
       } else {
         // one resident wave: each thread folds several items before the
         // block's FP64 tree (the FP64 pipe is narrow on this GPU)
