@@ -183,6 +183,38 @@ def test_server_rejects_invalid_requests(gpu_lib):
         check(gpu_lib.prtcl_gpu_server_create_custom(C.byref(srv._ops), None, C.byref(sp), C.byref(h)))
 
 
+def test_server_abi_argument_checks(gpu_lib):
+    from prtcl_gb300 import PrtclGpuError
+    from prtcl_gb300._lib import INVALID, RequestResult, ServerStatus, check
+    assert gpu_lib.prtcl_gpu_server_turn(None, None) == INVALID
+    assert gpu_lib.prtcl_gpu_server_status_get(None, None) == INVALID
+    assert gpu_lib.prtcl_gpu_server_create(None, None, None) == INVALID
+    assert gpu_lib.prtcl_gpu_server_destroy(None) == 0
+    clock = Clock()
+    srv = Server(lambda p: FakeBatch(clock), driver.DAM_BREAK_27K, budget_bytes=1e12, clock=clock, sleep=clock.sleep)
+    x = np.zeros((8, 3), np.float32)
+    assert gpu_lib.prtcl_gpu_server_submit(srv._h, 0, 0.0, x.ctypes.data, -1, x.ctypes.data, 8, 2) == INVALID
+    check(gpu_lib.prtcl_gpu_server_submit(srv._h, 7, 0.0, x.ctypes.data, 8, x.ctypes.data, 8, 2))
+    stepped = C.c_int32(0)
+    for _ in range(2):
+        check(gpu_lib.prtcl_gpu_server_turn(srv._h, C.byref(stepped)))
+        assert stepped.value == 1
+    st = ServerStatus()
+    check(gpu_lib.prtcl_gpu_server_status_get(srv._h, C.byref(st)))
+    assert (st.pending, st.running, st.results, st.steps_run, st.particle_steps) == (0, 0, 1, 2, 16)
+    res, has = RequestResult(), C.c_int32(0)
+    small = np.zeros((4, 3), np.float32)
+    with pytest.raises(PrtclGpuError, match="smaller than"):
+        check(gpu_lib.prtcl_gpu_server_next_result(srv._h, C.byref(res), small.ctypes.data, 4, C.byref(has)))
+    out = np.ones((8, 3), np.float32)
+    check(gpu_lib.prtcl_gpu_server_next_result(srv._h, C.byref(res), out.ctypes.data, 8, C.byref(has)))
+    assert has.value == 1 and res.request_id == 7 and res.steps == 2 and (out == 0).all()
+    check(gpu_lib.prtcl_gpu_server_next_result(srv._h, C.byref(res), None, 0, C.byref(has)))
+    assert has.value == 0
+    check(gpu_lib.prtcl_gpu_server_turn(srv._h, C.byref(stepped)))
+    assert stepped.value == 0
+
+
 @pytest.mark.gpu
 def test_served_results_match_alone():
     from prtcl_gb300.batch import Batch
