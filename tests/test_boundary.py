@@ -70,14 +70,23 @@ def test_no_cpu_fallback(gpu_lib):
 
 
 @pytest.mark.skipif(shutil.which("g++") is None, reason="no C++ compiler")
-def test_cpp_facade_compiles(tmp_path):
+def test_cpp_facade_compiles(tmp_path, gpu_lib):
+    """Driver code over the façade compiles and links against the library
+    (not run: no device here)."""
     src = tmp_path / "use.cpp"
     src.write_text('#include "prtcl_gpu.hpp"\n'
                    'int main() { prtcl_gpu::Model m; auto f = m.AddGroup("f", "fluid"); f.AddTag("dynamic");\n'
                    '  prtcl_gpu::Neighborhood n; n.Load(m); n.SetRadius(0.05); n.Update();\n'
                    '  auto s = prtcl_gpu::SchemeRegistry::NewScheme("prtcl::schemes::iisph[T=f32, N=3, K=Cubic Spline]");\n'
-                   '  s->Load(m); s->RunProcedure("setup", n); return 0; }\n')
-    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), str(src)],
+                   '  s->Load(m); s->RunProcedure("setup", n);\n'
+                   '  prtcl_gpu_batch_params bp{}; prtcl_gpu_server_params sp{}; sp.max_scenes = 8;\n'
+                   '  prtcl_gpu::Batch b(bp); auto id = b.AddScene({0, 0, 0}, {}); b.Step(); b.Positions(id);\n'
+                   '  prtcl_gpu::Server srv(bp, sp); srv.Submit(1, 0.0, {0, 0, 0}, {}, 2);\n'
+                   '  while (srv.Turn()) srv.TakeResults();\n'
+                   '  return int(srv.Status().pending); }\n')
+    lib_dir = os.path.dirname(gpu_lib._name)
+    r = subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                        str(tmp_path / "use"), "-L", lib_dir, "-lprtcl_gpu", "-Wl,-rpath," + lib_dir],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
 
