@@ -156,3 +156,18 @@ def test_reference_schemes():
             except DslError as ex:
                 raise AssertionError((s.name, ex))
     assert len(generated) == 14
+
+
+def test_reference_schemes_compile_and_register(gpu_lib):
+    """The plugin of all 14 reference schemes compiles for sm_103a, loads and
+    registers every scheme (registration needs no device)."""
+    from prtcl_gb300.core import get_scheme_names
+    from prtcl_gb300.dsl.build import compile_scheme
+    root = _reference_schemes()
+    if not os.path.isdir(root):
+        pytest.skip("the reference's scheme sources are not present")
+    text = "\n".join(open(os.path.join(root, f)).read() for f in sorted(os.listdir(root)) if f.endswith(".prtcl"))
+    names = compile_scheme(text, prefix="ref_")
+    assert len(names) == 14
+    registered = set(get_scheme_names())
+    assert all(n in registered for n in names)
