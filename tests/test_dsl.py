@@ -160,8 +160,9 @@ def test_reference_schemes():
 
 def test_reference_schemes_compile_and_register(gpu_lib):
     """The plugin of all 14 reference schemes compiles for sm_103a, loads and
-    registers every scheme (registration needs no device)."""
-    from prtcl_gb300.core import get_scheme_names
+    registers every scheme, each with the procedures of its source
+    (registration and the procedure table need no device)."""
+    from prtcl_gb300.core import get_scheme_names, make_scheme
     from prtcl_gb300.dsl.build import compile_scheme
     root = _reference_schemes()
     if not os.path.isdir(root):
@@ -171,3 +172,5 @@ def test_reference_schemes_compile_and_register(gpu_lib):
     assert len(names) == 14
     registered = set(get_scheme_names())
     assert all(n in registered for n in names)
+    for sc, full in zip(parse(text), names):
+        assert sorted(make_scheme(full).get_procedure_names()) == sorted(p.name for p in sc.procedures), sc.name
