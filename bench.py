@@ -436,17 +436,7 @@ def run_search(peak, n=4_000_000, reps=5, target=40.0):
             d.update()
             return d.nhood.query(0, count_pairs=True) / n
 
-        lo, hi = 0.2 * scenes.uniform_radius_for_mean_neighbours(n, target), \
-            scenes.uniform_radius_for_mean_neighbours(n, target)
-        while mean_nbrs(hi) < target:
-            lo, hi = hi, 2.0 * hi
-        for _ in range(14):
-            mid = 0.5 * (lo + hi)
-            if mean_nbrs(mid) < target:
-                lo = mid
-            else:
-                hi = mid
-        r = float(np.float32(hi))
+        r = scenes.calibrate_radius(mean_nbrs, n, target)
         nbar = mean_nbrs(r)
         s = torch.cuda.ExternalStream(d.model.stream_handle())
         for _ in range(2):

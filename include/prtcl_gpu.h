@@ -87,10 +87,13 @@ int prtcl_gpu_field_upload_async(prtcl_gpu_model *model, const char *group, cons
  * real[3][3] fields are staged through one fixed 8 MiB device array of the
  * library (at most 699,050 vector or 233,016 matrix items per call; larger
  * counts return PRTCL_GPU_ERROR and change nothing); other fields are copied
- * directly and have no limit.  The first call on a device looks up the
- * array's address, so make it before any stream capture.  Synchronous.  The
- * array is shared by the whole process and keeps the last call's bytes:
- * calls that overlap in time, from different threads, race on it. */
+ * directly and have no limit.  prtcl_gpu_model_create makes the array and
+ * its kernels resident on the current device, so create the model before
+ * the host takes the remaining device memory (a model used on another device
+ * does this on its first call there).  Synchronous, hence not capturable: a
+ * call on a stream under capture returns PRTCL_GPU_ERROR.  The array is
+ * shared by the whole process and keeps the last call's bytes: calls that
+ * overlap in time, from different threads, race on it. */
 int prtcl_gpu_field_upload_noalloc(prtcl_gpu_model *model, const char *group, const char *field, const void *host,
                                    int64_t count, void *stream);
 /* Copy the field to host memory in the reference layout (synchronous). */

@@ -122,7 +122,12 @@ uint64_t prtcl_gpu_launch_count(void) { return launch_count() + device_loop_kern
 
 int prtcl_gpu_model_create(prtcl_gpu_model **out) {
   NEED(out);
-  return guard([&] { *out = new prtcl_gpu_model(); });
+  return guard([&] {
+    // the no-alloc upload's staging array and kernels are made resident now,
+    // before a host can hand the rest of the device memory to its own pool
+    noalloc_prepare();
+    *out = new prtcl_gpu_model();
+  });
 }
 int prtcl_gpu_model_destroy(prtcl_gpu_model *model) {
   return guard([&] { delete model; });

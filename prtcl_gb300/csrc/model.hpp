@@ -220,6 +220,8 @@ void upload_varying(VaryingField &f, size_t count, void const *host, size_t n_it
 // (noalloc.cu); synchronous, and not safe to overlap with another such call
 void upload_varying_noalloc(VaryingField &f, size_t count, void const *host, size_t n_items, cudaStream_t s);
 size_t noalloc_stage_bytes();
+// looks up the staging array and loads its kernels on the current device
+void noalloc_prepare();
 void download_varying(VaryingField const &f, size_t count, void *host, size_t n_items, cudaStream_t s);
 // the model in the reference's native binary archive format (archive.cu)
 void save_model(Model &m, std::string const &path, cudaStream_t s);

@@ -11,9 +11,14 @@
 // fixed, statically sized device array instead.
 //
 // The array below is one per process and device.  Its device address is
-// looked up once per device, on the first call made with that device
-// current; make that first call before any stream capture begins.  Calls are
-// synchronous: each returns after its stream has finished with the array.
+// looked up once per device, and the module that holds it and the staging
+// kernels is loaded then too (the runtime loads modules lazily): model
+// creation does both for the device current at that time (noalloc_prepare),
+// so a host that then hands all remaining device memory to its own pool
+// still finds the array resident.  A model used on another device does it on
+// its first call there.  Calls are synchronous (each returns after its
+// stream has finished with the array) and so cannot be captured into a CUDA
+// graph: a call on a capturing stream is refused.
 // The array keeps the bytes of the last call; nothing reads it before the
 // same call's copy has overwritten the part it uses, so nothing in it has to
 // start at zero.  Two calls that overlap in time (from two host threads, on
@@ -66,6 +71,13 @@ __global__ void k_stage_planar9(float const *__restrict__ stage, float *__restri
 
 size_t noalloc_stage_bytes() { return kStageBytes; }
 
+void noalloc_prepare() {
+  stage_address();
+  cudaFuncAttributes a;
+  PG_CUDA(cudaFuncGetAttributes(&a, k_stage_vec3));
+  PG_CUDA(cudaFuncGetAttributes(&a, k_stage_planar9));
+}
+
 void upload_varying_noalloc(VaryingField &f, size_t count, void const *host, size_t n_items, cudaStream_t s) {
   if (n_items != count)
     throw Error("upload: item count " + std::to_string(n_items) + " != group count " + std::to_string(count));
@@ -75,6 +87,10 @@ void upload_varying_noalloc(VaryingField &f, size_t count, void const *host, siz
     throw Error("no-alloc upload: " + std::to_string(count) + " items of " + std::to_string(f.type.host_item_bytes()) +
                 " bytes need " + std::to_string(hbytes) + " staging bytes, more than the fixed " +
                 std::to_string(kStageBytes) + "; use prtcl_gpu_field_upload");
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  PG_CUDA(cudaStreamIsCapturing(s, &cap));
+  if (cap != cudaStreamCaptureStatusNone)
+    throw Error("no-alloc upload: the stream is being captured; the call is synchronous and cannot be captured");
   void *stage = staged ? stage_address() : nullptr;
   f.version++;
   if (count == 0) return;

@@ -28,11 +28,11 @@ _loaded = {}
 _lib_lock = threading.Lock()  # one library build at a time
 
 
-def plugin_source(source: str, prefix: str = ""):
+def plugin_source(source: str, prefix: str = "", embed_source: bool = True):
     """(full names, CUDA source) of the plugin of a ``.prtcl`` text: every
     scheme of the text in one translation unit."""
     schemes = parse(source)
-    return [full_name(s, prefix) for s in schemes], generate_all(schemes, prefix)
+    return [full_name(s, prefix) for s in schemes], generate_all(schemes, prefix, embed_source)
 
 
 def _compile(name: str, cu: str) -> str:
@@ -60,8 +60,14 @@ def _compile(name: str, cu: str) -> str:
 def compile_scheme(source: str, prefix: str = ""):
     """Generate, compile and load every scheme of a ``.prtcl`` text (one
     plugin); returns their full names."""
-    from .._lib import check, load
     names, cu = plugin_source(source, prefix)
+    return load_plugin_source(names, cu)
+
+
+def load_plugin_source(names, cu: str):
+    """Compile and load an already generated plugin source (e.g. one
+    generated elsewhere and kept as a file) whose schemes are ``names``."""
+    from .._lib import check, load
     done = [n for n in names if n in _loaded]
     if done:
         if all(_loaded.get(n) == cu for n in names):

@@ -109,10 +109,11 @@ class _Kernel:
 
 
 class Emitter:
-    def __init__(self, scheme: Scheme, info: Info, prefix: str = ""):
+    def __init__(self, scheme: Scheme, info: Info, prefix: str = "", embed_source: bool = True):
         self.s = scheme
         self.info = info
         self.prefix = prefix
+        self.embed_source = embed_source
         self.full_short = prefix + scheme.name
         uid = hashlib.sha1((prefix + scheme.source).encode()).hexdigest()[:12]
         self.ns = f"gen_{_ident(scheme.name)}_{uid}"
@@ -631,7 +632,7 @@ class Emitter:
         w("")
 
     def emit_class(self, w):
-        src = self.s.source
+        src = self.s.source if self.embed_source else "(scheme source text not embedded in this build)"
         w("class Scheme_ : public Scheme {")
         w("public:")
         w("  Scheme_() {")
@@ -806,9 +807,11 @@ def generate(scheme: Scheme, prefix: str = "") -> str:
     return Emitter(scheme, info, prefix).source()
 
 
-def generate_all(schemes, prefix: str = "") -> str:
-    """One plugin source for several schemes (one nvcc run)."""
-    ems = [Emitter(s, resolve(s), prefix) for s in schemes]
+def generate_all(schemes, prefix: str = "", embed_source: bool = True) -> str:
+    """One plugin source for several schemes (one nvcc run).  Without
+    ``embed_source`` the schemes' GetPrtclSourceCode text is a fixed note
+    instead of the ``.prtcl`` text."""
+    ems = [Emitter(s, resolve(s), prefix, embed_source) for s in schemes]
     names = [e.full_short for e in ems]
     if len(set(names)) != len(names):
         raise DslError("two schemes of the same name in one plugin")

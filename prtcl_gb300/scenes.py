@@ -78,6 +78,24 @@ def uniform_radius_for_mean_neighbours(n, mean_neighbours=40.0):
     return (mean_neighbours / (n * 4.0 / 3.0 * math.pi)) ** (1.0 / 3.0)
 
 
+def calibrate_radius(mean_neighbours_at, n, target=40.0, steps=14):
+    """Radius (rounded to float32) at which ``mean_neighbours_at(r)`` first
+    reaches ``target``: doubling from the uniform estimate, then ``steps``
+    bisections.  ``mean_neighbours_at`` counts on whatever grid the caller
+    holds (the device's, for the search workload)."""
+    lo = 0.2 * uniform_radius_for_mean_neighbours(n, target)
+    hi = uniform_radius_for_mean_neighbours(n, target)
+    while mean_neighbours_at(hi) < target:
+        lo, hi = hi, 2.0 * hi
+    for _ in range(steps):
+        mid = 0.5 * (lo + hi)
+        if mean_neighbours_at(mid) < target:
+            lo = mid
+        else:
+            hi = mid
+    return float(np.float32(hi))
+
+
 def mixed_batch(count=256, lo=2000, hi=200000, seed=3, spacing=0.025, layers=2):
     """``count`` dam-break scenes with fluid counts log-uniform in [lo, hi],
     block aspect ratios uniform in [0.5, 2] and boxes 2x the fluid extent."""

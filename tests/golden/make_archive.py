@@ -17,7 +17,17 @@ import types
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_PY = os.path.join(os.environ.get("PRTCL_REFERENCE", "/root/reference"), "share", "python")
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+
+def reference_python():
+    """share/python of the reference checkout (located by oracle/Makefile,
+    PRTCL_REFERENCE overrides); exits with a message where it is absent."""
+    from oracle import ref_build
+    root = ref_build.reference_root()
+    if not root:
+        raise SystemExit("the reference checkout is needed: set PRTCL_REFERENCE")
+    return os.path.join(root, "share", "python")
 
 
 def w_size(f, v):
@@ -103,7 +113,7 @@ def write(path, m):
 def check_with_reference(path, m):
     sys.modules.setdefault("matplotlib", types.ModuleType("matplotlib"))
     sys.modules.setdefault("matplotlib.pyplot", types.ModuleType("matplotlib.pyplot"))
-    sys.path.insert(0, REF_PY)
+    sys.path.insert(0, reference_python())
     import prtcl_archive
     with open(path, "rb") as f:
         r = prtcl_archive.load_model(f)

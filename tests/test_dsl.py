@@ -17,7 +17,8 @@ def _reference_schemes():
     """The reference's own scheme sources, where its checkout is present
     (located by the oracle's build recipe)."""
     from oracle import ref_build
-    return os.path.join(ref_build.reference_root(), "share", "schemes")
+    root = ref_build.reference_root()
+    return os.path.join(root, "share", "schemes") if root else ""
 
 
 def _scheme(body, groups=None, glob="field hs = real smoothing_scale;"):
@@ -174,3 +175,22 @@ def test_reference_schemes_compile_and_register(gpu_lib):
     assert all(n in registered for n in names)
     for sc, full in zip(parse(text), names):
         assert sorted(make_scheme(full).get_procedure_names()) == sorted(p.name for p in sc.procedures), sc.name
+
+
+def test_reference_scheme_fixture_is_current():
+    """tests/golden/reference_schemes_plugin.cu (run on the device by
+    tests/test_gpu_reference_schemes.py) is what the generator emits now
+    for the reference's scheme sources."""
+    import json
+    import sys
+    sys.path.insert(0, os.path.join(HERE, "golden"))
+    import make_reference_schemes as mk
+    from oracle import ref_build
+    root = ref_build.reference_root()
+    if not root or not os.path.isdir(_reference_schemes()):
+        pytest.skip("the reference's scheme sources are not present")
+    names, cu, meta = mk.generate(root)
+    with open(mk.OUT) as f:
+        assert f.read() == cu, "regenerate with tests/golden/make_reference_schemes.py"
+    with open(mk.META) as f:
+        assert json.load(f) == meta

@@ -2,9 +2,10 @@
 
 Both entry points must leave the same device contents (compared bit for bit
 after a download), on two calls in a row, with the second call smaller than
-the first so that bytes the first call left in the fixed staging array would
-show up if they were read.  Counts above the staging limit are refused and
-leave the field unchanged.
+the first (vectors and matrices alike) so that bytes the first call left in
+the fixed staging array would show up if they were read.  Counts above the
+staging limit are refused and leave the field unchanged; so is a call on a
+stream that is being captured into a CUDA graph.
 """
 import ctypes as C
 
@@ -44,8 +45,9 @@ def test_noalloc_upload_matches_upload(gpu_lib, first, second):
     rng = np.random.default_rng(7)
     for call, n in enumerate((first, second)):
         g.resize(n)
-        # a matrix field of n items needs 36 n staging bytes: keep it inside
-        nm = min(n, STAGE_BYTES // 36)
+        # a matrix field of n items needs 36 n staging bytes: keep it inside,
+        # and make the second matrix call smaller than the first as well
+        nm = min(n, STAGE_BYTES // 36) // (1 + call)
         x = rng.standard_normal((n, 3)).astype(np.float32)
         mat = rng.standard_normal((n, 9)).astype(np.float32)
         s = rng.standard_normal(n).astype(np.float32)
@@ -90,3 +92,22 @@ def test_noalloc_upload_limit(gpu_lib):
     from prtcl_gb300._lib import load
     rc = load().prtcl_gpu_field_upload_noalloc(m._h, b"f", b"s_a", s.ctypes.data, n - 1, None)
     assert rc != 0
+
+
+def test_noalloc_upload_refused_under_capture(gpu_lib):
+    """The call synchronises its stream, which a capture forbids: it returns
+    an error before touching the stream, and the field keeps its values."""
+    import torch
+    from prtcl_gb300._lib import load
+    m, g = _model()
+    g.resize(1000)
+    x = np.ones((1000, 3), np.float32)
+    g.varying.get_field("x_a").upload(np.zeros((1000, 3), np.float32))
+    s = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=s, capture_error_mode="relaxed"):
+        rc = load().prtcl_gpu_field_upload_noalloc(m._h, b"f", b"x_a", x.ctypes.data, 1000,
+                                                   C.c_void_p(s.cuda_stream))
+    assert rc != 0
+    assert "captured" in load().prtcl_gpu_last_error().decode()
+    assert not g.varying.get_field("x_a").download().any()
