@@ -308,14 +308,26 @@ int prtcl_gpu_batch_profile_read(prtcl_gpu_batch *batch, char *buf, int64_t size
  *   1. admits the submitted requests whose arrival time has come, in arrival
  *      order (ties in submission order), while a scene slot is free and the
  *      batch's device bytes plus the request's estimate (its particles times
- *      the largest bytes per particle seen so far) stay within the budget; a
- *      request is always admitted when nothing is resident;
+ *      the largest bytes per particle seen so far) stay within the budget;
  *   2. steps every resident scene once;
  *   3. retires, in admission order, the requests that have taken all their
  *      steps: their scene information and (keep_results) final fluid
  *      positions are kept until read with prtcl_gpu_server_next_result.
  * Every scene converges on its own, so a request's result is the same, bit
- * for bit, alone and in the mix.  Times are seconds on the server's clock. */
+ * for bit, alone and in the mix.  Times are seconds on the server's clock.
+ *
+ * Failures.  A request whose own estimate exceeds the budget is refused at
+ * submit (PRTCL_GPU_ERROR), and one whose estimate has grown beyond the
+ * budget by the time it could be admitted is retired unrun with status
+ * PRTCL_GPU_REQUEST_REJECTED: no request reaches the device allocator with
+ * more than the budget.  prtcl_gpu_server_cancel retires a queued or
+ * resident request with status PRTCL_GPU_REQUEST_CANCELLED.  If a batch step
+ * fails, every resident request is retired with status
+ * PRTCL_GPU_REQUEST_FAILED (its scene removed from the batch) and the turn
+ * returns the step's error; queued requests stay queued.  If reading a
+ * finished request's results fails, that request alone is retired with
+ * status PRTCL_GPU_REQUEST_FAILED and is never stepped again.  A scene the
+ * batch failed to remove is removed again at the start of later turns. */
 typedef struct prtcl_gpu_server prtcl_gpu_server;
 typedef double (*prtcl_gpu_clock_fn)(void *user);
 typedef struct prtcl_gpu_server_params {
@@ -338,11 +350,19 @@ typedef struct prtcl_gpu_server_batch_ops {
   int (*scene_info)(void *user, int64_t scene_id, prtcl_gpu_scene_info *out);
   int (*download_positions)(void *user, int64_t scene_id, float *host_xyz, int64_t count);
 } prtcl_gpu_server_batch_ops;
+enum {
+  PRTCL_GPU_REQUEST_DONE = 0,       /* took all its steps */
+  PRTCL_GPU_REQUEST_CANCELLED = 1,  /* prtcl_gpu_server_cancel */
+  PRTCL_GPU_REQUEST_REJECTED = 2,   /* its estimate exceeded the budget at admission */
+  PRTCL_GPU_REQUEST_FAILED = 3      /* a batch step, or reading its results, failed */
+};
 typedef struct prtcl_gpu_request_result {
   int64_t request_id;
-  int64_t fluid, boundary, steps;
-  double arrival, admitted, finished;
-  prtcl_gpu_scene_info info;         /* the scene's information at retirement */
+  int64_t fluid, boundary, steps;    /* steps taken */
+  double arrival, admitted, finished; /* admitted: -1 if never admitted */
+  prtcl_gpu_scene_info info;         /* the scene's information at retirement (zero if never admitted) */
+  int32_t status;                    /* PRTCL_GPU_REQUEST_* */
+  int32_t pad;
 } prtcl_gpu_request_result;
 typedef struct prtcl_gpu_server_status {
   int64_t pending, running, results; /* submitted, resident, retired and not yet read */
@@ -365,6 +385,11 @@ int prtcl_gpu_server_submit(prtcl_gpu_server *server, int64_t request_id, double
  * nothing was resident (wait for status.next_arrival). */
 int prtcl_gpu_server_turn(prtcl_gpu_server *server, int32_t *stepped_out);
 int prtcl_gpu_server_status_get(prtcl_gpu_server *server, prtcl_gpu_server_status *out);
+/* Cancel a queued or resident request: it is retired with status
+ * PRTCL_GPU_REQUEST_CANCELLED (a resident one with the steps it took and
+ * its scene removed).  *found_out = 0 if no queued or resident request has
+ * that id (already retired, or never submitted). */
+int prtcl_gpu_server_cancel(prtcl_gpu_server *server, int64_t request_id, int32_t *found_out);
 /* The oldest unread result (*has_out = 0 when there is none).  Its final
  * fluid positions are copied to `positions_xyz` (NULL: not copied; otherwise
  * `capacity` >= the request's fluid count, in particles). */

@@ -305,6 +305,12 @@ public:
     check(prtcl_gpu_server_turn(s_, &stepped));
     return stepped != 0;
   }
+  // retire a queued or resident request as cancelled; false if none has the id
+  bool Cancel(int64_t request_id) {
+    int32_t found = 0;
+    check(prtcl_gpu_server_cancel(s_, request_id, &found));
+    return found != 0;
+  }
   prtcl_gpu_server_status Status() {
     prtcl_gpu_server_status st{};
     check(prtcl_gpu_server_status_get(s_, &st));

@@ -111,6 +111,7 @@ SIGNATURES = {
     "prtcl_gpu_server_submit": [vp, i64, dbl, vp, i64, vp, i64, i64],
     "prtcl_gpu_server_turn": [vp, i32p],
     "prtcl_gpu_server_status_get": [vp, vp],
+    "prtcl_gpu_server_cancel": [vp, i64, i32p],
     "prtcl_gpu_server_next_result": [vp, vp, vp, i64, i32p],
 }
 
@@ -159,7 +160,12 @@ class ServerBatchOps(C.Structure):
 class RequestResult(C.Structure):
     """prtcl_gpu_request_result"""
     _fields_ = [("request_id", C.c_int64), ("fluid", C.c_int64), ("boundary", C.c_int64), ("steps", C.c_int64),
-                ("arrival", C.c_double), ("admitted", C.c_double), ("finished", C.c_double), ("info", SceneInfo)]
+                ("arrival", C.c_double), ("admitted", C.c_double), ("finished", C.c_double), ("info", SceneInfo),
+                ("status", C.c_int32), ("pad", C.c_int32)]
+
+
+# prtcl_gpu_request_result.status
+REQUEST_STATUS = {0: "done", 1: "cancelled", 2: "rejected", 3: "failed"}
 
 
 class ServerStatus(C.Structure):

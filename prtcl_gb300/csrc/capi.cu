@@ -643,6 +643,11 @@ int prtcl_gpu_server_status_get(prtcl_gpu_server *server, prtcl_gpu_server_statu
   NEED(out);
   return guard([&] { *out = server->s->status(); });
 }
+int prtcl_gpu_server_cancel(prtcl_gpu_server *server, int64_t request_id, int32_t *found_out) {
+  NEED(server);
+  NEED(found_out);
+  return guard([&] { *found_out = server->s->cancel(request_id) ? 1 : 0; });
+}
 int prtcl_gpu_server_next_result(prtcl_gpu_server *server, prtcl_gpu_request_result *out, float *positions_xyz,
                                  int64_t capacity, int32_t *has_out) {
   NEED(server);

@@ -474,7 +474,7 @@ struct ListOut {
   uint32_t *idx32[kMaxListGroups];
   uint32_t cap[kMaxListGroups];
   uint2 *cb;        // [G][n]
-  uint32_t *maxcnt; // [kMaxListGroups]
+  uint32_t *maxcnt; // [kMaxListGroups]: the longest row of each group
   uint32_t n;
   int G;
   int with_gf; // factors are written (lists built without them never read them)
@@ -688,8 +688,16 @@ __global__ void __launch_bounds__(kBuildNT, NG <= 2 ? 9 : 1) k_build_lists(GridV
     if (g >= lo.G) break;
     uint32_t n = R[g].c;
     lo.cb[size_t(g) * lo.n + i] = make_uint2(n | (R[g].wide ? kWide : 0u), R[g].j0);
+    {
+      // the longest row, one atomic per warp: the host grows the lists when
+      // it exceeds the capacity (the rows past it were cut) and shrinks them
+      // when it is far below
+      unsigned am = __activemask();
+      uint32_t wmax = __reduce_max_sync(am, n);
+      if (int(threadIdx.x & 31u) == __ffs(int(am)) - 1) atomicMax(&lo.maxcnt[g], wmax);
+    }
     if (n > lo.cap[g]) {
-      atomicMax(&lo.maxcnt[g], n);
+      // overflow: the row is rebuilt after the host grows the lists
     } else if (n % kChunk) {
       // the partial last chunk (and half-chunk of a wide row), zero-filled
       bool wide = R[g].wide;
@@ -1090,9 +1098,22 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
         alloc_slots(g, (stats_h_[8 + g] + kChunk - 1) / kChunk * kChunk + kChunk);
         grow = true;
       }
-    if (!grow) break;
+    if (!grow) {
+      // rows far shorter than the capacity (e.g. after a query at a much
+      // larger radius): give the storage back and build once more, so that
+      // the lists do not hold the largest capacity ever needed
+      bool shrink = false;
+      for (int g = 0; g < G && attempt < 7; ++g) {
+        uint32_t want = std::max<uint32_t>((stats_h_[8 + g] + kChunk - 1) / kChunk * kChunk + kChunk, 48u);
+        if (L.cap[g] > 2 * want && L.cap[g] > 128u) {
+          alloc_slots(g, want);
+          shrink = true;
+        }
+      }
+      if (!shrink) break;
+    }
     list_rebuilds++;
-    if (attempt == 7) throw Error("neighbour lists kept overflowing their capacity");
+    if (grow && attempt == 7) throw Error("neighbour lists kept overflowing their capacity");
   }
   L.epoch = epoch_;
   L.pos_versions = pos_versions();
@@ -1292,21 +1313,28 @@ void Nhood::copy_lists(int q, int ng, int64_t *offsets, uint32_t *idx, size_t ca
   offsets[0] = 0;
   if (n == 0) return;
   PG_CUDA(cudaMemcpyAsync(cb.data(), v.cb[ng], n * sizeof(uint2), cudaMemcpyDeviceToHost, s));
-  size_t rowbytes = size_t(v.cap[ng] / kChunk) * kChunkBytes;
+  PG_CUDA(cudaStreamSynchronize(s));
+  uint32_t used = 0; // longest row
+  for (size_t i = 0; i < n; ++i) {
+    offsets[i + 1] = offsets[i] + (cb[i].x & ~kWide);
+    used = std::max(used, cb[i].x & ~kWide);
+  }
+  if (size_t(offsets[n]) > cap) throw Error("copy_lists: capacity too small");
+  // only the chunk planes and the 32-bit columns that hold entries
+  used = std::min(v.cap[ng], (used + kChunk - 1) / kChunk * kChunk);
   std::vector<unsigned char> ch;
   std::vector<uint32_t> e32;
-  if (v.chunks[ng]) {
-    ch.resize(rowbytes * n);
-    e32.resize(size_t(v.cap[ng]) * n);
+  if (v.chunks[ng] && used) {
+    ch.resize(size_t(used / kChunk) * kChunkBytes * n);
+    e32.resize(size_t(used) * n);
     PG_CUDA(cudaMemcpyAsync(ch.data(), v.chunks[ng], ch.size(), cudaMemcpyDeviceToHost, s));
-    PG_CUDA(cudaMemcpyAsync(e32.data(), v.idx32[ng], e32.size() * 4, cudaMemcpyDeviceToHost, s));
+    PG_CUDA(cudaMemcpy2DAsync(e32.data(), size_t(used) * 4, v.idx32[ng], size_t(v.cap[ng]) * 4, size_t(used) * 4, n,
+                              cudaMemcpyDeviceToHost, s));
+    PG_CUDA(cudaStreamSynchronize(s));
   }
-  PG_CUDA(cudaStreamSynchronize(s));
-  for (size_t i = 0; i < n; ++i) offsets[i + 1] = offsets[i] + (cb[i].x & ~kWide);
-  if (size_t(offsets[n]) > cap) throw Error("copy_lists: capacity too small");
   for (size_t i = 0; i < n; ++i)
     for (uint32_t k = 0; k < (cb[i].x & ~kWide); ++k)
-      idx[offsets[i] + k] = nbr_host_decode(cb[i], ch.data(), n, i, e32.data() + i * v.cap[ng], k);
+      idx[offsets[i] + k] = nbr_host_decode(cb[i], ch.data(), n, i, e32.data() + i * used, k);
 }
 
 } // namespace prtcl_gpu

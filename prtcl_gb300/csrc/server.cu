@@ -92,6 +92,10 @@ void Server::submit(int64_t rid, double arrival, float const *xf, size_t nf, flo
   if (steps < 1) throw Error("server: a request needs at least one step");
   if (!std::isfinite(arrival)) throw Error("server: arrival time is not finite");
   if ((nf && !xf) || (nb && !xb)) throw Error("server: particle positions are null");
+  double need = double(nf + nb) * bpp_;
+  if (need > p_.budget_bytes)
+    throw Error("server: the request needs an estimated " + std::to_string(int64_t(need)) +
+                " device bytes, more than the budget of " + std::to_string(int64_t(p_.budget_bytes)));
   Request r;
   r.rid = rid;
   r.arrival = arrival;
@@ -106,13 +110,75 @@ void Server::submit(int64_t rid, double arrival, float const *xf, size_t nf, flo
   pending_.insert(at, std::move(r));
 }
 
+Server::Result Server::result_of(Request const &x, int32_t status, bool resident) {
+  Result res;
+  res.r.request_id = x.rid;
+  res.r.fluid = int64_t(x.nf);
+  res.r.boundary = int64_t(x.nb);
+  res.r.steps = x.done;
+  res.r.arrival = x.arrival;
+  res.r.admitted = resident ? x.admitted : -1.0;
+  res.r.status = status;
+  if (resident) {
+    try {
+      res.r.info = b_->info(x.sid);
+    } catch (std::exception const &) {
+      res.r.info = prtcl_gpu_scene_info{};
+      if (res.r.status == PRTCL_GPU_REQUEST_DONE) res.r.status = PRTCL_GPU_REQUEST_FAILED;
+    }
+  }
+  res.r.finished = now();
+  return res;
+}
+
+void Server::drop_scene(int64_t sid) {
+  try {
+    b_->remove(sid);
+  } catch (std::exception const &) {
+    orphans_.push_back(sid);
+  }
+}
+
+bool Server::cancel(int64_t rid) {
+  for (auto it = pending_.begin(); it != pending_.end(); ++it)
+    if (it->rid == rid) {
+      results_.push_back(result_of(*it, PRTCL_GPU_REQUEST_CANCELLED, false));
+      pending_.erase(it);
+      return true;
+    }
+  for (auto it = running_.begin(); it != running_.end(); ++it)
+    if (it->rid == rid) {
+      results_.push_back(result_of(*it, PRTCL_GPU_REQUEST_CANCELLED, true));
+      drop_scene(it->sid);
+      running_.erase(it);
+      held_ = running_.empty() ? 0.0 : double(b_->device_bytes());
+      return true;
+    }
+  return false;
+}
+
 bool Server::turn() {
+  // 0. scenes whose removal failed earlier
+  for (size_t k = 0; k < orphans_.size();) {
+    try {
+      b_->remove(orphans_[k]);
+      orphans_.erase(orphans_.begin() + std::ptrdiff_t(k));
+    } catch (std::exception const &) {
+      ++k;
+    }
+  }
   double t = now();
   // 1. admissions, in arrival order, within the slots and the budget
   while (!pending_.empty() && pending_.front().arrival <= t && running_.size() < size_t(p_.max_scenes)) {
     Request &q = pending_.front();
     double need = double(q.nf + q.nb) * bpp_;
-    if (!running_.empty() && held_ + need > p_.budget_bytes) break;
+    if (need > p_.budget_bytes) {
+      // the estimate grew past the budget after submission: never admitted
+      results_.push_back(result_of(q, PRTCL_GPU_REQUEST_REJECTED, false));
+      pending_.pop_front();
+      continue;
+    }
+    if (held_ + need > p_.budget_bytes) break;
     // the request leaves the queue only once the batch holds it
     int64_t sid = b_->add(q.xf.data(), q.nf, q.xb.data(), q.nb);
     Request r = std::move(q);
@@ -128,8 +194,19 @@ bool Server::turn() {
     if (parts) bpp_ = std::max(bpp_, held_ / double(parts));
   }
   if (running_.empty()) return false;
-  // 2. one step of every resident scene
-  b_->step(1);
+  // 2. one step of every resident scene; if it fails, the resident scenes'
+  // state is undefined: retire them all as failed, then report the error
+  try {
+    b_->step(1);
+  } catch (std::exception const &) {
+    for (auto &x : running_) {
+      results_.push_back(result_of(x, PRTCL_GPU_REQUEST_FAILED, true));
+      drop_scene(x.sid);
+    }
+    running_.clear();
+    held_ = 0.0;
+    throw;
+  }
   steps_run_++;
   for (auto &x : running_) {
     particle_steps_ += int64_t(x.nf);
@@ -144,22 +221,24 @@ bool Server::turn() {
       ++k;
       continue;
     }
-    Result res;
-    res.r.request_id = x.rid;
-    res.r.fluid = int64_t(x.nf);
-    res.r.boundary = int64_t(x.nb);
-    res.r.steps = x.done;
-    res.r.arrival = x.arrival;
-    res.r.admitted = x.admitted;
-    res.r.info = b_->info(x.sid);
-    if (p_.keep_results) {
-      res.x.resize(3 * x.nf);
-      b_->download_positions(x.sid, res.x.data(), x.nf);
-    } else {
-      b_->synchronize();
+    // a failure to read the results fails this request alone: it is
+    // retired all the same, so it is never stepped again
+    bool ok = true;
+    std::vector<float> xs;
+    try {
+      if (p_.keep_results) {
+        xs.resize(3 * x.nf);
+        b_->download_positions(x.sid, xs.data(), x.nf);
+      } else {
+        b_->synchronize();
+      }
+    } catch (std::exception const &) {
+      ok = false;
+      xs.clear();
     }
-    res.r.finished = now();
-    b_->remove(x.sid);
+    Result res = result_of(x, ok ? PRTCL_GPU_REQUEST_DONE : PRTCL_GPU_REQUEST_FAILED, true);
+    if (res.r.status == PRTCL_GPU_REQUEST_DONE) res.x = std::move(xs);
+    drop_scene(x.sid);
     results_.push_back(std::move(res));
     running_.erase(running_.begin() + std::ptrdiff_t(k));
     retired = true;
@@ -186,6 +265,7 @@ bool Server::next_result(prtcl_gpu_request_result &out, float *x, size_t capacit
   if (x) {
     if (capacity < size_t(r.r.fluid)) throw Error("server: result buffer smaller than the request's fluid count");
     if (!r.x.empty()) std::copy(r.x.begin(), r.x.end(), x);
+    else std::fill(x, x + 3 * size_t(r.r.fluid), 0.0f);
   }
   out = r.r;
   results_.pop_front();

@@ -40,6 +40,8 @@ public:
   // one turn; false when nothing was resident to step
   bool turn();
   prtcl_gpu_server_status status() const;
+  // retire a queued or resident request as cancelled; false if none has the id
+  bool cancel(int64_t rid);
   // the oldest unread result, its positions copied to `x` when non-null
   bool next_result(prtcl_gpu_request_result &out, float *x, size_t capacity);
 
@@ -55,6 +57,10 @@ private:
     std::vector<float> x;
   };
   double now() const;
+  // a result for a request leaving the queue or the resident set
+  Result result_of(Request const &x, int32_t status, bool resident);
+  // remove a scene from the batch; on failure, retried at later turns
+  void drop_scene(int64_t sid);
 
   std::unique_ptr<ServeBatch> b_;
   prtcl_gpu_server_params p_;
@@ -62,6 +68,7 @@ private:
   std::deque<Request> pending_;  // arrival order, ties in submission order
   std::vector<Request> running_; // admission order
   std::deque<Result> results_;
+  std::vector<int64_t> orphans_; // scenes the batch failed to remove
   double held_ = 0.0, bpp_ = 0.0;
   int64_t steps_run_ = 0, particle_steps_ = 0;
 };

@@ -80,13 +80,21 @@ def uniform_radius_for_mean_neighbours(n, mean_neighbours=40.0):
 
 def calibrate_radius(mean_neighbours_at, n, target=40.0, steps=14):
     """Radius (rounded to float32) at which ``mean_neighbours_at(r)`` first
-    reaches ``target``: doubling from the uniform estimate, then ``steps``
-    bisections.  ``mean_neighbours_at`` counts on whatever grid the caller
-    holds (the device's, for the search workload)."""
-    lo = 0.2 * uniform_radius_for_mean_neighbours(n, target)
-    hi = uniform_radius_for_mean_neighbours(n, target)
-    while mean_neighbours_at(hi) < target:
-        lo, hi = hi, 2.0 * hi
+    reaches ``target``: a bracket found in steps of 1.25x from a quarter of
+    the uniform estimate, then ``steps`` bisections.  Steps of 1.25x in the
+    radius at most double the mean count, so no trial radius builds lists
+    far longer than the target's (clustered points can have many times the
+    uniform count at the uniform radius).  ``mean_neighbours_at`` counts on
+    whatever grid the caller holds (the device's, for the search workload)."""
+    r = 0.25 * uniform_radius_for_mean_neighbours(n, target)
+    if mean_neighbours_at(r) >= target:
+        hi, lo = r, r / 1.25
+        while mean_neighbours_at(lo) >= target:
+            hi, lo = lo, lo / 1.25
+    else:
+        lo, hi = r, 1.25 * r
+        while mean_neighbours_at(hi) < target:
+            lo, hi = hi, 1.25 * hi
     for _ in range(steps):
         mid = 0.5 * (lo + hi)
         if mean_neighbours_at(mid) < target:

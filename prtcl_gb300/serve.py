@@ -35,6 +35,7 @@ class Request:
     fluid_cells: tuple      # fluid block in lattice cells
     steps: int
     seed: int = 0
+    cancel_at: float = math.inf  # the client cancels the request at this time
     # filled in by the server
     admitted: float = math.nan
     finished: float = math.nan
@@ -43,6 +44,7 @@ class Request:
     boundary: int = 0
     info: dict = field(default_factory=dict)
     result: np.ndarray | None = None
+    status: str = ""        # done, cancelled, rejected or failed
     _scene: dict | None = field(default=None, repr=False)
 
     @property
@@ -130,7 +132,8 @@ class Server:
 
     def _callback_ops(self, bt):
         """prtcl_gpu_server_batch_ops over a Python batch object; an exception
-        in a callback fails the operation and is raised after the call."""
+        in a callback fails the operation and, if the server call then fails,
+        is raised after the call."""
         from ._lib import SceneInfo, ServerBatchOps
 
         def guarded(fn):
@@ -176,10 +179,21 @@ class Server:
         from ._lib import check
         self._error = None
         rc = fn(self._h, *args)
-        if self._error is not None:
-            e, self._error = self._error, None
-            raise e
+        err, self._error = self._error, None
+        # a callback error the server handled itself (a failed retirement)
+        # leaves the call successful: it shows in that request's status
+        if rc != 0 and err is not None:
+            raise err
         check(rc)
+
+    def cancel(self, key):
+        """Cancel the submitted request ``key`` (queued or resident): it is
+        retired with status ``cancelled``.  False if no queued or resident
+        request has that key."""
+        from ._lib import load
+        found = C.c_int32(0)
+        self._call(load().prtcl_gpu_server_cancel, int(key), C.byref(found))
+        return bool(found.value)
 
     def _status(self):
         from ._lib import ServerStatus, load
@@ -188,18 +202,20 @@ class Server:
         return st
 
     def run(self, requests):
-        """Serve ``requests`` (each submitted when its arrival time has come)
-        until all are done; returns them in retirement order."""
-        from ._lib import RequestResult, load
+        """Serve ``requests`` (each submitted when its arrival time has come,
+        and cancelled at its ``cancel_at``) until all are retired; returns
+        them in retirement order, each with its ``status``.  If a turn
+        raises (a failed batch step), the requests retired so far, the
+        failed ones included, are in ``self.done``."""
+        from ._lib import load
         L = load()
         self._t0 = self.clock()
         pending = deque(sorted(requests, key=lambda r: r.arrival))
         inflight = {}
-        done = []
+        done = self.done = []  # also readable when a turn raised
         buf = np.empty((0, 3), np.float32)
-        res = RequestResult()
-        has = C.c_int32(0)
         stepped = C.c_int32(0)
+        cancelled = set()
         while True:
             now = self.clock() - self._t0
             while pending and pending[0].arrival <= now:
@@ -215,36 +231,52 @@ class Server:
                 req.fluid, req.boundary = len(f), len(bd)
                 req.release()
                 inflight[key] = req
+            for key, req in list(inflight.items()):
+                if req.cancel_at <= now and key not in cancelled:
+                    cancelled.add(key)
+                    self.cancel(key)
             st = self._status()
             if not pending and st.pending == 0 and st.running == 0 and st.results == 0:
                 break
-            self._call(L.prtcl_gpu_server_turn, C.byref(stepped))
-            if self.keep_results and inflight:
-                need = max(r.fluid for r in inflight.values())
-                if len(buf) < need:
-                    buf = np.empty((need, 3), np.float32)
-            while True:
-                self._call(L.prtcl_gpu_server_next_result, C.byref(res),
-                           buf.ctypes.data if self.keep_results else None, len(buf), C.byref(has))
-                if not has.value:
-                    break
-                req = inflight.pop(res.request_id)
-                req.admitted, req.finished = res.admitted, res.finished
-                req.done_steps = int(res.steps)
-                req.info = {k: getattr(res.info, k) for k, _ in res.info._fields_ if k != "pad"}
-                if self.keep_results:
-                    req.result = buf[:req.fluid].copy()
-                done.append(req)
+            try:
+                self._call(L.prtcl_gpu_server_turn, C.byref(stepped))
+            finally:
+                # results retired by the turn, also those of a failed step
+                buf = self._collect(inflight, done, buf)
             if not stepped.value:
                 # nothing resident: wait for the next arrival
                 st = self._status()
-                nxt = min(st.next_arrival, pending[0].arrival if pending else math.inf)
+                nxt = min([st.next_arrival, pending[0].arrival if pending else math.inf]
+                          + [r.cancel_at for k, r in inflight.items() if k not in cancelled])
                 if math.isfinite(nxt):
                     self.sleep(max(0.0, nxt - (self.clock() - self._t0)))
         st = self._status()
         self.steps_run, self.particle_steps = int(st.steps_run), int(st.particle_steps)
         self.makespan = self.clock() - self._t0
         return done
+
+    def _collect(self, inflight, done, buf):
+        """Move the server's unread results onto their requests."""
+        from ._lib import REQUEST_STATUS, RequestResult, load
+        L = load()
+        res, has = RequestResult(), C.c_int32(0)
+        if self.keep_results and inflight:
+            need = max(r.fluid for r in inflight.values())
+            if len(buf) < need:
+                buf = np.empty((need, 3), np.float32)
+        while True:
+            self._call(L.prtcl_gpu_server_next_result, C.byref(res),
+                       buf.ctypes.data if self.keep_results else None, len(buf), C.byref(has))
+            if not has.value:
+                return buf
+            req = inflight.pop(res.request_id)
+            req.admitted, req.finished = res.admitted, res.finished
+            req.done_steps = int(res.steps)
+            req.status = REQUEST_STATUS.get(int(res.status), str(res.status))
+            req.info = {k: getattr(res.info, k) for k, _ in res.info._fields_ if k != "pad"}
+            if self.keep_results and req.status == "done":
+                req.result = buf[:req.fluid].copy()
+            done.append(req)
 
 
 def report(done, makespan, particle_steps, eta=1e-3):

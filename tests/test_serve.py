@@ -152,6 +152,119 @@ def test_batch_errors_reach_the_caller():
         serve(reqs, budget=1e12, batch=FailingBatch)
 
 
+def test_failed_step_retires_the_resident_requests():
+    """A failed batch step leaves the resident scenes' state undefined: each
+    resident request is retired as failed, with the steps it completed, and
+    its scene removed; queued requests stay queued; the server serves on."""
+    clock = Clock()
+    holder = {}
+
+    def factory(p):
+        holder["b"] = FailingBatch(clock)
+        return holder["b"]
+
+    srv = Server(factory, driver.DAM_BREAK_27K, budget_bytes=1e12, clock=clock, sleep=clock.sleep,
+                 bytes_per_particle=1000.0, max_scenes=2)
+    reqs = [Request(rid=k, arrival=0.0, fluid_cells=(2, 2, 2), steps=20) for k in range(3)]
+    with pytest.raises(RuntimeError, match="stand-in step failed"):
+        srv.run(reqs)
+    assert sorted(r.rid for r in srv.done) == [0, 1]
+    assert all(r.status == "failed" and r.result is None and 0 < r.done_steps < 20 for r in srv.done)
+    st = srv._status()
+    assert (st.pending, st.running, st.results) == (1, 0, 0)
+    assert holder["b"].scenes == {}
+
+
+def test_oversized_request_is_refused_at_submit():
+    """A request whose own estimate exceeds the budget is refused even when
+    nothing is resident: it never reaches the device allocator."""
+    from prtcl_gb300 import PrtclGpuError
+    with pytest.raises(PrtclGpuError, match="more than the budget"):
+        serve([Request(rid=0, arrival=0.0, fluid_cells=(4, 4, 4), steps=2)], budget=1000.0 * 100)
+
+
+def test_request_rejected_when_its_estimate_outgrows_the_budget():
+    """The estimate per particle is learnt from the batch: a request that
+    fitted the first estimate at submit but not the learnt one is retired
+    unrun as rejected, and the others are served."""
+    clock = Clock()
+    srv = Server(lambda p: FakeBatch(clock), driver.DAM_BREAK_27K, budget_bytes=1000.0 * 800, clock=clock,
+                 sleep=clock.sleep, bytes_per_particle=10.0)
+    small = Request(rid=0, arrival=0.0, fluid_cells=(2, 2, 2), steps=3)
+    large = Request(rid=1, arrival=0.0, fluid_cells=(6, 6, 6), steps=3)   # 216 fluid + its walls
+    done = srv.run([small, large])
+    st = {r.rid: r for r in done}
+    assert st[0].status == "done" and st[0].done_steps == 3
+    assert st[1].status == "rejected" and st[1].done_steps == 0 and st[1].admitted == -1.0
+
+
+def test_cancel_queued_and_resident_requests():
+    clock = Clock()
+    holder = {}
+
+    def factory(p):
+        holder["b"] = FakeBatch(clock)
+        return holder["b"]
+
+    srv = Server(factory, driver.DAM_BREAK_27K, budget_bytes=1e12, clock=clock, sleep=clock.sleep,
+                 bytes_per_particle=1000.0, max_scenes=1)
+    reqs = [Request(rid=0, arrival=0.0, fluid_cells=(2, 2, 2), steps=10, cancel_at=0.055),   # resident
+            Request(rid=1, arrival=0.0, fluid_cells=(2, 2, 2), steps=10, cancel_at=0.025),   # queued
+            Request(rid=2, arrival=0.0, fluid_cells=(2, 2, 2), steps=4)]
+    done = srv.run(reqs)
+    st = {r.rid: r for r in done}
+    assert st[1].status == "cancelled" and st[1].done_steps == 0 and st[1].admitted == -1.0
+    assert st[0].status == "cancelled" and 0 < st[0].done_steps < 10 and st[0].result is None
+    assert st[2].status == "done" and st[2].done_steps == 4
+    assert [r.rid for r in done] == [1, 0, 2]
+    assert holder["b"].scenes == {}
+    assert srv.cancel(2) is False  # already retired
+
+
+class FlakyReadBatch(FakeBatch):
+    """Stand-in whose download fails once and whose remove fails once."""
+
+    def __init__(self, clock):
+        super().__init__(clock)
+        self.download_failures = 1
+        self.remove_failures = 1
+
+    def download(self, sid, field):
+        if self.download_failures:
+            self.download_failures -= 1
+            raise RuntimeError("stand-in download failed")
+        return super().download(sid, field)
+
+    def remove_scene(self, sid):
+        if self.remove_failures:
+            self.remove_failures -= 1
+            raise RuntimeError("stand-in remove failed")
+        super().remove_scene(sid)
+
+
+def test_failed_retirement_fails_that_request_alone():
+    """A request whose results cannot be read is retired as failed with the
+    steps it asked for (never stepped again); a scene whose removal failed
+    is removed at a later turn."""
+    clock = Clock()
+    holder = {}
+
+    def factory(p):
+        holder["b"] = FlakyReadBatch(clock)
+        return holder["b"]
+
+    srv = Server(factory, driver.DAM_BREAK_27K, budget_bytes=1e12, clock=clock, sleep=clock.sleep,
+                 bytes_per_particle=1000.0)
+    reqs = [Request(rid=0, arrival=0.0, fluid_cells=(2, 2, 2), steps=3),
+            Request(rid=1, arrival=0.0, fluid_cells=(2, 2, 2), steps=6)]
+    done = srv.run(reqs)
+    st = {r.rid: r for r in done}
+    assert st[0].status == "failed" and st[0].done_steps == 3 and st[0].result is None
+    assert st[1].status == "done" and st[1].done_steps == 6 and st[1].result.shape == (8, 3)
+    assert holder["b"].scenes == {}
+    assert srv.particle_steps == 8 * 3 + 8 * 6
+
+
 class RefusingBatch(FakeBatch):
     def add_scene(self, f, b):
         raise MemoryError("stand-in batch is full")
