@@ -22,6 +22,8 @@ Arms:
                      re-query) on all host threads, same scene and metric.
 
 Extra measurements in the same line (rank 0, one GPU; --no-extras skips them):
+  long_run  the 1M dam break over all 500 steps of its configuration: rate and
+            iteration counts over steps 1-250 and 251-500
   plain_27k the reference's plain 27k dam break (IISPH), beside the CPU oracle
   search    neighbour search only, 4M points (uniform / 64 Gaussian blobs),
             radius for 40 mean neighbours, GB/s of algorithmic bytes vs HBM
@@ -48,7 +50,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-from prtcl_gb300 import driver, scenes  # noqa: E402
+from prtcl_gb300 import driver, scenes, tune  # noqa: E402
 
 METRIC = "IISPH particle-steps/s, plain vs batched, at <=0.1% density error; serve p99"
 UNIT = "particle-steps/s"
@@ -85,11 +87,46 @@ def load_peaks():
 
 
 def load_traffic():
+    """Per-launch DRAM bytes (dram__bytes_read.sum + write.sum) of kernels
+    captured with ncu, with the capture's command and the commit of the
+    build it ran on (profiles/ncu_traffic.json)."""
     p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     if os.path.exists(p):
         with open(p) as f:
             return json.load(f)
     return {}
+
+
+TRAFFIC_1M = "dam break 1M fluid + 363,436 boundary"
+
+
+def roofline_block(name, launches, ms, algo_bytes_total, peak, peak_kind, timing, workload=None):
+    """Achieved algorithmic GB/s of one kernel (its algorithmic bytes over
+    all launches / its total CUDA-event time) against the HBM peak; the
+    measured DRAM traffic per launch where a capture of this kernel on this
+    workload is recorded."""
+    avg_s = ms / 1e3 / launches
+    per_launch = algo_bytes_total / launches
+    ach = per_launch / avg_s / 1e9
+    tr = load_traffic()
+    rec = tr.get("kernels", {}).get(name)
+    if rec is not None and rec.get("workload") != workload:
+        rec = None
+    return {"bound": "hbm", "kernel": name, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(ach / peak, 4), "traffic": rec["dram_bytes_per_launch"] if rec else None,
+            "traffic_source": (f"profiles/ncu_traffic.json: {rec['workload']}, captured at commit {tr.get('commit')}"
+                               if rec else None),
+            "peak_kind": peak_kind, "algorithmic_bytes_per_launch": int(per_launch),
+            "avg_launch_us": round(avg_s * 1e6, 2), "launches": launches, "timing": timing}
+
+
+def kernel_bytes(name, launches, nf, nb):
+    """Algorithmic bytes of `launches` launches of a kernel over nf fluid and
+    nb boundary items each (None for kernels without a formula)."""
+    if name not in ALGO_BYTES:
+        return None
+    bf, bb = ALGO_BYTES[name]
+    return launches * (bf * nf + bb * nb)
 
 
 class Clocks:
@@ -211,19 +248,45 @@ def timed_steps(d, loop, K):
     return e0.elapsed_time(e1) / 1e3, wall, launches
 
 
+def config_of(args, nf, nb, world):
+    """The workload description both arms print (identical keys and values
+    for the same arguments)."""
+    return {"workload": ("dam break 1M fluid + %d boundary, IISPH + WKBB18 PCG, dt 5e-4 s" % nb)
+            if args.config == "1m" else "dam break 27k fluid + %d boundary, IISPH + WKBB18 PCG, dt 1e-3 s" % nb,
+            "fluid_particles": nf, "boundary_particles": nb, "replicas": world,
+            "parallelism": "replicas only" if world > 1 else "single GPU",
+            "l2": "inputs larger than L2 (no flush)", "steps_timed": f"{args.steps} after {args.warmup} warm-up"}
+
+
 def workload(args):
     if args.config == "1m":
         return scenes.dam_break_1m(), driver.DAM_BREAK_1M
     return scenes.dam_break(), dict(driver.DAM_BREAK_27K, viscosity=True)
 
 
+def tuned(kind, sc, p):
+    """The autotuner's knob choice for a workload (tuned on a copy of it
+    unless cached) and how it was obtained."""
+    t0 = time.perf_counter()
+    if kind == "plain":
+        choice, source, _ = tune.tune_plain(sc, p)
+        wl = tune.workload_class("plain", len(sc["fluid"]))
+    else:
+        choice, source, _ = tune.tune_batched(sc, p)
+        wl = tune.workload_class("batched", sum(len(x["fluid"]) for x in sc), len(sc))
+    return choice, {"choice": choice, "source": source, "workload_class": wl,
+                    "seconds": round(time.perf_counter() - t0, 2)}
+
+
 def run_ours(args, rank, world, dist):
     from prtcl_gb300.core import DeviceScene
     sc, p = workload(args)
     nf, nb = len(sc["fluid"]), len(sc["boundary"])
+    choice, tuning = tuned("plain", sc, p)
 
     d = DeviceScene()
     driver.setup_dam_break(d, sc, p)
+    tune.apply(d.model, choice)
     loop = driver.StepLoop(d, p, device_loop=True)
     for _ in range(args.warmup):
         loop.step(quiet=True)
@@ -240,43 +303,18 @@ def run_ours(args, rank, world, dist):
     # per-kernel CUDA-event timing, live in this process: a few more steps
     # with timing events around every launch (device loops driven from the
     # host so that each launch is timed; same kernels)
-    d.model.profile(True)
-    d.model.profile_reset()
     nvtx = nvtx_range("profile_pass")
-    for _ in range(args.profile_steps):
-        loop.step(quiet=True)
-    d.synchronize()
+    prof = profile_pass(d, loop, args.profile_steps)
     nvtx_end(nvtx)
-    prof = d.model.profile_read()
-    d.model.profile(False)
 
     peak, peak_kind = load_peaks()
-    top = max(prof.items(), key=lambda kv: kv[1][1]) if prof else None
-    roof = None
-    if top:
-        name, (cnt, ms) = top
-        bf, bb = ALGO_BYTES.get(name, (0, 0))
-        per_launch = bf * nf + bb * nb
-        if name == "nhood_lists":
-            # per fluid query its position and count (16 B), per listed pair
-            # (fluid and boundary neighbours) an index and a gradient factor
-            # (8 B); the pairs of the lists as they stand after the pass
-            d.update()
-            pairs = d.nhood.query(d.model.get_group("f").index, count_pairs=True)
-            per_launch = LIST_BYTES_PER_QUERY * nf + LIST_BYTES_PER_PAIR * pairs
-        avg_s = ms / 1e3 / cnt
-        ach = per_launch / avg_s / 1e9
-        tr = load_traffic().get(name)
-        total_ms = sum(m for _, m in prof.values())
-        roof = {"bound": "hbm", "kernel": name, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(ach / peak, 4), "traffic": tr, "peak_kind": peak_kind,
-                "algorithmic_bytes_per_launch": per_launch, "avg_launch_us": round(avg_s * 1e6, 2),
-                "launches": cnt, "share_of_kernel_time": round(ms / total_ms, 4),
-                "timing": f"CUDA events around each launch over {args.profile_steps} extra steps"}
+    roof = plain_roofline(d, prof, nf, nb, peak, peak_kind,
+                          f"CUDA events around each launch over {args.profile_steps} extra steps",
+                          TRAFFIC_1M if args.config == "1m" else None)
 
     e2e = None
     if not args.no_e2e:
-        e2e = run_e2e(args, sc, p, nf, dist, world)
+        e2e = run_e2e(args, sc, p, nf, dist, world, choice)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -284,9 +322,10 @@ def run_ours(args, rank, world, dist):
 
     extras = {}
     if rank == 0 and world == 1 and not args.no_extras:
-        extras["plain_27k"] = run_plain_27k(args.no_cpu_baseline)
-        extras["search"] = run_search(peak)
-        extras["batched"] = run_batched()
+        extras["long_run"] = run_long(peak)
+        extras["plain_27k"] = run_plain_27k(args.no_cpu_baseline, peak=peak, peak_kind=peak_kind)
+        extras["search"] = run_search(peak, no_cpu=args.no_cpu_baseline)
+        extras["batched"] = run_batched(peak=peak, peak_kind=peak_kind, no_cpu=args.no_cpu_baseline)
         extras["serving"] = run_serving()
 
     solves = max(st["jacobi_solves"], 1.0)
@@ -295,17 +334,14 @@ def run_ours(args, rank, world, dist):
         "warmup": args.warmup, "ms_per_step": round(secs * 1e3 / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 convergence reductions)",
         "data": "synthetic (seeded lattice dam break generated in-process)",
-        "config": {"workload": ("dam break 1M fluid + %d boundary, IISPH + WKBB18 PCG, dt 5e-4 s" % nb)
-                   if args.config == "1m" else "dam break 27k fluid, IISPH + WKBB18 PCG, dt 1e-3 s",
-                   "fluid_particles": nf, "boundary_particles": nb, "replicas": world,
-                   "parallelism": "replicas only" if world > 1 else "single GPU",
-                   "l2": "inputs larger than L2 (no flush)",
-                   "jacobi_iterations_mean": round(st["jacobi_iterations"] / solves, 3),
+        "config": config_of(args, nf, nb, world),
+        "solver": {"jacobi_iterations_mean": round(st["jacobi_iterations"] / solves, 3),
                    "jacobi_capped_steps": int(st["jacobi_capped"]),
                    "max_relative_density_error": st["max_relative_aprde"],
                    "pcg_iterations_mean": round(st["pcg_iterations"] / max(st["pcg_solves"], 1.0), 3),
                    "wall_s": round(wall, 3)},
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": int(launches),
+        "tuning": tuning,
         "kernels": {k: {"launches": c, "ms": round(m, 3), "us_per_launch": round(1e3 * m / c, 2)}
                     for k, (c, m) in prof.items()},
         **extras,
@@ -314,7 +350,27 @@ def run_ours(args, rank, world, dist):
         print(json.dumps(line))
 
 
-def run_e2e(args, sc, p, nf, dist, world):
+def plain_roofline(d, prof, nf, nb, peak, peak_kind, timing, workload=None):
+    """Roofline block of the dominant kernel of a single-scene profile."""
+    if not prof:
+        return None
+    name, (cnt, ms) = max(prof.items(), key=lambda kv: kv[1][1])
+    total = kernel_bytes(name, cnt, nf, nb)
+    if name == "nhood_lists":
+        # per fluid query its position and count (16 B), per listed pair
+        # (fluid and boundary neighbours) an index and a gradient factor
+        # (8 B); the pairs of the lists as they stand after the pass
+        d.update()
+        pairs = d.nhood.query(d.model.get_group("f").index, count_pairs=True)
+        total = cnt * (LIST_BYTES_PER_QUERY * nf + LIST_BYTES_PER_PAIR * pairs)
+    if total is None:
+        return {"kernel": name, "frac": None, "note": "no algorithmic-byte formula for this kernel"}
+    roof = roofline_block(name, cnt, ms, total, peak, peak_kind, timing, workload)
+    roof["share_of_kernel_time"] = round(ms / sum(m for _, m in prof.values()), 4)
+    return roof
+
+
+def run_e2e(args, sc, p, nf, dist, world, choice=None):
     """Same metric through the public API with host buffers: upload of the
     scene from pinned host memory (set-up included) and a per-step download
     of the fluid positions, all inside the timed region."""
@@ -343,6 +399,8 @@ def run_e2e(args, sc, p, nf, dist, world):
     barrier(dist)
     t0 = time.perf_counter()
     d = DeviceScene()
+    if choice:
+        tune.apply(d.model, choice)
     h2d = 0
     driver.setup_dam_break(d, scene, p)
     h2d += sum(a.nbytes for a in host.values()) + nf * (12 + 12 + 4 + 4) + len(sc["boundary"]) * 4
@@ -375,28 +433,54 @@ def cpu_baseline(sc, p, nf, steps=2, threads=0):
             "sample": f"{steps} steps of the same scene after set-up and one warm step ({secs:.1f} s)"}
 
 
-def run_plain_27k(no_cpu=False, steps=100, warmup=3, cpu_steps=10):
+def profile_pass(d, loop, steps):
+    """{kernel: (launches, ms)} over `steps` more steps with CUDA events
+    around every launch (device loops driven from the host)."""
+    d.model.profile(True)
+    d.model.profile_reset()
+    for _ in range(steps):
+        loop.step(quiet=True)
+    d.synchronize()
+    prof = d.model.profile_read()
+    d.model.profile(False)
+    return prof
+
+
+def run_plain_27k(no_cpu=False, steps=100, warmup=3, cpu_steps=10, peak=None, peak_kind=None):
     """The reference's plain configuration: the 27,000-particle dam break
     (spacing 0.025 m, 2 x 1 x 1 m box, dt 1e-3 s, IISPH to 0.1 % or 100
     iterations), `steps` timed steps of the device step loop after `warmup`,
-    beside the CPU oracle (reference mode, all host threads) on `cpu_steps`
-    steps of the same scene."""
+    the roofline of its dominant kernel, the same steps end to end through
+    the public API (upload from pinned host memory, a position frame
+    downloaded per step), beside the CPU oracle (reference mode, all host
+    threads) on `cpu_steps` steps of the same scene."""
+    from types import SimpleNamespace
+
     from prtcl_gb300.core import DeviceScene
     sc, p = scenes.dam_break(), dict(driver.DAM_BREAK_27K)
-    nf = len(sc["fluid"])
+    nf, nb = len(sc["fluid"]), len(sc["boundary"])
+    choice, tuning = tuned("plain", sc, p)
     d = DeviceScene()
     driver.setup_dam_break(d, sc, p)
+    tune.apply(d.model, choice)
     loop = driver.StepLoop(d, p, device_loop=True)
     for _ in range(warmup):
         loop.step(quiet=True)
     d.model.stats(reset=True)
-    secs, wall, _ = timed_steps(d, loop, steps)
+    secs, wall, launches = timed_steps(d, loop, steps)
     st = d.model.stats(reset=True)
-    out = {"workload": "dam break 27k fluid + %d boundary, IISPH, dt 1e-3 s" % len(sc["boundary"]),
+    out = {"workload": "dam break 27k fluid + %d boundary, IISPH, dt 1e-3 s" % nb,
            "steps": steps, "warmup": warmup, "value": round(nf * steps / secs, 1), "unit": UNIT,
-           "ms_per_step": round(secs * 1e3 / steps, 4),
+           "ms_per_step": round(secs * 1e3 / steps, 4), "gpu_launches": int(launches),
            "jacobi_iterations_mean": round(st["jacobi_iterations"] / max(st["jacobi_solves"], 1.0), 3),
-           "jacobi_capped_steps": int(st["jacobi_capped"]), "max_relative_density_error": st["max_relative_aprde"]}
+           "jacobi_capped_steps": int(st["jacobi_capped"]), "max_relative_density_error": st["max_relative_aprde"],
+           "tuning": tuning}
+    if peak is not None:
+        prof = profile_pass(d, loop, 5)
+        out["roofline"] = plain_roofline(d, prof, nf, nb, peak, peak_kind,
+                                         "CUDA events around each launch over 5 extra steps")
+    del loop, d
+    out["e2e"] = run_e2e(SimpleNamespace(steps=steps), sc, p, nf, None, 1, choice)
     if not no_cpu:
         from oracle import oracle as O
         O.build()
@@ -415,7 +499,59 @@ def run_plain_27k(no_cpu=False, steps=100, warmup=3, cpu_steps=10):
     return out
 
 
-def run_search(peak, n=4_000_000, reps=5, target=40.0):
+def run_long(peak, steps=500, split=250):
+    """Config 2 over its full 500 steps (the dam break develops, so the
+    iteration counts change): particle-steps/s, mean Jacobi and PCG
+    iterations over steps 1-250 and 251-500, each half timed with CUDA
+    events on the model's stream."""
+    from prtcl_gb300.core import DeviceScene
+    sc, p = scenes.dam_break_1m(), driver.DAM_BREAK_1M
+    nf = len(sc["fluid"])
+    choice, tuning = tuned("plain", sc, p)
+    d = DeviceScene()
+    driver.setup_dam_break(d, sc, p)
+    tune.apply(d.model, choice)
+    loop = driver.StepLoop(d, p, device_loop=True)
+    out = {"workload": "dam break 1M fluid, IISPH + WKBB18 PCG, dt 5e-4 s, steps 1-%d" % steps, "unit": UNIT,
+           "tuning": tuning}
+    for lo, hi in ((1, split), (split + 1, steps)):
+        d.model.stats(reset=True)
+        secs, _, _ = timed_steps(d, loop, hi - lo + 1)
+        st = d.model.stats(reset=True)
+        out[f"steps_{lo}_{hi}"] = {
+            "value": round(nf * (hi - lo + 1) / secs, 1), "ms_per_step": round(secs * 1e3 / (hi - lo + 1), 3),
+            "jacobi_iterations_mean": round(st["jacobi_iterations"] / max(st["jacobi_solves"], 1.0), 3),
+            "jacobi_capped_steps": int(st["jacobi_capped"]),
+            "max_relative_density_error": st["max_relative_aprde"],
+            "pcg_iterations_mean": round(st["pcg_iterations"] / max(st["pcg_solves"], 1.0), 3)}
+    x = d.get_varying("f", "position")
+    out["final_state_finite"] = bool(np.isfinite(x).all())
+    return out
+
+
+def search_cpu_baseline(pts, r, n):
+    """The oracle's grid update + the neighbour sets of every point (the
+    reference's grid restated, OpenMP on all host threads), one full 4M
+    search timed on the host."""
+    from oracle import oracle as O
+    O.build()
+    th = O.set_threads(0)
+    o = O.Scene(np.float32)
+    o.add_group("p", "fluid")
+    o.resize("p", n)
+    o.set_varying("p", "position", pts)
+    o.set_radius(r)
+    t0 = time.perf_counter()
+    o.update()
+    offs, _ = o.neighbor_lists(0, 0, n, cap=n * 48)
+    sec = time.perf_counter() - t0
+    nbar = offs[-1] / n
+    return {"value": round(n / sec, 1), "unit": "points/s", "cores": th, "kind": "port",
+            "ms_per_search": round(sec * 1e3, 1), "achieved_GBps": round(float((32 + 4 * nbar) * n / sec / 1e9), 2),
+            "sample": f"one full search (grid update + neighbour sets of all {n} points)"}
+
+
+def run_search(peak, n=4_000_000, reps=5, target=40.0, no_cpu=False):
     """Neighbour search only (4M points in the unit cube, uniform and 64
     Gaussian blobs): grid update + the neighbour sets of every point, radius
     calibrated on the device to a mean of `target` neighbours (self
@@ -457,10 +593,65 @@ def run_search(peak, n=4_000_000, reps=5, target=40.0):
                      "achieved_GBps": round(algo / sec / 1e9, 1), "frac_of_hbm_peak": round(algo / sec / 1e9 / peak, 4),
                      "algorithmic_bytes": int(algo)}
         del d
+        if not no_cpu:
+            out[dist]["cpu_baseline"] = search_cpu_baseline(pts, r, n)
     return out
 
 
-def run_batched(count=256, steps=10, warmup=3, plain_steps=5):
+def batched_roofline(prof, sc, before, after, peak, peak_kind, timing):
+    """Roofline of the dominant kernel of a batch profile.  A launch of a
+    per-step procedure covers every scene; a relaxed-Jacobi sweep covers the
+    scenes still iterating, so its items are the scenes' iteration counts
+    over the profiled steps times their particle counts."""
+    nf = sum(len(x["fluid"]) for x in sc)
+    nb = sum(len(x["boundary"]) for x in sc)
+    dit = [a["jacobi_iterations"] - b["jacobi_iterations"] for a, b in zip(after, before)]
+    jf = sum(k * len(x["fluid"]) for k, x in zip(dit, sc))
+    jb = sum(k * len(x["boundary"]) for k, x in zip(dit, sc))
+    best = None
+    for name, (cnt, ms) in prof.items():
+        if name in ("iisph_accel", "iisph_pressure"):
+            bf, bb = ALGO_BYTES[name]
+            total = bf * jf + bb * jb
+        else:
+            total = kernel_bytes(name, cnt, nf, nb)
+        if total is not None and (best is None or ms > best[2]):
+            best = (name, cnt, ms, total)
+    if best is None:
+        return None
+    roof = roofline_block(*best, peak, peak_kind, timing)
+    top = max(prof.items(), key=lambda kv: kv[1][1])
+    roof["share_of_kernel_time"] = round(best[2] / sum(m for _, m in prof.values()), 4)
+    if top[0] != best[0]:
+        roof["top_kernel_without_formula"] = {"kernel": top[0], "ms": round(top[1][1], 3)}
+    return roof
+
+
+def batched_cpu_baseline(sc, p, every=32, steps=3):
+    """The oracle (reference mode, all host threads) on a fixed subset of the
+    batch's scenes (every `every`-th), one after another, `steps` steps each
+    after set-up and one warm step."""
+    from oracle import oracle as O
+    O.build()
+    th = O.set_threads(0)
+    sub = sc[::every]
+    secs, work = 0.0, 0
+    for x in sub:
+        o = O.Scene(np.float32, fp64_reductions=False)
+        driver.setup_dam_break(o, x, p)
+        o.step(permute=False, max_iters=p["max_iters"], eta=p["eta"], viscosity=False)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            o.step(permute=False, max_iters=p["max_iters"], eta=p["eta"], viscosity=False)
+        secs += time.perf_counter() - t0
+        work += len(x["fluid"]) * steps
+    return {"value": round(work / secs, 1), "unit": UNIT, "cores": th, "kind": "port",
+            "sample": f"{len(sub)} of the {len(sc)} scenes (one in {every}, {sum(len(x['fluid']) for x in sub)} "
+                      f"fluid particles), {steps} steps each after set-up and one warm step"}
+
+
+def run_batched(count=256, steps=10, warmup=3, plain_steps=5, peak=None, peak_kind=None, no_cpu=False,
+                profile_steps=3):
     """256 dam-break scenes, fluid counts log-uniform in 2,000-200,000,
     aspect ratios uniform in [0.5, 2], boxes 2x the fluid extent, parameters
     of the 27k dam break: all scenes stepped together by one batch, against
@@ -473,7 +664,9 @@ def run_batched(count=256, steps=10, warmup=3, plain_steps=5):
     sc = scenes.mixed_batch(count=count)
     nf = sum(len(x["fluid"]) for x in sc)
     nb = sum(len(x["boundary"]) for x in sc)
+    choice, tuning = tuned("batched", sc, p)
     bt = Batch(p)
+    tune.apply(bt, choice)
     ids = [bt.add_scene(x["fluid"], x["boundary"]) for x in sc]
     bt.step(warmup)
     bt.synchronize()
@@ -487,11 +680,28 @@ def run_batched(count=256, steps=10, warmup=3, plain_steps=5):
     solves = sum(a["jacobi_solves"] - b["jacobi_solves"] for a, b in zip(after, before))
     iters = sum(a["jacobi_iterations"] - b["jacobi_iterations"] for a, b in zip(after, before))
     capped = sum(a["jacobi_capped"] - b["jacobi_capped"] for a, b in zip(after, before))
+    roof, kernels = None, None
+    if peak is not None:
+        bt.profile(True)
+        bt.step(1)
+        bt.synchronize()
+        bt.profile_read()
+        b0 = [bt.info(i) for i in ids]
+        bt.step(profile_steps)
+        bt.synchronize()
+        prof = bt.profile_read()
+        b1 = [bt.info(i) for i in ids]
+        bt.profile(False)
+        roof = batched_roofline(prof, sc, b0, b1, peak, peak_kind,
+                                f"CUDA events around each launch over {profile_steps} extra steps")
+        kernels = {k: {"launches": c, "ms_per_step": round(m / profile_steps, 3)} for k, (c, m) in prof.items()}
     del bt
     tp, work = 0.0, 0
     for x in sc:
+        cx, _ = tuned("plain", x, p)  # tuned per size class too, so the ratio compares tuned paths
         d = DeviceScene()
         driver.setup_dam_break(d, x, p)
+        tune.apply(d.model, cx)
         loop = driver.StepLoop(d, p, device_loop=True)
         for _ in range(warmup):
             loop.step(quiet=True)
@@ -509,7 +719,9 @@ def run_batched(count=256, steps=10, warmup=3, plain_steps=5):
             "value": round(v, 1), "unit": UNIT, "ms_per_step": round(secs * 1e3 / steps, 3),
             "plain_value": round(vp, 1), "plain_sample": f"{plain_steps} steps of each scene after {warmup} warm-up",
             "batched_over_plain": round(v / vp, 2), "jacobi_iterations_mean": round(iters / max(solves, 1), 3),
-            "jacobi_capped_steps": int(capped), "device_GB": round(gb, 2)}
+            "jacobi_capped_steps": int(capped), "device_GB": round(gb, 2), "roofline": roof, "kernels": kernels,
+            "tuning": tuning,
+            "cpu_baseline": None if no_cpu else batched_cpu_baseline(sc, p)}
 
 
 def run_serving(count=48, rate=4.0):
@@ -559,9 +771,8 @@ def run_reference(args, rank, world, dist):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs * 1e3 / args.steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded lattice dam break generated in-process)",
-            "config": {"workload": "dam break 1M fluid, IISPH + WKBB18 PCG, dt 5e-4 s" if args.config == "1m"
-                       else "dam break 27k fluid, IISPH + WKBB18 PCG, dt 1e-3 s",
-                       "jacobi_iterations_mean": float(np.mean(its))},
+            "config": config_of(args, nf, len(sc["boundary"]), world),
+            "solver": {"jacobi_iterations_mean": float(np.mean(its))},
             "cpu_baseline": {"value": round(v, 1), "unit": UNIT, "cores": th, "kind": "port",
                              "sample": f"{args.steps} full steps after {args.warmup} warm-up steps"},
             "e2e": {"value": round(v, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

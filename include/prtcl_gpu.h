@@ -163,6 +163,21 @@ int prtcl_gpu_profile_enable(prtcl_gpu_model *model, int32_t enable);
 int prtcl_gpu_profile_read(prtcl_gpu_model *model, char *buf, int64_t size, int64_t *needed_out);
 int prtcl_gpu_profile_reset(prtcl_gpu_model *model);
 
+/* Launch-shape knobs of the neighbour sweeps and the relaxed-Jacobi loop
+ * (no counterpart in the reference, whose loops are OpenMP-scheduled).
+ * Every value gives bit-identical results; they change only speed.  Knobs
+ * carry the kernels' profile names: density, iisph_setup, iisph_accel,
+ * iisph_pressure, wkbb18_diag, pcg_init, pcg_q (values 0..3, a launch
+ * shape each) and jacobi_unroll (1, 2 or 4 relaxed-Jacobi iterations per
+ * iteration of the device loop's graph).  prtcl_gb300/tune.py searches them
+ * per workload and caches the choice.  prtcl_gpu_tune_knobs returns one line
+ * per knob: "name default value=shape ...", a shape written as threads per
+ * block x blocks per SM / neighbour-walk batch.  An unknown knob gives
+ * PRTCL_GPU_NOT_FOUND, a value outside its set PRTCL_GPU_INVALID. */
+int prtcl_gpu_tune_knobs(char *buf, int64_t size, int64_t *needed_out);
+int prtcl_gpu_model_tune_set(prtcl_gpu_model *model, const char *knob, int32_t value);
+int prtcl_gpu_model_tune_get(prtcl_gpu_model *model, const char *knob, int32_t *value_out);
+
 /* ---- neighbourhood: replaces prtcl::Neighborhood (util/neighborhood.hpp:23-42) ---- */
 
 int prtcl_gpu_nhood_create(prtcl_gpu_nhood **out);
@@ -300,6 +315,10 @@ int prtcl_gpu_batch_device_bytes(prtcl_gpu_batch *batch, int64_t *bytes_out);
 int prtcl_gpu_batch_profile_enable(prtcl_gpu_batch *batch, int32_t enable);
 /* Per-kernel timing lines "name launches total_ms", as prtcl_gpu_profile_read. */
 int prtcl_gpu_batch_profile_read(prtcl_gpu_batch *batch, char *buf, int64_t size, int64_t *needed_out);
+/* The knobs of prtcl_gpu_model_tune_set for the batch's model; the tiled
+ * sweeps of a batch use the batched shapes of prtcl_gpu_tune_knobs. */
+int prtcl_gpu_batch_tune_set(prtcl_gpu_batch *batch, const char *knob, int32_t value);
+int prtcl_gpu_batch_tune_get(prtcl_gpu_batch *batch, const char *knob, int32_t *value_out);
 
 /* ---- Serving: continuous batching of simulation requests ----------------
  * The reference runs one scene per process (share/scripts/prtcl-lua.example.lua);

@@ -68,6 +68,9 @@ SIGNATURES = {
     "prtcl_gpu_profile_enable": [vp, i32],
     "prtcl_gpu_profile_read": [vp, C.c_char_p, i64, i64p],
     "prtcl_gpu_profile_reset": [vp],
+    "prtcl_gpu_tune_knobs": [C.c_char_p, i64, i64p],
+    "prtcl_gpu_model_tune_set": [vp, cp, i32],
+    "prtcl_gpu_model_tune_get": [vp, cp, i32p],
     "prtcl_gpu_nhood_create": [pp],
     "prtcl_gpu_nhood_destroy": [vp],
     "prtcl_gpu_nhood_set_radius": [vp, dbl],
@@ -105,6 +108,8 @@ SIGNATURES = {
     "prtcl_gpu_batch_device_bytes": [vp, i64p],
     "prtcl_gpu_batch_profile_enable": [vp, i32],
     "prtcl_gpu_batch_profile_read": [vp, C.c_char_p, i64, i64p],
+    "prtcl_gpu_batch_tune_set": [vp, cp, i32],
+    "prtcl_gpu_batch_tune_get": [vp, cp, i32p],
     "prtcl_gpu_server_create": [vp, vp, pp],
     "prtcl_gpu_server_create_custom": [vp, vp, vp, pp],
     "prtcl_gpu_server_destroy": [vp],

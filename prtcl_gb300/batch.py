@@ -108,6 +108,15 @@ class Batch:
     def profile(self, enable=True):
         check(load().prtcl_gpu_batch_profile_enable(self._h, 1 if enable else 0))
 
+    def tune_set(self, knob, value):
+        """Set a launch-shape knob of the batch's model (bit-identical)."""
+        check(load().prtcl_gpu_batch_tune_set(self._h, b(knob), int(value)))
+
+    def tune_get(self, knob):
+        v = C.c_int32(0)
+        check(load().prtcl_gpu_batch_tune_get(self._h, b(knob), C.byref(v)))
+        return v.value
+
     def profile_read(self):
         out = {}
         for line in read_str(load().prtcl_gpu_batch_profile_read, self._h).splitlines():

@@ -52,7 +52,10 @@ def build(force=False, verbose=False, extra=()):
 
     def compile_one(src):
         obj = os.path.join(OBJ, src.replace(".cu", ".o"))
-        cmd = [cc, *ARCH, *FLAGS, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
+        # the sweep kernels' variants make schemes.cu the longest unit:
+        # its device code is optimised in parallel partitions
+        split = [f"--split-compile={min(8, os.cpu_count() or 1)}"] if src == "schemes.cu" else []
+        cmd = [cc, *ARCH, *FLAGS, *split, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")

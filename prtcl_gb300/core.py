@@ -298,6 +298,16 @@ class Model:
     def profile_reset(self):
         check(load().prtcl_gpu_profile_reset(self._h))
 
+    def tune_set(self, knob, value):
+        """Set a launch-shape knob (prtcl_gpu_model_tune_set): bit-identical
+        results, different speed."""
+        check(load().prtcl_gpu_model_tune_set(self._h, b(knob), int(value)))
+
+    def tune_get(self, knob):
+        v = C.c_int32(0)
+        check(load().prtcl_gpu_model_tune_get(self._h, b(knob), C.byref(v)))
+        return v.value
+
     AddGroup = add_group
     GetGroup = get_group
     GetGroupCount = lambda self: self.group_count  # noqa: E731

@@ -376,6 +376,38 @@ int prtcl_gpu_profile_reset(prtcl_gpu_model *model) {
   return guard([&] { model->m.prof.reset(); });
 }
 
+namespace {
+int tune_set(Model &m, const char *knob, int32_t value) {
+  int k = tune_knob_find(knob);
+  if (k < 0) return fail(PRTCL_GPU_NOT_FOUND, std::string("unknown tuning knob: ") + knob);
+  if (!tune_value_ok(k, value))
+    return fail(PRTCL_GPU_INVALID, "invalid argument: value " + std::to_string(value) + " for knob " + knob);
+  m.tune.v[k] = value;
+  return PRTCL_GPU_OK;
+}
+int tune_get(Model &m, const char *knob, int32_t *value_out) {
+  int k = tune_knob_find(knob);
+  if (k < 0) return fail(PRTCL_GPU_NOT_FOUND, std::string("unknown tuning knob: ") + knob);
+  *value_out = m.tune.v[k];
+  return PRTCL_GPU_OK;
+}
+} // namespace
+
+int prtcl_gpu_tune_knobs(char *buf, int64_t size, int64_t *needed_out) {
+  return write_str(tune_knob_table(), buf, size, needed_out);
+}
+int prtcl_gpu_model_tune_set(prtcl_gpu_model *model, const char *knob, int32_t value) {
+  NEED(model);
+  NEED(knob);
+  return tune_set(model->m, knob, value);
+}
+int prtcl_gpu_model_tune_get(prtcl_gpu_model *model, const char *knob, int32_t *value_out) {
+  NEED(model);
+  NEED(knob);
+  NEED(value_out);
+  return tune_get(model->m, knob, value_out);
+}
+
 int prtcl_gpu_nhood_create(prtcl_gpu_nhood **out) {
   NEED(out);
   return guard([&] { *out = new prtcl_gpu_nhood(); });
@@ -578,6 +610,17 @@ int prtcl_gpu_batch_device_bytes(prtcl_gpu_batch *batch, int64_t *bytes_out) {
 int prtcl_gpu_batch_profile_enable(prtcl_gpu_batch *batch, int32_t enable) {
   NEED(batch);
   return guard([&] { batch->b->model().prof.enabled = enable != 0; });
+}
+int prtcl_gpu_batch_tune_set(prtcl_gpu_batch *batch, const char *knob, int32_t value) {
+  NEED(batch);
+  NEED(knob);
+  return tune_set(batch->b->model(), knob, value);
+}
+int prtcl_gpu_batch_tune_get(prtcl_gpu_batch *batch, const char *knob, int32_t *value_out) {
+  NEED(batch);
+  NEED(knob);
+  NEED(value_out);
+  return tune_get(batch->b->model(), knob, value_out);
 }
 int prtcl_gpu_batch_profile_read(prtcl_gpu_batch *batch, char *buf, int64_t size, int64_t *needed_out) {
   NEED(batch);

@@ -133,6 +133,36 @@ struct Segments {
   void assign(Group const *g, std::vector<uint32_t> const &count, cudaStream_t s);
 };
 
+// Launch-shape knobs of the neighbour sweeps and the relaxed-Jacobi loop,
+// set per model (by the autotuner, prtcl_gb300/tune.py, or by hand).  Every
+// value gives bit-identical fields: a sweep variant changes only the
+// threads per block (sweeps without a reduction), the blocks resident per SM
+// (the register cap) and the neighbour-walk batch; the Jacobi value repeats
+// the loop body that many times per graph iteration, the repeats past
+// convergence doing nothing.  The variants apply to models with one fluid
+// and at most one boundary group; other layouts use variant 0.
+enum TuneKnob : int {
+  kTuneDensity = 0,
+  kTuneSetup,
+  kTuneAccel,
+  kTunePressure,
+  kTuneDiag,
+  kTunePcgInit,
+  kTunePcgQ,
+  kTuneJacobiUnroll,
+  kTuneKnobs
+};
+struct Tuning {
+  int v[kTuneKnobs] = {0, 0, 0, 0, 0, 0, 0, 1};
+};
+// knob names (the kernels' profiler names; "jacobi_unroll") and allowed values
+char const *tune_knob_name(int k);
+int tune_knob_find(std::string const &name); // -1 if unknown
+bool tune_value_ok(int k, int v);
+// one line per knob: "name default: value=description ..." (plain and
+// batched variants differ for the reducing sweeps)
+std::string tune_knob_table();
+
 class Model {
 public:
   Model();
@@ -178,6 +208,7 @@ public:
   double *stats_d = nullptr;
   void stats_reset(cudaStream_t s);
   Profiler prof;                 // optional per-kernel CUDA-event timing
+  Tuning tune;                   // launch-shape knobs (all bit-identical)
   // scene segments (batched models only)
   std::unique_ptr<Segments> seg;
   // bytes of the varying fields and packed records

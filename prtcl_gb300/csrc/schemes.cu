@@ -24,6 +24,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <tuple>
 
 namespace prtcl_gpu {
 
@@ -132,6 +133,50 @@ __device__ bool reduce_commit(double const (&v)[NV], Red const &R, double (&out)
 
 unsigned red_grid(size_t n) { return unsigned(std::min<size_t>(div_up(n, kNT), kMaxRedBlocks)); }
 
+// Launch shapes of the tuned sweeps (Model::tune): threads per block,
+// blocks resident per SM (which caps the registers) and the neighbour-walk
+// batch.  Entry 0 is the default.  Every entry computes the same bits: the
+// per-item arithmetic does not depend on the shape, and the sweeps with an
+// FP64 reduction keep 128 threads per block and their grid, so the shape of
+// the reduction tree does not change.
+template <int NT_, int MINB_, int BT_> struct Shape {
+  static constexpr int nt = NT_, minb = MINB_, bt = BT_;
+};
+// sweeps without a reduction: the block size may change too
+template <int B0, int B1>
+using FreeShapes = std::tuple<Shape<kNT, kMinBlocks, B0>, Shape<kNT, kMinBlocks, B1>, Shape<256, 4, B0>,
+                              Shape<512, 2, B0>>;
+// sweeps with an FP64 reduction, and the tiled sweeps of a batched model
+template <int B0, int B1>
+using RedShapes = std::tuple<Shape<kNT, kMinBlocks, B0>, Shape<kNT, kMinBlocks, B1>, Shape<kNT, 6, B0>,
+                             Shape<kNT, 12, B0>>;
+// f(shape) with the knob's shape where the layout is tuned, else the default
+template <class Shapes, bool Tuned, class F> void with_shape(int v, F &&f) {
+  if constexpr (Tuned) {
+    switch (v) {
+    case 1: f(std::tuple_element_t<1, Shapes>{}); return;
+    case 2: f(std::tuple_element_t<2, Shapes>{}); return;
+    case 3: f(std::tuple_element_t<3, Shapes>{}); return;
+    default: break;
+    }
+  }
+  f(std::tuple_element_t<0, Shapes>{});
+}
+template <class Sh> std::string shape_text() {
+  return std::to_string(Sh::nt) + "x" + std::to_string(Sh::minb) + "/" + std::to_string(Sh::bt);
+}
+template <class Shapes> std::string shapes_text() {
+  return "0=" + shape_text<std::tuple_element_t<0, Shapes>>() + " 1=" + shape_text<std::tuple_element_t<1, Shapes>>() +
+         " 2=" + shape_text<std::tuple_element_t<2, Shapes>>() + " 3=" + shape_text<std::tuple_element_t<3, Shapes>>();
+}
+using DensityShapes = FreeShapes<16, 8>;
+using SetupShapes = FreeShapes<8, 16>;
+using AccelShapes = FreeShapes<8, 16>;
+using AccelSegShapes = RedShapes<8, 16>;
+using PressureShapes = RedShapes<16, 8>;
+using DiagShapes = FreeShapes<8, 16>;
+using PcgShapes = RedShapes<8, 16>;
+
 // Batched (segmented) models: block b of a tiled launch handles tile b, up to
 // kSegTile consecutive items of one slot (scene).  Reductions are per slot:
 // each tile stores its FP64 block sum; the last tile of the slot to finish
@@ -234,8 +279,8 @@ __global__ void k_seg_active(SegArgs S) { seg_list_active(S); }
 //   rho_i = sum_f m_j W(x_ij) + sum_b (V_j rho0) W(x_ij)
 // ---------------------------------------------------------------------------
 
-template <int NF, int NB>
-__global__ void __launch_bounds__(kNT, kMinBlocks) k_density(uint32_t n, float4 const *__restrict__ x, float *__restrict__ rho,
+template <int NF, int NB, int NT = kNT, int MINB = kMinBlocks, int BT = 16>
+__global__ void __launch_bounds__(NT, MINB) k_density(uint32_t n, float4 const *__restrict__ x, float *__restrict__ rho,
                                                  float const *rho0p, Globals G, Nbrs<NF, NB> N) {
   uint32_t i = grid_tid();
   if (i >= n) return;
@@ -246,7 +291,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_density(uint32_t n, float4 
 #pragma unroll
   for (int q = 0; q < NF; ++q) {
     FluidN const &F = N.f[q];
-    for_each_nbr(F.L, i, false, [&](uint32_t j_, float) {
+    for_each_nbr<BT>(F.L, i, false, [&](uint32_t j_, float) {
       float4 xm = __ldg(F.xm + j_);
       acc += xm.w * kW(K, sub3(xi, mk3(xm)));
     });
@@ -254,7 +299,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_density(uint32_t n, float4 
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
-    for_each_nbr(B.L, i, false, [&](uint32_t j_, float) {
+    for_each_nbr<BT>(B.L, i, false, [&](uint32_t j_, float) {
       float4 xv = __ldg(B.xV + j_);
       acc += (xv.w * rho0) * kW(K, sub3(xi, mk3(xv)));
     });
@@ -342,8 +387,8 @@ __global__ void k_max_speed_end(Globals G, unsigned const *maxord) { *G.max_spee
 // thread computes c over its neighbours, stores it, then walks the same (now
 // cached) neighbour rows again for s and AA, with the operations of the
 // generated passes.
-template <int NF, int NB>
-__global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_setup(uint32_t n, float4 const *__restrict__ x,
+template <int NF, int NB, int NT = kNT, int MINB = kMinBlocks, int BT = 8>
+__global__ void __launch_bounds__(NT, MINB) k_iisph_setup(uint32_t n, float4 const *__restrict__ x,
                                                                  float4 const *__restrict__ v,
                                                                  float4 *__restrict__ cout, float const *__restrict__ m,
                                                                  float const *__restrict__ rho, float *__restrict__ p,
@@ -361,7 +406,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_setup(uint32_t n, flo
 #pragma unroll
   for (int q = 0; q < NF; ++q) {
     FluidN const &F = N.f[q];
-    for_each_nbr<8>(F.L, i, uc, [&](uint32_t j_, float gf_) {
+    for_each_nbr<BT>(F.L, i, uc, [&](uint32_t j_, float gf_) {
       float4 xm = __ldg(F.xm + j_);
       c = sub3(c, scl3(xm.w / (ri * ri), pgrad(uc, gf_, K, sub3(xi, mk3(xm)))));
     }, true);
@@ -369,7 +414,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_setup(uint32_t n, flo
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
-    for_each_nbr<8>(B.L, i, uc, [&](uint32_t j_, float gf_) {
+    for_each_nbr<BT>(B.L, i, uc, [&](uint32_t j_, float gf_) {
       float4 xv = __ldg(B.xV + j_);
       c = sub3(c, scl3(((0.7f * 2.0f) * rho0) * (xv.w / (ri * ri)), pgrad(uc, gf_, K, sub3(xi, mk3(xv)))));
     }, true);
@@ -381,7 +426,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_setup(uint32_t n, flo
 #pragma unroll
   for (int q = 0; q < NF; ++q) {
     FluidN const &F = N.f[q];
-    for_each_nbr<8>(F.L, i, uc, [&](uint32_t j_, float gf_) {
+    for_each_nbr<BT>(F.L, i, uc, [&](uint32_t j_, float gf_) {
       uint32_t j = j_;
       float4 xm = __ldg(F.xm + j);
       f3 g = pgrad(uc, gf_, K, sub3(xi, mk3(xm)));
@@ -394,7 +439,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_setup(uint32_t n, flo
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
-    for_each_nbr<8>(B.L, i, uc, [&](uint32_t j_, float gf_) {
+    for_each_nbr<BT>(B.L, i, uc, [&](uint32_t j_, float gf_) {
       float4 xv = __ldg(B.xV + j_);
       f3 g = pgrad(uc, gf_, K, sub3(xi, mk3(xv)));
       float w = rho0 * xv.w;
@@ -412,7 +457,7 @@ __global__ void k_set_i32(int *p, int v) { *p = v; }
 
 // iisph.iteration_pressure_acceleration (schemes/iisph.hpp:358-423).
 // `done` (device-loop mode) skips the work once the loop has converged.
-template <int NF, int NB>
+template <int NF, int NB, int BT = 8>
 __device__ __forceinline__ void iisph_accel_item(uint32_t i, float4 const *__restrict__ x, float const *__restrict__ p,
                                                  float const *__restrict__ rho, float4 *__restrict__ a,
                                                  KernelParams const &K, bool uc, float rho0, Nbrs<NF, NB> const &N) {
@@ -423,7 +468,7 @@ __device__ __forceinline__ void iisph_accel_item(uint32_t i, float4 const *__res
 #pragma unroll
   for (int q = 0; q < NF; ++q) {
     FluidN const &F = N.f[q];
-    for_each_nbr<8>(F.L, i, uc, [&](uint32_t j_, float gf_) {
+    for_each_nbr<BT>(F.L, i, uc, [&](uint32_t j_, float gf_) {
       uint32_t j = j_;
       float4 xm = __ldg(F.xm + j);
       float coef = xm.w * (pri + __ldg(F.pr + j));
@@ -434,7 +479,7 @@ __device__ __forceinline__ void iisph_accel_item(uint32_t i, float4 const *__res
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
-    for_each_nbr<8>(B.L, i, uc, [&](uint32_t j_, float gf_) {
+    for_each_nbr<BT>(B.L, i, uc, [&](uint32_t j_, float gf_) {
       float4 xv = __ldg(B.xV + j_);
       float coef = ((0.7f * rho0) * xv.w) * bterm;
       acc = sub3(acc, scl3(coef, pgrad(uc, gf_, K, sub3(xi, mk3(xv)))));
@@ -442,19 +487,19 @@ __device__ __forceinline__ void iisph_accel_item(uint32_t i, float4 const *__res
   }
   a[i] = make_float4(acc.x, acc.y, acc.z, 0.0f);
 }
-template <int NF, int NB>
-__global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_accel(uint32_t n, float4 const *__restrict__ x, float const *__restrict__ p,
+template <int NF, int NB, int NT = kNT, int MINB = kMinBlocks, int BT = 8>
+__global__ void __launch_bounds__(NT, MINB) k_iisph_accel(uint32_t n, float4 const *__restrict__ x, float const *__restrict__ p,
                                                      float const *__restrict__ rho, float4 *__restrict__ a,
                                                      float const *rho0p, Globals G, Nbrs<NF, NB> N, int const *done) {
   if (done && *(volatile int const *)done) return;
   uint32_t i = grid_tid();
   if (i >= n) return;
   KernelParams K = kparams(*G.h);
-  iisph_accel_item<NF, NB>(i, x, p, rho, a, K, use_cache(N, K), *rho0p, N);
+  iisph_accel_item<NF, NB, BT>(i, x, p, rho, a, K, use_cache(N, K), *rho0p, N);
 }
 // batched models: the tiles of the slots still iterating
-template <int NF, int NB>
-__global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_accel_seg(float4 const *__restrict__ x, float const *__restrict__ p,
+template <int NF, int NB, int MINB = kMinBlocks, int BT = 8>
+__global__ void __launch_bounds__(kNT, MINB) k_iisph_accel_seg(float4 const *__restrict__ x, float const *__restrict__ p,
                                                          float const *__restrict__ rho, float4 *__restrict__ a,
                                                          float const *rho0p, Globals G, Nbrs<NF, NB> N, SegArgs S) {
   KernelParams K = kparams(*G.h);
@@ -464,7 +509,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_accel_seg(float4 cons
   for (uint32_t t = blockIdx.x; t < na; t += gridDim.x) {
     uint4 T = S.tiles[S.active[t]];
     uint32_t i = T.y + threadIdx.x;
-    if (i < T.z) iisph_accel_item<NF, NB>(i, x, p, rho, a, K, uc, rho0, N);
+    if (i < T.z) iisph_accel_item<NF, NB, BT>(i, x, p, rho, a, K, uc, rho0, N);
   }
 }
 
@@ -481,7 +526,7 @@ struct PressureArgs {
 };
 
 // one item of iteration_pressure; returns its density-error term
-template <int NF, int NB>
+template <int NF, int NB, int BT = 16>
 __device__ __forceinline__ double iisph_pressure_item(uint32_t i, PressureArgs const &A, KernelParams const &K, bool uc,
                                                       float rho0, float dt, float omega, Nbrs<NF, NB> const &N) {
   f3 xi = mk3(A.x[i]), ai = mk3(A.a[i]);
@@ -489,7 +534,7 @@ __device__ __forceinline__ double iisph_pressure_item(uint32_t i, PressureArgs c
 #pragma unroll
   for (int q = 0; q < NF; ++q) {
     FluidN const &F = N.f[q];
-    for_each_nbr(F.L, i, uc, [&](uint32_t j_, float gf_) {
+    for_each_nbr<BT>(F.L, i, uc, [&](uint32_t j_, float gf_) {
       uint32_t j = j_;
       float4 xm = __ldg(F.xm + j);
       ap += xm.w * dot3(sub3(ai, mk3(__ldg(F.a + j))), pgrad(uc, gf_, K, sub3(xi, mk3(xm))));
@@ -498,7 +543,7 @@ __device__ __forceinline__ double iisph_pressure_item(uint32_t i, PressureArgs c
 #pragma unroll
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
-    for_each_nbr(B.L, i, uc, [&](uint32_t j_, float gf_) {
+    for_each_nbr<BT>(B.L, i, uc, [&](uint32_t j_, float gf_) {
       float4 xv = __ldg(B.xV + j_);
       ap += (rho0 * xv.w) * dot3(sub3(ai, f3{0.0f, 0.0f, 0.0f}), pgrad(uc, gf_, K, sub3(xi, mk3(xv))));
     });
@@ -515,8 +560,8 @@ __device__ __forceinline__ double iisph_pressure_item(uint32_t i, PressureArgs c
   return f2d(((ap - si) / rho0) * ustep(1e-9f, pn));
 }
 
-template <int NF, int NB>
-__global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_pressure(uint32_t n, PressureArgs A, Globals G, Nbrs<NF, NB> N, Red R,
+template <int NF, int NB, int MINB = kMinBlocks, int BT = 16>
+__global__ void __launch_bounds__(kNT, MINB) k_iisph_pressure(uint32_t n, PressureArgs A, Globals G, Nbrs<NF, NB> N, Red R,
                                                         int first, int last_group, int const *done) {
   if (done && *(volatile int const *)done) return;
   KernelParams K = kparams(*G.h);
@@ -524,7 +569,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_pressure(uint32_t n, 
   float rho0 = *A.rho0, dt = *G.dt, omega = *G.omega;
   double part = 0.0;
   for (uint32_t i = grid_tid(); i < n; i += gridDim.x * blockDim.x)
-    part += iisph_pressure_item<NF, NB>(i, A, K, uc, rho0, dt, omega, N);
+    part += iisph_pressure_item<NF, NB, BT>(i, A, K, uc, rho0, dt, omega, N);
   double v[1] = {part}, out[1];
   if (reduce_commit<1>(v, R, out) && threadIdx.x == 0) {
     double start = first ? (done ? 0.0 : double(*G.aprde)) : R.scalars[kSJacobi];
@@ -536,8 +581,8 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_pressure(uint32_t n, 
 
 // iteration_pressure over the tiles of a batched model: the density error of
 // each slot's iteration goes to scal[slot][kSsAprde]
-template <int NF, int NB>
-__global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_pressure_seg(PressureArgs A, Globals G, Nbrs<NF, NB> N, SegArgs S) {
+template <int NF, int NB, int MINB = kMinBlocks, int BT = 16>
+__global__ void __launch_bounds__(kNT, MINB) k_iisph_pressure_seg(PressureArgs A, Globals G, Nbrs<NF, NB> N, SegArgs S) {
   // one active tile per block (the hardware's block scheduling balances the
   // tiles' uneven costs); the blocks past the active tiles exit at once
   if (blockIdx.x >= *S.nactive) return;
@@ -548,7 +593,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_iisph_pressure_seg(Pressure
   uint4 T = S.tiles[t];
   uint32_t slot = T.x;
   uint32_t i = T.y + threadIdx.x;
-  double part = (i < T.z) ? iisph_pressure_item<NF, NB>(i, A, K, uc, rho0, dt, omega, N) : 0.0;
+  double part = (i < T.z) ? iisph_pressure_item<NF, NB, BT>(i, A, K, uc, rho0, dt, omega, N) : 0.0;
   double v[1] = {part}, out[1];
   if (seg_commit<1>(v, S, slot, out, t) && threadIdx.x == 0) S.scal[slot * kSegScal + kSsAprde] = out[0];
 }
@@ -593,6 +638,7 @@ __global__ void k_seg_jacobi_control(Globals G, SegArgs S, cudaGraphConditionalH
   }
   any = __syncthreads_or(any);
   if (any) seg_list_active(S);
+  else if (threadIdx.x == 0) *S.nactive = 0; // repeats of the loop body after the end sweep nothing
   if (threadIdx.x == 0) {
     *all_done = any ? 0 : 1;
     if (kernels) atomicAdd(&g_loop_kernels, (unsigned long long)kernels);
@@ -619,7 +665,6 @@ __global__ void k_jacobi_control(Globals G, Red R, cudaGraphConditionalHandle h,
     if (converged || it >= maxit || it >= 100000) done = 1;
     R.status[kStJacDone] = done;
     *G.jac_iters = it;
-    if (kernels) atomicAdd(&g_loop_kernels, (unsigned long long)kernels);
     if (done) {
       R.stats[0] += 1.0;
       R.stats[1] += double(it);
@@ -627,6 +672,8 @@ __global__ void k_jacobi_control(Globals G, Red R, cudaGraphConditionalHandle h,
       if (rel > R.stats[3]) R.stats[3] = rel;
     }
   }
+  // the body's kernels ran (those of a repeat after the end return at once)
+  if (kernels) atomicAdd(&g_loop_kernels, (unsigned long long)kernels);
   if (use_handle) cudaGraphSetConditional(h, done ? 0u : 1u);
 }
 
@@ -734,8 +781,8 @@ __global__ void k_identity9(uint32_t n, uint32_t cap, float *L) {
 // (x, m / rho).
 // GC (wkbb18_gc, share/schemes/wkbb18_gc.prtcl): every kernel gradient
 // premultiplied by the item's gradient correction L_i (planar, capacity lcap)
-template <int NB, bool GC = false>
-__global__ void __launch_bounds__(kNT, kMinBlocks) k_wkbb18_diag(uint32_t n, uint32_t cap, float4 const *__restrict__ xmr,
+template <int NB, bool GC = false, int NT = kNT, int MINB = kMinBlocks, int BT = 8>
+__global__ void __launch_bounds__(NT, MINB) k_wkbb18_diag(uint32_t n, uint32_t cap, float4 const *__restrict__ xmr,
                                                      float const *__restrict__ rho, float *__restrict__ sp,
                                                      float const *rho0p, float const *mup, Globals G, NbrList self,
                                                      Nbrs<0, NB> N, float const *__restrict__ Lc, uint32_t lcap) {
@@ -755,7 +802,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_wkbb18_diag(uint32_t n, uin
   for (int k = 0; k < 9; ++k) S[k] = 0.0f;
   float hh = (0.01f * h) * h;
   float cmu = 10.0f * (mu / ri);
-  for_each_nbr<8>(self, i, uc, [&](uint32_t j_, float gf_) {
+  for_each_nbr<BT>(self, i, uc, [&](uint32_t j_, float gf_) {
     float4 xj = __ldg(xmr + j_);
     f3 xij = sub3(xi, mk3(xj));
     float coef = (cmu * xj.w) / (nsq3(xij) + hh);
@@ -772,7 +819,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_wkbb18_diag(uint32_t n, uin
   for (int q = 0; q < NB; ++q) {
     BoundN const &B = N.b[q];
     float bmu = *B.mu;
-    for_each_nbr<8>(B.L, i, uc, [&](uint32_t j_, float gf_) {
+    for_each_nbr<BT>(B.L, i, uc, [&](uint32_t j_, float gf_) {
       float4 xv = __ldg(B.xV + j_);
       f3 xij = sub3(xi, mk3(xv));
       float coef = ((10.0f * (bmu / ri)) * ((rho0 * xv.w) / ri)) / (nsq3(xij) + hh);
@@ -824,7 +871,7 @@ struct PcgArgs {
 
 // system product of wkbb18.accumulate_acceleration (schemes/wkbb18.hpp:
 // 339-396): (A w)_i = w_i - dt * a_f(w)_i
-template <int NB, bool GC>
+template <int NB, bool GC, int BT = 8>
 __device__ __forceinline__ f3 wkbb18_system(PcgArgs const &P, KernelParams const &K, bool uc, float dt, float rho0,
                                             float mu, Nbrs<0, NB> const &N, float4 const *__restrict__ w, uint32_t i) {
   float Li[9];
@@ -837,7 +884,7 @@ __device__ __forceinline__ f3 wkbb18_system(PcgArgs const &P, KernelParams const
   float ri = P.rho[i];
   float cmu = 10.0f * (mu / ri);
   f3 af = {0.0f, 0.0f, 0.0f};
-  for_each_nbr<8>(P.self, i, uc, [&](uint32_t j_, float gf_) {
+  for_each_nbr<BT>(P.self, i, uc, [&](uint32_t j_, float gf_) {
     uint32_t j = j_;
     float4 xj = __ldg(P.xmr + j);
     f3 xij = sub3(xi, mk3(xj));
@@ -852,7 +899,7 @@ __device__ __forceinline__ f3 wkbb18_system(PcgArgs const &P, KernelParams const
     BoundN const &B = N.b[q];
     float bmu = *B.mu;
     float cb_mu = 10.0f * (bmu / ri);
-    for_each_nbr<8>(B.L, i, uc, [&](uint32_t j_, float gf_) {
+    for_each_nbr<BT>(B.L, i, uc, [&](uint32_t j_, float gf_) {
       float4 xv = __ldg(B.xV + j_);
       f3 xij = sub3(xi, mk3(xv));
       float coef = ((cb_mu * ((rho0 * xv.w) / ri)) * dot3(wi, xij)) / (nsq3(xij) + hh);
@@ -875,11 +922,11 @@ __global__ void k_pcg_guess(PcgArgs P) {
 // y = M r, p = -y; dots b.b, r.r, r.y (solver/cg_openmp.hpp:48-96)
 // per-item parts of the PCG kernels (shared by the plain and the tiled
 // launches, so both compute the same values)
-template <int NB, bool GC>
+template <int NB, bool GC, int BT = 8>
 __device__ __forceinline__ void pcg_init_item(PcgArgs const &P, KernelParams const &K, bool uc, float dt, float rho0,
                                               float mu, Nbrs<0, NB> const &N, uint32_t i, double &bb, double &rr,
                                               double &ry) {
-  f3 ax = wkbb18_system<NB, GC>(P, K, uc, dt, rho0, mu, N, P.X, i);
+  f3 ax = wkbb18_system<NB, GC, BT>(P, K, uc, dt, rho0, mu, N, P.X, i);
   f3 b = mk3(P.v[i]);
   f3 r = sub3(ax, b);
   f3 y = precond(P.sp, P.cap, i, r);
@@ -890,10 +937,10 @@ __device__ __forceinline__ void pcg_init_item(PcgArgs const &P, KernelParams con
   rr += f2d(dot3(r, r));
   ry += f2d(dot3(r, y));
 }
-template <int NB, bool GC>
+template <int NB, bool GC, int BT = 8>
 __device__ __forceinline__ double pcg_q_item(PcgArgs const &P, KernelParams const &K, bool uc, float dt, float rho0,
                                              float mu, Nbrs<0, NB> const &N, uint32_t i) {
-  f3 q = wkbb18_system<NB, GC>(P, K, uc, dt, rho0, mu, N, P.P, i);
+  f3 q = wkbb18_system<NB, GC, BT>(P, K, uc, dt, rho0, mu, N, P.P, i);
   P.Q[i] = make_float4(q.x, q.y, q.z, 0.0f);
   return f2d(dot3(mk3(P.P[i]), q));
 }
@@ -951,27 +998,28 @@ __device__ __forceinline__ void pcg_update_scalars(double *sc, int *st, double r
   }
 }
 
-template <int NB, bool GC = false>
-__global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_init(PcgArgs P, Globals G, Nbrs<0, NB> N, Red R) {
+template <int NB, bool GC = false, int MINB = kMinBlocks, int BT = 8>
+__global__ void __launch_bounds__(kNT, MINB) k_pcg_init(PcgArgs P, Globals G, Nbrs<0, NB> N, Red R) {
   KernelParams K = kparams(*G.h);
   bool uc = use_cache(N, K);
   float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
   double bb = 0.0, rr = 0.0, ry = 0.0;
   for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x)
-    pcg_init_item<NB, GC>(P, K, uc, dt, rho0, mu, N, i, bb, rr, ry);
+    pcg_init_item<NB, GC, BT>(P, K, uc, dt, rho0, mu, N, i, bb, rr, ry);
   double v[3] = {bb, rr, ry}, out[3];
   if (reduce_commit<3>(v, R, out) && threadIdx.x == 0) pcg_init_scalars(R.scalars + kSPcg, R.status, out, *P.tol);
 }
 
 // q = A p; p.q; alpha or break (solver/cg_openmp.hpp:121-151)
-template <int NB, bool GC = false>
-__global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_q(PcgArgs P, Globals G, Nbrs<0, NB> N, Red R) {
+template <int NB, bool GC = false, int MINB = kMinBlocks, int BT = 8>
+__global__ void __launch_bounds__(kNT, MINB) k_pcg_q(PcgArgs P, Globals G, Nbrs<0, NB> N, Red R) {
   if (!*(volatile int *)&R.status[kStPcgActive]) return;
   KernelParams K = kparams(*G.h);
   bool uc = use_cache(N, K);
   float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
   double pq = 0.0;
-  for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x) pq += pcg_q_item<NB, GC>(P, K, uc, dt, rho0, mu, N, i);
+  for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x)
+    pq += pcg_q_item<NB, GC, BT>(P, K, uc, dt, rho0, mu, N, i);
   double v[1] = {pq}, out[1];
   if (reduce_commit<1>(v, R, out) && threadIdx.x == 0) pcg_q_scalars(R.scalars + kSPcg, R.status, out[0], *P.tol);
 }
@@ -1014,8 +1062,8 @@ __global__ void k_pcg_control(PcgArgs P, Red R, cudaGraphConditionalHandle h, in
 
 // --- the PCG loop over the tiles of a batched model, per slot -------------
 
-template <int NB, bool GC = false>
-__global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_init_seg(PcgArgs P, Globals G, Nbrs<0, NB> N, SegArgs S) {
+template <int NB, bool GC = false, int MINB = kMinBlocks, int BT = 8>
+__global__ void __launch_bounds__(kNT, MINB) k_pcg_init_seg(PcgArgs P, Globals G, Nbrs<0, NB> N, SegArgs S) {
   uint4 T = S.tiles[blockIdx.x];
   uint32_t slot = T.x;
   KernelParams K = kparams(*G.h);
@@ -1023,7 +1071,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_init_seg(PcgArgs P, Glo
   float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
   double bb = 0.0, rr = 0.0, ry = 0.0;
   uint32_t i = T.y + threadIdx.x;
-  if (i < T.z) pcg_init_item<NB, GC>(P, K, uc, dt, rho0, mu, N, i, bb, rr, ry);
+  if (i < T.z) pcg_init_item<NB, GC, BT>(P, K, uc, dt, rho0, mu, N, i, bb, rr, ry);
   double v[3] = {bb, rr, ry}, out[3];
   if (seg_commit<3>(v, S, slot, out, blockIdx.x) && threadIdx.x == 0) {
     int *st = S.stat + slot * kSegStat;
@@ -1032,8 +1080,8 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_init_seg(PcgArgs P, Glo
   }
 }
 
-template <int NB, bool GC = false>
-__global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_q_seg(PcgArgs P, Globals G, Nbrs<0, NB> N, SegArgs S) {
+template <int NB, bool GC = false, int MINB = kMinBlocks, int BT = 8>
+__global__ void __launch_bounds__(kNT, MINB) k_pcg_q_seg(PcgArgs P, Globals G, Nbrs<0, NB> N, SegArgs S) {
   uint4 T = S.tiles[blockIdx.x];
   uint32_t slot = T.x;
   if (!S.stat[slot * kSegStat + kStPcgActive]) return;
@@ -1041,7 +1089,7 @@ __global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_q_seg(PcgArgs P, Global
   bool uc = use_cache(N, K);
   float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
   uint32_t i = T.y + threadIdx.x;
-  double v[1] = {(i < T.z) ? pcg_q_item<NB, GC>(P, K, uc, dt, rho0, mu, N, i) : 0.0}, out[1];
+  double v[1] = {(i < T.z) ? pcg_q_item<NB, GC, BT>(P, K, uc, dt, rho0, mu, N, i) : 0.0}, out[1];
   if (seg_commit<1>(v, S, slot, out, blockIdx.x) && threadIdx.x == 0)
     pcg_q_scalars(S.scal + slot * kSegScal, S.stat + slot * kSegStat, out[0], *P.tol);
 }
@@ -1228,6 +1276,38 @@ template <class T> void sig_add(std::string &s, T const &v) { s.append(reinterpr
 } // namespace
 
 // ===========================================================================
+// Tuning knobs
+// ===========================================================================
+
+char const *tune_knob_name(int k) {
+  static char const *names[kTuneKnobs] = {"density", "iisph_setup", "iisph_accel", "iisph_pressure",
+                                          "wkbb18_diag", "pcg_init", "pcg_q", "jacobi_unroll"};
+  return (k >= 0 && k < kTuneKnobs) ? names[k] : "";
+}
+int tune_knob_find(std::string const &name) {
+  for (int k = 0; k < kTuneKnobs; ++k)
+    if (name == tune_knob_name(k)) return k;
+  return -1;
+}
+bool tune_value_ok(int k, int v) {
+  if (k == kTuneJacobiUnroll) return v == 1 || v == 2 || v == 4;
+  return k >= 0 && k < kTuneKnobs && v >= 0 && v <= 3;
+}
+std::string tune_knob_table() {
+  // shapes as threads-per-block x blocks-per-SM / walk batch
+  std::string t;
+  t += "density 0 " + shapes_text<DensityShapes>() + "\n";
+  t += "iisph_setup 0 " + shapes_text<SetupShapes>() + "\n";
+  t += "iisph_accel 0 " + shapes_text<AccelShapes>() + " batched: " + shapes_text<AccelSegShapes>() + "\n";
+  t += "iisph_pressure 0 " + shapes_text<PressureShapes>() + "\n";
+  t += "wkbb18_diag 0 " + shapes_text<DiagShapes>() + "\n";
+  t += "pcg_init 0 " + shapes_text<PcgShapes>() + "\n";
+  t += "pcg_q 0 " + shapes_text<PcgShapes>() + "\n";
+  t += "jacobi_unroll 1 1=1 2=2 4=4\n";
+  return t;
+}
+
+// ===========================================================================
 // Scheme base
 // ===========================================================================
 
@@ -1405,7 +1485,11 @@ public:
       uint32_t n = uint32_t(F.g->count);
       auto N = S->nbrs<NF, NB>(v, s);
       ProfScope ps(S->model_->prof, "density", s);
-      k_density<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(F.x), dptr<float>(F.rho), S->u(F.rho0), G, N);
+      with_shape<DensityShapes, NF == 1 && NB == 1>(S->model_->tune.v[kTuneDensity], [&](auto sh) {
+        using Sh = decltype(sh);
+        k_density<NF, NB, Sh::nt, Sh::minb, Sh::bt><<<div_up(n, Sh::nt), Sh::nt, 0, s>>>(
+            n, dptr<float4>(F.x), dptr<float>(F.rho), S->u(F.rho0), G, N);
+      });
       count_launch();
     }
   };
@@ -1623,10 +1707,12 @@ public:
       auto N = S->nbrs<NF, NB>(v, s);
       float *pr = S->model_->pr_buffer(F.g, s);
       ProfScope ps(S->model_->prof, "iisph_setup", s);
-      k_iisph_setup<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, dptr<float4>(F.x), dptr<float4>(F.v), dptr<float4>(F.c),
-                                                            dptr<float>(F.m), dptr<float>(F.rho), dptr<float>(F.p),
-                                                            pr, dptr<float>(F.s), dptr<float>(F.AA), S->u(F.rho0), G,
-                                                            N);
+      with_shape<SetupShapes, NF == 1 && NB == 1>(S->model_->tune.v[kTuneSetup], [&](auto sh) {
+        using Sh = decltype(sh);
+        k_iisph_setup<NF, NB, Sh::nt, Sh::minb, Sh::bt><<<div_up(n, Sh::nt), Sh::nt, 0, s>>>(
+            n, dptr<float4>(F.x), dptr<float4>(F.v), dptr<float4>(F.c), dptr<float>(F.m), dptr<float>(F.rho),
+            dptr<float>(F.p), pr, dptr<float>(F.s), dptr<float>(F.AA), S->u(F.rho0), G, N);
+      });
       count_launch();
     }
   };
@@ -1657,11 +1743,20 @@ public:
         return;
       }
       if (prof) S->model_->prof.begin("iisph_accel", s);
+      int tv = S->model_->tune.v[kTuneAccel];
       if (SA) {
         if (SA->ntiles)
-          k_iisph_accel_seg<NF, NB><<<std::min(SA->ntiles, kActiveBlocks), kNT, 0, s>>>(x, p, rho, a, rho0, G, N, *SA);
+          with_shape<AccelSegShapes, NF == 1 && NB == 1>(tv, [&](auto sh) {
+            using Sh = decltype(sh);
+            k_iisph_accel_seg<NF, NB, Sh::minb, Sh::bt><<<std::min(SA->ntiles, kActiveBlocks), kNT, 0, s>>>(
+                x, p, rho, a, rho0, G, N, *SA);
+          });
       } else {
-        k_iisph_accel<NF, NB><<<div_up(n, kNT), kNT, 0, s>>>(n, x, p, rho, a, rho0, G, N, done);
+        with_shape<AccelShapes, NF == 1 && NB == 1>(tv, [&](auto sh) {
+          using Sh = decltype(sh);
+          k_iisph_accel<NF, NB, Sh::nt, Sh::minb, Sh::bt><<<div_up(n, Sh::nt), Sh::nt, 0, s>>>(n, x, p, rho, a, rho0,
+                                                                                            G, N, done);
+        });
       }
       count_launch();
       if (prof) S->model_->prof.end(s);
@@ -1687,11 +1782,14 @@ public:
         return;
       }
       if (prof) S->model_->prof.begin("iisph_pressure", s);
-      if (SA) {
-        if (SA->ntiles) k_iisph_pressure_seg<NF, NB><<<SA->ntiles, kNT, 0, s>>>(PA, G, N, *SA);
-      } else {
-        k_iisph_pressure<NF, NB><<<red_grid(n), kNT, 0, s>>>(n, PA, G, N, R, first, last, done);
-      }
+      with_shape<PressureShapes, NF == 1 && NB == 1>(S->model_->tune.v[kTunePressure], [&](auto sh) {
+        using Sh = decltype(sh);
+        if (SA) {
+          if (SA->ntiles) k_iisph_pressure_seg<NF, NB, Sh::minb, Sh::bt><<<SA->ntiles, kNT, 0, s>>>(PA, G, N, *SA);
+        } else {
+          k_iisph_pressure<NF, NB, Sh::minb, Sh::bt><<<red_grid(n), kNT, 0, s>>>(n, PA, G, N, R, first, last, done);
+        }
+      });
       count_launch();
       if (prof) S->model_->prof.end(s);
     }
@@ -1804,20 +1902,27 @@ public:
     }
     PG_LAUNCH_CHECK();
     int kernels = 2 * int(act.size()) + 1;
+    // iterations per graph iteration (the jacobi_unroll knob): the kernels of
+    // the repeats after the control has ended the loop return at once, and
+    // the last control of the body decides whether the body runs again
+    int unroll = model_->tune.v[kTuneJacobiUnroll];
     auto body = [&](cudaStream_t cs, cudaGraphConditionalHandle h, bool use_handle, bool prof, std::string *sig) {
-      for (size_t k = 0; k < act.size(); ++k)
-        dispatch_fb<A>(nf, nb, this, *act[k], *views[k], G, cs, done, prof, sig, sa);
-      for (size_t k = 0; k < act.size(); ++k)
-        dispatch_fb<P>(nf, nb, this, *act[k], *views[k], G, cs, k == 0 ? 1 : 0, k + 1 == act.size() ? 1 : 0, done,
-                       prof, sig, sa);
-      if (sig) return;
-      if (seg) {
-        k_seg_jacobi_control<<<1, 1024, 0, cs>>>(G, SA, h, use_handle ? 1 : 0, use_handle ? kernels : 0,
-                                                 R.status + kStJacDone);
-      } else {
-        k_jacobi_control<<<1, 1, 0, cs>>>(G, R, h, use_handle ? 1 : 0, use_handle ? kernels : 0);
+      int reps = (sig || prof) ? 1 : unroll;
+      for (int rep = 0; rep < reps; ++rep) {
+        for (size_t k = 0; k < act.size(); ++k)
+          dispatch_fb<A>(nf, nb, this, *act[k], *views[k], G, cs, done, prof, sig, sa);
+        for (size_t k = 0; k < act.size(); ++k)
+          dispatch_fb<P>(nf, nb, this, *act[k], *views[k], G, cs, k == 0 ? 1 : 0, k + 1 == act.size() ? 1 : 0, done,
+                         prof, sig, sa);
+        if (sig) return;
+        if (seg) {
+          k_seg_jacobi_control<<<1, 1024, 0, cs>>>(G, SA, h, use_handle ? 1 : 0, use_handle ? kernels : 0,
+                                                   R.status + kStJacDone);
+        } else {
+          k_jacobi_control<<<1, 1, 0, cs>>>(G, R, h, use_handle ? 1 : 0, use_handle ? kernels : 0);
+        }
+        count_launch();
       }
-      count_launch();
     };
     if (model_->prof.enabled) {
       // host-driven: one iteration per round trip
@@ -1834,6 +1939,7 @@ public:
       body(s, cudaGraphConditionalHandle{}, true, false, &sig);
       sig_add(sig, G);
       sig_add(sig, R);
+      sig_add(sig, model_->tune); // a changed shape or repeat count rebuilds the graph
       loop_.run(s, sig, [&](cudaStream_t cs, cudaGraphConditionalHandle h) { body(cs, h, true, false, nullptr); });
       PG_LAUNCH_CHECK();
     }
@@ -1909,9 +2015,12 @@ public:
                                                               nl(v, F.g->index), N, dptr<float>(F.L),
                                                               uint32_t(F.L->cap));
     else
-      k_wkbb18_diag<NB, false><<<div_up(n, kNT), kNT, 0, s>>>(n, uint32_t(F.sp->cap), xmr, dptr<float>(F.rho),
-                                                               dptr<float>(F.sp), u(F.rho0), u(F.mu), G,
-                                                               nl(v, F.g->index), N, nullptr, 0u);
+      with_shape<DiagShapes, NB == 1>(fluid_.size() == 1 ? model_->tune.v[kTuneDiag] : 0, [&](auto sh) {
+        using Sh = decltype(sh);
+        k_wkbb18_diag<NB, false, Sh::nt, Sh::minb, Sh::bt><<<div_up(n, Sh::nt), Sh::nt, 0, s>>>(
+            n, uint32_t(F.sp->cap), xmr, dptr<float>(F.rho), dptr<float>(F.sp), u(F.rho0), u(F.mu), G,
+            nl(v, F.g->index), N, nullptr, 0u);
+      });
     count_launch();
   }
   void diag(Nhood &nh, cudaStream_t s) {
@@ -1969,24 +2078,35 @@ public:
     SegArgs SA = seg ? seg_args(F.g) : SegArgs{};
     unsigned tg = SA.ntiles;
     k_pcg_guess<<<eg, 256, 0, s>>>(P); count_launch();
+    constexpr bool kTuned = NB == 1 && !GC;
+    int tv_init = fluid_.size() == 1 ? model_->tune.v[kTunePcgInit] : 0;
+    int tv_q = fluid_.size() == 1 ? model_->tune.v[kTunePcgQ] : 0;
     {
       ProfScope ps(model_->prof, "pcg_init", s);
       if (seg) {
         k_seg_pcg_begin<<<div_up(std::max<uint32_t>(SA.slots, 1), 256), 256, 0, s>>>(SA); count_launch();
-        if (tg) k_pcg_init_seg<NB, GC><<<tg, kNT, 0, s>>>(P, G, N, SA);
-      } else {
-        k_pcg_init<NB, GC><<<rg, kNT, 0, s>>>(P, G, N, R);
       }
+      with_shape<PcgShapes, kTuned>(tv_init, [&](auto sh) {
+        using Sh = decltype(sh);
+        if (seg) {
+          if (tg) k_pcg_init_seg<NB, GC, Sh::minb, Sh::bt><<<tg, kNT, 0, s>>>(P, G, N, SA);
+        } else {
+          k_pcg_init<NB, GC, Sh::minb, Sh::bt><<<rg, kNT, 0, s>>>(P, G, N, R);
+        }
+      });
       count_launch();
     }
     PG_LAUNCH_CHECK();
     auto body = [&](cudaStream_t cs, cudaGraphConditionalHandle h, bool use_handle, bool prof) {
       if (prof) model_->prof.begin("pcg_q", cs);
-      if (seg) {
-        if (tg) k_pcg_q_seg<NB, GC><<<tg, kNT, 0, cs>>>(P, G, N, SA);
-      } else {
-        k_pcg_q<NB, GC><<<rg, kNT, 0, cs>>>(P, G, N, R);
-      }
+      with_shape<PcgShapes, kTuned>(tv_q, [&](auto sh) {
+        using Sh = decltype(sh);
+        if (seg) {
+          if (tg) k_pcg_q_seg<NB, GC, Sh::minb, Sh::bt><<<tg, kNT, 0, cs>>>(P, G, N, SA);
+        } else {
+          k_pcg_q<NB, GC, Sh::minb, Sh::bt><<<rg, kNT, 0, cs>>>(P, G, N, R);
+        }
+      });
       count_launch();
       if (prof) model_->prof.end(cs);
       if (prof) model_->prof.begin("pcg_update", cs);
@@ -2029,6 +2149,7 @@ public:
       sig_add(sig, G);
       sig_add(sig, rg);
       sig_add(sig, SA);
+      sig_add(sig, model_->tune); // a changed shape rebuilds the graph
       loops_[F.g].run(s, sig, [&](cudaStream_t cs, cudaGraphConditionalHandle h) { body(cs, h, true, false); });
       PG_LAUNCH_CHECK();
     }
