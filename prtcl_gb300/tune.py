@@ -187,7 +187,9 @@ class PlainTarget:
 
     def measure_steps(self):
         """Seconds per step (device loops in their graphs), host clock
-        around synchronised steps."""
+        around synchronised steps, after one untimed step (a changed knob
+        rebuilds the loops' graphs on their next launch)."""
+        self.loop.step(quiet=True)
         self.d.synchronize()
         t0 = time.perf_counter()
         for _ in range(self.n):
@@ -224,6 +226,7 @@ class BatchTarget:
         return {k: prof[k][1] / 1e3 / prof[k][0] for k in names if k in prof and prof[k][0]}
 
     def measure_steps(self):
+        self.b.step(1)  # untimed: a changed knob rebuilds the loops' graphs
         self.b.synchronize()
         t0 = time.perf_counter()
         self.b.step(self.n)
