@@ -877,6 +877,34 @@ GridView Nhood::view() const {
   return v;
 }
 
+// the cell-key layout of the bit statistics ne, eq, a1, a0 of k_cells_u
+static KeyInfo key_from_stats(uint32_t const *st) {
+  uint32_t ne = st[0], eq = st[1], a1 = st[2], a0 = st[3];
+  KeyInfo k{};
+  k.keep = ne & eq & 0x7FFFFFFFu;
+  k.rel_eq = eq & ~ne & 0x7FFFFFFFu;
+  k.rel_ne = ne & ~eq & 0x7FFFFFFFu;
+  if (a1 && a0) k.keep |= 0x80000000u;
+  else k.b31_const = a1 ? 0x80000000u : 0u;
+  k.bits = __builtin_popcount(k.keep);
+  key_runs(k);
+  return k;
+}
+static bool same_key(KeyInfo const &a, KeyInfo const &b) {
+  return a.keep == b.keep && a.rel_eq == b.rel_eq && a.rel_ne == b.rel_ne && a.b31_const == b.b31_const;
+}
+
+void Nhood::settle(cudaStream_t s) {
+  if (!key_check_) return;
+  PG_CUDA(cudaMemcpyAsync(stats_h_, stats_d_, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  PG_CUDA(cudaStreamSynchronize(s));
+  key_check_ = false;
+  if (!same_key(key_from_stats(stats_h_), key_)) {
+    key_known_ = false;
+    update(s);
+  }
+}
+
 // grouped_uniform_grid::update (util/grouped_uniform_grid.hpp:126-337)
 void Nhood::update(cudaStream_t s) {
   if (!model_) throw Error("Neighborhood::Update before Load");
@@ -901,6 +929,7 @@ void Nhood::update(cudaStream_t s) {
   epoch_++;
   has_grid_ = true;
   if (N == 0) {
+    key_check_ = false; // no statistics to confirm
     PG_CUDA(cudaMemsetAsync(ncells_d_, 0, sizeof(int), s));
     sorted_keys_ = keys_a_;
     sorted_vals_ = vals_a_;
@@ -916,17 +945,18 @@ void Nhood::update(cudaStream_t s) {
     k_cells_u<<<ub, kCellsUNT, 0, s>>>(pt, gv, G, N, ukeys_, vals_a_, stats_d_); count_launch();
   }
   PG_LAUNCH_CHECK();
-  PG_CUDA(cudaMemcpyAsync(stats_h_, stats_d_, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-  PG_CUDA(cudaStreamSynchronize(s));
-  uint32_t ne = stats_h_[0], eq = stats_h_[1], a1 = stats_h_[2], a0 = stats_h_[3];
   KeyInfo k{};
-  k.keep = ne & eq & 0x7FFFFFFFu;
-  k.rel_eq = eq & ~ne & 0x7FFFFFFFu;
-  k.rel_ne = ne & ~eq & 0x7FFFFFFFu;
-  if (a1 && a0) k.keep |= 0x80000000u;
-  else k.b31_const = a1 ? 0x80000000u : 0u;
-  k.bits = __builtin_popcount(k.keep);
-  key_runs(k);
+  if (key_known_) {
+    // the previous update's layout, confirmed before anything reads the grid
+    k = key_;
+    key_check_ = true;
+  } else {
+    PG_CUDA(cudaMemcpyAsync(stats_h_, stats_d_, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    PG_CUDA(cudaStreamSynchronize(s));
+    k = key_from_stats(stats_h_);
+    key_known_ = true;
+    key_check_ = false;
+  }
   if (k.bits > 21)
     throw Error("grid spans too many cells: " + std::to_string(k.bits) +
                 " informative bits per axis (at most 21 are supported)");
@@ -1090,8 +1120,23 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
       count_launch();
     }
     PG_LAUNCH_CHECK();
-    PG_CUDA(cudaMemcpyAsync(stats_h_ + 8, stats_d_ + 8, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    // one read-back: the rows' lengths, and the grid's key statistics when
+    // its layout is still to be confirmed
+    if (key_check_)
+      PG_CUDA(cudaMemcpyAsync(stats_h_, stats_d_, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    else
+      PG_CUDA(cudaMemcpyAsync(stats_h_ + 8, stats_d_ + 8, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     PG_CUDA(cudaStreamSynchronize(s));
+    if (key_check_) {
+      key_check_ = false;
+      if (!same_key(key_from_stats(stats_h_), key_)) {
+        // the layout changed: a new grid (read-back layout), then these lists
+        key_known_ = false;
+        update(s);
+        build_lists(q, L, s, h);
+        return;
+      }
+    }
     bool grow = false;
     for (int g = 0; g < G; ++g)
       if (stats_h_[8 + g] > L.cap[g]) {
@@ -1163,6 +1208,7 @@ NbrView const &Nhood::lists(int q, cudaStream_t s, float const *h) {
 void Nhood::permute(Model &m, cudaStream_t s) {
   if (&m != model_) throw Error("Neighborhood::Permute with a model that was not loaded");
   if (!has_grid_) update(s);
+  settle(s);
   int G = int(gg_.size());
   for (int g = 0; g < G; ++g) {
     if (!in_grid_[g] || gg_[g].g->count == 0) continue;
@@ -1185,6 +1231,7 @@ void Nhood::permute_segments(Model &m, uint8_t const *due_d, cudaStream_t s) {
   if (&m != model_) throw Error("Neighborhood::Permute with a model that was not loaded");
   if (!seg_count_) throw Error("permute_segments on an unsegmented neighbourhood");
   if (!has_grid_) update(s);
+  settle(s);
   int G = int(gg_.size());
   for (int g = 0; g < G; ++g) {
     if (!in_grid_[g] || gg_[g].g->count == 0) continue;
@@ -1248,6 +1295,7 @@ size_t Nhood::device_bytes() const {
 }
 
 size_t Nhood::cell_count(cudaStream_t s) {
+  settle(s);
   int c = 0;
   PG_CUDA(cudaMemcpyAsync(&c, ncells_d_, sizeof(int), cudaMemcpyDeviceToHost, s));
   PG_CUDA(cudaStreamSynchronize(s));

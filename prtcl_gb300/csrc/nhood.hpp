@@ -213,6 +213,11 @@ private:
   };
   void ensure_grid_capacity(size_t n);
   void build_lists(int q, Lists &L, cudaStream_t s, float const *h);
+  // Confirm the key layout an update took from the previous one (one
+  // synchronisation); on a mismatch, update again with a layout read back
+  // first.  Called before the grid is read on the host or permutes fields;
+  // the list build confirms it at its own synchronisation instead.
+  void settle(cudaStream_t s);
   bool lists_fresh(Lists const &L) const;
   std::vector<uint64_t> pos_versions() const;
   void free_lists(Lists &L);
@@ -224,6 +229,12 @@ private:
   uint32_t goff_[kMaxGroups + 1] = {};
   int in_grid_[kMaxGroups] = {};
   KeyInfo key_{};
+  // The cell-key layout is a function of four bit statistics of all items'
+  // grid indices (k_cells_u).  An update reuses the last layout without
+  // reading the statistics back (key_known_), and flags it for the check
+  // (key_check_) at the next synchronisation; in a simulation the layout
+  // changes only when the particles' grid indices gain or lose bit patterns.
+  bool key_known_ = false, key_check_ = false;
   // item count of each group when it was last permuted into cell order (the
   // list build walks a group that was not in grid order instead)
   size_t permuted_count_[kMaxGroups] = {};

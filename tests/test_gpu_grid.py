@@ -172,3 +172,34 @@ def test_scattered_grid_indices(oracle_mod, levels, near):
     groups = [("p", "fluid", pts, [])]
     d, o = make(oracle_mod, groups, r)
     compare(d, o, groups)
+
+
+@pytest.mark.parametrize("then_permute", [False, True])
+def test_key_layout_change_between_updates(oracle_mod, then_permute):
+    """An update reuses the previous cell-key layout and confirms it at the
+    next synchronisation (the list build, or a permute first).  Points moved
+    to cells whose indices carry new bit patterns change the layout: the
+    grid must be rebuilt with the new one before anything reads it, and the
+    lists equal the oracle's."""
+    rng = np.random.default_rng(21)
+    pts = (rng.random((20000, 3)) * 0.5).astype(np.float32)
+    groups = [("p", "fluid", pts, [])]
+    d, o = make(oracle_mod, groups, 0.02)
+    compare(d, o, groups)
+    moved = pts.copy()
+    moved[:300] -= np.float32(3.0)    # negative cells: bit 31 of the biased index flips
+    moved[300:600] += np.float32(40.0)  # far cells: new high bits
+    groups = [("p", "fluid", moved, [])]
+    for m in (d, o):
+        m.set_varying("p", "position", moved)
+        m.update()
+        if then_permute:
+            m.permute()
+    compare(d, o, groups)
+    # and back: the layout shrinks again
+    back = o.get_varying("p", "position", 3)
+    back[np.abs(back).max(axis=1) > 1.0] = np.float32(0.25)
+    for m in (d, o):
+        m.set_varying("p", "position", back)
+        m.update()
+    compare(d, o, [("p", "fluid", back, [])])
