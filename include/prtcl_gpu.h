@@ -168,7 +168,8 @@ int prtcl_gpu_profile_reset(prtcl_gpu_model *model);
  * Every value gives bit-identical results; they change only speed.  Knobs
  * carry the kernels' profile names: density, iisph_setup, iisph_accel,
  * iisph_pressure, wkbb18_diag, pcg_init, pcg_q (values 0..3, a launch
- * shape each) and jacobi_unroll (1, 2 or 4 relaxed-Jacobi iterations per
+ * shape each; pcg_q 4: a cell-tile sweep without neighbour lists, for
+ * unbatched models) and jacobi_unroll (1, 2 or 4 relaxed-Jacobi iterations per
  * iteration of the device loop's graph).  prtcl_gb300/tune.py searches them
  * per workload and caches the choice.  prtcl_gpu_tune_knobs returns one line
  * per knob: "name default value=shape ...", a shape written as threads per

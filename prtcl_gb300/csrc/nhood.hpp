@@ -187,6 +187,9 @@ public:
   void copy_lists(int q, int ng, int64_t *offsets, uint32_t *idx, size_t cap, cudaStream_t s);
 
   GridView view() const;
+  // sorted positions with their handles in w (current after the lists of a
+  // group have been built for the present positions)
+  float4 const *sorted_positions() const { return xsorted_; }
   // bytes of the grid arrays and the neighbour lists
   size_t device_bytes() const;
   uint64_t epoch() const { return epoch_; }

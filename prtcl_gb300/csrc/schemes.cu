@@ -1024,6 +1024,213 @@ __global__ void __launch_bounds__(kNT, MINB) k_pcg_q(PcgArgs P, Globals G, Nbrs<
   if (reduce_commit<1>(v, R, out) && threadIdx.x == 0) pcg_q_scalars(R.scalars + kSPcg, R.status, out[0], *P.tol);
 }
 
+// q = A p as a cell-tile sweep (the pcg_q knob's shape 4): no neighbour
+// lists.  A block stages, per tile of 128 consecutive fluid items, the
+// packed records of every cell adjacent to the tile's cells in shared
+// memory (position and handle; the search direction and m / rho for a fluid
+// item, the volume for a boundary item), and each thread walks its 27 cells
+// in the lists' traversal order (own cell, adjacency slots 0..25, sorted
+// order within a cell), fluid items first, then boundary items, testing
+// every candidate with the exact d^2 < T of the list build and computing the
+// gradient factor with the same operations.  The terms and their order are
+// those of wkbb18_system, so q is bit-identical; the grid and the
+// item-to-thread mapping are those of k_pcg_q, so the FP64 sum of p . q is
+// too.  A tile whose cells hold more than kTileStage items (or more than
+// kTileHash cells) takes the list walk instead.
+constexpr int kTileStage = 1536; // staged items per tile (2 x 16 bytes each)
+constexpr int kTileHash = 512;   // cells per tile (open-addressing table)
+
+__device__ __forceinline__ uint32_t tile_hash(int c) { return (uint32_t(c) * 2654435761u) >> 23; } // 9 bits
+
+// slot of cell c in the tile's table (the cell is present)
+__device__ __forceinline__ int tile_find(int const *hkey, int c) {
+  uint32_t h = tile_hash(c);
+  for (int probe = 0; probe < kTileHash; ++probe) {
+    int slot = int((h + uint32_t(probe)) & (kTileHash - 1));
+    if (hkey[slot] == c) return slot;
+  }
+  return -1;
+}
+
+template <int NB>
+__global__ void __launch_bounds__(kNT, 4) k_pcg_q_tiles(PcgArgs P, Globals G, Nbrs<0, NB> N, Red R, GridView gv,
+                                                         float4 const *__restrict__ xs, int fg, int bg) {
+  static_assert(NB == 1, "the cell-tile sweep handles one boundary group");
+  if (!*(volatile int *)&R.status[kStPcgActive]) return;
+  extern __shared__ float4 stage[]; // [kTileStage] records, then [kTileStage] payloads
+  __shared__ int hkey[kTileHash];
+  __shared__ uint32_t hval[kTileHash]; // base << 16 | count
+  __shared__ int homes[kNT];
+  __shared__ uint32_t wsum[kNT / 32], wocc[kNT / 32];
+  __shared__ int ccell[kTileHash];     // occupied slots' cells, compacted
+  __shared__ uint32_t cbase[kTileHash]; // and their staged bases (ascending)
+  __shared__ int s_over, s_cells;
+  float4 *pay = stage + kTileStage;
+  KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
+  float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
+  float hh = (0.01f * K.h) * K.h;
+  BoundN const &B = N.b[0];
+  float bmu = *B.mu;
+  double pq = 0.0;
+  for (uint32_t tile = blockIdx.x; size_t(tile) * kNT < P.n; tile += gridDim.x) {
+    uint32_t i = tile * kNT + threadIdx.x;
+    bool has = i < P.n;
+    for (int sl = threadIdx.x; sl < kTileHash; sl += kNT) {
+      hkey[sl] = -1;
+      hval[sl] = 0u;
+    }
+    if (threadIdx.x == 0) s_over = 0;
+    int home = has ? gv.s2c[gv.r2s[gv.goff[fg] + i]] : -1;
+    homes[threadIdx.x] = home;
+    __syncthreads();
+    // the first item of each run of equal home cells enters the run's 27 cells
+    if (has && (threadIdx.x == 0 || homes[threadIdx.x - 1] != home)) {
+      for (int k = -1; k < 26; ++k) {
+        int c = k < 0 ? home : gv.cell_adj[size_t(home) * 26 + k];
+        if (c < 0) continue;
+        uint32_t h = tile_hash(c);
+        bool placed = false;
+        for (int probe = 0; probe < kTileHash && !placed; ++probe) {
+          int slot = int((h + uint32_t(probe)) & (kTileHash - 1));
+          int old = atomicCAS(&hkey[slot], -1, c);
+          placed = old == -1 || old == c;
+        }
+        if (!placed) s_over = 1;
+      }
+    }
+    __syncthreads();
+    // staged ranges: each thread owns table slots tid, tid + 128, ...
+    uint32_t cnt[kTileHash / kNT], mine = 0;
+#pragma unroll
+    for (int m = 0; m < kTileHash / kNT; ++m) {
+      int c = hkey[threadIdx.x + m * kNT];
+      cnt[m] = c >= 0 ? uint32_t(gv.cell_start[c + 1] - gv.cell_start[c]) : 0u;
+      mine += cnt[m];
+    }
+    // block-exclusive prefix of the per-thread counts
+    uint32_t incl = mine;
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    uint32_t off = incl - mine, total = 0;
+    for (int k = 0; k < kNT / 32; ++k) {
+      if (k < w) off += wsum[k];
+      total += wsum[k];
+    }
+    if (total > uint32_t(kTileStage)) s_over = 1;
+    __syncthreads();
+    bool over = s_over != 0;
+    if (!over) {
+      // bases in (thread, m) order, and the occupied slots compacted in the
+      // same order, so that the compacted bases ascend
+      uint32_t occ = 0;
+#pragma unroll
+      for (int m = 0; m < kTileHash / kNT; ++m) occ += hkey[threadIdx.x + m * kNT] >= 0 ? 1u : 0u;
+      uint32_t oincl = occ;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        uint32_t v = __shfl_up_sync(0xffffffffu, oincl, o);
+        if (lane >= o) oincl += v;
+      }
+      if (lane == 31) wocc[w] = oincl;
+      __syncthreads();
+      uint32_t u = oincl - occ;
+      for (int k = 0; k < w; ++k) u += wocc[k];
+#pragma unroll
+      for (int m = 0; m < kTileHash / kNT; ++m) {
+        int sl = threadIdx.x + m * kNT;
+        int c = hkey[sl];
+        if (c >= 0) {
+          hval[sl] = (off << 16) | cnt[m];
+          ccell[u] = c;
+          cbase[u] = off;
+          off += cnt[m];
+          ++u;
+        }
+      }
+      if (threadIdx.x == kNT - 1) s_cells = u;
+    }
+    __syncthreads();
+    if (!over) {
+      // every thread copies staged items p = tid, tid + 128, ...: the cell of
+      // p is the last compacted cell whose base is <= p
+      int ncel = s_cells;
+      for (uint32_t pidx = threadIdx.x; pidx < total; pidx += kNT) {
+        int lo = 0, hi = ncel - 1;
+        while (lo < hi) {
+          int mid = (lo + hi + 1) >> 1;
+          if (cbase[mid] <= pidx) lo = mid;
+          else hi = mid - 1;
+        }
+        int c = ccell[lo];
+        uint32_t e = pidx - cbase[lo];
+        float4 X = xs[gv.cell_start[c] + int(e)];
+        uint32_t hd = __float_as_uint(X.w);
+        int g = int(hd >> 28);
+        uint32_t j = hd & 0x0FFFFFFFu;
+        float4 W = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (g == fg) {
+          float4 pj = P.P[j];
+          W = make_float4(pj.x, pj.y, pj.z, P.xmr[j].w);
+        } else if (g == bg) {
+          W.w = B.xV[j].w;
+        }
+        stage[pidx] = X;
+        pay[pidx] = W;
+      }
+    }
+    __syncthreads();
+    if (has) {
+      f3 q;
+      if (over) {
+        q = wkbb18_system<NB, false, 8>(P, K, uc, dt, rho0, mu, N, P.P, i);
+      } else {
+        f3 xi = mk3(P.xmr[i]), wi = mk3(P.P[i]);
+        float ri = P.rho[i];
+        float cmu = 10.0f * (mu / ri);
+        float cb_mu = 10.0f * (bmu / ri);
+        f3 af = {0.0f, 0.0f, 0.0f};
+        // fluid neighbours (the group's own lists), then boundary neighbours
+        for (int pass = 0; pass < 2; ++pass) {
+          int want = pass == 0 ? fg : bg;
+          for (int k = -1; k < 26; ++k) {
+            int c = k < 0 ? home : gv.cell_adj[size_t(home) * 26 + k];
+            if (c < 0) continue;
+            int sl = tile_find(hkey, c); // present: the run's first item entered it
+            uint32_t hv = sl >= 0 ? hval[sl] : 0u;
+            uint32_t b0 = hv >> 16, b1 = b0 + (hv & 0xFFFFu);
+            for (uint32_t e = b0; e < b1; ++e) {
+              float4 X = stage[e];
+              if (int(__float_as_uint(X.w) >> 28) != want) continue;
+              f3 xij = sub3(xi, mk3(X));
+              float d2 = nsq3(xij);
+              if (!(d2 < gv.r2lt)) continue;
+              float4 W = pay[e];
+              f3 g = kgrad_from(kgrad_factor(K, d2), xij);
+              float coef;
+              if (pass == 0) coef = ((cmu * W.w) * dot3(sub3(wi, mk3(W)), xij)) / (nsq3(xij) + hh);
+              else coef = ((cb_mu * ((rho0 * W.w) / ri)) * dot3(wi, xij)) / (nsq3(xij) + hh);
+              af = add3(af, scl3(coef, g));
+            }
+          }
+        }
+        q = sub3(wi, scl3(dt, af));
+      }
+      P.Q[i] = make_float4(q.x, q.y, q.z, 0.0f);
+      pq += f2d(dot3(mk3(P.P[i]), q));
+    }
+    __syncthreads(); // the next tile reuses the shared memory
+  }
+  double v[1] = {pq}, out[1];
+  if (reduce_commit<1>(v, R, out) && threadIdx.x == 0) pcg_q_scalars(R.scalars + kSPcg, R.status, out[0], *P.tol);
+}
+
 // x += alpha p; r += alpha q; y = M r; r.r; r.y; break / beta
 // (solver/cg_openmp.hpp:153-191)
 __global__ void __launch_bounds__(kNT, kMinBlocks) k_pcg_update(PcgArgs P, Red R) {
@@ -1291,6 +1498,7 @@ int tune_knob_find(std::string const &name) {
 }
 bool tune_value_ok(int k, int v) {
   if (k == kTuneJacobiUnroll) return v == 1 || v == 2 || v == 4;
+  if (k == kTunePcgQ) return v >= 0 && v <= 4; // 4: the cell-tile sweep
   return k >= 0 && k < kTuneKnobs && v >= 0 && v <= 3;
 }
 std::string tune_knob_table() {
@@ -1302,7 +1510,7 @@ std::string tune_knob_table() {
   t += "iisph_pressure 0 " + shapes_text<PressureShapes>() + "\n";
   t += "wkbb18_diag 0 " + shapes_text<DiagShapes>() + "\n";
   t += "pcg_init 0 " + shapes_text<PcgShapes>() + "\n";
-  t += "pcg_q 0 " + shapes_text<PcgShapes>() + "\n";
+  t += "pcg_q 0 " + shapes_text<PcgShapes>() + " 4=cell-tiles (no lists; plain models)\n";
   t += "jacobi_unroll 1 1=1 2=2 4=4\n";
   return t;
 }
@@ -2040,11 +2248,11 @@ public:
 
   // solver/cg_openmp.hpp:35-215 on the device: guess and initial residual,
   // then a device loop of [q = A p, update, p update, control], then apply
-  template <int NB> void pcg_group(FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
-    if (gc_) pcg_group_t<NB, true>(F, v, G, s);
-    else pcg_group_t<NB, false>(F, v, G, s);
+  template <int NB> void pcg_group(FluidG &F, NbrView const &v, Globals G, cudaStream_t s, Nhood &nh) {
+    if (gc_) pcg_group_t<NB, true>(F, v, G, s, nh);
+    else pcg_group_t<NB, false>(F, v, G, s, nh);
   }
-  template <int NB, bool GC> void pcg_group_t(FluidG &F, NbrView const &v, Globals G, cudaStream_t s) {
+  template <int NB, bool GC> void pcg_group_t(FluidG &F, NbrView const &v, Globals G, cudaStream_t s, Nhood &nh) {
     uint32_t n = uint32_t(F.g->count);
     ensure_vectors(n);
     PcgArgs P{};
@@ -2097,16 +2305,40 @@ public:
       count_launch();
     }
     PG_LAUNCH_CHECK();
+    // shape 4 of pcg_q: the cell-tile sweep (plain models of the tuned layout)
+    bool tiles = false;
+    GridView gv{};
+    float4 const *xs = nullptr;
+    int fg = F.g->index, bg = bound_.empty() ? -1 : bound_[0].g->index;
+    if constexpr (kTuned) {
+      gv = nh.view();
+      // the tiles walk the grid's cells: the fluid group must be in the grid
+      if (!seg && tv_q == 4 && gv.in_grid[fg]) {
+        tiles = true;
+        xs = nh.sorted_positions();
+        static bool attr_set = false;
+        if (!attr_set) {
+          PG_CUDA(cudaFuncSetAttribute(k_pcg_q_tiles<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(2 * kTileStage * sizeof(float4))));
+          attr_set = true;
+        }
+      }
+    }
     auto body = [&](cudaStream_t cs, cudaGraphConditionalHandle h, bool use_handle, bool prof) {
       if (prof) model_->prof.begin("pcg_q", cs);
-      with_shape<PcgShapes, kTuned>(tv_q, [&](auto sh) {
-        using Sh = decltype(sh);
-        if (seg) {
-          if (tg) k_pcg_q_seg<NB, GC, Sh::minb, Sh::bt><<<tg, kNT, 0, cs>>>(P, G, N, SA);
-        } else {
-          k_pcg_q<NB, GC, Sh::minb, Sh::bt><<<rg, kNT, 0, cs>>>(P, G, N, R);
-        }
-      });
+      if constexpr (kTuned) {
+        if (tiles)
+          k_pcg_q_tiles<NB><<<rg, kNT, 2 * kTileStage * sizeof(float4), cs>>>(P, G, N, R, gv, xs, fg, bg);
+      }
+      if (!tiles)
+        with_shape<PcgShapes, kTuned>(tv_q, [&](auto sh) {
+          using Sh = decltype(sh);
+          if (seg) {
+            if (tg) k_pcg_q_seg<NB, GC, Sh::minb, Sh::bt><<<tg, kNT, 0, cs>>>(P, G, N, SA);
+          } else {
+            k_pcg_q<NB, GC, Sh::minb, Sh::bt><<<rg, kNT, 0, cs>>>(P, G, N, R);
+          }
+        });
       count_launch();
       if (prof) model_->prof.end(cs);
       if (prof) model_->prof.begin("pcg_update", cs);
@@ -2150,6 +2382,10 @@ public:
       sig_add(sig, rg);
       sig_add(sig, SA);
       sig_add(sig, model_->tune); // a changed shape rebuilds the graph
+      if (tiles) {
+        sig_add(sig, gv);
+        sig_add(sig, xs);
+      }
       loops_[F.g].run(s, sig, [&](cudaStream_t cs, cudaGraphConditionalHandle h) { body(cs, h, true, false); });
       PG_LAUNCH_CHECK();
     }
@@ -2170,9 +2406,9 @@ public:
         continue;
       }
       NbrView const &v = lists(nh, F.g, G, s);
-      if (nb == 0) pcg_group<0>(F, v, G, s);
-      else if (nb == 1) pcg_group<1>(F, v, G, s);
-      else if (nb == 2) pcg_group<2>(F, v, G, s);
+      if (nb == 0) pcg_group<0>(F, v, G, s, nh);
+      else if (nb == 1) pcg_group<1>(F, v, G, s, nh);
+      else if (nb == 2) pcg_group<2>(F, v, G, s, nh);
       else throw Error("unsupported group configuration: at most 2 boundary groups");
     }
   }

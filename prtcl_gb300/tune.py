@@ -34,7 +34,7 @@ import os
 import time
 
 SWEEP_KNOBS = ("density", "iisph_setup", "iisph_accel", "iisph_pressure", "wkbb18_diag", "pcg_init", "pcg_q")
-VALUES = {**{k: (0, 1, 2, 3) for k in SWEEP_KNOBS}, "jacobi_unroll": (1, 2, 4)}
+VALUES = {**{k: (0, 1, 2, 3) for k in SWEEP_KNOBS}, "pcg_q": (0, 1, 2, 3, 4), "jacobi_unroll": (1, 2, 4)}
 DEFAULTS = {**{k: 0 for k in SWEEP_KNOBS}, "jacobi_unroll": 1}
 
 
@@ -125,13 +125,14 @@ class Autotuner:
         timings = {}
         sweeps = [k for k in SWEEP_KNOBS if k in target.knobs()]
         best = {}
-        for order in (VALUES["density"], tuple(reversed(VALUES["density"]))):
+        shapes = sorted({v for k in sweeps for v in VALUES[k]})
+        for order in (shapes, tuple(reversed(shapes))):
             for v in order:
                 for k in sweeps:
-                    target.set(k, v)
+                    target.set(k, v if v in VALUES[k] else DEFAULTS[k])
                 per = target.measure_kernels(sweeps)
                 for k in sweeps:
-                    if k in per:
+                    if k in per and v in VALUES[k]:
                         t = per[k]
                         key = f"{k}={v}"
                         timings[key] = min(timings.get(key, math.inf), t * 1e6)

@@ -13,6 +13,7 @@ SETTINGS = [
     {**{k: 1 for k in tune.SWEEP_KNOBS}, "jacobi_unroll": 2},
     {**{k: 2 for k in tune.SWEEP_KNOBS}, "jacobi_unroll": 4},
     {**{k: 3 for k in tune.SWEEP_KNOBS}, "jacobi_unroll": 1},
+    {"pcg_q": 4},  # the cell-tile sweep
 ]
 FIELDS = (("position", 3), ("velocity", 3), ("density", 1), ("pressure", 1), ("acceleration", 3),
           ("wkbb18_velocity_delta", 3))
@@ -41,6 +42,20 @@ def test_knobs_keep_results_bitwise(gpu_lib, setting):
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), name
     for k, v in SETTINGS[setting].items():
         assert d.model.tune_get(k) == v
+
+
+def test_cell_tile_sweep_at_1m(gpu_lib):
+    """The cell-tile PCG sweep on the 1M dam break (tiles along the walls,
+    tiles that overflow the staging and take the lists): two steps equal
+    the list sweep's bit for bit."""
+    sc = scenes.dam_break_1m()
+    p = driver.DAM_BREAK_1M
+    ref, cref = _run(sc, p, {}, 2)
+    d, c = _run(sc, p, {"pcg_q": 4}, 2)
+    assert c == cref
+    for name, nc in FIELDS:
+        a, b = d.get_varying("f", name, nc), ref.get_varying("f", name, nc)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), name
 
 
 def test_knobs_keep_batched_results_bitwise(gpu_lib):
@@ -85,5 +100,9 @@ def test_knob_errors(gpu_lib):
     with pytest.raises(PrtclGpuError, match="invalid argument"):
         m.tune_set("iisph_accel", 4)
     with pytest.raises(PrtclGpuError, match="invalid argument"):
+        m.tune_set("pcg_q", 5)
+    with pytest.raises(PrtclGpuError, match="invalid argument"):
         m.tune_set("jacobi_unroll", 3)
     assert m.tune_get("jacobi_unroll") == 1 and m.tune_get("pcg_q") == 0
+    m.tune_set("pcg_q", 4)
+    assert m.tune_get("pcg_q") == 4
