@@ -437,7 +437,12 @@ void Segments::assign(Group const *g, std::vector<uint32_t> const &count, cudaSt
     PG_CUDA(cudaMalloc(&G.tiles, G.tile_cap * sizeof(uint4)));
     PG_CUDA(cudaMalloc(&G.slot_tiles, G.tile_cap * sizeof(uint32_t)));
     PG_CUDA(cudaMalloc(&G.active, G.tile_cap * sizeof(uint32_t)));
-    if (!G.nactive) PG_CUDA(cudaMalloc(&G.nactive, sizeof(uint32_t)));
+    // [0] active tiles, [1] and [2] the work counters of the persistent
+    // tiled Jacobi sweeps
+    if (!G.nactive) {
+      PG_CUDA(cudaMalloc(&G.nactive, 4 * sizeof(uint32_t)));
+      PG_CUDA(cudaMemsetAsync(G.nactive, 0, 4 * sizeof(uint32_t), s));
+    }
   }
   G.ntiles = uint32_t(tiles.size());
   if (!tiles.empty())

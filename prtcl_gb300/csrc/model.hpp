@@ -101,7 +101,7 @@ struct SegGroup {
   // device: the tiles of the slots whose solver loop still iterates (the
   // first nactive[0] entries), rebuilt after each loop decision
   uint32_t *active = nullptr;
-  uint32_t *nactive = nullptr;
+  uint32_t *nactive = nullptr; // [0] the count; [1], [2] work counters of the persistent tiled sweeps
   size_t seg_cap = 0, tile_cap = 0;
 };
 constexpr uint32_t kSegTile = 128; // items per reduction tile (one block)

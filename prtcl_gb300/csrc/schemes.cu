@@ -197,7 +197,7 @@ struct SegArgs {
   int const *nprde;           // [slots]
   int *iters;                 // [slots]
   uint32_t *active;           // tiles of the slots still iterating ([nactive[0]])
-  uint32_t *nactive;
+  uint32_t *nactive;          // [0] their count, [1] / [2] work counters (acceleration / pressure)
 };
 constexpr int kSegScal = 16, kSegStat = 8, kSegStats = 8;
 // blocks of the kernels that walk the active tiles (a multiple of the SM
@@ -270,7 +270,11 @@ __device__ void seg_list_active(SegArgs const &S) {
     if (threadIdx.x == 0) base += total;
     __syncthreads();
   }
-  if (threadIdx.x == 0) *S.nactive = base;
+  if (threadIdx.x == 0) {
+    S.nactive[0] = base;
+    S.nactive[1] = 0u; // the persistent sweeps of the next iteration start at tile 0
+    S.nactive[2] = 0u;
+  }
 }
 __global__ void k_seg_active(SegArgs S) { seg_list_active(S); }
 
@@ -498,18 +502,29 @@ __global__ void __launch_bounds__(NT, MINB) k_iisph_accel(uint32_t n, float4 con
   iisph_accel_item<NF, NB, BT>(i, x, p, rho, a, K, use_cache(N, K), *rho0p, N);
 }
 // batched models: the tiles of the slots still iterating
-template <int NF, int NB, int MINB = kMinBlocks, int BT = 8>
+// (DYN: each block takes the next tile from a work counter instead of a
+// static share of the tiles; the tiles' items and arithmetic are the same)
+template <int NF, int NB, int MINB = kMinBlocks, int BT = 8, bool DYN = false>
 __global__ void __launch_bounds__(kNT, MINB) k_iisph_accel_seg(float4 const *__restrict__ x, float const *__restrict__ p,
                                                          float const *__restrict__ rho, float4 *__restrict__ a,
                                                          float const *rho0p, Globals G, Nbrs<NF, NB> N, SegArgs S) {
   KernelParams K = kparams(*G.h);
   bool uc = use_cache(N, K);
   float rho0 = *rho0p;
-  uint32_t na = *S.nactive;
-  for (uint32_t t = blockIdx.x; t < na; t += gridDim.x) {
+  uint32_t na = S.nactive[0];
+  __shared__ uint32_t next;
+  for (uint32_t t = blockIdx.x;;) {
+    if (DYN) {
+      if (threadIdx.x == 0) next = atomicAdd(&S.nactive[1], 1u);
+      __syncthreads();
+      t = next;
+      __syncthreads();
+    }
+    if (t >= na) break;
     uint4 T = S.tiles[S.active[t]];
     uint32_t i = T.y + threadIdx.x;
     if (i < T.z) iisph_accel_item<NF, NB, BT>(i, x, p, rho, a, K, uc, rho0, N);
+    if (!DYN) t += gridDim.x;
   }
 }
 
@@ -581,21 +596,35 @@ __global__ void __launch_bounds__(kNT, MINB) k_iisph_pressure(uint32_t n, Pressu
 
 // iteration_pressure over the tiles of a batched model: the density error of
 // each slot's iteration goes to scal[slot][kSsAprde]
-template <int NF, int NB, int MINB = kMinBlocks, int BT = 16>
+// (DYN: a persistent grid whose blocks take tiles from a work counter; the
+// per-tile partial sums and their per-slot commit are unchanged)
+template <int NF, int NB, int MINB = kMinBlocks, int BT = 16, bool DYN = false>
 __global__ void __launch_bounds__(kNT, MINB) k_iisph_pressure_seg(PressureArgs A, Globals G, Nbrs<NF, NB> N, SegArgs S) {
   // one active tile per block (the hardware's block scheduling balances the
   // tiles' uneven costs); the blocks past the active tiles exit at once
-  if (blockIdx.x >= *S.nactive) return;
+  uint32_t na = S.nactive[0];
+  if (!DYN && blockIdx.x >= na) return;
   KernelParams K = kparams(*G.h);
   bool uc = use_cache(N, K);
   float rho0 = *A.rho0, dt = *G.dt, omega = *G.omega;
-  uint32_t t = S.active[blockIdx.x];
-  uint4 T = S.tiles[t];
-  uint32_t slot = T.x;
-  uint32_t i = T.y + threadIdx.x;
-  double part = (i < T.z) ? iisph_pressure_item<NF, NB, BT>(i, A, K, uc, rho0, dt, omega, N) : 0.0;
-  double v[1] = {part}, out[1];
-  if (seg_commit<1>(v, S, slot, out, t) && threadIdx.x == 0) S.scal[slot * kSegScal + kSsAprde] = out[0];
+  __shared__ uint32_t next;
+  for (uint32_t k = blockIdx.x;;) {
+    if (DYN) {
+      if (threadIdx.x == 0) next = atomicAdd(&S.nactive[2], 1u);
+      __syncthreads();
+      k = next;
+      __syncthreads();
+      if (k >= na) break;
+    }
+    uint32_t t = S.active[k];
+    uint4 T = S.tiles[t];
+    uint32_t slot = T.x;
+    uint32_t i = T.y + threadIdx.x;
+    double part = (i < T.z) ? iisph_pressure_item<NF, NB, BT>(i, A, K, uc, rho0, dt, omega, N) : 0.0;
+    double v[1] = {part}, out[1];
+    if (seg_commit<1>(v, S, slot, out, t) && threadIdx.x == 0) S.scal[slot * kSegScal + kSsAprde] = out[0];
+    if (!DYN) break;
+  }
 }
 
 // per-slot loop start: a slot without fluid items does not iterate
@@ -638,7 +667,12 @@ __global__ void k_seg_jacobi_control(Globals G, SegArgs S, cudaGraphConditionalH
   }
   any = __syncthreads_or(any);
   if (any) seg_list_active(S);
-  else if (threadIdx.x == 0) *S.nactive = 0; // repeats of the loop body after the end sweep nothing
+  else if (threadIdx.x == 0) {
+    // repeats of the loop body after the end sweep nothing
+    S.nactive[0] = 0u;
+    S.nactive[1] = 0u;
+    S.nactive[2] = 0u;
+  }
   if (threadIdx.x == 0) {
     *all_done = any ? 0 : 1;
     if (kernels) atomicAdd(&g_loop_kernels, (unsigned long long)kernels);
@@ -1499,6 +1533,8 @@ int tune_knob_find(std::string const &name) {
 bool tune_value_ok(int k, int v) {
   if (k == kTuneJacobiUnroll) return v == 1 || v == 2 || v == 4;
   if (k == kTunePcgQ) return v >= 0 && v <= 4; // 4: the cell-tile sweep
+  // 4: the persistent tiled sweeps of a batched model (work counter)
+  if (k == kTuneAccel || k == kTunePressure) return v >= 0 && v <= 4;
   return k >= 0 && k < kTuneKnobs && v >= 0 && v <= 3;
 }
 std::string tune_knob_table() {
@@ -1506,8 +1542,9 @@ std::string tune_knob_table() {
   std::string t;
   t += "density 0 " + shapes_text<DensityShapes>() + "\n";
   t += "iisph_setup 0 " + shapes_text<SetupShapes>() + "\n";
-  t += "iisph_accel 0 " + shapes_text<AccelShapes>() + " batched: " + shapes_text<AccelSegShapes>() + "\n";
-  t += "iisph_pressure 0 " + shapes_text<PressureShapes>() + "\n";
+  t += "iisph_accel 0 " + shapes_text<AccelShapes>() + " batched: " + shapes_text<AccelSegShapes>() +
+       " 4=persistent tiles (batched; 0 otherwise)\n";
+  t += "iisph_pressure 0 " + shapes_text<PressureShapes>() + " 4=persistent tiles (batched; 0 otherwise)\n";
   t += "wkbb18_diag 0 " + shapes_text<DiagShapes>() + "\n";
   t += "pcg_init 0 " + shapes_text<PcgShapes>() + "\n";
   t += "pcg_q 0 " + shapes_text<PcgShapes>() + " 4=cell-tiles (no lists; plain models)\n";
@@ -1953,12 +1990,17 @@ public:
       if (prof) S->model_->prof.begin("iisph_accel", s);
       int tv = S->model_->tune.v[kTuneAccel];
       if (SA) {
-        if (SA->ntiles)
-          with_shape<AccelSegShapes, NF == 1 && NB == 1>(tv, [&](auto sh) {
-            using Sh = decltype(sh);
-            k_iisph_accel_seg<NF, NB, Sh::minb, Sh::bt><<<std::min(SA->ntiles, kActiveBlocks), kNT, 0, s>>>(
+        if (SA->ntiles) {
+          if (NF == 1 && NB == 1 && tv == 4)
+            k_iisph_accel_seg<NF, NB, kMinBlocks, 8, true><<<std::min(SA->ntiles, kActiveBlocks), kNT, 0, s>>>(
                 x, p, rho, a, rho0, G, N, *SA);
-          });
+          else
+            with_shape<AccelSegShapes, NF == 1 && NB == 1>(tv, [&](auto sh) {
+              using Sh = decltype(sh);
+              k_iisph_accel_seg<NF, NB, Sh::minb, Sh::bt><<<std::min(SA->ntiles, kActiveBlocks), kNT, 0, s>>>(
+                  x, p, rho, a, rho0, G, N, *SA);
+            });
+        }
       } else {
         with_shape<AccelShapes, NF == 1 && NB == 1>(tv, [&](auto sh) {
           using Sh = decltype(sh);
@@ -1990,7 +2032,13 @@ public:
         return;
       }
       if (prof) S->model_->prof.begin("iisph_pressure", s);
-      with_shape<PressureShapes, NF == 1 && NB == 1>(S->model_->tune.v[kTunePressure], [&](auto sh) {
+      int tvp = S->model_->tune.v[kTunePressure];
+      if (SA && NF == 1 && NB == 1 && tvp == 4) {
+        if (SA->ntiles)
+          k_iisph_pressure_seg<NF, NB, kMinBlocks, 16, true><<<std::min(SA->ntiles, kActiveBlocks), kNT, 0, s>>>(
+              PA, G, N, *SA);
+      } else
+      with_shape<PressureShapes, NF == 1 && NB == 1>(tvp, [&](auto sh) {
         using Sh = decltype(sh);
         if (SA) {
           if (SA->ntiles) k_iisph_pressure_seg<NF, NB, Sh::minb, Sh::bt><<<SA->ntiles, kNT, 0, s>>>(PA, G, N, *SA);

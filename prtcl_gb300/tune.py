@@ -34,7 +34,8 @@ import os
 import time
 
 SWEEP_KNOBS = ("density", "iisph_setup", "iisph_accel", "iisph_pressure", "wkbb18_diag", "pcg_init", "pcg_q")
-VALUES = {**{k: (0, 1, 2, 3) for k in SWEEP_KNOBS}, "pcg_q": (0, 1, 2, 3, 4), "jacobi_unroll": (1, 2, 4)}
+VALUES = {**{k: (0, 1, 2, 3) for k in SWEEP_KNOBS}, "pcg_q": (0, 1, 2, 3, 4), "iisph_accel": (0, 1, 2, 3, 4),
+          "iisph_pressure": (0, 1, 2, 3, 4), "jacobi_unroll": (1, 2, 4)}
 DEFAULTS = {**{k: 0 for k in SWEEP_KNOBS}, "jacobi_unroll": 1}
 
 

@@ -63,7 +63,8 @@ def test_knobs_keep_batched_results_bitwise(gpu_lib):
     p = dict(driver.DAM_BREAK_27K)
     sc = scenes.mixed_batch(count=6, lo=600, hi=6000, seed=11)
     out = []
-    for knobs in ({}, SETTINGS[0], SETTINGS[1]):
+    # the last setting: the persistent tiled sweeps taking tiles from a work counter
+    for knobs in ({}, SETTINGS[0], SETTINGS[1], {"iisph_accel": 4, "iisph_pressure": 4, "jacobi_unroll": 2}):
         bt = Batch(p)
         for k, v in knobs.items():
             bt.tune_set(k, v)
@@ -98,7 +99,9 @@ def test_knob_errors(gpu_lib):
     with pytest.raises(PrtclNotFound, match="unknown tuning knob"):
         m.tune_set("no_such_knob", 0)
     with pytest.raises(PrtclGpuError, match="invalid argument"):
-        m.tune_set("iisph_accel", 4)
+        m.tune_set("iisph_accel", 5)
+    with pytest.raises(PrtclGpuError, match="invalid argument"):
+        m.tune_set("density", 4)
     with pytest.raises(PrtclGpuError, match="invalid argument"):
         m.tune_set("pcg_q", 5)
     with pytest.raises(PrtclGpuError, match="invalid argument"):

@@ -34,7 +34,8 @@ class FakeTarget:
         return self.unroll_cost[self.v["jacobi_unroll"]]
 
 
-COSTS = {"iisph_accel": [1.0e-4, 0.9e-4, 1.2e-4, 0.8e-4], "iisph_pressure": [1.4e-4, 1.5e-4, 1.1e-4, 2.0e-4],
+COSTS = {"iisph_accel": [1.0e-4, 0.9e-4, 1.2e-4, 0.8e-4, 0.85e-4],
+         "iisph_pressure": [1.4e-4, 1.5e-4, 1.1e-4, 2.0e-4, 1.6e-4],
          "density": [1.0e-4, 1.0e-4, 1.0e-4, 1.0e-4]}
 UNROLL = {1: 3.0e-3, 2: 2.9e-3, 4: 2.95e-3}
 
@@ -46,8 +47,11 @@ def test_search_picks_the_fastest_variant_per_knob(tmp_path):
     assert source == "tuned"
     assert choice == {"iisph_accel": 3, "iisph_pressure": 2, "density": 0, "jacobi_unroll": 2}
     assert tgt.v["iisph_accel"] == 3 and tgt.v["jacobi_unroll"] == 2  # applied
-    # each shape index twice (rising and falling), each repeat count twice
-    assert tgt.calls == 2 * 4 + 2 * 3
+    # each shape index (0..4: some knobs have a fifth form) twice, rising and
+    # falling, and each repeat count twice; a knob without the index keeps
+    # its default in that run
+    assert tgt.calls == 2 * 5 + 2 * 3
+    assert "density=4" not in timings and "iisph_accel=4" in timings
     assert timings["iisph_pressure=2"] == pytest.approx(110.0)
 
 
