@@ -446,10 +446,11 @@ def profile_pass(d, loop, steps):
     return prof
 
 
-def run_plain_27k(no_cpu=False, steps=100, warmup=3, cpu_steps=10, peak=None, peak_kind=None):
+def run_plain_27k(no_cpu=False, steps=1000, warmup=3, cpu_steps=10, peak=None, peak_kind=None):
     """The reference's plain configuration: the 27,000-particle dam break
     (spacing 0.025 m, 2 x 1 x 1 m box, dt 1e-3 s, IISPH to 0.1 % or 100
-    iterations), `steps` timed steps of the device step loop after `warmup`,
+    iterations), all 1000 steps of the configuration timed on the device
+    after `warmup` steps,
     the roofline of its dominant kernel, the same steps end to end through
     the public API (upload from pinned host memory, a position frame
     downloaded per step), beside the CPU oracle (reference mode, all host
