@@ -2364,12 +2364,9 @@ public:
       if (!seg && tv_q == 4 && gv.in_grid[fg]) {
         tiles = true;
         xs = nh.sorted_positions();
-        static bool attr_set = false;
-        if (!attr_set) {
-          PG_CUDA(cudaFuncSetAttribute(k_pcg_q_tiles<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       int(2 * kTileStage * sizeof(float4))));
-          attr_set = true;
-        }
+        // per device and cheap: set on every solve (never inside a capture)
+        PG_CUDA(cudaFuncSetAttribute(k_pcg_q_tiles<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     int(2 * kTileStage * sizeof(float4))));
       }
     }
     auto body = [&](cudaStream_t cs, cudaGraphConditionalHandle h, bool use_handle, bool prof) {
