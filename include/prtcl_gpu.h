@@ -169,8 +169,11 @@ int prtcl_gpu_profile_reset(prtcl_gpu_model *model);
  * carry the kernels' profile names: density, iisph_setup, iisph_accel,
  * iisph_pressure, wkbb18_diag, pcg_init, pcg_q (values 0..3, a launch
  * shape each; pcg_q 4: a cell-tile sweep without neighbour lists, for
- * unbatched models) and jacobi_unroll (1, 2 or 4 relaxed-Jacobi iterations per
- * iteration of the device loop's graph).  prtcl_gb300/tune.py searches them
+ * unbatched models), jacobi_unroll (1, 2 or 4 relaxed-Jacobi iterations per
+ * iteration of the device loop's graph) and staging (1: unbatched models with
+ * one fluid and one boundary group build staged lists, and the
+ * relaxed-Jacobi and PCG sweeps read their neighbours' records from shared
+ * memory per tile of 128 items).  prtcl_gb300/tune.py searches them
  * per workload and caches the choice.  prtcl_gpu_tune_knobs returns one line
  * per knob: "name default value=shape ...", a shape written as threads per
  * block x blocks per SM / neighbour-walk batch.  An unknown knob gives
@@ -212,6 +215,13 @@ int prtcl_gpu_nhood_copy_neighbors(prtcl_gpu_nhood *nhood, int32_t group, int64_
  * neighbours in `neighbor_group`; offsets_out has count + 1 entries. */
 int prtcl_gpu_nhood_copy_lists(prtcl_gpu_nhood *nhood, int32_t query_group, int32_t neighbor_group,
                                int64_t *offsets_out, uint32_t *indices_out, int64_t capacity);
+/* Introspection of staged lists (the `staging` knob; no counterpart in the
+ * reference): of the tiles of 128 consecutive items of `query_group`'s
+ * last built lists, *staged_out receives those whose neighbours' records
+ * fit the staged sweeps' shared memory, *tiles_out all of them; both 0 when
+ * the lists were not built staged.  Synchronises. */
+int prtcl_gpu_nhood_staged_tiles(prtcl_gpu_nhood *nhood, int32_t query_group, int64_t *staged_out,
+                                 int64_t *tiles_out);
 /* Grid introspection for parity checks: the sorted item handles
  * (group << 28 | raw index, util/grouped_uniform_grid.hpp:104-110), and per
  * cell its grid index (3 x int32), its [first, last) sorted range and its

@@ -79,6 +79,7 @@ SIGNATURES = {
     "prtcl_gpu_nhood_permute": [vp, vp, vp],
     "prtcl_gpu_nhood_copy_neighbors": [vp, i32, i64, i64p, i64p, i64, i64p],
     "prtcl_gpu_nhood_copy_lists": [vp, i32, i32, i64p, u32p, i64],
+    "prtcl_gpu_nhood_staged_tiles": [vp, i32, i64p, i64p],
     "prtcl_gpu_nhood_grid_size": [vp, i64p, i64p],
     "prtcl_gpu_nhood_copy_grid": [vp, u32p, i32p, i32p, i32p],
     "prtcl_gpu_scheme_new": [cp, pp],

@@ -354,6 +354,14 @@ class Neighborhood:
                                            _stream(stream)))
         return n.value if count_pairs else None
 
+    def staged_tiles(self, group_index):
+        """(staged, tiles) of the group's last built lists: the tiles of 128
+        items whose neighbours' records fit shared memory, and all tiles;
+        (0, 0) when they were not built staged."""
+        k, t = C.c_int64(0), C.c_int64(0)
+        check(load().prtcl_gpu_nhood_staged_tiles(self._h, int(group_index), C.byref(k), C.byref(t)))
+        return k.value, t.value
+
     def copy_neighbors(self, group_index, index):
         """Neighbours of (group, index): one int64 array per group."""
         G = self._model.group_count

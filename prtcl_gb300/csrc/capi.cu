@@ -468,6 +468,17 @@ int prtcl_gpu_nhood_copy_lists(prtcl_gpu_nhood *nhood, int32_t query_group, int3
                         nhood->n.model()->stream());
   });
 }
+int prtcl_gpu_nhood_staged_tiles(prtcl_gpu_nhood *nhood, int32_t query_group, int64_t *staged_out,
+                                 int64_t *tiles_out) {
+  NEED(nhood);
+  return guard([&] {
+    if (!nhood->n.loaded()) throw Error("Neighborhood not loaded");
+    size_t tiles = 0;
+    size_t k = nhood->n.staged_tiles(query_group, tiles, nhood->n.model()->stream());
+    if (staged_out) *staged_out = int64_t(k);
+    if (tiles_out) *tiles_out = int64_t(tiles);
+  });
+}
 int prtcl_gpu_nhood_grid_size(prtcl_gpu_nhood *nhood, int64_t *sorted_count_out, int64_t *cell_count_out) {
   NEED(nhood);
   return guard([&] {

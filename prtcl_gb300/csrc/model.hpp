@@ -139,8 +139,11 @@ struct Segments {
 // threads per block (sweeps without a reduction), the blocks resident per SM
 // (the register cap) and the neighbour-walk batch; the Jacobi value repeats
 // the loop body that many times per graph iteration, the repeats past
-// convergence doing nothing.  The variants apply to models with one fluid
-// and at most one boundary group; other layouts use variant 0.
+// convergence doing nothing.  With staging, the lists of the fluid group
+// also carry each entry's slot among its tile's staged items (nhood.hpp),
+// and the Jacobi and PCG sweeps read their neighbours' records from shared
+// memory.  The variants apply to models with one fluid and at most one
+// boundary group; other layouts use variant 0 and no staging.
 enum TuneKnob : int {
   kTuneDensity = 0,
   kTuneSetup,
@@ -150,10 +153,11 @@ enum TuneKnob : int {
   kTunePcgInit,
   kTunePcgQ,
   kTuneJacobiUnroll,
+  kTuneStaging, // 1: staged lists and the staged Jacobi / PCG sweeps
   kTuneKnobs
 };
 struct Tuning {
-  int v[kTuneKnobs] = {0, 0, 0, 0, 0, 0, 0, 1};
+  int v[kTuneKnobs] = {0, 0, 0, 0, 0, 0, 0, 1, 0};
 };
 // knob names (the kernels' profiler names; "jacobi_unroll") and allowed values
 char const *tune_knob_name(int k);

@@ -83,4 +83,44 @@ __device__ __forceinline__ void for_each_nbr(NbrList const &L, uint32_t i, bool 
   }
 }
 
+// Calls f(slot, factor) for the neighbours of item i, in list order, from
+// staged lists (nhood.hpp): slot is the neighbour's place among the staged
+// items of the item's tile, which the caller has copied to shared memory.
+// The slots of chunk c of item i are the 16 halves at (c * n + i) * 16 of
+// `slots`; the factors are those of the chunks.
+template <uint32_t kNbrBatch = kNbrBatchDefault, class F>
+__device__ __forceinline__ void for_each_staged(NbrList const &L, uint16_t const *slots, uint32_t i, F &&f) {
+  uint2 cb = __ldg(L.cb + i);
+  uint32_t c = min(cb.x & ~kWide, L.cap);
+  for (uint32_t kb = 0; kb < c; kb += kNbrBatch) {
+    uint32_t h = (kb % kChunk) / kNbrBatch;
+    size_t ci = size_t(kb / kChunk) * L.n + i;
+    uint4 const *ch = reinterpret_cast<uint4 const *>(L.chunks + ci * kChunkBytes);
+    uint4 const *sp = reinterpret_cast<uint4 const *>(slots + ci * kChunk);
+    uint32_t sl[kNbrBatch];
+#pragma unroll
+    for (int v = 0; v < int(kNbrBatch / 8); ++v) {
+      uint4 a = __ldcs(sp + h * (kNbrBatch / 8) + v);
+      uint32_t w[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        sl[8 * v + 2 * t] = w[t] & 0xFFFFu;
+        sl[8 * v + 2 * t + 1] = w[t] >> 16;
+      }
+    }
+    float g[kNbrBatch];
+#pragma unroll
+    for (int v = 0; v < int(kNbrBatch / 4); ++v) {
+      uint4 a = __ldcs(ch + 2 + h * (kNbrBatch / 4) + v);
+      g[4 * v] = __uint_as_float(a.x);
+      g[4 * v + 1] = __uint_as_float(a.y);
+      g[4 * v + 2] = __uint_as_float(a.z);
+      g[4 * v + 3] = __uint_as_float(a.w);
+    }
+#pragma unroll
+    for (int t = 0; t < int(kNbrBatch); ++t)
+      if (kb + t < c) f(sl[t], g[t]);
+  }
+}
+
 } // namespace prtcl_gpu

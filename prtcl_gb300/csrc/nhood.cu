@@ -471,6 +471,8 @@ constexpr int kBuildNT = 128; // query items (threads) per list-build block
 
 struct ListOut {
   unsigned char *chunks[kMaxListGroups];
+  uint16_t *slots[kMaxListGroups]; // staged lists: each entry's staged slot
+  uint2 *tile_info, *tile_cells;   // staged lists: per tile (see nhood.hpp)
   uint32_t *idx32[kMaxListGroups];
   uint32_t cap[kMaxListGroups];
   uint2 *cb;        // [G][n]
@@ -497,31 +499,44 @@ struct RowState {
   bool wide;
 };
 
-__device__ __forceinline__ uint32_t &bufw(uint32_t *buf, int g, int w) {
-  return buf[(size_t(g) * 24 + w) * kBuildNT + threadIdx.x];
+// BW: buffered words per thread and group: 24 (8 of packed offsets, 16 of
+// factors), or 32 for staged lists (8 more of packed slots)
+template <int BW> __device__ __forceinline__ uint32_t &bufw(uint32_t *buf, int g, int w) {
+  return buf[(size_t(g) * BW + w) * kBuildNT + threadIdx.x];
 }
 
+template <int BW>
 __device__ __forceinline__ void flush_chunk(ListOut const &lo, int g, uint32_t i, uint32_t chunk, bool wide,
                                             uint32_t *buf) {
-  uint4 *dst = reinterpret_cast<uint4 *>(lo.chunks[g] + (size_t(chunk) * lo.n + i) * kChunkBytes);
+  size_t ci = size_t(chunk) * lo.n + i;
+  uint4 *dst = reinterpret_cast<uint4 *>(lo.chunks[g] + ci * kChunkBytes);
   // offsets (2 vectors, not for a wide row), then the factors (4 vectors)
   // when the lists carry them: sweeps read factors only from lists built
   // with a smoothing scale
   int v0 = wide ? 2 : 0, nv = lo.with_gf ? 6 : 2;
   for (int v = v0; v < nv; ++v)
-    dst[v] = make_uint4(bufw(buf, g, 4 * v), bufw(buf, g, 4 * v + 1), bufw(buf, g, 4 * v + 2), bufw(buf, g, 4 * v + 3));
+    dst[v] = make_uint4(bufw<BW>(buf, g, 4 * v), bufw<BW>(buf, g, 4 * v + 1), bufw<BW>(buf, g, 4 * v + 2),
+                        bufw<BW>(buf, g, 4 * v + 3));
+  if (BW == 32) {
+    uint4 *sd = reinterpret_cast<uint4 *>(lo.slots[g] + ci * kChunk);
+    for (int v = 0; v < 2; ++v)
+      sd[v] = make_uint4(bufw<BW>(buf, g, 24 + 4 * v), bufw<BW>(buf, g, 25 + 4 * v), bufw<BW>(buf, g, 26 + 4 * v),
+                         bufw<BW>(buf, g, 27 + 4 * v));
+  }
 }
 
 // the 8 buffered indices of a wide row's entries e0..e0+7 (e0 % 8 == 0) to
 // idx32: 32 aligned bytes (cap is a multiple of 16)
+template <int BW>
 __device__ __forceinline__ void flush_wide_half(ListOut const &lo, int g, uint32_t i, uint32_t e0, uint32_t *buf) {
   uint4 *dst = reinterpret_cast<uint4 *>(lo.idx32[g] + size_t(i) * lo.cap[g] + e0);
-  dst[0] = make_uint4(bufw(buf, g, 0), bufw(buf, g, 1), bufw(buf, g, 2), bufw(buf, g, 3));
-  dst[1] = make_uint4(bufw(buf, g, 4), bufw(buf, g, 5), bufw(buf, g, 6), bufw(buf, g, 7));
+  dst[0] = make_uint4(bufw<BW>(buf, g, 0), bufw<BW>(buf, g, 1), bufw<BW>(buf, g, 2), bufw<BW>(buf, g, 3));
+  dst[1] = make_uint4(bufw<BW>(buf, g, 4), bufw<BW>(buf, g, 5), bufw<BW>(buf, g, 6), bufw<BW>(buf, g, 7));
 }
 
+template <int BW>
 __device__ __forceinline__ void row_add(ListOut const &lo, int g, uint32_t i, RowState &R, uint32_t j, float f,
-                                        uint32_t *buf) {
+                                        uint32_t slot16, uint32_t *buf) {
   uint32_t k = R.c++;
   if (k >= lo.cap[g]) return; // overflow: the host grows the lists and builds again
   if (k == 0) R.j0 = j;
@@ -533,31 +548,34 @@ __device__ __forceinline__ void row_add(ListOut const &lo, int g, uint32_t i, Ro
     R.wide = true;
     for (uint32_t e = 0; e < k; ++e) {
       uint32_t w;
-      if (e / kChunk == k / kChunk) w = bufw(buf, g, int((e % kChunk) / 2));
+      if (e / kChunk == k / kChunk) w = bufw<BW>(buf, g, int((e % kChunk) / 2));
       else w = reinterpret_cast<uint32_t const *>(lo.chunks[g] + (size_t(e / kChunk) * lo.n + i) * kChunkBytes)[(e % kChunk) / 2];
       int32_t de = int32_t(int16_t((e & 1) ? (w >> 16) : (w & 0xFFFFu)));
       lo.idx32[g][size_t(i) * lo.cap[g] + e] = R.j0 + uint32_t(de);
     }
     // the current half-chunk's entries back into the buffer as indices (the
     // packed words they came from are no longer needed)
-    for (uint32_t e = k - slot % 8; e < k; ++e) bufw(buf, g, int(e % 8)) = lo.idx32[g][size_t(i) * lo.cap[g] + e];
+    for (uint32_t e = k - slot % 8; e < k; ++e) bufw<BW>(buf, g, int(e % 8)) = lo.idx32[g][size_t(i) * lo.cap[g] + e];
   }
   if (R.wide) {
-    bufw(buf, g, int(slot % 8)) = j;
+    bufw<BW>(buf, g, int(slot % 8)) = j;
   } else {
     // the slot's half-word (little-endian: even slots low); a stale upper
     // half past the row's end is cleared when the last chunk is written
-    reinterpret_cast<uint16_t *>(&bufw(buf, g, int(slot / 2)))[slot & 1] = uint16_t(uint32_t(d) & 0xFFFFu);
+    reinterpret_cast<uint16_t *>(&bufw<BW>(buf, g, int(slot / 2)))[slot & 1] = uint16_t(uint32_t(d) & 0xFFFFu);
   }
-  if (lo.with_gf) bufw(buf, g, 8 + int(slot)) = __float_as_uint(f);
-  if (R.wide && slot % 8 == 7) flush_wide_half(lo, g, i, k - 7, buf);
-  if (slot == kChunk - 1) flush_chunk(lo, g, i, k / kChunk, R.wide, buf);
+  if (lo.with_gf) bufw<BW>(buf, g, 8 + int(slot)) = __float_as_uint(f);
+  if (BW == 32) reinterpret_cast<uint16_t *>(&bufw<BW>(buf, g, 24 + int(slot / 2)))[slot & 1] = uint16_t(slot16);
+  if (R.wide && slot % 8 == 7) flush_wide_half<BW>(lo, g, i, k - 7, buf);
+  if (slot == kChunk - 1) flush_chunk<BW>(lo, g, i, k / kChunk, R.wide, buf);
 }
 
-template <int NG>
+// cbase (staged lists, BW == 32): the cell's first slot among the tile's
+// staged items, so that the hit at sorted index s has slot cbase + (s - s0)
+template <int NG, int BW>
 __device__ __forceinline__ void visit_cell(GridView const &gv, float4 const *__restrict__ xs, int cell, f3 xi,
                                            uint32_t i, ListOut const &lo, RowState *R, KernelParams const &K,
-                                           bool with_gf, uint32_t *buf) {
+                                           bool with_gf, uint32_t *buf, uint32_t cbase = 0u) {
   if (cell < 0) return;
   int s0 = gv.cell_start[cell], s1 = gv.cell_start[cell + 1];
   // the distance tests of up to 32 candidates into a mask, then the
@@ -588,9 +606,10 @@ __device__ __forceinline__ void visit_cell(GridView const &gv, float4 const *__r
       uint32_t h = __float_as_uint(xj.w);
       uint32_t g = h >> 28, j = h & 0x0FFFFFFFu;
       float f = with_gf ? kgrad_factor(K, nsq3(sub3(xi, mk3(xj)))) : 0.0f;
+      uint32_t slot16 = BW == 32 ? cbase + uint32_t(base + t - s0) : 0u;
 #pragma unroll
       for (int q = 0; q < NG; ++q)
-        if (q == int(g)) row_add(lo, q, i, R[q], j, f, buf);
+        if (q == int(g)) row_add<BW>(lo, q, i, R[q], j, f, slot16, buf);
     }
   }
 }
@@ -624,16 +643,131 @@ __device__ __forceinline__ bool face_bounds(float x, float rinv, int gi, float &
 // With one or two neighbour groups (24.6 KB of row buffers per block at
 // most) nine blocks fit an SM's shared memory; holding the registers to
 // that (56) took the 1M dam break's list build from 604 to 585 µs.
-template <int NG>
-__global__ void __launch_bounds__(kBuildNT, NG <= 2 ? 9 : 1) k_build_lists(GridView gv, float4 const *__restrict__ xs,
-                                                          float4 const *__restrict__ qpos, int q, ListOut lo,
-                                                          float const *hp, float *hcache,
-                                                          uint32_t const *__restrict__ order) {
+// Staged lists: the tile's staged cells (the cells adjacent to its items'
+// cells, own cell included) in an open-addressing table of kStageHash
+// slots, their first staged slots, and the tile's table in global memory
+// (nhood.hpp).  All threads of the block take part; returns whether the
+// tile's staged items fit (kStageCap items, kStageCells cells).
+__device__ __forceinline__ uint32_t stage_hash(int c) { return (uint32_t(c) * 2654435761u) >> 23; } // 9 bits
+static_assert(kStageHash == 512, "stage_hash yields 9 bits");
+
+__device__ __forceinline__ int stage_find(int const *hkey, int c) {
+  uint32_t h = stage_hash(c);
+  for (uint32_t probe = 0; probe < kStageHash; ++probe) {
+    uint32_t sl = (h + probe) & (kStageHash - 1);
+    if (hkey[sl] == c) return int(sl);
+  }
+  return -1;
+}
+
+__device__ bool stage_tile(GridView const &gv, int home, bool has, uint32_t tile, ListOut const &lo, int *hkey,
+                           uint32_t *hbase) {
+  __shared__ int homes[kBuildNT];
+  __shared__ uint32_t wsum[kBuildNT / 32], wocc[kBuildNT / 32];
+  __shared__ int over;
+  for (uint32_t sl = threadIdx.x; sl < kStageHash; sl += kBuildNT) hkey[sl] = -1;
+  if (threadIdx.x == 0) over = 0;
+  homes[threadIdx.x] = home;
+  __syncthreads();
+  // the first item of each run of equal home cells enters the run's 27 cells
+  if (has && (threadIdx.x == 0 || homes[threadIdx.x - 1] != home)) {
+    for (int k = -1; k < 26; ++k) {
+      int c = k < 0 ? home : gv.cell_adj[size_t(home) * 26 + k];
+      if (c < 0) continue;
+      uint32_t h = stage_hash(c);
+      bool placed = false;
+      for (uint32_t probe = 0; probe < kStageHash && !placed; ++probe) {
+        int old = atomicCAS(&hkey[(h + probe) & (kStageHash - 1)], -1, c);
+        placed = old == -1 || old == c;
+      }
+      if (!placed) over = 1;
+    }
+  }
+  __syncthreads();
+  // the staged items of each table slot; slots in (thread, m) order
+  constexpr int M = kStageHash / kBuildNT;
+  uint32_t cnt[M], mine = 0, occ = 0;
+#pragma unroll
+  for (int m = 0; m < M; ++m) {
+    int c = hkey[threadIdx.x + m * kBuildNT];
+    cnt[m] = c >= 0 ? uint32_t(gv.cell_start[c + 1] - gv.cell_start[c]) : 0u;
+    mine += cnt[m];
+    occ += c >= 0 ? 1u : 0u;
+  }
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t incl = mine, oincl = occ;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t v = __shfl_up_sync(0xffffffffu, incl, o), vo = __shfl_up_sync(0xffffffffu, oincl, o);
+    if (lane >= o) {
+      incl += v;
+      oincl += vo;
+    }
+  }
+  if (lane == 31) {
+    wsum[w] = incl;
+    wocc[w] = oincl;
+  }
+  __syncthreads();
+  uint32_t off = incl - mine, u = oincl - occ, total = 0, ncells = 0;
+  for (int k = 0; k < int(kBuildNT / 32); ++k) {
+    if (k < w) {
+      off += wsum[k];
+      u += wocc[k];
+    }
+    total += wsum[k];
+    ncells += wocc[k];
+  }
+  if (total > kStageCap || ncells > kStageCells) over = 1;
+  __syncthreads();
+  bool fit = over == 0;
+  if (fit) {
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+      uint32_t sl = threadIdx.x + m * kBuildNT;
+      int c = hkey[sl];
+      if (c >= 0) {
+        hbase[sl] = off;
+        lo.tile_cells[size_t(tile) * kStageCells + u] = make_uint2(uint32_t(gv.cell_start[c]), off);
+        off += cnt[m];
+        ++u;
+      }
+    }
+  }
+  if (threadIdx.x == 0) lo.tile_info[tile] = make_uint2(ncells, fit ? total : kNoStage);
+  __syncthreads();
+  return fit;
+}
+
+// neighbour lists of one query group (grid query of util/grouped_uniform_grid.hpp:407-531)
+// `order` (optional): thread t builds the row of item order[t] (the group's
+// items in grid order), so that the threads of a warp walk nearby cells.
+// Adjacent cells whose box is farther than the radius from the query (with a
+// margin of 1e-4 of the radius, far above the rounding of the exact test)
+// cannot hold a neighbour and are not scanned; the lists are unchanged.
+// With one or two neighbour groups (24.6 KB of row buffers per block at
+// most) nine blocks fit an SM's shared memory; holding the registers to
+// that (56) took the 1M dam break's list build from 604 to 585 µs.
+// STAGE: staged lists (a group in cell order, no `order`): the block is the
+// tile of items it builds, and every entry also gets its staged slot.
+template <int NG, bool STAGE>
+__global__ void __launch_bounds__(kBuildNT, STAGE ? 5 : (NG <= 2 ? 9 : 1))
+    k_build_lists(GridView gv, float4 const *__restrict__ xs, float4 const *__restrict__ qpos, int q, ListOut lo,
+                  float const *hp, float *hcache, uint32_t const *__restrict__ order) {
+  constexpr int BW = STAGE ? 32 : 24;
   extern __shared__ uint32_t buf[];
+  __shared__ int s_hkey[STAGE ? kStageHash : 1];
+  __shared__ uint32_t s_hbase[STAGE ? kStageHash : 1];
   uint32_t t = blockIdx.x * kBuildNT + threadIdx.x;
   bool with_gf = hp != nullptr;
   KernelParams K = kparams(with_gf ? *hp : 1.0f);
   if (t == 0) *hcache = with_gf ? K.h : __int_as_float(0x7fc00000);
+  bool staged = false;
+  if constexpr (STAGE) {
+    bool has = t < lo.n;
+    int home = has ? gv.s2c[gv.r2s[gv.goff[q] + t]] : -1;
+    staged = stage_tile(gv, home, has, blockIdx.x, lo, s_hkey, s_hbase);
+  }
   if (t >= lo.n) return;
   uint32_t i = order ? order[t] : t;
   RowState R[NG];
@@ -651,6 +785,13 @@ __global__ void __launch_bounds__(kBuildNT, NG <= 2 ? 9 : 1) k_build_lists(GridV
     cell = find_cell(gv, gi, item_seg(gv, q, i));
     fallback = cell < 0;
   }
+  // the staged base of a visited cell (0 where the tile is not staged: the
+  // slots are then never read)
+  auto cbase = [&](int c) -> uint32_t {
+    if (!STAGE || !staged || c < 0) return 0u;
+    int sl = stage_find(s_hkey, c);
+    return sl >= 0 ? s_hbase[sl] : 0u;
+  };
   if (!fallback) {
     float lo3[3], hi3[3];
     int4 cg = gv.cell_gi[cell];
@@ -659,7 +800,7 @@ __global__ void __launch_bounds__(kBuildNT, NG <= 2 ? 9 : 1) k_build_lists(GridV
     inside = face_bounds(x4.z, gv.rinv, cg.z, lo3[2], hi3[2]) && inside;
     if (!inside)
       for (int a = 0; a < 3; ++a) lo3[a] = hi3[a] = 0.0f;
-    visit_cell<NG>(gv, xs, cell, xi, i, lo, R, K, with_gf, buf);
+    visit_cell<NG, BW>(gv, xs, cell, xi, i, lo, R, K, with_gf, buf, cbase(cell));
     for (int k = 0; k < 26; ++k) {
       // slot k < 13: +offset[k]; slot 25 - k: -offset[k]
       int kk = k < 13 ? k : 25 - k;
@@ -672,15 +813,16 @@ __global__ void __launch_bounds__(kBuildNT, NG <= 2 ? 9 : 1) k_build_lists(GridV
         lb += b * b;
       }
       if (lb > 1.0001f) continue;
-      visit_cell<NG>(gv, xs, gv.cell_adj[size_t(cell) * 26 + k], xi, i, lo, R, K, with_gf, buf);
+      int c = gv.cell_adj[size_t(cell) * 26 + k];
+      visit_cell<NG, BW>(gv, xs, c, xi, i, lo, R, K, with_gf, buf, cbase(c));
     }
   } else {
     uint32_t sq = item_seg(gv, q, i);
     for (int k = 0; k < 13; ++k) {
       int3 p = make_int3(gi.x + c_offsets[k][0], gi.y + c_offsets[k][1], gi.z + c_offsets[k][2]);
-      visit_cell<NG>(gv, xs, find_cell(gv, p, sq), xi, i, lo, R, K, with_gf, buf);
+      visit_cell<NG, BW>(gv, xs, find_cell(gv, p, sq), xi, i, lo, R, K, with_gf, buf);
       int3 m = make_int3(gi.x - c_offsets[k][0], gi.y - c_offsets[k][1], gi.z - c_offsets[k][2]);
-      visit_cell<NG>(gv, xs, find_cell(gv, m, sq), xi, i, lo, R, K, with_gf, buf);
+      visit_cell<NG, BW>(gv, xs, find_cell(gv, m, sq), xi, i, lo, R, K, with_gf, buf);
     }
   }
 #pragma unroll
@@ -702,27 +844,31 @@ __global__ void __launch_bounds__(kBuildNT, NG <= 2 ? 9 : 1) k_build_lists(GridV
       // the partial last chunk (and half-chunk of a wide row), zero-filled
       bool wide = R[g].wide;
       if (wide && n % 8) {
-        for (uint32_t e = n % 8; e < 8; ++e) bufw(buf, g, int(e)) = 0u;
-        flush_wide_half(lo, g, i, n - n % 8, buf);
+        for (uint32_t e = n % 8; e < 8; ++e) bufw<BW>(buf, g, int(e)) = 0u;
+        flush_wide_half<BW>(lo, g, i, n - n % 8, buf);
       }
       for (uint32_t slot = n % kChunk; slot < kChunk; ++slot) {
         if (!wide) {
-          uint32_t &w = bufw(buf, g, int(slot / 2));
+          uint32_t &w = bufw<BW>(buf, g, int(slot / 2));
           w = (slot & 1) ? (w & 0xFFFFu) : 0u;
         }
-        bufw(buf, g, 8 + int(slot)) = 0u;
+        bufw<BW>(buf, g, 8 + int(slot)) = 0u;
+        if (BW == 32) {
+          uint32_t &w = bufw<BW>(buf, g, 24 + int(slot / 2));
+          w = (slot & 1) ? (w & 0xFFFFu) : 0u;
+        }
       }
-      flush_chunk(lo, g, i, n / kChunk, wide, buf);
+      flush_chunk<BW>(lo, g, i, n / kChunk, wide, buf);
     }
   }
 }
 
-template <int NG>
+template <int NG, bool STAGE>
 void launch_build_lists(size_t n, size_t smem, cudaStream_t s, GridView const &gv, float4 const *xs,
                         float4 const *qpos, int q, ListOut const &lo, float const *h, float *hcache,
                         uint32_t const *order) {
-  PG_CUDA(cudaFuncSetAttribute(k_build_lists<NG>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-  k_build_lists<NG><<<div_up(n, kBuildNT), kBuildNT, smem, s>>>(gv, xs, qpos, q, lo, h, hcache, order);
+  PG_CUDA(cudaFuncSetAttribute(k_build_lists<NG, STAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  k_build_lists<NG, STAGE><<<div_up(n, kBuildNT), kBuildNT, smem, s>>>(gv, xs, qpos, q, lo, h, hcache, order);
 }
 
 __global__ void k_pair_count(uint2 const *cb, size_t n, unsigned long long *total) {
@@ -792,9 +938,17 @@ void Nhood::free_lists(Lists &L) {
   for (int g = 0; g < kMaxGroups; ++g) {
     if (L.idx32[g]) cudaFree(L.idx32[g]);
     if (L.chunks[g]) cudaFree(L.chunks[g]);
+    if (L.slots[g]) cudaFree(L.slots[g]);
     L.idx32[g] = nullptr;
     L.chunks[g] = nullptr;
+    L.slots[g] = nullptr;
   }
+  if (L.tile_info) cudaFree(L.tile_info);
+  if (L.tile_cells) cudaFree(L.tile_cells);
+  L.tile_info = nullptr;
+  L.tile_cells = nullptr;
+  L.tile_cap = 0;
+  L.staged = false;
   if (L.cb) cudaFree(L.cb);
   if (L.hcache) cudaFree(L.hcache);
   L.cb = nullptr;
@@ -1043,7 +1197,7 @@ std::vector<uint64_t> Nhood::pos_versions() const {
 
 bool Nhood::lists_fresh(Lists const &L) const { return L.epoch == epoch_ && L.pos_versions == pos_versions(); }
 
-void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
+void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h, bool stage) {
   int G = int(gg_.size());
   if (G > kMaxListGroups) throw Error("neighbour lists support at most 8 groups");
   size_t n = gg_[q].g->count;
@@ -1070,14 +1224,46 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
     PG_LAUNCH_CHECK();
     order = order_;
   }
+  // staged lists: with factors, for a group in cell order, at most two
+  // neighbour groups (the staged sweeps' layout)
+  bool st = stage && h && in_grid_[q] && !order && G <= 2;
+  if (st != L.staged) {
+    // a change of form reallocates every list of the group
+    for (int g = 0; g < kMaxGroups; ++g) L.cap[g] = 0;
+    for (int g = 0; g < kMaxGroups; ++g) {
+      if (L.idx32[g]) PG_CUDA(cudaFree(L.idx32[g]));
+      if (L.chunks[g]) PG_CUDA(cudaFree(L.chunks[g]));
+      if (L.slots[g]) PG_CUDA(cudaFree(L.slots[g]));
+      L.idx32[g] = nullptr;
+      L.chunks[g] = nullptr;
+      L.slots[g] = nullptr;
+    }
+    L.staged = st;
+  }
+  // the staged tile tables (after any free_lists() below, which drops them)
+  auto ensure_tiles = [&] {
+    size_t ntiles = div_up(n, kStageTile);
+    if (!st || ntiles <= L.tile_cap) return;
+    if (L.tile_info) PG_CUDA(cudaFree(L.tile_info));
+    if (L.tile_cells) PG_CUDA(cudaFree(L.tile_cells));
+    L.tile_info = nullptr;
+    L.tile_cells = nullptr;
+    L.tile_cap = 0;
+    PG_CUDA(cudaMalloc(&L.tile_info, (ntiles + ntiles / 8 + 1) * sizeof(uint2)));
+    PG_CUDA(cudaMalloc(&L.tile_cells, (ntiles + ntiles / 8 + 1) * kStageCells * sizeof(uint2)));
+    L.tile_cap = ntiles + ntiles / 8 + 1;
+  };
   auto alloc_slots = [&](int g, uint32_t want) {
     if (L.idx32[g]) PG_CUDA(cudaFree(L.idx32[g]));
     if (L.chunks[g]) PG_CUDA(cudaFree(L.chunks[g]));
+    if (L.slots[g]) PG_CUDA(cudaFree(L.slots[g]));
     L.idx32[g] = nullptr;
     L.chunks[g] = nullptr;
+    L.slots[g] = nullptr;
     if (n > 0) {
       PG_CUDA(cudaMalloc(&L.idx32[g], size_t(want) * n * 4));
       PG_CUDA(cudaMalloc(&L.chunks[g], size_t(want / kChunk) * kChunkBytes * n));
+      if (L.staged) PG_CUDA(cudaMalloc(&L.slots[g], size_t(want) * n * sizeof(uint16_t)));
     }
     L.cap[g] = want;
   };
@@ -1088,6 +1274,8 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
       L.n = n;
       if (n > 0) PG_CUDA(cudaMalloc(&L.cb, size_t(G) * n * sizeof(uint2)));
     }
+    L.staged = st; // free_lists() clears it, with every array
+    ensure_tiles();
     for (int g = 0; g < G; ++g)
       if (!L.idx32[g] || L.cap[g] == 0) alloc_slots(g, L.cap[g] ? L.cap[g] : 48u);
     // after any free_lists() above: the kernel always writes *hcache
@@ -1097,9 +1285,17 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
     for (int g = 0; g < G; ++g) {
       lo.idx32[g] = L.idx32[g];
       lo.chunks[g] = L.chunks[g];
+      lo.slots[g] = L.slots[g];
       lo.cap[g] = L.cap[g];
     }
-    size_t smem = size_t(G) * 24 * kBuildNT * 4;
+    lo.tile_info = L.tile_info;
+    lo.tile_cells = L.tile_cells;
+    if (st) {
+      bool ok = lo.tile_info && lo.tile_cells;
+      for (int g = 0; g < G; ++g) ok = ok && lo.slots[g];
+      if (!ok) throw Error("staged lists: tile tables or slot arrays missing");
+    }
+    size_t smem = size_t(G) * (st ? 32 : 24) * kBuildNT * 4;
     lo.cb = L.cb;
     lo.maxcnt = stats_d_ + 8;
     lo.n = uint32_t(n);
@@ -1110,12 +1306,18 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
     float4 const *qpos = static_cast<float4 const *>(gg_[q].pos->d);
     {
       ProfScope ps(model_->prof, "nhood_lists", s);
-      switch (G) {
-      case 1: launch_build_lists<1>(n, smem, s, gv, xsorted_, qpos, q, lo, h, L.hcache, order); break;
-      case 2: launch_build_lists<2>(n, smem, s, gv, xsorted_, qpos, q, lo, h, L.hcache, order); break;
-      case 3: launch_build_lists<3>(n, smem, s, gv, xsorted_, qpos, q, lo, h, L.hcache, order); break;
-      case 4: launch_build_lists<4>(n, smem, s, gv, xsorted_, qpos, q, lo, h, L.hcache, order); break;
-      default: launch_build_lists<kMaxListGroups>(n, smem, s, gv, xsorted_, qpos, q, lo, h, L.hcache, order);
+      if (st) {
+        if (G == 1) launch_build_lists<1, true>(n, smem, s, gv, xsorted_, qpos, q, lo, h, L.hcache, order);
+        else launch_build_lists<2, true>(n, smem, s, gv, xsorted_, qpos, q, lo, h, L.hcache, order);
+      } else {
+        switch (G) {
+        case 1: launch_build_lists<1, false>(n, smem, s, gv, xsorted_, qpos, q, lo, h, L.hcache, order); break;
+        case 2: launch_build_lists<2, false>(n, smem, s, gv, xsorted_, qpos, q, lo, h, L.hcache, order); break;
+        case 3: launch_build_lists<3, false>(n, smem, s, gv, xsorted_, qpos, q, lo, h, L.hcache, order); break;
+        case 4: launch_build_lists<4, false>(n, smem, s, gv, xsorted_, qpos, q, lo, h, L.hcache, order); break;
+        default:
+          launch_build_lists<kMaxListGroups, false>(n, smem, s, gv, xsorted_, qpos, q, lo, h, L.hcache, order);
+        }
       }
       count_launch();
     }
@@ -1133,7 +1335,7 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
         // the layout changed: a new grid (read-back layout), then these lists
         key_known_ = false;
         update(s);
-        build_lists(q, L, s, h);
+        build_lists(q, L, s, h, stage);
         return;
       }
     }
@@ -1170,11 +1372,14 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h) {
     L.view.chunks[g] = L.chunks[g];
     L.view.cb[g] = L.cb ? L.cb + size_t(g) * n : nullptr;
     L.view.cap[g] = L.cap[g];
+    L.view.slots[g] = L.staged ? L.slots[g] : nullptr;
   }
+  L.view.tile_info = L.staged ? L.tile_info : nullptr;
+  L.view.tile_cells = L.staged ? L.tile_cells : nullptr;
   L.view.n = uint32_t(n);
 }
 
-NbrView const &Nhood::lists(int q, cudaStream_t s, float const *h) {
+NbrView const &Nhood::lists(int q, cudaStream_t s, float const *h, bool stage) {
   if (!has_grid_) throw Error("Neighborhood has not been updated");
   if (q < 0 || q >= int(gg_.size())) throw Error("invalid group index");
   Lists &L = lists_[q];
@@ -1199,7 +1404,10 @@ NbrView const &Nhood::lists(int q, cudaStream_t s, float const *h) {
     }
     return L.view;
   }
-  if (!lists_fresh(L) || (h && !L.has_gf)) build_lists(q, L, s, h);
+  // stale lists are built in the form asked for; fresh staged lists also
+  // serve a caller that did not ask for staging
+  if (!lists_fresh(L) || (h && !L.has_gf)) build_lists(q, L, s, h, stage);
+  else if (stage && !L.staged) build_lists(q, L, s, h, true);
   return L.view;
 }
 
@@ -1278,6 +1486,21 @@ uint64_t Nhood::pair_count(int q, cudaStream_t s) {
   PG_CUDA(cudaFreeAsync(d, s));
   PG_CUDA(cudaStreamSynchronize(s));
   return uint64_t(h);
+}
+
+size_t Nhood::staged_tiles(int q, size_t &tiles, cudaStream_t s) {
+  tiles = 0;
+  auto it = lists_.find(q);
+  if (it == lists_.end() || !it->second.staged) return 0;
+  Lists const &L = it->second;
+  size_t nt = div_up(L.n, kStageTile);
+  std::vector<uint2> info(nt);
+  if (nt) PG_CUDA(cudaMemcpyAsync(info.data(), L.tile_info, nt * sizeof(uint2), cudaMemcpyDeviceToHost, s));
+  PG_CUDA(cudaStreamSynchronize(s));
+  tiles = nt;
+  size_t k = 0;
+  for (auto const &e : info) k += e.y != kNoStage ? 1 : 0;
+  return k;
 }
 
 size_t Nhood::device_bytes() const {

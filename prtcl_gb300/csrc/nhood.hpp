@@ -60,6 +60,24 @@ namespace prtcl_gpu {
 // smoothing scale and evaluate the gradient in full otherwise.
 constexpr uint32_t kChunk = 16;
 constexpr uint32_t kChunkBytes = kChunk * 2 + kChunk * 4;
+// Staged lists (built on request for a query group in cell order): the
+// query items form tiles of kStageTile consecutive items (the list build's
+// blocks, and the staged sweeps' blocks).  The cells adjacent to a tile's
+// cells (own cell included) are its staged cells; their sorted items, cell
+// after cell in the tile's table order, are the tile's staged items, at most
+// kStageCap.  Besides the offsets and factors, each entry then has its
+// neighbour's position among the tile's staged items (slot, 16 bits),
+// chunk-major like the offsets (chunk c of item i at (c * n + i), 16 slots
+// of 2 bytes), so that a sweep that copies a tile's staged items to shared
+// memory reads its gathers from there.  tile_info[t] = (staged cells, staged
+// items), the items 0xFFFFFFFF for a tile that did not fit (no slots; the
+// sweep takes the offsets); tile_cells[t * kStageCells + u] = (first sorted
+// index of the cell, its first staged slot).
+constexpr uint32_t kStageTile = 128;
+constexpr uint32_t kStageCap = 1536;
+constexpr uint32_t kStageCells = 256;
+constexpr uint32_t kStageHash = 512;
+constexpr uint32_t kNoStage = 0xFFFFFFFFu;
 struct NbrView {
   unsigned char const *chunks[kMaxGroups];
   uint32_t const *idx32[kMaxGroups];
@@ -67,6 +85,10 @@ struct NbrView {
   uint32_t cap[kMaxGroups]; // a multiple of kChunk
   uint32_t n;               // query items
   float const *hcache;      // NaN when no factors were computed
+  // staged lists (nullptr when not built staged)
+  uint16_t const *slots[kMaxGroups];
+  uint2 const *tile_info;
+  uint2 const *tile_cells;
 };
 
 constexpr uint32_t kWide = 0x80000000u;
@@ -173,7 +195,7 @@ public:
   // neighbour lists of query group q (rebuilt when stale); with `h` (the
   // smoothing scale on the device) they also hold each pair's kernel
   // gradient factor
-  NbrView const &lists(int q, cudaStream_t s, float const *h = nullptr);
+  NbrView const &lists(int q, cudaStream_t s, float const *h = nullptr, bool stage = false);
 
   // introspection (tests): sizes and host copies of the grid
   size_t sorted_count() const { return N_; }
@@ -185,6 +207,9 @@ public:
   uint64_t pair_count(int q, cudaStream_t s);
   // CSR copy of the lists of query group q to neighbour group ng
   void copy_lists(int q, int ng, int64_t *offsets, uint32_t *idx, size_t cap, cudaStream_t s);
+  // tiles of query group q's last built lists whose staged records fit, and
+  // all tiles (0, 0 when they were not built staged; synchronises)
+  size_t staged_tiles(int q, size_t &tiles, cudaStream_t s);
 
   GridView view() const;
   // sorted positions with their handles in w (current after the lists of a
@@ -207,6 +232,10 @@ private:
     uint32_t cap[kMaxGroups] = {};
     uint32_t *idx32[kMaxGroups] = {};
     unsigned char *chunks[kMaxGroups] = {};
+    uint16_t *slots[kMaxGroups] = {};   // staged lists only
+    uint2 *tile_info = nullptr, *tile_cells = nullptr;
+    size_t tile_cap = 0;
+    bool staged = false;
     uint2 *cb = nullptr; // [G][n]
     float *hcache = nullptr;
     bool has_gf = false;
@@ -215,7 +244,7 @@ private:
     NbrView view{};
   };
   void ensure_grid_capacity(size_t n);
-  void build_lists(int q, Lists &L, cudaStream_t s, float const *h);
+  void build_lists(int q, Lists &L, cudaStream_t s, float const *h, bool stage);
   // Confirm the key layout an update took from the previous one (one
   // synchronisation); on a mismatch, update again with a layout read back
   // first.  Called before the grid is read on the host or permutes fields;

@@ -177,6 +177,73 @@ using PressureShapes = RedShapes<16, 8>;
 using DiagShapes = FreeShapes<8, 16>;
 using PcgShapes = RedShapes<8, 16>;
 
+// Staged sweeps (the `staging` knob; lists built staged, nhood.hpp): a
+// block's items are the tiles of kStageTile consecutive items the list build
+// staged; per tile the block copies the tile's staged items' records to
+// shared memory (two float4 per item, in slot order) and the threads read
+// their neighbours from there by the lists' slots.  A tile that did not fit
+// takes the global gathers.  The records and the order of the terms are
+// those of the unstaged sweeps, so the results are bit-identical.
+static_assert(kNT == int(kStageTile), "a staged sweep's block is one tile");
+struct StageArgs {
+  uint16_t const *fslots, *bslots; // slots of the fluid group's lists towards itself and the boundary group
+  uint2 const *tile_info, *tile_cells;
+  uint32_t const *sorted;          // sorted handles (group << 28 | index)
+  int fg, bg;                      // the two groups' indices
+};
+constexpr size_t kStageSmem = 2 * kStageCap * sizeof(float4);
+
+// copies tile `tile`'s staged records (rec(handle, x, y) per item) to sx, sy;
+// false (block-uniform) for a tile that was not staged
+// asynchronous global -> shared copies (cp.async): 16 bytes (L2 only), or
+// 4 bytes; the records of a tile are all in flight at once
+__device__ __forceinline__ void cp_async16(float4 *dst, void const *src) {
+  uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(float *dst, void const *src) {
+  uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// copies tile `tile`'s staged records to sx, sy: rec(handle, sx + p, sy + p)
+// issues the copies of slot p (only the parts its sweep reads); false
+// (block-uniform) for a tile that was not staged
+template <class Rec>
+__device__ bool stage_copy(StageArgs const &SA, uint32_t tile, float4 *sx, float4 *sy, Rec &&rec) {
+  __shared__ uint32_t s_src[kStageCap]; // sorted index of each staged slot
+  __shared__ uint2 s_info;
+  if (threadIdx.x == 0) s_info = SA.tile_info[tile];
+  __syncthreads();
+  uint2 info = s_info;
+  if (info.y == kNoStage) return false;
+  // each staged cell's slots name its sorted range
+  for (uint32_t u = threadIdx.x; u < info.x; u += blockDim.x) {
+    uint2 e = SA.tile_cells[size_t(tile) * kStageCells + u];
+    uint32_t end = u + 1 < info.x ? SA.tile_cells[size_t(tile) * kStageCells + u + 1].y : info.y;
+    for (uint32_t q = e.y; q < end; ++q) s_src[q] = e.x + (q - e.y);
+  }
+  __syncthreads();
+  constexpr int kU = 4; // handles loaded together
+  for (uint32_t p0 = threadIdx.x; p0 < info.y; p0 += kU * blockDim.x) {
+    uint32_t h[kU];
+#pragma unroll
+    for (int k = 0; k < kU; ++k) {
+      uint32_t p = p0 + k * blockDim.x;
+      h[k] = p < info.y ? __ldg(SA.sorted + s_src[p]) : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < kU; ++k) {
+      uint32_t p = p0 + k * blockDim.x;
+      if (p < info.y) rec(h[k], sx + p, sy + p);
+    }
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  return true;
+}
+
 // Batched (segmented) models: block b of a tiled launch handles tile b, up to
 // kSegTile consecutive items of one slot (scene).  Reductions are per slot:
 // each tile stores its FP64 block sum; the last tile of the slot to finish
@@ -540,6 +607,22 @@ struct PressureArgs {
   float const *rho0;
 };
 
+// the end of iteration_pressure for one item, from its neighbour sum ap:
+// Ap, the new pressure (and p / rho^2); returns the density-error term
+__device__ __forceinline__ double pressure_finish(uint32_t i, PressureArgs const &A, float ap, float rho0, float dt,
+                                                  float omega) {
+  float ri = A.rho[i];
+  ap *= (dt * dt) * (rho0 / ri);
+  A.Ap[i] = ap;
+  float si = A.s[i], aai = A.AA[i];
+  float t = A.p[i] + ((omega * (si - ap)) * rcp0(aai, 1e-9f));
+  // std::max({0, t}) returns the first largest element: t only if 0 < t
+  float pn = ((0.0f < t) ? t : 0.0f) * ustep(1e-9f, fabsf(aai));
+  A.p[i] = pn;
+  A.pr[i] = pn / (ri * ri);
+  return f2d(((ap - si) / rho0) * ustep(1e-9f, pn));
+}
+
 // one item of iteration_pressure; returns its density-error term
 template <int NF, int NB, int BT = 16>
 __device__ __forceinline__ double iisph_pressure_item(uint32_t i, PressureArgs const &A, KernelParams const &K, bool uc,
@@ -563,16 +646,7 @@ __device__ __forceinline__ double iisph_pressure_item(uint32_t i, PressureArgs c
       ap += (rho0 * xv.w) * dot3(sub3(ai, f3{0.0f, 0.0f, 0.0f}), pgrad(uc, gf_, K, sub3(xi, mk3(xv))));
     });
   }
-  float ri = A.rho[i];
-  ap *= (dt * dt) * (rho0 / ri);
-  A.Ap[i] = ap;
-  float si = A.s[i], aai = A.AA[i];
-  float t = A.p[i] + ((omega * (si - ap)) * rcp0(aai, 1e-9f));
-  // std::max({0, t}) returns the first largest element: t only if 0 < t
-  float pn = ((0.0f < t) ? t : 0.0f) * ustep(1e-9f, fabsf(aai));
-  A.p[i] = pn;
-  A.pr[i] = pn / (ri * ri);
-  return f2d(((ap - si) / rho0) * ustep(1e-9f, pn));
+  return pressure_finish(i, A, ap, rho0, dt, omega);
 }
 
 template <int NF, int NB, int MINB = kMinBlocks, int BT = 16>
@@ -624,6 +698,117 @@ __global__ void __launch_bounds__(kNT, MINB) k_iisph_pressure_seg(PressureArgs A
     double v[1] = {part}, out[1];
     if (seg_commit<1>(v, S, slot, out, t) && threadIdx.x == 0) S.scal[slot * kSegScal + kSsAprde] = out[0];
     if (!DYN) break;
+  }
+}
+
+// staged relaxed-Jacobi sweeps (one fluid and one boundary group; the
+// `staging` knob).  Per tile, the staged records: a fluid item's (x, m) and
+// p / rho^2 (acceleration) or acceleration (pressure); a boundary item's
+// (x, V).
+template <int BT = 8>
+__global__ void __launch_bounds__(kNT, 4) k_iisph_accel_staged(uint32_t n, float4 const *__restrict__ x,
+                                                               float const *__restrict__ p,
+                                                               float const *__restrict__ rho, float4 *__restrict__ a,
+                                                               float const *rho0p, Globals G, Nbrs<1, 1> N,
+                                                               int const *done, StageArgs SA) {
+  if (done && *(volatile int const *)done) return;
+  extern __shared__ float4 sm[];
+  float4 *sx = sm, *sy = sm + kStageCap;
+  KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
+  float rho0 = *rho0p;
+  FluidN const &F = N.f[0];
+  BoundN const &B = N.b[0];
+  for (uint32_t tile = blockIdx.x; size_t(tile) * kNT < n; tile += gridDim.x) {
+    uint32_t i = tile * kNT + threadIdx.x;
+    // fluid: (x, m) and p / rho^2 (in .x); boundary: (x, V)
+    bool st = stage_copy(SA, tile, sx, sy, [&](uint32_t h, float4 *dx, float4 *dy) {
+      uint32_t j = h & 0x0FFFFFFFu;
+      if (int(h >> 28) == SA.fg) {
+        cp_async16(dx, F.xm + j);
+        cp_async4(&dy->x, F.pr + j);
+      } else if (int(h >> 28) == SA.bg) {
+        cp_async16(dx, B.xV + j);
+      }
+    });
+    if (i < n) {
+      if (st) {
+        f3 xi = mk3(x[i]);
+        float pi = p[i], ri = rho[i];
+        float pri = pi / (ri * ri);
+        f3 acc = {0.0f, 0.0f, 0.0f};
+        for_each_staged<BT>(F.L, SA.fslots, i, [&](uint32_t sl, float gf_) {
+          float4 xm = sx[sl];
+          float coef = xm.w * (pri + sy[sl].x);
+          acc = sub3(acc, scl3(coef, pgrad(uc, gf_, K, sub3(xi, mk3(xm)))));
+        });
+        float bterm = (2.0f * pi) / (ri * ri);
+        for_each_staged<BT>(B.L, SA.bslots, i, [&](uint32_t sl, float gf_) {
+          float4 xv = sx[sl];
+          float coef = ((0.7f * rho0) * xv.w) * bterm;
+          acc = sub3(acc, scl3(coef, pgrad(uc, gf_, K, sub3(xi, mk3(xv)))));
+        });
+        a[i] = make_float4(acc.x, acc.y, acc.z, 0.0f);
+      } else {
+        iisph_accel_item<1, 1, BT>(i, x, p, rho, a, K, uc, rho0, N);
+      }
+    }
+    __syncthreads(); // the next tile reuses the shared memory
+  }
+}
+
+// the tiles of a block are those of k_iisph_pressure's grid-stride items,
+// so the FP64 partial sums are the same
+template <int BT = 8>
+__global__ void __launch_bounds__(kNT, 4) k_iisph_pressure_staged(uint32_t n, PressureArgs A, Globals G,
+                                                                  Nbrs<1, 1> N, Red R, int first, int last_group,
+                                                                  int const *done, StageArgs SA) {
+  if (done && *(volatile int const *)done) return;
+  extern __shared__ float4 sm[];
+  float4 *sx = sm, *sy = sm + kStageCap;
+  KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
+  float rho0 = *A.rho0, dt = *G.dt, omega = *G.omega;
+  FluidN const &F = N.f[0];
+  BoundN const &B = N.b[0];
+  double part = 0.0;
+  for (uint32_t tile = blockIdx.x; size_t(tile) * kNT < n; tile += gridDim.x) {
+    uint32_t i = tile * kNT + threadIdx.x;
+    // fluid: (x, m) and the acceleration; boundary: (x, V)
+    bool st = stage_copy(SA, tile, sx, sy, [&](uint32_t h, float4 *dx, float4 *dy) {
+      uint32_t j = h & 0x0FFFFFFFu;
+      if (int(h >> 28) == SA.fg) {
+        cp_async16(dx, F.xm + j);
+        cp_async16(dy, F.a + j);
+      } else if (int(h >> 28) == SA.bg) {
+        cp_async16(dx, B.xV + j);
+      }
+    });
+    if (i < n) {
+      if (st) {
+        f3 xi = mk3(A.x[i]), ai = mk3(A.a[i]);
+        float ap = 0.0f;
+        for_each_staged<BT>(F.L, SA.fslots, i, [&](uint32_t sl, float gf_) {
+          float4 xm = sx[sl];
+          ap += xm.w * dot3(sub3(ai, mk3(sy[sl])), pgrad(uc, gf_, K, sub3(xi, mk3(xm))));
+        });
+        for_each_staged<BT>(B.L, SA.bslots, i, [&](uint32_t sl, float gf_) {
+          float4 xv = sx[sl];
+          ap += (rho0 * xv.w) * dot3(sub3(ai, f3{0.0f, 0.0f, 0.0f}), pgrad(uc, gf_, K, sub3(xi, mk3(xv))));
+        });
+        part += pressure_finish(i, A, ap, rho0, dt, omega);
+      } else {
+        part += iisph_pressure_item<1, 1, BT>(i, A, K, uc, rho0, dt, omega, N);
+      }
+    }
+    __syncthreads();
+  }
+  double v[1] = {part}, out[1];
+  if (reduce_commit<1>(v, R, out) && threadIdx.x == 0) {
+    double start = first ? (done ? 0.0 : double(*G.aprde)) : R.scalars[kSJacobi];
+    double acc = start + out[0];
+    R.scalars[kSJacobi] = acc;
+    if (last_group) *G.aprde = float(acc);
   }
 }
 
@@ -952,6 +1137,14 @@ __global__ void k_pcg_guess(PcgArgs P) {
   if (i < P.n) P.X[i] = P.v[i];
 }
 
+__device__ __forceinline__ void pcg_init_finish(PcgArgs const &P, uint32_t i, f3 ax, double &bb, double &rr,
+                                                double &ry);
+// the rest of pcg_q_item from q = A p: stores q, returns p . q
+__device__ __forceinline__ double pcg_q_finish(PcgArgs const &P, uint32_t i, f3 q) {
+  P.Q[i] = make_float4(q.x, q.y, q.z, 0.0f);
+  return f2d(dot3(mk3(P.P[i]), q));
+}
+
 // r = A x - b (b = v: the right-hand side's boundary term has v_b = 0),
 // y = M r, p = -y; dots b.b, r.r, r.y (solver/cg_openmp.hpp:48-96)
 // per-item parts of the PCG kernels (shared by the plain and the tiled
@@ -960,7 +1153,11 @@ template <int NB, bool GC, int BT = 8>
 __device__ __forceinline__ void pcg_init_item(PcgArgs const &P, KernelParams const &K, bool uc, float dt, float rho0,
                                               float mu, Nbrs<0, NB> const &N, uint32_t i, double &bb, double &rr,
                                               double &ry) {
-  f3 ax = wkbb18_system<NB, GC, BT>(P, K, uc, dt, rho0, mu, N, P.X, i);
+  pcg_init_finish(P, i, wkbb18_system<NB, GC, BT>(P, K, uc, dt, rho0, mu, N, P.X, i), bb, rr, ry);
+}
+// the rest of pcg_init_item from A x
+__device__ __forceinline__ void pcg_init_finish(PcgArgs const &P, uint32_t i, f3 ax, double &bb, double &rr,
+                                                double &ry) {
   f3 b = mk3(P.v[i]);
   f3 r = sub3(ax, b);
   f3 y = precond(P.sp, P.cap, i, r);
@@ -974,9 +1171,7 @@ __device__ __forceinline__ void pcg_init_item(PcgArgs const &P, KernelParams con
 template <int NB, bool GC, int BT = 8>
 __device__ __forceinline__ double pcg_q_item(PcgArgs const &P, KernelParams const &K, bool uc, float dt, float rho0,
                                              float mu, Nbrs<0, NB> const &N, uint32_t i) {
-  f3 q = wkbb18_system<NB, GC, BT>(P, K, uc, dt, rho0, mu, N, P.P, i);
-  P.Q[i] = make_float4(q.x, q.y, q.z, 0.0f);
-  return f2d(dot3(mk3(P.P[i]), q));
+  return pcg_q_finish(P, i, wkbb18_system<NB, GC, BT>(P, K, uc, dt, rho0, mu, N, P.P, i));
 }
 __device__ __forceinline__ void pcg_update_item(PcgArgs const &P, float alpha, uint32_t i, double &rr, double &ry) {
   f3 x = mk3(P.X[i]), p = mk3(P.P[i]), r = mk3(P.Rr[i]), q = mk3(P.Q[i]);
@@ -1054,6 +1249,102 @@ __global__ void __launch_bounds__(kNT, MINB) k_pcg_q(PcgArgs P, Globals G, Nbrs<
   double pq = 0.0;
   for (uint32_t i = grid_tid(); i < P.n; i += gridDim.x * blockDim.x)
     pq += pcg_q_item<NB, GC, BT>(P, K, uc, dt, rho0, mu, N, i);
+  double v[1] = {pq}, out[1];
+  if (reduce_commit<1>(v, R, out) && threadIdx.x == 0) pcg_q_scalars(R.scalars + kSPcg, R.status, out[0], *P.tol);
+}
+
+// the system product from staged lists (one boundary group, no gradient
+// correction): the staged records are a fluid item's (x, m / rho) and w, a
+// boundary item's (x, V); terms and order those of wkbb18_system
+template <int BT = 8>
+__device__ __forceinline__ f3 wkbb18_system_staged(PcgArgs const &P, KernelParams const &K, bool uc, float dt,
+                                                   float rho0, float mu, float bmu, StageArgs const &SA,
+                                                   BoundN const &B, float4 const *sx, float4 const *sy,
+                                                   float4 const *__restrict__ w, uint32_t i) {
+  float h = K.h;
+  float hh = (0.01f * h) * h;
+  f3 xi = mk3(P.xmr[i]), wi = mk3(w[i]);
+  float ri = P.rho[i];
+  float cmu = 10.0f * (mu / ri);
+  f3 af = {0.0f, 0.0f, 0.0f};
+  for_each_staged<BT>(P.self, SA.fslots, i, [&](uint32_t sl, float gf_) {
+    float4 xj = sx[sl];
+    f3 xij = sub3(xi, mk3(xj));
+    float coef = ((cmu * xj.w) * dot3(sub3(wi, mk3(sy[sl])), xij)) / (nsq3(xij) + hh);
+    af = add3(af, scl3(coef, pgrad(uc, gf_, K, xij)));
+  });
+  float cb_mu = 10.0f * (bmu / ri);
+  for_each_staged<BT>(B.L, SA.bslots, i, [&](uint32_t sl, float gf_) {
+    float4 xv = sx[sl];
+    f3 xij = sub3(xi, mk3(xv));
+    float coef = ((cb_mu * ((rho0 * xv.w) / ri)) * dot3(wi, xij)) / (nsq3(xij) + hh);
+    af = add3(af, scl3(coef, pgrad(uc, gf_, K, xij)));
+  });
+  return sub3(wi, scl3(dt, af));
+}
+
+// stages tile `tile` for the system product with vector w
+__device__ __forceinline__ bool stage_system(StageArgs const &SA, uint32_t tile, float4 *sx, float4 *sy,
+                                             PcgArgs const &P, BoundN const &B, float4 const *w) {
+  // fluid: (x, m / rho) and w; boundary: (x, V)
+  return stage_copy(SA, tile, sx, sy, [&](uint32_t h, float4 *dx, float4 *dy) {
+    uint32_t j = h & 0x0FFFFFFFu;
+    if (int(h >> 28) == SA.fg) {
+      cp_async16(dx, P.xmr + j);
+      cp_async16(dy, w + j);
+    } else if (int(h >> 28) == SA.bg) {
+      cp_async16(dx, B.xV + j);
+    }
+  });
+}
+
+// staged k_pcg_init / k_pcg_q (the `staging` knob): a block's tiles are the
+// items of the plain kernels' grid-stride loop, so the FP64 sums are the same
+template <int BT = 8>
+__global__ void __launch_bounds__(kNT, 4) k_pcg_init_staged(PcgArgs P, Globals G, Nbrs<0, 1> N, Red R, StageArgs SA) {
+  extern __shared__ float4 sm[];
+  float4 *sx = sm, *sy = sm + kStageCap;
+  KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
+  float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
+  BoundN const &B = N.b[0];
+  float bmu = *B.mu;
+  double bb = 0.0, rr = 0.0, ry = 0.0;
+  for (uint32_t tile = blockIdx.x; size_t(tile) * kNT < P.n; tile += gridDim.x) {
+    uint32_t i = tile * kNT + threadIdx.x;
+    bool st = stage_system(SA, tile, sx, sy, P, B, P.X);
+    if (i < P.n) {
+      if (st)
+        pcg_init_finish(P, i, wkbb18_system_staged<BT>(P, K, uc, dt, rho0, mu, bmu, SA, B, sx, sy, P.X, i), bb, rr,
+                        ry);
+      else
+        pcg_init_item<1, false, BT>(P, K, uc, dt, rho0, mu, N, i, bb, rr, ry);
+    }
+    __syncthreads();
+  }
+  double v[3] = {bb, rr, ry}, out[3];
+  if (reduce_commit<3>(v, R, out) && threadIdx.x == 0) pcg_init_scalars(R.scalars + kSPcg, R.status, out, *P.tol);
+}
+
+template <int BT = 8>
+__global__ void __launch_bounds__(kNT, 4) k_pcg_q_staged(PcgArgs P, Globals G, Nbrs<0, 1> N, Red R, StageArgs SA) {
+  if (!*(volatile int *)&R.status[kStPcgActive]) return;
+  extern __shared__ float4 sm[];
+  float4 *sx = sm, *sy = sm + kStageCap;
+  KernelParams K = kparams(*G.h);
+  bool uc = use_cache(N, K);
+  float dt = *G.dt, rho0 = *P.rho0, mu = *P.mu;
+  BoundN const &B = N.b[0];
+  float bmu = *B.mu;
+  double pq = 0.0;
+  for (uint32_t tile = blockIdx.x; size_t(tile) * kNT < P.n; tile += gridDim.x) {
+    uint32_t i = tile * kNT + threadIdx.x;
+    bool st = stage_system(SA, tile, sx, sy, P, B, P.P);
+    if (i < P.n)
+      pq += st ? pcg_q_finish(P, i, wkbb18_system_staged<BT>(P, K, uc, dt, rho0, mu, bmu, SA, B, sx, sy, P.P, i))
+               : pcg_q_item<1, false, BT>(P, K, uc, dt, rho0, mu, N, i);
+    __syncthreads();
+  }
   double v[1] = {pq}, out[1];
   if (reduce_commit<1>(v, R, out) && threadIdx.x == 0) pcg_q_scalars(R.scalars + kSPcg, R.status, out[0], *P.tol);
 }
@@ -1522,7 +1813,7 @@ template <class T> void sig_add(std::string &s, T const &v) { s.append(reinterpr
 
 char const *tune_knob_name(int k) {
   static char const *names[kTuneKnobs] = {"density", "iisph_setup", "iisph_accel", "iisph_pressure",
-                                          "wkbb18_diag", "pcg_init", "pcg_q", "jacobi_unroll"};
+                                          "wkbb18_diag", "pcg_init", "pcg_q", "jacobi_unroll", "staging"};
   return (k >= 0 && k < kTuneKnobs) ? names[k] : "";
 }
 int tune_knob_find(std::string const &name) {
@@ -1532,6 +1823,7 @@ int tune_knob_find(std::string const &name) {
 }
 bool tune_value_ok(int k, int v) {
   if (k == kTuneJacobiUnroll) return v == 1 || v == 2 || v == 4;
+  if (k == kTuneStaging) return v == 0 || v == 1;
   if (k == kTunePcgQ) return v >= 0 && v <= 4; // 4: the cell-tile sweep
   // 4: the persistent tiled sweeps of a batched model (work counter)
   if (k == kTuneAccel || k == kTunePressure) return v >= 0 && v <= 4;
@@ -1549,6 +1841,7 @@ std::string tune_knob_table() {
   t += "pcg_init 0 " + shapes_text<PcgShapes>() + "\n";
   t += "pcg_q 0 " + shapes_text<PcgShapes>() + " 4=cell-tiles (no lists; plain models)\n";
   t += "jacobi_unroll 1 1=1 2=2 4=4\n";
+  t += "staging 0 0=off 1=staged lists and sweeps (unbatched models)\n";
   return t;
 }
 
@@ -1683,7 +1976,29 @@ protected:
     N.hcache = v.hcache;
     return N;
   }
-  NbrView const &lists(Nhood &nh, Group *g, Globals const &G, cudaStream_t s) { return nh.lists(g->index, s, G.h); }
+  // staged lists when the model's staging knob is on (fluid groups of an
+  // unbatched model; the neighbourhood builds them only for the layouts the
+  // staged sweeps handle)
+  NbrView const &lists(Nhood &nh, Group *g, Globals const &G, cudaStream_t s) {
+    bool stage = model_->tune.v[kTuneStaging] != 0 && g->type == "fluid" && !segmented(g);
+    return nh.lists(g->index, s, G.h, stage);
+  }
+  // the staged sweeps' arguments for fluid group F (one fluid and one
+  // boundary group, unbatched); false where the lists are not staged
+  bool stage_args(Nhood &nh, NbrView const &v, FluidG const &F, StageArgs &SA) {
+    if (!model_->tune.v[kTuneStaging] || fluid_.size() != 1 || bound_.size() != 1 || segmented(F.g)) return false;
+    int fg = F.g->index, bg = bound_[0].g->index;
+    if (!v.tile_info || !v.tile_cells || !v.slots[fg] || !v.slots[bg]) return false;
+    SA = StageArgs{v.slots[fg], v.slots[bg], v.tile_info, v.tile_cells, nh.view().sorted, fg, bg};
+    // per device and cheap: set on every solve (never inside a capture)
+    static_assert(kStageSmem <= 64 * 1024, "staged records fit four blocks per SM");
+    PG_CUDA(cudaFuncSetAttribute(k_iisph_accel_staged<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kStageSmem)));
+    PG_CUDA(cudaFuncSetAttribute(k_iisph_pressure_staged<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 int(kStageSmem)));
+    PG_CUDA(cudaFuncSetAttribute(k_pcg_init_staged<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kStageSmem)));
+    PG_CUDA(cudaFuncSetAttribute(k_pcg_q_staged<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kStageSmem)));
+    return true;
+  }
   float const *u(SmallField *f) { return static_cast<float const *>(model_->small_ptr(*f)); }
   void need(std::initializer_list<std::pair<void const *, char const *>> l) {
     for (auto &p : l)
@@ -1968,7 +2283,7 @@ public:
   // timing events (never on a capture stream).
   template <int NF, int NB> struct A {
     static void go(Iisph *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s, int const *done, bool prof,
-                   std::string *sig, SegArgs const *SA = nullptr) {
+                   std::string *sig, SegArgs const *SA = nullptr, StageArgs const *ST = nullptr) {
       uint32_t n = uint32_t(F.g->count);
       auto N = S->nbrs<NF, NB>(v, s);
       for (int q = 0; q < NF; ++q) N.f[q].pr = S->model_->packed_pr(S->fluid_[q].g, S->fluid_[q].p, S->fluid_[q].rho, s);
@@ -1985,11 +2300,20 @@ public:
         sig_add(*sig, a);
         sig_add(*sig, rho0);
         if (SA) sig_add(*sig, *SA);
+        if (ST) sig_add(*sig, *ST);
         return;
       }
       if (prof) S->model_->prof.begin("iisph_accel", s);
       int tv = S->model_->tune.v[kTuneAccel];
-      if (SA) {
+      bool staged = false;
+      if constexpr (NF == 1 && NB == 1) {
+        if (ST && !SA) {
+          k_iisph_accel_staged<8><<<div_up(n, kNT), kNT, kStageSmem, s>>>(n, x, p, rho, a, rho0, G, N, done, *ST);
+          staged = true;
+        }
+      }
+      if (staged) {
+      } else if (SA) {
         if (SA->ntiles) {
           if (NF == 1 && NB == 1 && tv == 4)
             k_iisph_accel_seg<NF, NB, kMinBlocks, 8, true><<<std::min(SA->ntiles, kActiveBlocks), kNT, 0, s>>>(
@@ -2014,7 +2338,8 @@ public:
   };
   template <int NF, int NB> struct P {
     static void go(Iisph *S, FluidG &F, NbrView const &v, Globals G, cudaStream_t s, int first, int last,
-                   int const *done, bool prof, std::string *sig, SegArgs const *SA = nullptr) {
+                   int const *done, bool prof, std::string *sig, SegArgs const *SA = nullptr,
+                   StageArgs const *ST = nullptr) {
       uint32_t n = uint32_t(F.g->count);
       auto N = S->nbrs<NF, NB>(v, s);
       float *pr = S->model_->pr_buffer(F.g, s);
@@ -2029,11 +2354,20 @@ public:
         sig_add(*sig, first);
         sig_add(*sig, last);
         if (SA) sig_add(*sig, *SA);
+        if (ST) sig_add(*sig, *ST);
         return;
       }
       if (prof) S->model_->prof.begin("iisph_pressure", s);
       int tvp = S->model_->tune.v[kTunePressure];
-      if (SA && NF == 1 && NB == 1 && tvp == 4) {
+      bool staged = false;
+      if constexpr (NF == 1 && NB == 1) {
+        if (ST && !SA) {
+          k_iisph_pressure_staged<16><<<red_grid(n), kNT, kStageSmem, s>>>(n, PA, G, N, R, first, last, done, *ST);
+          staged = true;
+        }
+      }
+      if (staged) {
+      } else if (SA && NF == 1 && NB == 1 && tvp == 4) {
         if (SA->ntiles)
           k_iisph_pressure_seg<NF, NB, kMinBlocks, 16, true><<<std::min(SA->ntiles, kActiveBlocks), kNT, 0, s>>>(
               PA, G, N, *SA);
@@ -2149,6 +2483,10 @@ public:
     }
     for (auto &B : bound_)
       if (B.g->count) model_->packed_xs(B.g, B.x, B.V, "xV", s);
+    // staged sweeps (the staging knob): one fluid group, staged lists
+    StageArgs st{};
+    bool staged = !seg && act.size() == 1 && stage_args(nh, *views[0], *act[0], st);
+    StageArgs const *stp = staged ? &st : nullptr;
     if (seg) {
       k_seg_jacobi_begin<<<div_up(std::max<uint32_t>(SA.slots, 1), 256), 256, 0, s>>>(SA); count_launch();
       k_seg_active<<<1, 1024, 0, s>>>(SA); count_launch();
@@ -2166,10 +2504,10 @@ public:
       int reps = (sig || prof) ? 1 : unroll;
       for (int rep = 0; rep < reps; ++rep) {
         for (size_t k = 0; k < act.size(); ++k)
-          dispatch_fb<A>(nf, nb, this, *act[k], *views[k], G, cs, done, prof, sig, sa);
+          dispatch_fb<A>(nf, nb, this, *act[k], *views[k], G, cs, done, prof, sig, sa, stp);
         for (size_t k = 0; k < act.size(); ++k)
           dispatch_fb<P>(nf, nb, this, *act[k], *views[k], G, cs, k == 0 ? 1 : 0, k + 1 == act.size() ? 1 : 0, done,
-                         prof, sig, sa);
+                         prof, sig, sa, stp);
         if (sig) return;
         if (seg) {
           k_seg_jacobi_control<<<1, 1024, 0, cs>>>(G, SA, h, use_handle ? 1 : 0, use_handle ? kernels : 0,
@@ -2337,11 +2675,19 @@ public:
     constexpr bool kTuned = NB == 1 && !GC;
     int tv_init = fluid_.size() == 1 ? model_->tune.v[kTunePcgInit] : 0;
     int tv_q = fluid_.size() == 1 ? model_->tune.v[kTunePcgQ] : 0;
+    // staged sweeps (the staging knob) for the tuned layout, except with the
+    // cell-tile sweep
+    StageArgs st{};
+    bool staged = false;
+    if constexpr (kTuned) staged = !seg && tv_q != 4 && stage_args(nh, v, F, st);
     {
       ProfScope ps(model_->prof, "pcg_init", s);
       if (seg) {
         k_seg_pcg_begin<<<div_up(std::max<uint32_t>(SA.slots, 1), 256), 256, 0, s>>>(SA); count_launch();
       }
+      if constexpr (kTuned)
+        if (staged) k_pcg_init_staged<8><<<rg, kNT, kStageSmem, s>>>(P, G, N, R, st);
+      if (!staged)
       with_shape<PcgShapes, kTuned>(tv_init, [&](auto sh) {
         using Sh = decltype(sh);
         if (seg) {
@@ -2374,8 +2720,10 @@ public:
       if constexpr (kTuned) {
         if (tiles)
           k_pcg_q_tiles<NB><<<rg, kNT, 2 * kTileStage * sizeof(float4), cs>>>(P, G, N, R, gv, xs, fg, bg);
+        else if (staged)
+          k_pcg_q_staged<8><<<rg, kNT, kStageSmem, cs>>>(P, G, N, R, st);
       }
-      if (!tiles)
+      if (!tiles && !staged)
         with_shape<PcgShapes, kTuned>(tv_q, [&](auto sh) {
           using Sh = decltype(sh);
           if (seg) {
@@ -2431,6 +2779,7 @@ public:
         sig_add(sig, gv);
         sig_add(sig, xs);
       }
+      if (staged) sig_add(sig, st);
       loops_[F.g].run(s, sig, [&](cudaStream_t cs, cudaGraphConditionalHandle h) { body(cs, h, true, false); });
       PG_LAUNCH_CHECK();
     }

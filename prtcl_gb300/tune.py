@@ -8,7 +8,10 @@ the tuner is free to pick the fastest per workload:
   wkbb18_diag, pcg_init, pcg_q) select a launch shape: threads per block,
   blocks resident per SM (the register cap) and neighbour-walk batch;
 * jacobi_unroll is the number of relaxed-Jacobi iterations per iteration of
-  the device loop's graph (1, 2 or 4).
+  the device loop's graph (1, 2 or 4);
+* staging (single-scene models) builds staged neighbour lists and runs the
+  staged relaxed-Jacobi and PCG sweeps, which read their neighbours'
+  records from shared memory (0 or 1).
 
 The cell size is not a knob: it equals the search radius, as in the
 reference's grid (util/grouped_uniform_grid.hpp:621-632), because the
@@ -17,7 +20,8 @@ neighbour order, and with it every sum, depends on it.
 Search.  The sweeps are independent kernels, so one profiled run per shape
 index times every sweep knob at once (each kernel with its own variant);
 each (knob, value) is measured twice, in rising and falling order, and the
-smaller time counts.  jacobi_unroll is timed over whole steps.  Workloads
+smaller time counts.  The step knobs (staging, then jacobi_unroll) are
+timed over whole steps, one after the other, the same way.  Workloads
 run on their own copy of the scene, so a tuned run starts from the same
 state as an untuned one.
 
@@ -35,8 +39,10 @@ import time
 
 SWEEP_KNOBS = ("density", "iisph_setup", "iisph_accel", "iisph_pressure", "wkbb18_diag", "pcg_init", "pcg_q")
 VALUES = {**{k: (0, 1, 2, 3) for k in SWEEP_KNOBS}, "pcg_q": (0, 1, 2, 3, 4), "iisph_accel": (0, 1, 2, 3, 4),
-          "iisph_pressure": (0, 1, 2, 3, 4), "jacobi_unroll": (1, 2, 4)}
-DEFAULTS = {**{k: 0 for k in SWEEP_KNOBS}, "jacobi_unroll": 1}
+          "iisph_pressure": (0, 1, 2, 3, 4), "jacobi_unroll": (1, 2, 4), "staging": (0, 1)}
+DEFAULTS = {**{k: 0 for k in SWEEP_KNOBS}, "jacobi_unroll": 1, "staging": 0}
+# knobs timed over whole steps, in this order
+STEP_KNOBS = ("staging", "jacobi_unroll")
 
 
 def knob_table():
@@ -141,15 +147,17 @@ class Autotuner:
             cand = [(timings[f"{k}={v}"], v) for v in VALUES[k] if f"{k}={v}" in timings]
             best[k] = min(cand)[1] if cand else DEFAULTS[k]
             target.set(k, best[k])
-        if "jacobi_unroll" in target.knobs():
-            for order in (VALUES["jacobi_unroll"], tuple(reversed(VALUES["jacobi_unroll"]))):
+        for k in STEP_KNOBS:
+            if k not in target.knobs():
+                continue
+            for order in (VALUES[k], tuple(reversed(VALUES[k]))):
                 for v in order:
-                    target.set("jacobi_unroll", v)
+                    target.set(k, v)
                     t = target.measure_steps()
-                    key = f"jacobi_unroll={v}"
+                    key = f"{k}={v}"
                     timings[key] = min(timings.get(key, math.inf), t * 1e6)
-            best["jacobi_unroll"] = min((timings[f"jacobi_unroll={v}"], v) for v in VALUES["jacobi_unroll"])[1]
-            target.set("jacobi_unroll", best["jacobi_unroll"])
+            best[k] = min((timings[f"{k}={v}"], v) for v in VALUES[k])[1]
+            target.set(k, best[k])
         self.store(workload, best, {k: round(v, 2) for k, v in timings.items()})
         return best, "tuned", timings
 
@@ -163,7 +171,7 @@ class PlainTarget:
         self.viscosity = bool(loop.p.get("viscosity"))
 
     def knobs(self):
-        k = ["density", "iisph_setup", "iisph_accel", "iisph_pressure", "jacobi_unroll"]
+        k = ["density", "iisph_setup", "iisph_accel", "iisph_pressure", "jacobi_unroll", "staging"]
         if self.viscosity:
             k += ["wkbb18_diag", "pcg_init", "pcg_q"]
         return k

@@ -14,6 +14,8 @@ SETTINGS = [
     {**{k: 2 for k in tune.SWEEP_KNOBS}, "jacobi_unroll": 4},
     {**{k: 3 for k in tune.SWEEP_KNOBS}, "jacobi_unroll": 1},
     {"pcg_q": 4},  # the cell-tile sweep
+    {"staging": 1},  # staged lists and sweeps
+    {"staging": 1, "jacobi_unroll": 2, "iisph_pressure": 2},
 ]
 FIELDS = (("position", 3), ("velocity", 3), ("density", 1), ("pressure", 1), ("acceleration", 3),
           ("wkbb18_velocity_delta", 3))
@@ -55,6 +57,48 @@ def test_cell_tile_sweep_at_1m(gpu_lib):
     assert c == cref
     for name, nc in FIELDS:
         a, b = d.get_varying("f", name, nc), ref.get_varying("f", name, nc)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), name
+
+
+def test_staged_sweeps_at_1m(gpu_lib):
+    """Staged lists and sweeps on the 1M dam break: most tiles stage (the
+    others take the global gathers) and two steps equal the unstaged run's
+    bit for bit."""
+    sc = scenes.dam_break_1m()
+    p = driver.DAM_BREAK_1M
+    ref, cref = _run(sc, p, {}, 2)
+    d, c = _run(sc, p, {"staging": 1}, 2)
+    assert c == cref
+    for name, nc in FIELDS:
+        a, b = d.get_varying("f", name, nc), ref.get_varying("f", name, nc)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), name
+    fg = d.model.get_group("f").index
+    staged, tiles = d.nhood.staged_tiles(fg)
+    assert tiles == (len(sc["fluid"]) + 127) // 128
+    assert staged >= 0.5 * tiles, (staged, tiles)
+    assert ref.nhood.staged_tiles(fg) == (0, 0)
+
+
+def test_staging_switches_off(gpu_lib):
+    """Turning staging off after staged steps rebuilds plain lists; the run
+    continues bit-identically to one that never staged."""
+    sc = scenes.dam_break(fluid_cells=(16, 18, 12), spacing=0.025, box=(0.8, 0.7, 0.5))
+    p = dict(driver.DAM_BREAK_27K, viscosity=True)
+    from prtcl_gb300.core import DeviceScene
+    runs = []
+    for knobs in ((0, 0), (1, 0)):
+        d = DeviceScene()
+        driver.setup_dam_break(d, sc, p)
+        loop = driver.StepLoop(d, p, device_loop=True)
+        for k in knobs:
+            d.model.tune_set("staging", k)
+            for _ in range(4):
+                loop.step()
+        runs.append(d)
+    fg = runs[1].model.get_group("f").index
+    assert runs[1].nhood.staged_tiles(fg) == (0, 0)
+    for name, nc in FIELDS:
+        a, b = runs[1].get_varying("f", name, nc), runs[0].get_varying("f", name, nc)
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), name
 
 
@@ -106,6 +150,8 @@ def test_knob_errors(gpu_lib):
         m.tune_set("pcg_q", 5)
     with pytest.raises(PrtclGpuError, match="invalid argument"):
         m.tune_set("jacobi_unroll", 3)
+    with pytest.raises(PrtclGpuError, match="invalid argument"):
+        m.tune_set("staging", 2)
     assert m.tune_get("jacobi_unroll") == 1 and m.tune_get("pcg_q") == 0
     m.tune_set("pcg_q", 4)
     assert m.tune_get("pcg_q") == 4

@@ -10,10 +10,11 @@ from prtcl_gb300 import tune
 
 class FakeTarget:
     """Per-kernel seconds per launch by variant; whole-step seconds by
-    Jacobi repeat count.  Counts the measurements."""
+    Jacobi repeat count (plus the staging knob's cost, when given).  Counts
+    the measurements."""
 
-    def __init__(self, costs, unroll_cost, knobs=None):
-        self.costs, self.unroll_cost = costs, unroll_cost
+    def __init__(self, costs, unroll_cost, knobs=None, staging_cost=None):
+        self.costs, self.unroll_cost, self.staging_cost = costs, unroll_cost, staging_cost or {0: 0.0, 1: 0.0}
         self.v = dict(tune.DEFAULTS)
         self.calls = 0
         self._knobs = knobs or list(costs) + ["jacobi_unroll"]
@@ -31,7 +32,7 @@ class FakeTarget:
 
     def measure_steps(self):
         self.calls += 1
-        return self.unroll_cost[self.v["jacobi_unroll"]]
+        return self.unroll_cost[self.v["jacobi_unroll"]] + self.staging_cost[self.v["staging"]]
 
 
 COSTS = {"iisph_accel": [1.0e-4, 0.9e-4, 1.2e-4, 0.8e-4, 0.85e-4],
@@ -53,6 +54,20 @@ def test_search_picks_the_fastest_variant_per_knob(tmp_path):
     assert tgt.calls == 2 * 5 + 2 * 3
     assert "density=4" not in timings and "iisph_accel=4" in timings
     assert timings["iisph_pressure=2"] == pytest.approx(110.0)
+
+
+def test_step_knobs_are_timed_over_steps_in_turn(tmp_path):
+    t = tune.Autotuner(cache_path=str(tmp_path / "c.json"), device="d")
+    tgt = FakeTarget(COSTS, UNROLL, knobs=list(COSTS) + ["staging", "jacobi_unroll"],
+                     staging_cost={0: 1.0e-3, 1: 0.4e-3})
+    choice, _, timings = t.tune(tgt, "w")
+    assert choice["staging"] == 1 and choice["jacobi_unroll"] == 2
+    assert tgt.v["staging"] == 1
+    # staging is decided first (at the default repeat count), then the
+    # repeat count with staging on
+    assert timings["staging=0"] == pytest.approx(4000.0) and timings["staging=1"] == pytest.approx(3400.0)
+    assert timings["jacobi_unroll=2"] == pytest.approx(3300.0)
+    assert tgt.calls == 2 * 5 + 2 * 2 + 2 * 3
 
 
 def test_ties_keep_the_default(tmp_path):
