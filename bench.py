@@ -208,8 +208,10 @@ def max_over_ranks(dist, v):
 
 
 def nvtx_range(name):
-    """An NVTX range around the profile pass (every kernel there is its own
-    launch), so that a profiler can select exactly those launches."""
+    """An NVTX range around a measured pass (profile_pass: every kernel of
+    the headline's profile steps is its own launch; search_uniform,
+    search_blobs: the timed searches; batched_profile_pass), so that a
+    profiler can select exactly those launches."""
     try:
         import torch
         torch.cuda.nvtx.range_push(name)
@@ -282,7 +284,13 @@ def run_ours(args, rank, world, dist):
     from prtcl_gb300.core import DeviceScene
     sc, p = workload(args)
     nf, nb = len(sc["fluid"]), len(sc["boundary"])
-    choice, tuning = tuned("plain", sc, p)
+    if args.no_tune:
+        choice, tuning = dict(tune.DEFAULTS), {"choice": dict(tune.DEFAULTS), "source": "defaults (--no-tune)"}
+    else:
+        choice, tuning = tuned("plain", sc, p)
+    if args.knob:
+        choice = dict(choice, **args.knob)
+        tuning = dict(tuning, choice=choice, overrides=args.knob)
 
     d = DeviceScene()
     driver.setup_dam_break(d, sc, p)
@@ -322,11 +330,14 @@ def run_ours(args, rank, world, dist):
 
     extras = {}
     if rank == 0 and world == 1 and not args.no_extras:
-        extras["long_run"] = run_long(peak)
-        extras["plain_27k"] = run_plain_27k(args.no_cpu_baseline, peak=peak, peak_kind=peak_kind)
-        extras["search"] = run_search(peak, no_cpu=args.no_cpu_baseline)
-        extras["batched"] = run_batched(peak=peak, peak_kind=peak_kind, no_cpu=args.no_cpu_baseline)
-        extras["serving"] = run_serving()
+        legs = {"long_run": lambda: run_long(peak),
+                "plain_27k": lambda: run_plain_27k(args.no_cpu_baseline, peak=peak, peak_kind=peak_kind),
+                "search": lambda: run_search(peak, no_cpu=args.no_cpu_baseline),
+                "batched": lambda: run_batched(peak=peak, peak_kind=peak_kind, no_cpu=args.no_cpu_baseline),
+                "serving": run_serving}
+        for name, leg in legs.items():
+            if args.extras is None or name in args.extras:
+                extras[name] = leg()
 
     solves = max(st["jacobi_solves"], 1.0)
     line = {
@@ -581,12 +592,14 @@ def run_search(peak, n=4_000_000, reps=5, target=40.0, no_cpu=False):
             d.nhood.query(0)
         d.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        nvtx = nvtx_range(f"search_{dist}")
         e0.record(s)
         for _ in range(reps):
             d.update()
             d.nhood.query(0)
         e1.record(s)
         e1.synchronize()
+        nvtx_end(nvtx)
         sec = e0.elapsed_time(e1) / 1e3 / reps
         algo = (32 + 4 * nbar) * n
         out[dist] = {"points": n, "radius": r, "mean_neighbours": round(nbar, 3),
@@ -688,8 +701,10 @@ def run_batched(count=256, steps=10, warmup=3, plain_steps=5, peak=None, peak_ki
         bt.synchronize()
         bt.profile_read()
         b0 = [bt.info(i) for i in ids]
+        nvtx = nvtx_range("batched_profile_pass")
         bt.step(profile_steps)
         bt.synchronize()
+        nvtx_end(nvtx)
         prof = bt.profile_read()
         b1 = [bt.info(i) for i in ids]
         bt.profile(False)
@@ -793,7 +808,24 @@ def main():
     ap.add_argument("--profile-steps", type=int, default=3)
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the neighbour-search, batched-scenes and serving measurements")
+    ap.add_argument("--extras", type=lambda v: v.split(","), default=None, metavar="LEG,...",
+                    help="run only these of the extra legs: long_run, plain_27k, search, batched, serving")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="headline workload with the default knob values instead of the autotuner's choice")
+    ap.add_argument("--knob", action="append", default=[], metavar="NAME=VALUE",
+                    help="override one autotuner knob of the headline workload (repeatable), e.g. staging=1")
     args = ap.parse_args()
+    knobs = {}
+    for kv in args.knob:
+        name, _, val = kv.partition("=")
+        if name not in tune.VALUES or not val.lstrip("-").isdigit() or int(val) not in tune.VALUES[name]:
+            ap.error(f"--knob {kv}: knobs are " + ", ".join(f"{k}={'/'.join(map(str, v))}"
+                                                            for k, v in tune.VALUES.items()))
+        knobs[name] = int(val)
+    args.knob = knobs
+    legs = ("long_run", "plain_27k", "search", "batched", "serving")
+    if args.extras is not None and not set(args.extras) <= set(legs):
+        ap.error("--extras: legs are " + ", ".join(legs))
     if args.warmup < 3 and args.impl != "reference":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     rank, world, dist = dist_setup(args.gpus)
