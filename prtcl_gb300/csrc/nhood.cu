@@ -280,10 +280,14 @@ __device__ __forceinline__ int group_of(uint32_t const *goff, int G, uint32_t n)
 // pass 1: per item in group-major order, the biased grid indices and the
 // handle; OR-reductions of the bit statistics that select the key bits
 // (grid-stride; the OR of the block is committed with one atomic per word,
-// so that the atomics on the four shared words do not serialise the pass)
+// so that the atomics on the four shared words do not serialise the pass).
+// KEY: the key layout of the previous update is taken (it is confirmed
+// against these statistics before the grid is read), so the pass writes the
+// Z-order keys themselves (the work of k_cells_key) instead of the indices.
 constexpr int kCellsUNT = 256;
-__global__ void __launch_bounds__(kCellsUNT) k_cells_u(PosTable pt, GridView gv, int G, size_t N, uint32_t *ukeys,
-                                                       uint32_t *vals, uint32_t *stats) {
+template <bool KEY>
+__global__ void __launch_bounds__(kCellsUNT) k_cells_u(const __grid_constant__ PosTable pt, GridView gv, int G, size_t N, uint32_t *ukeys,
+                                                       uint64_t *keys, uint32_t *vals, uint32_t *stats) {
   __shared__ uint32_t sh[4][kCellsUNT / 32];
   uint32_t ne = 0, eq = 0, a1 = 0, a0 = 0;
   for (size_t n = blockIdx.x * size_t(blockDim.x) + threadIdx.x; n < N; n += size_t(gridDim.x) * blockDim.x) {
@@ -298,7 +302,10 @@ __global__ void __launch_bounds__(kCellsUNT) k_cells_u(PosTable pt, GridView gv,
       a1 |= u[a] & 0x80000000u;
       a0 |= ~u[a] & 0x80000000u;
     }
-    reinterpret_cast<uint4 *>(ukeys)[n] = make_uint4(u[0], u[1], u[2], 0u);
+    if constexpr (KEY)
+      keys[n] = make_key(u[0], u[1], u[2], gv.key) | seg_key(gv, item_seg(gv, g, i));
+    else
+      reinterpret_cast<uint4 *>(ukeys)[n] = make_uint4(u[0], u[1], u[2], 0u);
     vals[n] = (uint32_t(g) << 28) | i;
   }
   ne = __reduce_or_sync(kFull, ne);
@@ -329,36 +336,83 @@ __global__ void k_cells_key(uint32_t const *ukeys, uint32_t const *vals, size_t 
   }
 }
 
-__global__ void k_cell_flags(uint64_t const *keys, size_t N, uint32_t *flags) {
-  size_t s = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
-  if (s < N) flags[s] = (s == 0 || keys[s] != keys[s - 1]) ? 1u : 0u;
+// The cells from the sorted keys in three launches: per tile of kScanTile
+// sorted items the number of cell starts (k_cf_count, an item starts a cell
+// where its key differs from its predecessor's), their exclusive scan over
+// the tiles (k_scan_single), then every item's cell and the cell tables
+// (k_cf_fill).  A thread holds kScanIPT consecutive items.
+__global__ void __launch_bounds__(kScanNT) k_cf_count(uint64_t const *__restrict__ keys, size_t N, uint32_t *sums) {
+  __shared__ uint32_t sh[32];
+  size_t base = size_t(blockIdx.x) * kScanTile + size_t(threadIdx.x) * kScanIPT;
+  uint32_t f = 0;
+  if (base < N) {
+    uint64_t prev = base > 0 ? keys[base - 1] : 0ull;
+#pragma unroll
+    for (int k = 0; k < kScanIPT; ++k)
+      if (base + k < N) {
+        uint64_t key = keys[base + k];
+        f += (base + k == 0 || key != prev) ? 1u : 0u;
+        prev = key;
+      }
+  }
+  uint32_t total;
+  block_excl_scan<kScanNT>(f, sh, total);
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
 }
 
-// excl = exclusive scan of flags: cell(s) = excl[s] + flag[s] - 1
-__global__ void k_cells_fill(PosTable pt, GridView gv, uint64_t const *keys, uint32_t const *vals, uint32_t const *flags,
-                             uint32_t const *excl, size_t N, int32_t *s2c, int32_t *r2s, int32_t *cell_start,
-                             uint64_t *cell_key, int4 *cell_gi, int *ncells, int32_t *cell_adj) {
-  size_t s = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
-  if (s >= N) return;
-  uint32_t f = flags[s];
-  int32_t c = int32_t(excl[s] + f) - 1;
-  s2c[s] = c;
-  uint32_t h = vals[s];
-  uint32_t g = h >> 28, i = h & 0x0FFFFFFFu;
-  r2s[gv.goff[g] + i] = int32_t(s);
-  if (f) {
-    cell_start[c] = int32_t(s);
-    cell_key[c] = keys[s];
-    int3 gi = x_to_gi(pt.pos[g][i], gv);
-    cell_gi[c] = make_int4(gi.x, gi.y, gi.z, 0);
-    // no neighbour yet (k_cells_adj fills the slots it finds)
-    // (a cell's 26 slots start at a multiple of 104 bytes: 8-byte stores)
-    int2 *a = reinterpret_cast<int2 *>(cell_adj + size_t(c) * 26);
-    for (int k = 0; k < 13; ++k) a[k] = make_int2(-1, -1);
+// excl_tiles: the exclusive scan of k_cf_count's sums; cell(s) is the
+// number of cell starts at or before s, minus one
+__global__ void __launch_bounds__(kScanNT) k_cf_fill(const __grid_constant__ PosTable pt, GridView gv, uint64_t const *__restrict__ keys,
+                                                     uint32_t const *__restrict__ vals, uint32_t const *excl_tiles,
+                                                     size_t N, int32_t *s2c, int32_t *r2s, int32_t *cell_start,
+                                                     uint64_t *cell_key, int4 *cell_gi, int *ncells,
+                                                     int32_t *cell_adj) {
+  __shared__ uint32_t sh[32];
+  size_t base = size_t(blockIdx.x) * kScanTile + size_t(threadIdx.x) * kScanIPT;
+  uint64_t key[kScanIPT];
+  uint32_t fl[kScanIPT], f = 0;
+  if (base < N) {
+    uint64_t prev = base > 0 ? keys[base - 1] : 0ull;
+#pragma unroll
+    for (int k = 0; k < kScanIPT; ++k) {
+      key[k] = base + k < N ? keys[base + k] : 0ull;
+      fl[k] = base + k < N && (base + k == 0 || key[k] != prev) ? 1u : 0u;
+      prev = key[k];
+      f += fl[k];
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < kScanIPT; ++k) {
+      key[k] = 0ull;
+      fl[k] = 0u;
+    }
   }
-  if (s == N - 1) {
-    cell_start[c + 1] = int32_t(N);
-    *ncells = c + 1;
+  uint32_t total;
+  uint32_t run = block_excl_scan<kScanNT>(f, sh, total) + excl_tiles[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < kScanIPT; ++k) {
+    size_t si = base + k;
+    if (si >= N) break;
+    run += fl[k];
+    int32_t c = int32_t(run) - 1;
+    s2c[si] = c;
+    uint32_t h = vals[si];
+    uint32_t g = h >> 28, i = h & 0x0FFFFFFFu;
+    r2s[gv.goff[g] + i] = int32_t(si);
+    if (fl[k]) {
+      cell_start[c] = int32_t(si);
+      cell_key[c] = key[k];
+      int3 gi = x_to_gi(pt.pos[g][i], gv);
+      cell_gi[c] = make_int4(gi.x, gi.y, gi.z, 0);
+      // no neighbour yet (the adjacency kernel fills the slots it finds)
+      // (a cell's 26 slots start at a multiple of 104 bytes: 8-byte stores)
+      int2 *a = reinterpret_cast<int2 *>(cell_adj + size_t(c) * 26);
+      for (int q = 0; q < 13; ++q) a[q] = make_int2(-1, -1);
+    }
+    if (si == N - 1) {
+      cell_start[c + 1] = int32_t(N);
+      *ncells = c + 1;
+    }
   }
 }
 
@@ -457,7 +511,48 @@ __global__ void k_cells_adj(GridView gv, int4 const *cell_gi, size_t N, int32_t 
   }
 }
 
-__global__ void k_xsorted(PosTable pt, uint32_t const *vals, size_t N, float4 *xs) {
+// The same adjacency through the hash table, with the 13 lookups of a cell
+// in flight together: every home slot is read first, then the values of the
+// slots that hold their key; a lookup whose home slot holds another key
+// continues with the probe loop of hash_find.  The slots found are those of
+// hash_find, so the adjacency is the same.
+__global__ void __launch_bounds__(128) k_cells_adj_hash(GridView gv, int4 const *cell_gi, size_t N, int32_t *adj,
+                                                        uint64_t const *__restrict__ hk,
+                                                        int32_t const *__restrict__ hv, uint32_t mask) {
+  size_t c = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  int C = *gv.ncells;
+  if (c >= N || int(c) >= C) return;
+  int4 g = cell_gi[c];
+  uint64_t kc = gv.cell_key[c];
+  uint64_t sk = seg_key(gv, gv.seg_shift < 64 ? uint32_t(kc >> gv.seg_shift) : 0u);
+  uint64_t kt[13], got[13];
+  uint32_t slot[13], valid = 0;
+#pragma unroll
+  for (int k = 0; k < 13; ++k) {
+    int3 p = make_int3(g.x + c_offsets[k][0], g.y + c_offsets[k][1], g.z + c_offsets[k][2]);
+    uint32_t u0 = unsign(p.x), u1 = unsign(p.y), u2 = unsign(p.z);
+    bool ok = key_valid(u0, gv.key) && key_valid(u1, gv.key) && key_valid(u2, gv.key);
+    kt[k] = ok ? (make_key(u0, u1, u2, gv.key) | sk) : kEmptyKey;
+    slot[k] = key_hash(kt[k], mask);
+    valid |= ok ? (1u << k) : 0u;
+  }
+#pragma unroll
+  for (int k = 0; k < 13; ++k) got[k] = (valid >> k) & 1u ? hk[slot[k]] : kEmptyKey;
+  int d[13];
+#pragma unroll
+  for (int k = 0; k < 13; ++k) d[k] = ((valid >> k) & 1u) && got[k] == kt[k] ? hv[slot[k]] : -1;
+#pragma unroll
+  for (int k = 0; k < 13; ++k) {
+    if (!((valid >> k) & 1u)) continue;
+    if (got[k] != kt[k] && got[k] != kEmptyKey) d[k] = hash_find(hk, hv, mask, kt[k]);
+    if (d[k] >= 0) {
+      adj[c * 26 + k] = d[k];
+      adj[size_t(d[k]) * 26 + 25 - k] = int32_t(c);
+    }
+  }
+}
+
+__global__ void k_xsorted(const __grid_constant__ PosTable pt, uint32_t const *vals, size_t N, float4 *xs) {
   size_t s = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
   if (s < N) {
     uint32_t h = vals[s];
@@ -900,15 +995,19 @@ __global__ void k_perm_keep(uint16_t const *seg, uint8_t const *due, size_t n, u
 // host side
 // ---------------------------------------------------------------------------
 
-static void exclusive_scan(uint32_t const *in, uint32_t *out, size_t n, uint32_t *&sums, size_t &sums_cap,
-                           cudaStream_t s) {
-  if (n == 0) return;
-  size_t nb = (n + kScanTile - 1) / kScanTile;
+static void ensure_sums(size_t nb, uint32_t *&sums, size_t &sums_cap) {
   if (nb > sums_cap) {
     if (sums) PG_CUDA(cudaFree(sums));
     sums_cap = std::max<size_t>(nb, 1024);
     PG_CUDA(cudaMalloc(&sums, sums_cap * sizeof(uint32_t)));
   }
+}
+
+static void exclusive_scan(uint32_t const *in, uint32_t *out, size_t n, uint32_t *&sums, size_t &sums_cap,
+                           cudaStream_t s) {
+  if (n == 0) return;
+  size_t nb = (n + kScanTile - 1) / kScanTile;
+  ensure_sums(nb, sums, sums_cap);
   k_scan_reduce<<<unsigned(nb), kScanNT, 0, s>>>(in, n, sums); count_launch();
   k_scan_single<<<1, 1024, 0, s>>>(sums, nb); count_launch();
   k_scan_apply<<<unsigned(nb), kScanNT, 0, s>>>(in, n, sums, out); count_launch();
@@ -1096,10 +1195,13 @@ void Nhood::update(cudaStream_t s) {
   {
     ProfScope ps(model_->prof, "grid_keys", s);
     unsigned ub = std::min<unsigned>(div_up(N, kCellsUNT), 152u * 8u);
-    k_cells_u<<<ub, kCellsUNT, 0, s>>>(pt, gv, G, N, ukeys_, vals_a_, stats_d_); count_launch();
+    if (key_known_) k_cells_u<true><<<ub, kCellsUNT, 0, s>>>(pt, gv, G, N, nullptr, keys_a_, vals_a_, stats_d_);
+    else k_cells_u<false><<<ub, kCellsUNT, 0, s>>>(pt, gv, G, N, ukeys_, nullptr, vals_a_, stats_d_);
+    count_launch();
   }
   PG_LAUNCH_CHECK();
   KeyInfo k{};
+  bool keyed = key_known_; // the keys are written already
   if (key_known_) {
     // the previous update's layout, confirmed before anything reads the grid
     k = key_;
@@ -1121,8 +1223,10 @@ void Nhood::update(cudaStream_t s) {
   gv = view();
   // 2. compressed Z-order keys (segment above them)
   model_->prof.begin("grid_sort", s);
-  k_cells_key<<<nb, 256, 0, s>>>(ukeys_, vals_a_, N, gv, keys_a_); count_launch();
-  PG_LAUNCH_CHECK();
+  if (!keyed) {
+    k_cells_key<<<nb, 256, 0, s>>>(ukeys_, vals_a_, N, gv, keys_a_); count_launch();
+    PG_LAUNCH_CHECK();
+  }
   // 3. stable LSD radix sort over the informative bits
   int total_bits = 3 * k.bits + (seg_count_ ? seg_bits_ : 0);
   uint64_t *kin = keys_a_, *kout = keys_b_;
@@ -1157,12 +1261,16 @@ void Nhood::update(cudaStream_t s) {
   model_->prof.end(s); // grid_sort
   model_->prof.begin("grid_cells", s);
   // 4. cells
-  k_cell_flags<<<nb, 256, 0, s>>>(kin, N, flags_); count_launch();
-  PG_LAUNCH_CHECK();
-  exclusive_scan(flags_, scan_, N, block_sums_, block_sums_cap_, s);
-  k_cells_fill<<<nb, 256, 0, s>>>(pt, gv, kin, vin, flags_, scan_, N, s2c_, r2s_, cell_start_, cell_key_, cell_gi_,
-                                  ncells_d_, cell_adj_); count_launch();
-  PG_LAUNCH_CHECK();
+  {
+    size_t tiles_c = (N + kScanTile - 1) / kScanTile;
+    ensure_sums(tiles_c, block_sums_, block_sums_cap_);
+    k_cf_count<<<unsigned(tiles_c), kScanNT, 0, s>>>(kin, N, block_sums_); count_launch();
+    k_scan_single<<<1, 1024, 0, s>>>(block_sums_, tiles_c); count_launch();
+    k_cf_fill<<<unsigned(tiles_c), kScanNT, 0, s>>>(pt, gv, kin, vin, block_sums_, N, s2c_, r2s_, cell_start_,
+                                                   cell_key_, cell_gi_, ncells_d_, cell_adj_);
+    count_launch();
+    PG_LAUNCH_CHECK();
+  }
   // 5. adjacency (cells <= N; slots without a neighbour stay -1)
   uint64_t *hk = nullptr;
   int32_t *hv = nullptr;
@@ -1183,7 +1291,9 @@ void Nhood::update(cudaStream_t s) {
     hv = hvals_;
     k_hash_insert<<<nb, 256, 0, s>>>(gv, N, hk, hv, mask); count_launch();
   }
-  k_cells_adj<<<nb, 256, 0, s>>>(gv, cell_gi_, N, cell_adj_, hk, hv, mask); count_launch();
+  if (hk) k_cells_adj_hash<<<div_up(N, 128), 128, 0, s>>>(gv, cell_gi_, N, cell_adj_, hk, hv, mask);
+  else k_cells_adj<<<nb, 256, 0, s>>>(gv, cell_gi_, N, cell_adj_, hk, hv, mask);
+  count_launch();
   model_->prof.end(s); // grid_cells
   PG_LAUNCH_CHECK();
 }
