@@ -170,10 +170,12 @@ int prtcl_gpu_profile_reset(prtcl_gpu_model *model);
  * iisph_pressure, wkbb18_diag, pcg_init, pcg_q (values 0..3, a launch
  * shape each; pcg_q 4: a cell-tile sweep without neighbour lists, for
  * unbatched models), jacobi_unroll (1, 2 or 4 relaxed-Jacobi iterations per
- * iteration of the device loop's graph) and staging (1: unbatched models with
+ * iteration of the device loop's graph), staging (1: unbatched models with
  * one fluid and one boundary group build staged lists, and the
  * relaxed-Jacobi and PCG sweeps read their neighbours' records from shared
- * memory per tile of 128 items).  prtcl_gb300/tune.py searches them
+ * memory per tile of 128 items) and grid_sort (1, the default: a grid of at
+ * most 128,000 items is sorted in one launch of a thread-block cluster of 8
+ * or 16 CTAs; 0: the tiled radix-sort launches at every size).  prtcl_gb300/tune.py searches them
  * per workload and caches the choice.  prtcl_gpu_tune_knobs returns one line
  * per knob: "name default value=shape ...", a shape written as threads per
  * block x blocks per SM / neighbour-walk batch.  An unknown knob gives

@@ -153,11 +153,12 @@ enum TuneKnob : int {
   kTunePcgInit,
   kTunePcgQ,
   kTuneJacobiUnroll,
-  kTuneStaging, // 1: staged lists and the staged Jacobi / PCG sweeps
+  kTuneStaging,  // 1: staged lists and the staged Jacobi / PCG sweeps
+  kTuneGridSort, // 1: grids of at most 128k items sorted in one launch of a thread-block cluster
   kTuneKnobs
 };
 struct Tuning {
-  int v[kTuneKnobs] = {0, 0, 0, 0, 0, 0, 0, 1, 0};
+  int v[kTuneKnobs] = {0, 0, 0, 0, 0, 0, 0, 1, 0, 1};
 };
 // knob names (the kernels' profiler names; "jacobi_unroll") and allowed values
 char const *tune_knob_name(int k);

@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cooperative_groups.h>
 #include <cstring>
 #include <limits>
 
@@ -260,6 +261,122 @@ __global__ void k_rs_scatter(uint64_t const *__restrict__ kin, uint32_t const *_
       if (lane == __ffs(peers) - 1) cnt[w][d] = pos + __popc(peers);
     }
     __syncwarp();
+  }
+}
+
+// The same stable LSD sort for small grids in one launch of a thread-block
+// cluster, over 8-bit digits: CTA r of the cluster holds sorted positions
+// [r M, (r + 1) M) in shared memory (keys and values, two buffers).  Per
+// pass every CTA ranks its items by digit as k_rs_scatter does (per-warp
+// counts, ranks within a warp by lane), publishes its digit totals, and
+// after a cluster barrier each item's new position is the cluster-wide
+// start of its digit, plus the totals of that digit in the CTAs before, plus
+// its rank in the CTA; it is stored straight into the owning CTA's shared
+// memory.  A second barrier ends the pass.  The order is the tiled sort's:
+// by digit, then by position before the pass.
+constexpr int kRcNT = 1024, kRcWarps = kRcNT / 32;
+constexpr uint32_t kRcMaxPerCta = 8000; // 24 bytes per item + 32 KB of counters fit 227 KB
+__global__ void __launch_bounds__(kRcNT, 1) k_rs_cluster(uint64_t const *__restrict__ kin,
+                                                         uint32_t const *__restrict__ vin, uint64_t *kout,
+                                                         uint32_t *vout, uint32_t N, uint32_t M, int total_bits) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  uint32_t r = cl.block_rank(), C = cl.num_blocks();
+  extern __shared__ __align__(16) unsigned char rc_smem[];
+  uint64_t *ka = reinterpret_cast<uint64_t *>(rc_smem), *kb = ka + M;
+  uint32_t *va = reinterpret_cast<uint32_t *>(kb + M), *vb = va + M;
+  uint32_t(*cnt)[256] = reinterpret_cast<uint32_t(*)[256]>(vb + M); // [kRcWarps][256]
+  __shared__ uint32_t tot[256], base[256], wsum[8];
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t lo = r * M, nl = lo < N ? min(M, N - lo) : 0u;
+  for (uint32_t i = threadIdx.x; i < nl; i += kRcNT) {
+    ka[i] = kin[lo + i];
+    va[i] = vin[lo + i];
+  }
+  // warp w ranks the local items [w * wi, (w + 1) * wi)
+  uint32_t wi = (M + kRcWarps - 1) / kRcWarps;
+  wi = (wi + 31u) & ~31u;
+  uint32_t w0 = min(nl, uint32_t(w) * wi), w1 = min(nl, w0 + wi);
+  uint32_t lt = (1u << lane) - 1u;
+  for (int shift = 0; shift < total_bits; shift += 8) {
+    for (uint32_t d = threadIdx.x; d < kRcWarps * 256u; d += kRcNT) cnt[d / 256][d % 256] = 0u;
+    __syncthreads();
+    for (uint32_t b = w0; b < w1; b += 32) {
+      uint32_t i = b + lane;
+      uint32_t d = i < w1 ? uint32_t((ka[i] >> shift) & 0xFFu) : 256u;
+      uint32_t peers = __match_any_sync(kFull, d);
+      if (d != 256u && lane == __ffs(peers) - 1) cnt[w][d] += __popc(peers);
+      __syncwarp();
+    }
+    __syncthreads();
+    // per digit: exclusive offsets over the warps, the CTA's total
+    if (threadIdx.x < 256) {
+      uint32_t d = threadIdx.x, run = 0;
+      for (int ww = 0; ww < kRcWarps; ++ww) {
+        uint32_t c = cnt[ww][d];
+        cnt[ww][d] = run;
+        run += c;
+      }
+      tot[d] = run;
+    }
+    cl.sync(); // every CTA's totals are complete
+    // cluster-wide totals per digit, their exclusive scan over the digits,
+    // and the totals of this digit in the CTAs before this one
+    uint32_t T = 0, before = 0;
+    if (threadIdx.x < 256) {
+      for (uint32_t q = 0; q < C; ++q) {
+        uint32_t t = *cl.map_shared_rank(&tot[threadIdx.x], q);
+        T += t;
+        if (q < r) before += t;
+      }
+      uint32_t x = T;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(kFull, x, o);
+        if (lane >= o) x += y;
+      }
+      if (lane == 31) wsum[w] = x;
+      base[threadIdx.x] = x - T + before; // exclusive within the warp's 32 digits
+    }
+    __syncthreads();
+    if (threadIdx.x < 256) {
+      uint32_t add = 0;
+      for (int ww = 0; ww < w; ++ww) add += wsum[ww];
+      base[threadIdx.x] += add;
+    }
+    __syncthreads();
+    for (uint32_t b = w0; b < w1; b += 32) {
+      uint32_t i = b + lane;
+      uint64_t key = 0;
+      uint32_t val = 0, d = 256u;
+      if (i < w1) {
+        key = ka[i];
+        val = va[i];
+        d = uint32_t((key >> shift) & 0xFFu);
+      }
+      uint32_t peers = __match_any_sync(kFull, d);
+      uint32_t pos = d != 256u ? base[d] + cnt[w][d] : 0u;
+      __syncwarp();
+      if (d != 256u) {
+        uint32_t dst = pos + __popc(peers & lt);
+        uint32_t q = dst / M, li = dst - q * M;
+        *cl.map_shared_rank(kb + li, q) = key;
+        *cl.map_shared_rank(vb + li, q) = val;
+        if (lane == __ffs(peers) - 1) cnt[w][d] += __popc(peers);
+      }
+      __syncwarp();
+    }
+    cl.sync(); // every item has landed; the totals may be reused
+    uint64_t *tk = ka;
+    ka = kb;
+    kb = tk;
+    uint32_t *tv = va;
+    va = vb;
+    vb = tv;
+  }
+  for (uint32_t i = threadIdx.x; i < nl; i += kRcNT) {
+    kout[lo + i] = ka[i];
+    vout[lo + i] = va[i];
   }
 }
 
@@ -995,6 +1112,44 @@ __global__ void k_perm_keep(uint16_t const *seg, uint8_t const *due, size_t n, u
 // host side
 // ---------------------------------------------------------------------------
 
+// The cluster sort's launch for a grid of N items: 8 CTAs up to
+// 8 * kRcMaxPerCta items, 16 (a non-portable cluster size) up to twice that;
+// false where N is larger or the device cannot hold such a cluster (probed
+// once per device and size with the largest shared-memory footprint).
+static bool cluster_sort_config(size_t N, cudaLaunchConfig_t &cfg, cudaLaunchAttribute &attr, uint32_t &M) {
+  if (N == 0 || N > 16 * size_t(kRcMaxPerCta)) return false;
+  int C = N <= 8 * size_t(kRcMaxPerCta) ? 8 : 16;
+  int dev = 0;
+  PG_CUDA(cudaGetDevice(&dev));
+  static int ok[2][64] = {}; // 0 unknown, 1 yes, 2 no
+  int &known = ok[C == 16][dev & 63];
+  size_t smax = size_t(kRcMaxPerCta) * 24 + size_t(kRcWarps) * 256 * 4;
+  M = uint32_t((N + C - 1) / C);
+  cfg = cudaLaunchConfig_t{};
+  cfg.gridDim = dim3(unsigned(C));
+  cfg.blockDim = dim3(unsigned(kRcNT));
+  attr = cudaLaunchAttribute{};
+  attr.id = cudaLaunchAttributeClusterDimension;
+  attr.val.clusterDim.x = unsigned(C);
+  attr.val.clusterDim.y = 1;
+  attr.val.clusterDim.z = 1;
+  cfg.attrs = &attr;
+  cfg.numAttrs = 1;
+  if (known == 0) {
+    // the attributes are set per device: with a device change the probe of
+    // the new device sets them again
+    PG_CUDA(cudaFuncSetAttribute(k_rs_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smax)));
+    if (C > 8) PG_CUDA(cudaFuncSetAttribute(k_rs_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    cfg.dynamicSmemBytes = smax;
+    int clusters = 0;
+    cudaError_t e = cudaOccupancyMaxActiveClusters(&clusters, k_rs_cluster, &cfg);
+    if (e != cudaSuccess) (void)cudaGetLastError(); // a size the device does not take: no cluster sort
+    known = (e == cudaSuccess && clusters > 0) ? 1 : 2;
+  }
+  cfg.dynamicSmemBytes = size_t(M) * 24 + size_t(kRcWarps) * 256 * 4;
+  return known == 1;
+}
+
 static void ensure_sums(size_t nb, uint32_t *&sums, size_t &sums_cap) {
   if (nb > sums_cap) {
     if (sums) PG_CUDA(cudaFree(sums));
@@ -1241,7 +1396,20 @@ void Nhood::update(cudaStream_t s) {
     hist_cap_ = hl + hl / 4;
     PG_CUDA(cudaMalloc(&hist_, hist_cap_ * 4));
   }
-  for (int shift = 0; shift < total_bits; shift += dbits) {
+  cudaLaunchConfig_t rc_cfg;
+  cudaLaunchAttribute rc_attr;
+  uint32_t rc_m = 0;
+  bool rc = model_->tune.v[kTuneGridSort] != 0 && cluster_sort_config(N, rc_cfg, rc_attr, rc_m);
+  if (rc) {
+    rc_cfg.stream = s;
+    PG_CUDA(cudaLaunchKernelEx(&rc_cfg, k_rs_cluster, static_cast<uint64_t const *>(kin),
+                               static_cast<uint32_t const *>(vin), kout, vout, uint32_t(N), rc_m, total_bits));
+    count_launch();
+    PG_LAUNCH_CHECK();
+    std::swap(kin, kout);
+    std::swap(vin, vout);
+  }
+  for (int shift = 0; !rc && shift < total_bits; shift += dbits) {
     if (dbits == 8) k_rs_hist<8><<<tiles, kRsNT, 0, s>>>(kin, N, shift, hist_, tiles);
     else if (dbits == 9) k_rs_hist<9><<<tiles, kRsNT, 0, s>>>(kin, N, shift, hist_, tiles);
     else k_rs_hist<10><<<tiles, kRsNT, 0, s>>>(kin, N, shift, hist_, tiles);

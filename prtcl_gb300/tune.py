@@ -11,7 +11,10 @@ the tuner is free to pick the fastest per workload:
   the device loop's graph (1, 2 or 4);
 * staging (single-scene models) builds staged neighbour lists and runs the
   staged relaxed-Jacobi and PCG sweeps, which read their neighbours'
-  records from shared memory (0 or 1).
+  records from shared memory (0 or 1);
+* grid_sort (single-scene models whose grid holds at most 128k items)
+  sorts the grid in one launch of a thread-block cluster instead of the
+  tiled radix-sort launches (0 or 1).
 
 The cell size is not a knob: it equals the search radius, as in the
 reference's grid (util/grouped_uniform_grid.hpp:621-632), because the
@@ -20,8 +23,9 @@ neighbour order, and with it every sum, depends on it.
 Search.  The sweeps are independent kernels, so one profiled run per shape
 index times every sweep knob at once (each kernel with its own variant);
 each (knob, value) is measured twice, in rising and falling order, and the
-smaller time counts.  The step knobs (staging, then jacobi_unroll) are
-timed over whole steps, one after the other, the same way.  Workloads
+smaller time counts.  The step knobs (grid_sort, staging, then
+jacobi_unroll) are timed over whole steps, one after the other, the same
+way.  Workloads
 run on their own copy of the scene, so a tuned run starts from the same
 state as an untuned one.
 
@@ -39,10 +43,10 @@ import time
 
 SWEEP_KNOBS = ("density", "iisph_setup", "iisph_accel", "iisph_pressure", "wkbb18_diag", "pcg_init", "pcg_q")
 VALUES = {**{k: (0, 1, 2, 3) for k in SWEEP_KNOBS}, "pcg_q": (0, 1, 2, 3, 4), "iisph_accel": (0, 1, 2, 3, 4),
-          "iisph_pressure": (0, 1, 2, 3, 4), "jacobi_unroll": (1, 2, 4), "staging": (0, 1)}
-DEFAULTS = {**{k: 0 for k in SWEEP_KNOBS}, "jacobi_unroll": 1, "staging": 0}
+          "iisph_pressure": (0, 1, 2, 3, 4), "jacobi_unroll": (1, 2, 4), "staging": (0, 1), "grid_sort": (0, 1)}
+DEFAULTS = {**{k: 0 for k in SWEEP_KNOBS}, "jacobi_unroll": 1, "staging": 0, "grid_sort": 1}
 # knobs timed over whole steps, in this order
-STEP_KNOBS = ("staging", "jacobi_unroll")
+STEP_KNOBS = ("grid_sort", "staging", "jacobi_unroll")
 
 
 def knob_table():
@@ -166,12 +170,17 @@ class PlainTarget:
     """A single-scene model stepped by the reference driver loop
     (prtcl_gb300.driver.StepLoop with the device Jacobi loop)."""
 
-    def __init__(self, scene, loop, probe_steps=3):
+    def __init__(self, scene, loop, probe_steps=3, grid_items=None):
         self.d, self.loop, self.n = scene, loop, probe_steps
         self.viscosity = bool(loop.p.get("viscosity"))
+        # items of the grid (fluid and boundary), where known: grid_sort is
+        # a knob only for grids the cluster sort takes
+        self.grid_items = float("inf") if grid_items is None else grid_items
 
     def knobs(self):
         k = ["density", "iisph_setup", "iisph_accel", "iisph_pressure", "jacobi_unroll", "staging"]
+        if self.grid_items <= 128_000:
+            k.append("grid_sort")
         if self.viscosity:
             k += ["wkbb18_diag", "pcg_init", "pcg_q"]
         return k
@@ -259,7 +268,8 @@ def tune_plain(scene, params, tuner=None, warmup=3, force=False):
     loop = driver.StepLoop(d, params, device_loop=True)
     for _ in range(warmup):
         loop.step(quiet=True)
-    return tuner.tune(PlainTarget(d, loop), workload, force=True)
+    return tuner.tune(PlainTarget(d, loop, grid_items=len(scene["fluid"]) + len(scene.get("boundary", ()))),
+                      workload, force=True)
 
 
 def tune_batched(scene_list, params, tuner=None, warmup=2, force=False):

@@ -11,9 +11,11 @@ from tests.helpers import assert_bitwise, point_scene
 pytestmark = pytest.mark.gpu
 
 
-def make(oracle_mod, groups, radius):
+def make(oracle_mod, groups, radius, knobs=None):
     from prtcl_gb300.core import DeviceScene
     d = DeviceScene()
+    for k, v in (knobs or {}).items():
+        d.model.tune_set(k, v)
     o = oracle_mod.Scene(np.float32)
     point_scene(d, groups, radius)
     point_scene(o, groups, radius)
@@ -203,3 +205,37 @@ def test_key_layout_change_between_updates(oracle_mod, then_permute):
         m.set_varying("p", "position", back)
         m.update()
     compare(d, o, [("p", "fluid", back, [])])
+
+
+@pytest.mark.parametrize("grid_sort", [0, 1])
+@pytest.mark.parametrize("n", [1, 2, 4095, 4096, 4097, 8193])
+def test_cell_pass_tile_boundaries(oracle_mod, n, grid_sort):
+    """The cell pass counts cell starts per tile of 4,096 sorted items and
+    fills the tables per tile: sizes at the tile boundaries (about 38 items
+    a cell, so cells straddle the tiles' ends) equal the oracle's grid and
+    lists, with either sort.  A second update of moved points takes the
+    previous key layout (the keyed first pass) and must agree too."""
+    rng = np.random.default_rng(31 + n)
+    pts = (rng.random((n, 3)) * 0.3).astype(np.float32)
+    groups = [("p", "fluid", pts, [])]
+    d, o = make(oracle_mod, groups, 0.05, {"grid_sort": grid_sort})
+    compare(d, o, groups)
+    moved = (pts + (rng.random((n, 3)).astype(np.float32) - 0.5) * np.float32(0.01)).astype(np.float32)
+    for m in (d, o):
+        m.set_varying("p", "position", moved)
+        m.update()
+    compare(d, o, [("p", "fluid", moved, [])])
+
+
+@pytest.mark.parametrize("n", [1000, 64000, 64001, 100000, 128000])
+def test_cluster_sort_sizes(oracle_mod, n):
+    """The one-launch cluster sort (grid_sort 1): 8 CTAs up to 64,000 grid
+    items, 16 up to 128,000, with two groups so that handles of both sit in
+    the sort; the grid and the lists equal the oracle's."""
+    rng = np.random.default_rng(41)
+    a = (rng.random((n - n // 3, 3)) * 0.6).astype(np.float32)
+    b = (rng.random((n // 3, 3)) * 0.6).astype(np.float32)
+    groups = [("a", "fluid", a, []), ("b", "boundary", b, [])]
+    r = scenes.uniform_radius_for_mean_neighbours(n, 20.0) * 0.6
+    d, o = make(oracle_mod, groups, r, {"grid_sort": 1})
+    compare(d, o, groups)

@@ -16,6 +16,8 @@ SETTINGS = [
     {"pcg_q": 4},  # the cell-tile sweep
     {"staging": 1},  # staged lists and sweeps
     {"staging": 1, "jacobi_unroll": 2, "iisph_pressure": 2},
+    {"grid_sort": 0},  # the grid sorted by the tiled launches (default: one cluster launch)
+    {"grid_sort": 0, "staging": 1},
 ]
 FIELDS = (("position", 3), ("velocity", 3), ("density", 1), ("pressure", 1), ("acceleration", 3),
           ("wkbb18_velocity_delta", 3))
@@ -152,6 +154,8 @@ def test_knob_errors(gpu_lib):
         m.tune_set("jacobi_unroll", 3)
     with pytest.raises(PrtclGpuError, match="invalid argument"):
         m.tune_set("staging", 2)
+    with pytest.raises(PrtclGpuError, match="invalid argument"):
+        m.tune_set("grid_sort", 2)
     assert m.tune_get("jacobi_unroll") == 1 and m.tune_get("pcg_q") == 0
     m.tune_set("pcg_q", 4)
     assert m.tune_get("pcg_q") == 4
