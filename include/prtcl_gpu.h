@@ -175,7 +175,10 @@ int prtcl_gpu_profile_reset(prtcl_gpu_model *model);
  * relaxed-Jacobi and PCG sweeps read their neighbours' records from shared
  * memory per tile of 128 items) and grid_sort (1, the default: a grid of at
  * most 128,000 items is sorted in one launch of a thread-block cluster of 8
- * or 16 CTAs; 0: the tiled radix-sort launches at every size).  prtcl_gb300/tune.py searches them
+ * or 16 CTAs; 0: the tiled radix-sort launches at every size) and list_split
+ * (1, the default: the lists of a query group of at most 65,536 items are
+ * built by four threads per query, each walking a quarter of its cells; 0:
+ * one thread per query at every size).  prtcl_gb300/tune.py searches them
  * per workload and caches the choice.  prtcl_gpu_tune_knobs returns one line
  * per knob: "name default value=shape ...", a shape written as threads per
  * block x blocks per SM / neighbour-walk batch.  An unknown knob gives

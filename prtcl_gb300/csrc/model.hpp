@@ -155,10 +155,11 @@ enum TuneKnob : int {
   kTuneJacobiUnroll,
   kTuneStaging,  // 1: staged lists and the staged Jacobi / PCG sweeps
   kTuneGridSort, // 1: grids of at most 128k items sorted in one launch of a thread-block cluster
+  kTuneListSplit, // 1: lists of query groups of at most 64k items built by four threads per query
   kTuneKnobs
 };
 struct Tuning {
-  int v[kTuneKnobs] = {0, 0, 0, 0, 0, 0, 0, 1, 0, 1};
+  int v[kTuneKnobs] = {0, 0, 0, 0, 0, 0, 0, 1, 0, 1, 1};
 };
 // knob names (the kernels' profiler names; "jacobi_unroll") and allowed values
 char const *tune_knob_name(int k);

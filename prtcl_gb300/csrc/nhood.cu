@@ -1075,6 +1075,178 @@ __global__ void __launch_bounds__(kBuildNT, STAGE ? 5 : (NG <= 2 ? 9 : 1))
   }
 }
 
+// Lists of a small query group (the list_split knob): kSplit threads per
+// query, each walking a contiguous part of the query's visit sequence (own
+// cell, then adjacency slots 0..25: parts of 7, 7, 7 and 6 cells), so that
+// a query's dependent chain of cell walks is a quarter as long.  A first
+// walk counts each part's neighbours per group (with the first index and
+// the index range); the query's threads combine them by shuffles into each
+// row's count, base index and wide / narrow form, and a second walk writes
+// every entry straight to its place in the chunks (or idx32 for a wide
+// row), with its gradient factor.  The visited cells, the distance test and
+// the factor arithmetic are those of k_build_lists, so the rows are the
+// same entry for entry; the tail of a row's last chunk is zero-filled as
+// there.  For a query group of the grid (no fallback search).
+constexpr int kSplit = 4, kSplitNT = 128;
+constexpr size_t kSplitMaxQueries = 65536;
+__device__ __forceinline__ int split_first_visit(int sub) { return sub * 7; } // 0, 7, 14, 21; 27 at the end
+
+template <class F>
+__device__ __forceinline__ void split_walk(GridView const &gv, float4 const *__restrict__ xs, int cell,
+                                           float const *lo3, float const *hi3, int v0, int v1, f3 xi, F &&f) {
+  for (int v = v0; v < v1; ++v) {
+    int c = cell;
+    if (v > 0) {
+      int k = v - 1;
+      // slot k < 13: +offset[k]; slot 25 - k: -offset[k]
+      int kk = k < 13 ? k : 25 - k;
+      int sg = k < 13 ? 1 : -1;
+      float lb = 0.0f;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        int o = sg * c_offsets[kk][a];
+        float b = o > 0 ? hi3[a] : (o < 0 ? lo3[a] : 0.0f);
+        lb += b * b;
+      }
+      if (lb > 1.0001f) continue;
+      c = gv.cell_adj[size_t(cell) * 26 + k];
+    }
+    if (c < 0) continue;
+    int s0 = gv.cell_start[c], s1 = gv.cell_start[c + 1];
+    for (int base = s0; base < s1; base += 32) {
+      int e = min(s1 - base, 32);
+      uint32_t mask = 0;
+      for (int t = 0; t < e; ++t) {
+        float d2 = nsq3(sub3(xi, mk3(xs[base + t])));
+        if (d2 < gv.r2lt) mask |= 1u << t;
+      }
+      while (mask) {
+        int t = __ffs(int(mask)) - 1;
+        mask &= mask - 1u;
+        f(base + t);
+      }
+    }
+  }
+}
+
+template <int NG>
+__global__ void __launch_bounds__(kSplitNT) k_build_lists_split(GridView gv, float4 const *__restrict__ xs,
+                                                               float4 const *__restrict__ qpos, int q, ListOut lo,
+                                                               float const *hp, float *hcache,
+                                                               uint32_t const *__restrict__ order) {
+  uint32_t gt = blockIdx.x * kSplitNT + threadIdx.x;
+  uint32_t t = gt / kSplit;
+  int sub = int(gt % kSplit);
+  bool with_gf = hp != nullptr;
+  KernelParams K = kparams(with_gf ? *hp : 1.0f);
+  if (gt == 0) *hcache = with_gf ? K.h : __int_as_float(0x7fc00000);
+  bool active = t < lo.n; // the same for a query's kSplit threads (one warp holds whole queries)
+  uint32_t i = active ? (order ? order[t] : t) : 0u;
+  f3 xi = {0.0f, 0.0f, 0.0f};
+  int cell = -1;
+  float lo3[3] = {0.0f, 0.0f, 0.0f}, hi3[3] = {0.0f, 0.0f, 0.0f};
+  if (active) {
+    float4 x4 = qpos[i];
+    xi = mk3(x4);
+    cell = gv.s2c[gv.r2s[gv.goff[q] + i]];
+    int4 cg = gv.cell_gi[cell];
+    bool inside = face_bounds(x4.x, gv.rinv, cg.x, lo3[0], hi3[0]);
+    inside = face_bounds(x4.y, gv.rinv, cg.y, lo3[1], hi3[1]) && inside;
+    inside = face_bounds(x4.z, gv.rinv, cg.z, lo3[2], hi3[2]) && inside;
+    if (!inside)
+      for (int a = 0; a < 3; ++a) lo3[a] = hi3[a] = 0.0f;
+  }
+  int v0 = split_first_visit(sub), v1 = sub + 1 < kSplit ? split_first_visit(sub + 1) : 27;
+  // 1. per group: hits, the first hit's index, the index range
+  uint32_t cnt[NG], first[NG];
+  int32_t mn[NG], mx[NG];
+#pragma unroll
+  for (int g = 0; g < NG; ++g) {
+    cnt[g] = 0u;
+    first[g] = 0u;
+    mn[g] = INT32_MAX;
+    mx[g] = INT32_MIN;
+  }
+  if (active)
+    split_walk(gv, xs, cell, lo3, hi3, v0, v1, xi, [&](int s) {
+      uint32_t h = __float_as_uint(xs[s].w);
+      uint32_t g = h >> 28, j = h & 0x0FFFFFFFu;
+#pragma unroll
+      for (int qq = 0; qq < NG; ++qq)
+        if (qq == int(g)) {
+          if (cnt[qq] == 0u) first[qq] = j;
+          mn[qq] = min(mn[qq], int32_t(j));
+          mx[qq] = max(mx[qq], int32_t(j));
+          ++cnt[qq];
+        }
+    });
+  // 2. the query's rows: each part's first entry, the count, base and form
+  uint32_t pre[NG], total[NG], j0[NG];
+  bool wide[NG];
+#pragma unroll
+  for (int g = 0; g < NG; ++g) {
+    uint32_t x = cnt[g];
+#pragma unroll
+    for (int o = 1; o < kSplit; o <<= 1) {
+      uint32_t y = __shfl_up_sync(kFull, x, o, kSplit);
+      if (sub >= o) x += y;
+    }
+    pre[g] = x - cnt[g];
+    total[g] = __shfl_sync(kFull, x, kSplit - 1, kSplit);
+    int src = cnt[g] ? sub : kSplit;
+    int32_t lo_j = mn[g], hi_j = mx[g];
+#pragma unroll
+    for (int o = 1; o < kSplit; o <<= 1) {
+      src = min(src, __shfl_xor_sync(kFull, src, o, kSplit));
+      lo_j = min(lo_j, __shfl_xor_sync(kFull, lo_j, o, kSplit));
+      hi_j = max(hi_j, __shfl_xor_sync(kFull, hi_j, o, kSplit));
+    }
+    j0[g] = __shfl_sync(kFull, first[g], src < kSplit ? src : 0, kSplit);
+    if (src >= kSplit) j0[g] = 0u;
+    wide[g] = total[g] > 0u && (hi_j - int32_t(j0[g]) > 32767 || lo_j - int32_t(j0[g]) < -32768);
+  }
+  if (!active) return;
+  // 3. the entries at their places
+  uint32_t run[NG];
+#pragma unroll
+  for (int g = 0; g < NG; ++g) run[g] = pre[g];
+  split_walk(gv, xs, cell, lo3, hi3, v0, v1, xi, [&](int s) {
+    float4 xj = xs[s];
+    uint32_t h = __float_as_uint(xj.w);
+    uint32_t g = h >> 28, j = h & 0x0FFFFFFFu;
+    float f = with_gf ? kgrad_factor(K, nsq3(sub3(xi, mk3(xj)))) : 0.0f;
+#pragma unroll
+    for (int qq = 0; qq < NG; ++qq)
+      if (qq == int(g)) {
+        uint32_t k = run[qq]++;
+        if (k < lo.cap[qq]) {
+          unsigned char *ch = lo.chunks[qq] + (size_t(k / kChunk) * lo.n + i) * kChunkBytes;
+          if (wide[qq]) lo.idx32[qq][size_t(i) * lo.cap[qq] + k] = j;
+          else reinterpret_cast<uint16_t *>(ch)[k % kChunk] = uint16_t(uint32_t(int32_t(j - j0[qq])) & 0xFFFFu);
+          if (lo.with_gf) reinterpret_cast<uint32_t *>(ch + 32)[k % kChunk] = __float_as_uint(f);
+        }
+      }
+  });
+  if (sub != 0) return;
+#pragma unroll
+  for (int g = 0; g < NG; ++g) {
+    if (g >= lo.G) break;
+    uint32_t n = total[g];
+    lo.cb[size_t(g) * lo.n + i] = make_uint2(n | (wide[g] ? kWide : 0u), j0[g]);
+    atomicMax(&lo.maxcnt[g], n);
+    if (n > lo.cap[g] || n % kChunk == 0) continue;
+    // the partial last chunk (and half-chunk of a wide row), zero-filled
+    unsigned char *ch = lo.chunks[g] + (size_t(n / kChunk) * lo.n + i) * kChunkBytes;
+    if (wide[g]) {
+      for (uint32_t e = n; e % 8; ++e) lo.idx32[g][size_t(i) * lo.cap[g] + e] = 0u;
+    } else {
+      for (uint32_t slot = n % kChunk; slot < kChunk; ++slot) reinterpret_cast<uint16_t *>(ch)[slot] = 0u;
+    }
+    if (lo.with_gf)
+      for (uint32_t slot = n % kChunk; slot < kChunk; ++slot) reinterpret_cast<uint32_t *>(ch + 32)[slot] = 0u;
+  }
+}
+
 template <int NG, bool STAGE>
 void launch_build_lists(size_t n, size_t smem, cudaStream_t s, GridView const &gv, float4 const *xs,
                         float4 const *qpos, int q, ListOut const &lo, float const *h, float *hcache,
@@ -1584,7 +1756,12 @@ void Nhood::build_lists(int q, Lists &L, cudaStream_t s, float const *h, bool st
     float4 const *qpos = static_cast<float4 const *>(gg_[q].pos->d);
     {
       ProfScope ps(model_->prof, "nhood_lists", s);
-      if (st) {
+      bool split = !st && model_->tune.v[kTuneListSplit] != 0 && n <= kSplitMaxQueries && in_grid_[q] && G <= 2;
+      if (split) {
+        unsigned nb2 = unsigned(div_up(n * kSplit, size_t(kSplitNT)));
+        if (G == 1) k_build_lists_split<1><<<nb2, kSplitNT, 0, s>>>(gv, xsorted_, qpos, q, lo, h, L.hcache, order);
+        else k_build_lists_split<2><<<nb2, kSplitNT, 0, s>>>(gv, xsorted_, qpos, q, lo, h, L.hcache, order);
+      } else if (st) {
         if (G == 1) launch_build_lists<1, true>(n, smem, s, gv, xsorted_, qpos, q, lo, h, L.hcache, order);
         else launch_build_lists<2, true>(n, smem, s, gv, xsorted_, qpos, q, lo, h, L.hcache, order);
       } else {

@@ -1814,7 +1814,7 @@ template <class T> void sig_add(std::string &s, T const &v) { s.append(reinterpr
 char const *tune_knob_name(int k) {
   static char const *names[kTuneKnobs] = {"density", "iisph_setup", "iisph_accel", "iisph_pressure",
                                           "wkbb18_diag", "pcg_init", "pcg_q", "jacobi_unroll", "staging",
-                                          "grid_sort"};
+                                          "grid_sort", "list_split"};
   return (k >= 0 && k < kTuneKnobs) ? names[k] : "";
 }
 int tune_knob_find(std::string const &name) {
@@ -1824,7 +1824,7 @@ int tune_knob_find(std::string const &name) {
 }
 bool tune_value_ok(int k, int v) {
   if (k == kTuneJacobiUnroll) return v == 1 || v == 2 || v == 4;
-  if (k == kTuneStaging || k == kTuneGridSort) return v == 0 || v == 1;
+  if (k == kTuneStaging || k == kTuneGridSort || k == kTuneListSplit) return v == 0 || v == 1;
   if (k == kTunePcgQ) return v >= 0 && v <= 4; // 4: the cell-tile sweep
   // 4: the persistent tiled sweeps of a batched model (work counter)
   if (k == kTuneAccel || k == kTunePressure) return v >= 0 && v <= 4;
@@ -1844,6 +1844,7 @@ std::string tune_knob_table() {
   t += "jacobi_unroll 1 1=1 2=2 4=4\n";
   t += "staging 0 0=off 1=staged lists and sweeps (unbatched models)\n";
   t += "grid_sort 1 0=tiled launches 1=one cluster launch for grids of at most 128k items\n";
+  t += "list_split 1 0=one thread per query 1=four threads per query for query groups of at most 64k items\n";
   return t;
 }
 

@@ -14,7 +14,9 @@ the tuner is free to pick the fastest per workload:
   records from shared memory (0 or 1);
 * grid_sort (single-scene models whose grid holds at most 128k items)
   sorts the grid in one launch of a thread-block cluster instead of the
-  tiled radix-sort launches (0 or 1).
+  tiled radix-sort launches (0 or 1);
+* list_split (query groups of at most 64k items) builds each query's lists
+  with four threads, each walking a quarter of its cells (0 or 1).
 
 The cell size is not a knob: it equals the search radius, as in the
 reference's grid (util/grouped_uniform_grid.hpp:621-632), because the
@@ -23,9 +25,9 @@ neighbour order, and with it every sum, depends on it.
 Search.  The sweeps are independent kernels, so one profiled run per shape
 index times every sweep knob at once (each kernel with its own variant);
 each (knob, value) is measured twice, in rising and falling order, and the
-smaller time counts.  The step knobs (grid_sort, staging, then
-jacobi_unroll) are timed over whole steps, one after the other, the same
-way.  Workloads
+smaller time counts.  The step knobs (grid_sort, list_split, staging,
+then jacobi_unroll) are timed over whole steps, one after the other, the
+same way.  Workloads
 run on their own copy of the scene, so a tuned run starts from the same
 state as an untuned one.
 
@@ -43,10 +45,11 @@ import time
 
 SWEEP_KNOBS = ("density", "iisph_setup", "iisph_accel", "iisph_pressure", "wkbb18_diag", "pcg_init", "pcg_q")
 VALUES = {**{k: (0, 1, 2, 3) for k in SWEEP_KNOBS}, "pcg_q": (0, 1, 2, 3, 4), "iisph_accel": (0, 1, 2, 3, 4),
-          "iisph_pressure": (0, 1, 2, 3, 4), "jacobi_unroll": (1, 2, 4), "staging": (0, 1), "grid_sort": (0, 1)}
-DEFAULTS = {**{k: 0 for k in SWEEP_KNOBS}, "jacobi_unroll": 1, "staging": 0, "grid_sort": 1}
+          "iisph_pressure": (0, 1, 2, 3, 4), "jacobi_unroll": (1, 2, 4), "staging": (0, 1), "grid_sort": (0, 1),
+          "list_split": (0, 1)}
+DEFAULTS = {**{k: 0 for k in SWEEP_KNOBS}, "jacobi_unroll": 1, "staging": 0, "grid_sort": 1, "list_split": 1}
 # knobs timed over whole steps, in this order
-STEP_KNOBS = ("grid_sort", "staging", "jacobi_unroll")
+STEP_KNOBS = ("grid_sort", "list_split", "staging", "jacobi_unroll")
 
 
 def knob_table():
@@ -170,17 +173,20 @@ class PlainTarget:
     """A single-scene model stepped by the reference driver loop
     (prtcl_gb300.driver.StepLoop with the device Jacobi loop)."""
 
-    def __init__(self, scene, loop, probe_steps=3, grid_items=None):
+    def __init__(self, scene, loop, probe_steps=3, grid_items=None, fluid_items=None):
         self.d, self.loop, self.n = scene, loop, probe_steps
         self.viscosity = bool(loop.p.get("viscosity"))
-        # items of the grid (fluid and boundary), where known: grid_sort is
-        # a knob only for grids the cluster sort takes
+        # items of the grid (fluid and boundary) and of the fluid group, where
+        # known: grid_sort and list_split are knobs only for the sizes they take
         self.grid_items = float("inf") if grid_items is None else grid_items
+        self.fluid_items = float("inf") if fluid_items is None else fluid_items
 
     def knobs(self):
         k = ["density", "iisph_setup", "iisph_accel", "iisph_pressure", "jacobi_unroll", "staging"]
         if self.grid_items <= 128_000:
             k.append("grid_sort")
+        if self.fluid_items <= 65_536:
+            k.append("list_split")
         if self.viscosity:
             k += ["wkbb18_diag", "pcg_init", "pcg_q"]
         return k
@@ -268,7 +274,8 @@ def tune_plain(scene, params, tuner=None, warmup=3, force=False):
     loop = driver.StepLoop(d, params, device_loop=True)
     for _ in range(warmup):
         loop.step(quiet=True)
-    return tuner.tune(PlainTarget(d, loop, grid_items=len(scene["fluid"]) + len(scene.get("boundary", ()))),
+    return tuner.tune(PlainTarget(d, loop, grid_items=len(scene["fluid"]) + len(scene.get("boundary", ())),
+                                  fluid_items=len(scene["fluid"])),
                       workload, force=True)
 
 

@@ -207,9 +207,9 @@ def test_key_layout_change_between_updates(oracle_mod, then_permute):
     compare(d, o, [("p", "fluid", back, [])])
 
 
-@pytest.mark.parametrize("grid_sort", [0, 1])
+@pytest.mark.parametrize("grid_sort,list_split", [(0, 0), (1, 0), (1, 1)])
 @pytest.mark.parametrize("n", [1, 2, 4095, 4096, 4097, 8193])
-def test_cell_pass_tile_boundaries(oracle_mod, n, grid_sort):
+def test_cell_pass_tile_boundaries(oracle_mod, n, grid_sort, list_split):
     """The cell pass counts cell starts per tile of 4,096 sorted items and
     fills the tables per tile: sizes at the tile boundaries (about 38 items
     a cell, so cells straddle the tiles' ends) equal the oracle's grid and
@@ -218,7 +218,7 @@ def test_cell_pass_tile_boundaries(oracle_mod, n, grid_sort):
     rng = np.random.default_rng(31 + n)
     pts = (rng.random((n, 3)) * 0.3).astype(np.float32)
     groups = [("p", "fluid", pts, [])]
-    d, o = make(oracle_mod, groups, 0.05, {"grid_sort": grid_sort})
+    d, o = make(oracle_mod, groups, 0.05, {"grid_sort": grid_sort, "list_split": list_split})
     compare(d, o, groups)
     moved = (pts + (rng.random((n, 3)).astype(np.float32) - 0.5) * np.float32(0.01)).astype(np.float32)
     for m in (d, o):
@@ -238,4 +238,32 @@ def test_cluster_sort_sizes(oracle_mod, n):
     groups = [("a", "fluid", a, []), ("b", "boundary", b, [])]
     r = scenes.uniform_radius_for_mean_neighbours(n, 20.0) * 0.6
     d, o = make(oracle_mod, groups, r, {"grid_sort": 1})
+    compare(d, o, groups)
+
+
+@pytest.mark.parametrize("case", ["dam_break", "wide_rows", "negative"])
+def test_split_list_build(oracle_mod, case):
+    """The list build with four threads per query (list_split 1) equals the
+    oracle's lists: the 27k dam break (two groups, narrow rows), an
+    unpermuted group whose rows are wide (scattered raw indices walked in
+    grid order), and a lattice straddling the origin with neighbours at
+    exactly the radius."""
+    if case == "dam_break":
+        sc = scenes.dam_break()
+        groups = [("f", "fluid", sc["fluid"], ["dynamic"]), ("b", "boundary", sc["boundary"], [])]
+        r = 2 * np.float64(np.float32(0.025))
+    elif case == "wide_rows":
+        rng = np.random.default_rng(13)
+        pts = rng.random((60000, 3)).astype(np.float32)
+        groups = [("p", "fluid", pts, [])]
+        r = scenes.uniform_radius_for_mean_neighbours(60000, 40.0)
+    else:
+        s = 0.025
+        ax = (np.arange(-10, 10) + 0.5) * s
+        g = np.stack(np.meshgrid(ax, ax, ax, indexing="ij"), -1).reshape(-1, 3).astype(np.float32)
+        rng = np.random.default_rng(5)
+        b = (rng.random((3000, 3)) * 0.6 - 0.3).astype(np.float32)
+        groups = [("a", "fluid", g, []), ("b", "boundary", b, [])]
+        r = 2 * np.float64(np.float32(s))
+    d, o = make(oracle_mod, groups, r, {"list_split": 1})
     compare(d, o, groups)

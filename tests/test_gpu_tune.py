@@ -18,6 +18,8 @@ SETTINGS = [
     {"staging": 1, "jacobi_unroll": 2, "iisph_pressure": 2},
     {"grid_sort": 0},  # the grid sorted by the tiled launches (default: one cluster launch)
     {"grid_sort": 0, "staging": 1},
+    {"list_split": 0},  # one thread per query builds the lists (default: four for small groups)
+    {"list_split": 1, "staging": 1},  # staging takes precedence over the split build
 ]
 FIELDS = (("position", 3), ("velocity", 3), ("density", 1), ("pressure", 1), ("acceleration", 3),
           ("wkbb18_velocity_delta", 3))
@@ -156,6 +158,8 @@ def test_knob_errors(gpu_lib):
         m.tune_set("staging", 2)
     with pytest.raises(PrtclGpuError, match="invalid argument"):
         m.tune_set("grid_sort", 2)
+    with pytest.raises(PrtclGpuError, match="invalid argument"):
+        m.tune_set("list_split", 2)
     assert m.tune_get("jacobi_unroll") == 1 and m.tune_get("pcg_q") == 0
     m.tune_set("pcg_q", 4)
     assert m.tune_get("pcg_q") == 4
