@@ -1307,11 +1307,12 @@ static bool cluster_sort_config(size_t N, cudaLaunchConfig_t &cfg, cudaLaunchAtt
   attr.val.clusterDim.z = 1;
   cfg.attrs = &attr;
   cfg.numAttrs = 1;
+  if (known == 2) return false;
+  // the function's attributes belong to the current device's context: set
+  // on every call (host-side and cheap), so a new context gets them too
+  PG_CUDA(cudaFuncSetAttribute(k_rs_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smax)));
+  if (C > 8) PG_CUDA(cudaFuncSetAttribute(k_rs_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   if (known == 0) {
-    // the attributes are set per device: with a device change the probe of
-    // the new device sets them again
-    PG_CUDA(cudaFuncSetAttribute(k_rs_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smax)));
-    if (C > 8) PG_CUDA(cudaFuncSetAttribute(k_rs_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     cfg.dynamicSmemBytes = smax;
     int clusters = 0;
     cudaError_t e = cudaOccupancyMaxActiveClusters(&clusters, k_rs_cluster, &cfg);
