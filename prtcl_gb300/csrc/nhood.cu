@@ -2,6 +2,7 @@
 #include "nhood.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cooperative_groups.h>
 #include <cstring>
@@ -1293,8 +1294,10 @@ static bool cluster_sort_config(size_t N, cudaLaunchConfig_t &cfg, cudaLaunchAtt
   int C = N <= 8 * size_t(kRcMaxPerCta) ? 8 : 16;
   int dev = 0;
   PG_CUDA(cudaGetDevice(&dev));
-  static int ok[2][64] = {}; // 0 unknown, 1 yes, 2 no
-  int &known = ok[C == 16][dev & 63];
+  // per device and cluster size: 0 unknown, 1 yes, 2 no (models on several
+  // host threads may probe at once; every probe of a device finds the same)
+  static std::atomic<int> ok[2][64];
+  std::atomic<int> &known = ok[C == 16][dev & 63];
   size_t smax = size_t(kRcMaxPerCta) * 24 + size_t(kRcWarps) * 256 * 4;
   M = uint32_t((N + C - 1) / C);
   cfg = cudaLaunchConfig_t{};
@@ -1317,7 +1320,7 @@ static bool cluster_sort_config(size_t N, cudaLaunchConfig_t &cfg, cudaLaunchAtt
     int clusters = 0;
     cudaError_t e = cudaOccupancyMaxActiveClusters(&clusters, k_rs_cluster, &cfg);
     if (e != cudaSuccess) (void)cudaGetLastError(); // a size the device does not take: no cluster sort
-    known = (e == cudaSuccess && clusters > 0) ? 1 : 2;
+    known.store((e == cudaSuccess && clusters > 0) ? 1 : 2);
   }
   cfg.dynamicSmemBytes = size_t(M) * 24 + size_t(kRcWarps) * 256 * 4;
   return known == 1;
