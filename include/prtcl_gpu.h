@@ -173,7 +173,7 @@ int prtcl_gpu_profile_reset(prtcl_gpu_model *model);
  * iteration of the device loop's graph), staging (1: unbatched models with
  * one fluid and one boundary group build staged lists, and the
  * relaxed-Jacobi and PCG sweeps read their neighbours' records from shared
- * memory per tile of 128 items) and grid_sort (1, the default: a grid of at
+ * memory per tile of 128 items), grid_sort (1, the default: a grid of at
  * most 128,000 items is sorted in one launch of a thread-block cluster of 8
  * or 16 CTAs; 0: the tiled radix-sort launches at every size) and list_split
  * (1, the default: the lists of a query group of at most 65,536 items are
